@@ -1,0 +1,397 @@
+"""Benchmark: batched InsPIRe^2 Respond on one GB300 (or N replicas).
+
+Workload (the metric's configuration): a 2^24-entry x 32-byte database of
+uniform random bytes (seed 1) encoded resident in HBM (8192 shards of 2048
+entries), d = 2048, CRT q = [268369921, 249561089], p = 2^16; each step is one
+launch answering B = 128 seeded queries (real client queries made by the
+oracle client, each routed to a uniformly drawn shard), with per-client
+packing keys resident.  Metric: Respond queries/s.
+
+  value : device-resident inputs, CUDA-event time of the Respond launches.
+  e2e   : the same batches through the host-buffer C ABI call
+          (inspire_respond_seeded_batch) from pinned host memory, copies inside.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "inspire-rs_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+N = 2048
+ENTRY = 32
+GAMMA = 16
+LOG2_ENTRIES = 24
+BATCH = 128
+W_SEED = bytes(range(100, 132))
+METRIC = "Respond queries/s (batched InsPIRe^2, seeded queries, InspiRING packing)"
+# algorithmic bytes per query (raw shard 64 KiB + query b-rows 48 KiB + y_body 48 KiB + response 32 KiB)
+ALG_BYTES_PER_QUERY = 192 * 1024
+# exact modular multiplies per query (transform butterflies + pointwise products), see the design doc
+MULMODS_PER_QUERY = 3.4e6
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_query_pool(ctx, pack, n_queries, seed):
+    """Real seeded queries and the client's y_body from the oracle client."""
+    from oracle import oracle as O
+
+    client = O.Client(ctx, seed=seed, rng_seed=seed + 1000)
+    rng = np.random.default_rng(seed)
+    locals_ = rng.integers(0, N, size=n_queries)
+    seeds = np.zeros((n_queries, 6, 32), dtype=np.uint8)
+    brows = np.zeros((n_queries, 6, 2 * N), dtype=np.uint64)
+    for k, li in enumerate(locals_):
+        seeds[k], brows[k] = client.query_seeded(int(li))
+    y_body, _ = client.packing_keys(pack)
+    return client, locals_, seeds, brows, y_body
+
+
+def cpu_baseline(ctx, pack, db_raw, pool, budget_s=12.0, max_queries=200):
+    """Oracle (C restatement of the crate) respond_seeded_inspiring with
+    PackParams / OfflinePackingKeys built once, OpenMP over the 16 columns."""
+    from oracle import oracle as O
+
+    client, locals_, seeds, brows, y_body = pool
+    rng = np.random.default_rng(99)
+    nshards = (len(db_raw) // ENTRY) // N
+    t0 = time.perf_counter()
+    done = 0
+    while done < max_queries and (time.perf_counter() - t0) < budget_s:
+        k = done % len(locals_)
+        shard = ctx.encode_shard(db_raw, ENTRY, int(rng.integers(0, nshards)))
+        rgsw = ctx.expand_rgsw(seeds[k], brows[k])
+        ctx.respond_inspiring(shard, rgsw, W_SEED, mode=O.MODE_CRT_FIXED, pack=pack, y_body=y_body)
+        done += 1
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt
+
+
+def reference_arm(args):
+    """The crate's Respond path restated on the host cores: respond_seeded_inspiring
+    exactly as respond.rs:391-398 runs it, including PackParams::new (brute-force
+    automorphism tables) and OfflinePackingKeys::generate per query."""
+    from oracle import oracle as O
+
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    ctx = O.Ctx()
+    pack_tmp = O.Pack(ctx, GAMMA, W_SEED, mode=O.MODE_COMPAT)
+    pool = make_query_pool(ctx, pack_tmp, 8, 7)
+    client, locals_, seeds, brows, y_body = pool
+    rng = np.random.default_rng(1)
+    shard_db = rng.integers(0, 256, size=N * ENTRY, dtype=np.uint8)
+    shard = ctx.encode_shard(shard_db, ENTRY, 0)
+    times = []
+    for step in range(args.warmup + args.steps):
+        k = step % len(locals_)
+        t0 = time.perf_counter()
+        rgsw = ctx.expand_rgsw(seeds[k], brows[k])
+        ctx.respond_inspiring(shard, rgsw, W_SEED, mode=O.MODE_COMPAT, pack=None, y_body=y_body)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    qps = len(times) / total
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64 modular integer",
+        "data": "synthetic",
+        "config": {"workload": "InsPIRe^2 respond, d=2048 CRT [268369921,249561089], p=2^16, 32-B entries, "
+                               "one seeded query per step (the crate answers one query per call)",
+                   "mode": "compat (the crate's own semantics)"},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
+                         "sample": f"{len(times)} queries, one per step, PackParams::new + OfflinePackingKeys "
+                                   "rebuilt per query as respond.rs:360-361 do"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--log2-entries", type=int, default=LOG2_ENTRIES)
+    ap.add_argument("--mode", default="crt_fixed", choices=["crt_fixed", "compat"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    import build_lib
+
+    if rank == 0:
+        build_lib.build()
+    if ws > 1:
+        torch.distributed.barrier()
+
+    import inspire
+    from oracle import oracle as O
+
+    B = args.batch
+    n_entries = 1 << args.log2_entries
+    nshards = n_entries // N
+    # each rank holds its own partition of n_entries entries (weak scaling)
+    rng = np.random.default_rng(1 + rank)
+    db_raw = rng.integers(0, 256, size=n_entries * ENTRY, dtype=np.uint8)
+    crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, GAMMA, mode=args.mode, device=local)
+    t0 = time.perf_counter()
+    edb = inspire.EncodedDatabase(crs, db_raw, ENTRY)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+
+    ctx = O.Ctx()
+    omode = O.MODE_CRT_FIXED if args.mode == "crt_fixed" else O.MODE_COMPAT
+    pack = O.Pack(ctx, GAMMA, W_SEED, mode=omode)
+    pool = make_query_pool(ctx, pack, 32, 3 + rank)
+    client, locals_, seeds, brows, y_body = pool
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+
+    steps_total = args.warmup + args.steps
+    qrng = np.random.default_rng(5 + rank)
+    pool_idx = qrng.integers(0, len(locals_), size=(steps_total, B))
+    shard_ids = qrng.integers(0, nshards, size=(steps_total, B)).astype(np.uint32)
+
+    # device-resident inputs for every step (rows ELL..2ELL-1 only)
+    d_seeds = torch.from_numpy(np.ascontiguousarray(seeds[pool_idx][:, :, 3:6, :])).to(dev)
+    d_brows = torch.from_numpy(np.ascontiguousarray(brows[pool_idx][:, :, 3:6, :]).view(np.int64)).to(dev)
+    d_shard = torch.from_numpy(shard_ids.view(np.int32)).to(dev)
+    d_client = torch.full((steps_total, B), cid, dtype=torch.int32, device=dev)
+    d_out = torch.zeros((steps_total, B, 2, 2 * N), dtype=torch.int64, device=dev)
+    d_status = torch.zeros((steps_total, B), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def launch(s, n=B):
+        inspire.respond_seeded_batch_device(crs, edb, n, d_shard[s].data_ptr(), d_seeds[s].data_ptr(),
+                                            d_brows[s].data_ptr(), d_client[s].data_ptr(), d_out[s].data_ptr(),
+                                            d_status[s].data_ptr(), sp)
+
+    for s in range(args.warmup):
+        launch(s)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)  # evict the previous step's shards from L2 (untimed)
+            evs[k][0].record(stream)
+            launch(args.warmup + k)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    if ws > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    kern_s = sum(step_ms) / 1e3
+    if ws > 1:
+        t = torch.tensor([kern_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        kern_s = float(t.item())
+    value = ws * B * args.steps / kern_s
+
+    # correctness of what was timed: status and client-side extraction on samples
+    status = d_status[args.warmup:].cpu().numpy()
+    assert not status.any(), "respond kernel reported a nonzero status"
+    outs = d_out[-1].cpu().numpy().view(np.uint64)
+    for j in range(0, B, max(1, B // 8)):
+        s = steps_total - 1
+        gi = int(shard_ids[s, j]) * N + int(locals_[pool_idx[s, j]])
+        got = client.extract_inspiring(outs[j], ENTRY)
+        if args.mode == "crt_fixed":
+            assert np.array_equal(got, db_raw[gi * ENTRY:(gi + 1) * ENTRY]), "timed response failed to decrypt"
+
+    # batch-size sweep (single query = the plain GPU path)
+    sweep = {}
+    for bs in (1, 8, 32, 128):
+        if bs > B:
+            continue
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 20 if bs < 32 else 5
+        e0.record(stream)
+        for r in range(reps):
+            launch(args.warmup + (r % args.steps), bs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sweep[str(bs)] = bs * reps / (e0.elapsed_time(e1) / 1e3)
+
+    # end to end through the host-buffer C ABI call, pinned host memory
+    h_seeds = torch.empty((B, 6, 32), dtype=torch.uint8, pin_memory=True)
+    h_brows = torch.empty((B, 6, 2 * N), dtype=torch.int64, pin_memory=True)
+    h_out = torch.empty((B, 2, 2 * N), dtype=torch.int64, pin_memory=True)
+    hs, hb, ho = h_seeds.numpy(), h_brows.numpy().view(np.uint64), h_out.numpy().view(np.uint64)
+    e2e_times = []
+    for k in range(args.warmup + args.steps):
+        s = k % steps_total
+        hs[:] = seeds[pool_idx[s]]
+        hb[:] = brows[pool_idx[s]]
+        t0 = time.perf_counter()
+        _respond_into(crs, edb, shard_ids[s], hs, hb, np.full(B, cid, np.int32), ho)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            e2e_times.append(dt)
+    e2e_s = sum(e2e_times)
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = ws * B * args.steps / e2e_s
+    h2d = B * (4 + 4 + 32 * 3 + 3 * 2 * N * 8)
+    d2h = B * (2 * 2 * N * 8 + 4)
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    mean_kernel_s = kern_s / args.steps
+    achieved_gbs = ALG_BYTES_PER_QUERY * B / mean_kernel_s / 1e9
+    resident_bytes = edb.device_bytes
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline and ws == 1:
+            qps, nq, dt = cpu_baseline(ctx, pack, db_raw, pool)
+            cpu = {"value": qps, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"{nq} queries in {dt:.1f} s (oracle C restatement, PackParams/OfflinePackingKeys "
+                             f"hoisted, OpenMP over 16 columns)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * kern_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 modular integer (exact)", "data": "synthetic",
+            "config": {"workload": f"batched InsPIRe^2 respond: 2^{args.log2_entries} entries x 32 B resident "
+                                   f"({nshards} shards), B={B} seeded queries per launch, uniform shard ids",
+                       "mode": args.mode, "global_batch": B * ws, "ring_dim": N,
+                       "crt_moduli": [268369921, 249561089], "p": 65536,
+                       "l2": "flushed between timed steps (256 MiB write); resident DB 6.5 GiB > L2",
+                       "db_setup_s": setup_s, "db_device_bytes": resident_bytes},
+            "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved_gbs / hbm_peak, "traffic": None,
+                         "note": "algorithmic bytes 192 KiB/query; the kernel is integer-issue bound, see DESIGN.md"},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps,
+            "batch_sweep_qps": sweep,
+            "plain_single_query_qps": sweep.get("1"),
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _respond_into(crs, edb, shard_ids, seeds, brows, client_ids, out):
+    """inspire_respond_seeded_batch into a caller-owned (pinned) output."""
+    import ctypes as C
+
+    from inspire.pir import _check
+
+    sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+    cids = np.ascontiguousarray(client_ids, dtype=np.int32)
+    v = C.c_void_p
+    _check(crs.L.inspire_respond_seeded_batch(crs.h, edb.h, len(sid), sid.ctypes.data_as(v), seeds.ctypes.data_as(v),
+                                              brows.ctypes.data_as(v), cids.ctypes.data_as(v), out.ctypes.data_as(v)))
+
+
+if __name__ == "__main__":
+    main()

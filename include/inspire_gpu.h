@@ -1,0 +1,180 @@
+/*
+ * inspire_gpu.h -- C ABI of the GB300-native InsPIRe server Respond path.
+ *
+ * This is the drop-in boundary for the Respond path of the Rust crate
+ * igor53627/inspire-rs v0.1.2: every entry point below replaces one public
+ * item of that crate (cited per declaration as crate-relative file:line), so a
+ * thin `-sys` binding can route the crate's API onto the GPU.  Plain pointers
+ * and sizes only; no C++ or torch types cross this boundary.
+ *
+ * Conventions
+ *  - A polynomial is `crt_count * ring_dim` u64 values, residue-major
+ *    ([residues mod q0..., residues mod q1...]), each canonical (< its modulus):
+ *    the layout of the crate's `Poly::coeffs` (src/math/poly.rs:64-77).
+ *  - Functions return INSPIRE_OK (0) or a positive inspire_status; the text of
+ *    the last error of the calling thread is inspire_last_error().  Texts of
+ *    the errors the crate reports follow its `PirError` messages
+ *    (src/pir/respond.rs:82, 141-143, 299, 367-369).
+ *  - `*_device` functions take device pointers and a cudaStream_t (as void*)
+ *    and are asynchronous; all other functions take host pointers and return
+ *    when the result is in host memory.
+ *  - One context owns one GPU.  Host-pointer calls on one context are
+ *    serialised internally; they may be made from several threads.
+ */
+#ifndef INSPIRE_GPU_H
+#define INSPIRE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  INSPIRE_OK = 0,
+  INSPIRE_ERR_INVALID_ARGUMENT = 1,
+  INSPIRE_ERR_SHARD_NOT_FOUND = 2,  /* "Shard {id} not found" (respond.rs:301-305) */
+  INSPIRE_ERR_KEYS_MISSING = 3,     /* "InspiRING client packing keys missing from query" (respond.rs:296-299) */
+  INSPIRE_ERR_KEYS_INVALID = 4,     /* "InspiRING packing keys invalid: y_all and y_body are both empty" (respond.rs:365-370) */
+  INSPIRE_ERR_UNSUPPORTED = 5,      /* parameters outside the GPU path */
+  INSPIRE_ERR_CUDA = 6,
+  INSPIRE_ERR_OUT_OF_MEMORY = 7,
+  INSPIRE_ERR_NO_CRS = 8,
+  INSPIRE_ERR_DEVICE_STATUS = 9     /* a kernel reported a failed bounded loop or a bad index */
+} inspire_status;
+
+/* NTT-domain automorphism semantics of InspiRING packing
+ * (src/inspiring/inspiring2.rs:279-296).  COMPAT is the crate's behaviour,
+ * bit for bit: only the residue-0 slice is permuted and residue 1 is rebuilt
+ * from it.  With two CRT moduli those responses do not decrypt.  CRT_FIXED
+ * permutes every residue; its responses decrypt. */
+typedef enum { INSPIRE_MODE_COMPAT = 0, INSPIRE_MODE_CRT_FIXED = 1 } inspire_mode;
+
+/* InspireParams (src/params.rs:135-185).  The GPU path requires
+ * ring_dim = 2048, two CRT primes < 2^30 with q_i = 1 mod 4096 and q0 < 2 q1,
+ * gadget_base = 2^20 and gadget_len = 3 (secure_128_d2048, params.rs:213-230;
+ * p may be 65537 or 2^16). */
+typedef struct {
+  uint32_t ring_dim;
+  uint32_t crt_count;
+  uint64_t crt_moduli[2];
+  uint64_t p;
+  double sigma;
+  uint64_t gadget_base;
+  uint32_t gadget_len;
+} inspire_params;
+
+typedef struct inspire_ctx inspire_ctx;
+typedef struct inspire_db inspire_db;
+
+/* Text of the calling thread's last error ("" if none). */
+const char *inspire_last_error(void);
+/* Library version string. */
+const char *inspire_version(void);
+
+/* InspireParams::secure_128_d2048 with p = 2^16 (params.rs:213-230). */
+void inspire_params_default(inspire_params *out);
+
+/* Create a context on CUDA device `device`: validates parameters
+ * (InspireParams::validate, params.rs:348-387), builds NTT twiddles and
+ * constants (NttContext::with_moduli, src/math/ntt.rs:116-164) in HBM. */
+int inspire_ctx_create(const inspire_params *params, int device, int mode, inspire_ctx **out);
+void inspire_ctx_destroy(inspire_ctx *ctx);
+
+/* Load the InspiRING part of ServerCrs (src/pir/setup.rs:52-87): the shared
+ * seed `inspiring_w_seed` and `inspiring_num_columns` (gamma).  Builds the
+ * rotated w_mask table of OfflinePackingKeys::generate
+ * (src/inspiring/inspiring2.rs:448-506) once; the crate rebuilds it and
+ * PackParams::new on every query (respond.rs:360-361).  gamma must be a power
+ * of two <= 16 on the GPU path. */
+int inspire_crs_load(inspire_ctx *ctx, const uint8_t w_seed[32], uint32_t num_columns);
+
+/* Encode a raw database resident in HBM: encode_database
+ * (src/pir/encode_db.rs:106-164) with shards of ring_dim entries
+ * (setup.rs:149-153), plus the per-shard contracted form the Respond kernel
+ * reads.  `raw` holds n_entries * entry_size bytes (host memory).
+ * ceil(entry_size / 2) must equal the CRS num_columns. */
+int inspire_db_create(inspire_ctx *ctx, const uint8_t *raw, uint64_t n_entries, uint32_t entry_size,
+                      inspire_db **out);
+void inspire_db_destroy(inspire_db *db);
+uint32_t inspire_db_num_shards(const inspire_db *db);
+/* Device bytes held by the database. */
+uint64_t inspire_db_device_bytes(const inspire_db *db);
+
+/* Register per-client packing keys (ClientPackingKeys,
+ * src/inspiring/inspiring2.rs:604-628) resident in HBM.  Give y_body
+ * (gadget_len polys; the server derives y_all with generate_rotations,
+ * inspiring2.rs:1309-1323, as respond.rs:365-377 does for wire queries) or
+ * y_all ((num_columns-1) * gadget_len polys, the in-process form).  y_all
+ * takes precedence.  Both NULL -> INSPIRE_ERR_KEYS_INVALID. */
+int inspire_client_register(inspire_ctx *ctx, const uint64_t *y_body, const uint64_t *y_all,
+                            int32_t *client_id);
+int inspire_client_release(inspire_ctx *ctx, int32_t client_id);
+
+/* SeededClientQuery (src/pir/query.rs:138-150) with its RGSW rows flattened:
+ * seeds = 2*gadget_len seeds of 32 bytes, b_rows = 2*gadget_len polys. */
+typedef struct {
+  uint32_t shard_id;
+  const uint8_t *seeds;
+  const uint64_t *b_rows;
+  /* inspiring_packing_keys: has_packing_keys = 0 is Option::None. */
+  int32_t has_packing_keys;
+  const uint64_t *y_body; /* gadget_len polys or NULL */
+  const uint64_t *y_all;  /* (num_columns-1)*gadget_len polys or NULL */
+} inspire_seeded_query;
+
+/* ClientQuery (query.rs:119-132): rgsw = 2*gadget_len rows of (a, b) polys. */
+typedef struct {
+  uint32_t shard_id;
+  const uint64_t *rgsw;
+  int32_t has_packing_keys;
+  const uint64_t *y_body;
+  const uint64_t *y_all;
+} inspire_query;
+
+/* respond_seeded_inspiring (src/pir/respond.rs:391-398): out_ct receives
+ * ServerResponse.ciphertext as [a poly, b poly] (column_ciphertexts is empty
+ * for InspiRING, respond.rs:382-385). */
+int inspire_respond_seeded_inspiring(inspire_ctx *ctx, const inspire_db *db, const inspire_seeded_query *query,
+                                     uint64_t *out_ct);
+
+/* respond_inspiring (src/pir/respond.rs:284-386). */
+int inspire_respond_inspiring(inspire_ctx *ctx, const inspire_db *db, const inspire_query *query,
+                              uint64_t *out_ct);
+
+/* Batched respond_seeded_inspiring over n queries with registered client
+ * keys, host buffers: shard_ids[n], seeds[n][2*gadget_len][32],
+ * b_rows[n][2*gadget_len][poly], client_ids[n], out_ct[n][2][poly].  Queries
+ * may name different shards.  Each result is the one respond_seeded_inspiring
+ * returns for that query alone. */
+int inspire_respond_seeded_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n, const uint32_t *shard_ids,
+                                 const uint8_t *seeds, const uint64_t *b_rows, const int32_t *client_ids,
+                                 uint64_t *out_ct);
+
+/* Same on device buffers, asynchronous on `stream`.  seeds holds only rows
+ * gadget_len..2*gadget_len-1 ([n][gadget_len][32]) and b_rows only those rows
+ * ([n][gadget_len][poly]); d_status[n] receives 0 or a nonzero kernel status
+ * (unknown shard or client id, exhausted expansion bound). */
+int inspire_respond_seeded_batch_device(inspire_ctx *ctx, const inspire_db *db, uint32_t n,
+                                        const uint32_t *d_shard_ids, const uint8_t *d_seeds,
+                                        const uint64_t *d_b_rows, const int32_t *d_client_ids, uint64_t *d_out_ct,
+                                        int32_t *d_status, void *stream);
+
+/* Batched NttContext::forward / inverse (src/math/ntt.rs:223-325) on device
+ * data polys[npolys][2][ring_dim] (u32 residues), in place.  Forward outputs
+ * the crate's NTT-domain values (Montgomery form, R = 2^64, bit-reversed slot
+ * order); inverse takes them and returns coefficients. */
+int inspire_ntt_forward_device(inspire_ctx *ctx, uint32_t *d_polys, uint32_t npolys, void *stream);
+int inspire_ntt_inverse_device(inspire_ctx *ctx, uint32_t *d_polys, uint32_t npolys, void *stream);
+
+/* Batched external_product (src/rgsw/external_product.rs:88-150) on device
+ * data: ct[n][2][2][ring_dim], rgsw[n][2*gadget_len][2][2][ring_dim],
+ * out[n][2][2][ring_dim] (u32 residues). */
+int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, const uint32_t *d_rgsw,
+                                    uint32_t *d_out, uint32_t npairs, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

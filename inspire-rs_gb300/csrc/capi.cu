@@ -1,0 +1,714 @@
+// capi.cu -- host side of the C ABI declared in include/inspire_gpu.h.
+//
+// Builds the per-context constants (the reference NttContext's psi and
+// twiddles, CRT and Montgomery factors), owns the resident device objects
+// (database, CRS key table, client key tables) and stages batched queries.
+// Nothing here computes a response: every Respond result comes from the
+// kernels in respond.cu.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "inspire_gpu.h"
+#include "kernels.h"
+
+using u128 = unsigned __int128;
+using namespace ig;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess)                                                                \
+      return fail(_e == cudaErrorMemoryAllocation ? INSPIRE_ERR_OUT_OF_MEMORY : INSPIRE_ERR_CUDA, \
+                  std::string(#expr) + ": " + cudaGetErrorString(_e));                   \
+  } while (0)
+
+uint64_t powmod(uint64_t b, uint64_t e, uint64_t m) {
+  uint64_t r = 1;
+  b %= m;
+  while (e) {
+    if (e & 1) r = (uint64_t)((u128)r * b % m);
+    b = (uint64_t)((u128)b * b % m);
+    e >>= 1;
+  }
+  return r;
+}
+
+uint64_t inv_prime(uint64_t a, uint64_t q) { return powmod(a % q, q - 2, q); }
+
+uint32_t shoup(uint64_t w, uint64_t q) { return (uint32_t)(((u128)w << 32) / q); }
+
+uint32_t brv(uint32_t x, int bits) {
+  uint32_t r = 0;
+  for (int i = 0; i < bits; i++) r |= ((x >> i) & 1u) << (bits - 1 - i);
+  return r;
+}
+
+bool is_prime(uint64_t q) {
+  if (q < 2) return false;
+  for (uint64_t d = 2; d * d <= q; d++)
+    if (q % d == 0) return false;
+  return true;
+}
+
+// NttContext::find_primitive_root (src/math/ntt.rs:525-538)
+uint64_t find_psi(uint64_t two_n, uint64_t q) {
+  const uint64_t e = (q - 1) / two_n;
+  for (uint64_t g = 2; g < q; g++) {
+    uint64_t c = powmod(g, e, q);
+    if (powmod(c, two_n, q) == 1 && powmod(c, two_n / 2, q) != 1) return c;
+  }
+  return 0;
+}
+
+struct DevMem {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevMem() = default;
+  DevMem(const DevMem&) = delete;
+  DevMem& operator=(const DevMem&) = delete;
+  ~DevMem() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// ChaCha20Rng::from_seed + next_u64 for generate_mask_from_seed
+// (src/inspiring/inspiring2.rs:816-835), host side.
+struct HostChaCha {
+  uint32_t key[8];
+  uint64_t ctr = 0;
+  uint32_t buf[16];
+  int idx = 16;
+  explicit HostChaCha(const uint8_t seed[32]) {
+    for (int i = 0; i < 8; i++)
+      key[i] = (uint32_t)seed[4 * i] | ((uint32_t)seed[4 * i + 1] << 8) | ((uint32_t)seed[4 * i + 2] << 16) |
+               ((uint32_t)seed[4 * i + 3] << 24);
+  }
+  static uint32_t rotl(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+  void block() {
+    uint32_t s[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u};
+    for (int i = 0; i < 8; i++) s[4 + i] = key[i];
+    s[12] = (uint32_t)ctr;
+    s[13] = (uint32_t)(ctr >> 32);
+    s[14] = s[15] = 0;
+    uint32_t x[16];
+    memcpy(x, s, sizeof x);
+    auto qr = [](uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d) {
+      a += b; d ^= a; d = rotl(d, 16);
+      c += d; b ^= c; b = rotl(b, 12);
+      a += b; d ^= a; d = rotl(d, 8);
+      c += d; b ^= c; b = rotl(b, 7);
+    };
+    for (int i = 0; i < 10; i++) {
+      qr(x[0], x[4], x[8], x[12]);
+      qr(x[1], x[5], x[9], x[13]);
+      qr(x[2], x[6], x[10], x[14]);
+      qr(x[3], x[7], x[11], x[15]);
+      qr(x[0], x[5], x[10], x[15]);
+      qr(x[1], x[6], x[11], x[12]);
+      qr(x[2], x[7], x[8], x[13]);
+      qr(x[3], x[4], x[9], x[14]);
+    }
+    for (int i = 0; i < 16; i++) buf[i] = x[i] + s[i];
+    ctr++;
+    idx = 0;
+  }
+  uint32_t next_u32() {
+    if (idx >= 16) block();
+    return buf[idx++];
+  }
+  uint64_t next_u64() {
+    uint64_t lo = next_u32();
+    uint64_t hi = next_u32();
+    return lo | (hi << 32);
+  }
+};
+
+}  // namespace
+
+struct inspire_ctx {
+  std::mutex mu;
+  int device = 0;
+  int mode = 0;
+  inspire_params params{};
+  uint64_t q = 0;  // composite modulus
+  DevParams P{};
+  DevMem tables;
+  // CRS
+  bool has_crs = false;
+  int gamma = 0;
+  uint8_t w_seed[32] = {};
+  DevMem what;
+  // clients
+  std::vector<DevMem*> clients;
+  std::vector<const uint32_t*> client_ptrs;
+  DevMem client_table;  // device copy of client_ptrs
+  bool client_table_dirty = true;
+  // staging for host-buffer calls
+  cudaStream_t stream = nullptr;
+  DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_status, d_keys;
+  std::vector<int32_t> h_status;
+
+  ~inspire_ctx() {
+    for (DevMem* m : clients) delete m;
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct inspire_db {
+  inspire_ctx* ctx = nullptr;
+  int gamma = 0;
+  uint64_t n_entries = 0;
+  uint32_t entry_size = 0;
+  int nshards = 0;
+  DevMem H, E;
+};
+
+namespace {
+
+size_t poly_words() { return (size_t)2 * N; }
+
+int sync_client_table(inspire_ctx* c) {
+  if (!c->client_table_dirty) return INSPIRE_OK;
+  const size_t bytes = sizeof(uint32_t*) * (c->client_ptrs.size() + 1);
+  CUDA_TRY(c->client_table.ensure(bytes));
+  if (!c->client_ptrs.empty())
+    CUDA_TRY(cudaMemcpy(c->client_table.p, c->client_ptrs.data(), sizeof(uint32_t*) * c->client_ptrs.size(),
+                        cudaMemcpyHostToDevice));
+  c->client_table_dirty = false;
+  return INSPIRE_OK;
+}
+
+int set_device(inspire_ctx* c) {
+  CUDA_TRY(cudaSetDevice(c->device));
+  return INSPIRE_OK;
+}
+
+int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all, int32_t* id) {
+  if (!y_body && !y_all)
+    return fail(INSPIRE_ERR_KEYS_INVALID, "InspiRING packing keys invalid: y_all and y_body are both empty");
+  const int gamma = c->gamma;
+  const size_t tbl_words = (size_t)std::max(1, (gamma - 1) * ELL) * poly_words();
+  DevMem* m = new DevMem();
+  cudaError_t e = m->ensure(tbl_words * sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    delete m;
+    return fail(INSPIRE_ERR_OUT_OF_MEMORY, "client key table allocation failed");
+  }
+  const size_t in_polys = y_all ? (size_t)(gamma - 1) * ELL : ELL;
+  if (gamma > 1) {
+    CUDA_TRY(c->d_keys.ensure(in_polys * poly_words() * sizeof(uint64_t)));
+    CUDA_TRY(cudaMemcpyAsync(c->d_keys.p, y_all ? y_all : y_body, in_polys * poly_words() * sizeof(uint64_t),
+                             cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(y_all ? launch_client_from_yall(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream)
+                   : launch_client_from_ybody(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  int slot = -1;
+  for (size_t i = 0; i < c->clients.size(); i++)
+    if (!c->clients[i]) {
+      slot = (int)i;
+      break;
+    }
+  if (slot < 0) {
+    slot = (int)c->clients.size();
+    c->clients.push_back(nullptr);
+    c->client_ptrs.push_back(nullptr);
+  }
+  c->clients[slot] = m;
+  c->client_ptrs[slot] = m->as<uint32_t>();
+  c->client_table_dirty = true;
+  *id = slot;
+  return INSPIRE_OK;
+}
+
+void release_keys(inspire_ctx* c, int32_t id) {
+  if (id < 0 || (size_t)id >= c->clients.size() || !c->clients[id]) return;
+  delete c->clients[id];
+  c->clients[id] = nullptr;
+  c->client_ptrs[id] = nullptr;
+  c->client_table_dirty = true;
+}
+
+// Stage n queries (rows ELL..2ELL-1 only) and run the Respond kernel.
+// seeds/b_rows/a_rows use the full 2*ELL-row host layout.
+// a_rows/b_rows point at the first needed poly of query 0 (ELL contiguous
+// polys per query, query pitch `stride_polys`); seeds at the first needed seed
+// (ELL contiguous seeds, query pitch `seed_stride` bytes).
+int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
+              size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
+              const int32_t* client_ids, uint64_t* out_ct) {
+  if (n == 0) return INSPIRE_OK;
+  const size_t pw = poly_words();
+  CUDA_TRY(c->d_shard.ensure(sizeof(uint32_t) * n));
+  CUDA_TRY(c->d_client.ensure(sizeof(int32_t) * n));
+  CUDA_TRY(c->d_brows.ensure(sizeof(uint64_t) * n * ELL * pw));
+  CUDA_TRY(c->d_out.ensure(sizeof(uint64_t) * n * 2 * pw));
+  CUDA_TRY(c->d_status.ensure(sizeof(int32_t) * n));
+  CUDA_TRY(cudaMemcpyAsync(c->d_shard.p, shard_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(c->d_client.p, client_ids, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
+  // b rows ELL..2ELL-1 of each query: one strided copy
+  CUDA_TRY(cudaMemcpy2DAsync(c->d_brows.p, sizeof(uint64_t) * ELL * pw, b_rows, sizeof(uint64_t) * stride_polys * pw,
+                             sizeof(uint64_t) * ELL * pw, n, cudaMemcpyHostToDevice, c->stream));
+  const bool seeded = seeds != nullptr;
+  if (seeded) {
+    CUDA_TRY(c->d_seeds.ensure((size_t)32 * ELL * n));
+    CUDA_TRY(cudaMemcpy2DAsync(c->d_seeds.p, (size_t)32 * ELL, seeds, seed_stride, (size_t)32 * ELL, n,
+                               cudaMemcpyHostToDevice, c->stream));
+  } else {
+    CUDA_TRY(c->d_arows.ensure(sizeof(uint64_t) * n * ELL * pw));
+    CUDA_TRY(cudaMemcpy2DAsync(c->d_arows.p, sizeof(uint64_t) * ELL * pw, a_rows, sizeof(uint64_t) * stride_polys * pw,
+                               sizeof(uint64_t) * ELL * pw, n, cudaMemcpyHostToDevice, c->stream));
+  }
+  int rc = sync_client_table(c);
+  if (rc) return rc;
+  RespondArgs a{};
+  a.P = c->P;
+  a.nq = (int)n;
+  a.shard = c->d_shard.as<uint32_t>();
+  a.seeds = seeded ? c->d_seeds.as<uint8_t>() : nullptr;
+  a.arows = seeded ? nullptr : c->d_arows.as<uint64_t>();
+  a.brows = c->d_brows.as<uint64_t>();
+  a.client = c->d_client.as<int32_t>();
+  a.yhat_table = c->client_table.as<const uint32_t*>();
+  a.nclients = (int)c->client_ptrs.size();
+  a.nshards = db->nshards;
+  a.E = db->E.as<uint32_t>();
+  a.H = db->H.as<uint16_t>();
+  a.what = c->what.as<uint32_t>();
+  a.out = c->d_out.as<uint64_t>();
+  a.status = c->d_status.as<int>();
+  CUDA_TRY(launch_respond(a, seeded, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(out_ct, c->d_out.p, sizeof(uint64_t) * n * 2 * pw, cudaMemcpyDeviceToHost, c->stream));
+  c->h_status.resize(n);
+  CUDA_TRY(cudaMemcpyAsync(c->h_status.data(), c->d_status.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                           c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (uint32_t i = 0; i < n; i++)
+    if (c->h_status[i] != 0)
+      return fail(INSPIRE_ERR_DEVICE_STATUS,
+                  "respond kernel status " + std::to_string(c->h_status[i]) + " for query " + std::to_string(i));
+  return INSPIRE_OK;
+}
+
+// Validation order of respond_inspiring (src/pir/respond.rs:295-305, 365-370).
+int single_query(inspire_ctx* c, const inspire_db* db, uint32_t shard_id, const uint8_t* seeds,
+                 const uint64_t* rgsw_full, const uint64_t* b_rows, int32_t has_keys, const uint64_t* y_body,
+                 const uint64_t* y_all, uint64_t* out_ct) {
+  if (!c || !db || !out_ct) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (!has_keys) return fail(INSPIRE_ERR_KEYS_MISSING, "InspiRING client packing keys missing from query");
+  if (shard_id >= (uint32_t)db->nshards)
+    return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(shard_id) + " not found");
+  if (!y_all && !y_body)
+    return fail(INSPIRE_ERR_KEYS_INVALID, "InspiRING packing keys invalid: y_all and y_body are both empty");
+  int32_t id = -1;
+  int rc = register_keys(c, y_body, y_all, &id);
+  if (rc) return rc;
+  if (seeds) {
+    rc = run_batch(c, db, 1, &shard_id, seeds + 32 * ELL, (size_t)64 * ELL, nullptr, b_rows + (size_t)ELL * poly_words(),
+                   2 * ELL, &id, out_ct);
+  } else {
+    // rgsw_full holds 2*ELL rows of (a, b): row r's a is poly 2r, its b poly 2r+1
+    const size_t pw = poly_words();
+    std::vector<uint64_t> ar((size_t)ELL * pw), br((size_t)ELL * pw);
+    for (int t = 0; t < ELL; t++) {
+      memcpy(ar.data() + t * pw, rgsw_full + (size_t)(2 * (ELL + t)) * pw, pw * sizeof(uint64_t));
+      memcpy(br.data() + t * pw, rgsw_full + (size_t)(2 * (ELL + t) + 1) * pw, pw * sizeof(uint64_t));
+    }
+    rc = run_batch(c, db, 1, &shard_id, nullptr, 0, ar.data(), br.data(), ELL, &id, out_ct);
+  }
+  release_keys(c, id);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* inspire_last_error(void) { return g_last_error.c_str(); }
+
+const char* inspire_version(void) { return "inspire-gb300 0.1.0 (sm_103a)"; }
+
+void inspire_params_default(inspire_params* out) {
+  if (!out) return;
+  memset(out, 0, sizeof(*out));
+  out->ring_dim = 2048;
+  out->crt_count = 2;
+  out->crt_moduli[0] = 268369921ULL;
+  out->crt_moduli[1] = 249561089ULL;
+  out->p = 1ULL << 16;
+  out->sigma = 6.4;
+  out->gadget_base = 1ULL << 20;
+  out->gadget_len = 3;
+}
+
+int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_ctx** out) {
+  if (!prm || !out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (mode != INSPIRE_MODE_COMPAT && mode != INSPIRE_MODE_CRT_FIXED)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "mode must be INSPIRE_MODE_COMPAT or INSPIRE_MODE_CRT_FIXED");
+  // InspireParams::validate (params.rs:348-387) + the GPU path's envelope
+  if (prm->ring_dim == 0 || (prm->ring_dim & (prm->ring_dim - 1)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ring_dim must be a power of two");
+  if (prm->crt_count != 2 || prm->ring_dim != (uint32_t)N || prm->gadget_base != (1ULL << ZBITS) ||
+      prm->gadget_len != (uint32_t)ELL)
+    return fail(INSPIRE_ERR_UNSUPPORTED,
+                "GPU path supports ring_dim=2048, two CRT moduli, gadget_base=2^20, gadget_len=3");
+  const uint64_t q0 = prm->crt_moduli[0], q1 = prm->crt_moduli[1];
+  for (uint64_t qm : {q0, q1}) {
+    if (qm % (2 * N) != 1) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "CRT moduli must be = 1 (mod 2d) for NTT");
+    if (qm >= (1ULL << 30) || qm <= (1ULL << ZBITS) || !is_prime(qm))
+      return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path needs prime CRT moduli in (2^20, 2^30)");
+  }
+  if (q0 == q1) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "CRT moduli must be coprime");
+  if (q0 >= 2 * q1) return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path needs q0 < 2 q1");
+  const uint64_t q = q0 * q1;
+  if (q < prm->p || prm->p < 2) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "q must be >= p");
+  // ceil(log2(q)/20) must be the gadget length (params.rs:224)
+  if (q >= (1ULL << (ZBITS * ELL)) || q < (1ULL << (ZBITS * (ELL - 1))))
+    return fail(INSPIRE_ERR_UNSUPPORTED, "gadget_len 3 does not cover q");
+
+  inspire_ctx* c = new inspire_ctx();
+  c->device = device;
+  c->mode = mode;
+  c->params = *prm;
+  c->q = q;
+  if (int rc = set_device(c)) {
+    delete c;
+    return rc;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(INSPIRE_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  // tables per residue: fwd_w, fwd_wp, inv_w, inv_wp (N each), psi_pow (2N)
+  const size_t per = 6 * (size_t)N;
+  std::vector<uint32_t> host(2 * per);
+  DevParams& P = c->P;
+  memset(&P, 0, sizeof(P));
+  for (int r = 0; r < 2; r++) {
+    const uint64_t qm = prm->crt_moduli[r];
+    uint32_t* t = host.data() + r * per;
+    const uint64_t psi = find_psi(2 * N, qm), psi_inv = inv_prime(psi, qm);
+    for (int k = 1; k < N; k++) {
+      const uint64_t w = powmod(psi, brv(k, LOGN), qm), wi = powmod(psi_inv, brv(k, LOGN), qm);
+      t[k] = (uint32_t)w;
+      t[N + k] = shoup(w, qm);
+      t[2 * N + k] = (uint32_t)wi;
+      t[3 * N + k] = shoup(wi, qm);
+    }
+    uint64_t pw = 1;
+    for (int k = 0; k < 2 * N; k++) {
+      t[4 * N + k] = (uint32_t)pw;
+      pw = (uint64_t)((u128)pw * psi % qm);
+    }
+    ResidueConsts& C = P.r[r];
+    C.q = (uint32_t)qm;
+    uint32_t inv = (uint32_t)qm;  // Newton: q^-1 mod 2^32
+    for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)qm * inv;
+    C.qinv = 0u - inv;
+    const uint64_t r64 = (uint64_t)(((u128)1 << 64) % qm);
+    const uint64_t r32 = (1ULL << 32) % qm;
+    const uint64_t ninv = inv_prime(N, qm), r64inv = inv_prime(r64, qm);
+    C.r64 = (uint32_t)r64;
+    C.r64_p = shoup(r64, qm);
+    const uint64_t ris = (uint64_t)((u128)ninv * r64inv % qm);
+    C.ref_inv_scale = (uint32_t)ris;
+    C.ref_inv_scale_p = shoup(ris, qm);
+    const uint64_t nm = (uint64_t)((u128)ninv * r32 % qm);
+    C.ninv_mont = (uint32_t)nm;
+    C.ninv_mont_p = shoup(nm, qm);
+    C.mont = (uint32_t)r32;
+    C.mont_p = shoup(r32, qm);
+    int lz = __builtin_clzll(qm);
+    C.zone = (qm << lz) - 1;
+  }
+  P.q0inv_q1 = (uint32_t)inv_prime(q0, q1);
+  P.q0inv_q1_p = shoup(P.q0inv_q1, q1);
+  {
+    const uint64_t r64_0 = (uint64_t)(((u128)1 << 64) % q0), r64_1 = (uint64_t)(((u128)1 << 64) % q1);
+    const uint64_t a = (uint64_t)((u128)N * r64_0 % q0);
+    const uint64_t b = (uint64_t)((u128)inv_prime(r64_1, q1) * inv_prime(N, q1) % q1);
+    P.conv_a = (uint32_t)a;
+    P.conv_a_p = shoup(a, q0);
+    P.conv_b = (uint32_t)b;
+    P.conv_b_p = shoup(b, q1);
+    P.conv0_a = (uint32_t)r64_0;
+    P.conv0_a_p = shoup(r64_0, q0);
+    const uint64_t b0 = inv_prime(r64_1, q1);
+    P.conv0_b = (uint32_t)b0;
+    P.conv0_b_p = shoup(b0, q1);
+  }
+  P.delta = q / prm->p;
+  P.mode = mode;
+  e = c->tables.ensure(host.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpy(c->tables.p, host.data(), host.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(INSPIRE_ERR_CUDA, std::string("table upload: ") + cudaGetErrorString(e));
+  }
+  for (int r = 0; r < 2; r++) {
+    const uint32_t* base = c->tables.as<uint32_t>() + r * per;
+    P.r[r].fwd_w = base;
+    P.r[r].fwd_wp = base + N;
+    P.r[r].inv_w = base + 2 * N;
+    P.r[r].inv_wp = base + 3 * N;
+    P.r[r].psi_pow = base + 4 * N;
+  }
+  *out = c;
+  return INSPIRE_OK;
+}
+
+void inspire_ctx_destroy(inspire_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  delete c;
+}
+
+int inspire_crs_load(inspire_ctx* c, const uint8_t w_seed[32], uint32_t num_columns) {
+  if (!c || !w_seed) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (int rc = set_device(c)) return rc;
+  if (num_columns == 0 || num_columns > (uint32_t)MAX_GAMMA || (num_columns & (num_columns - 1)))
+    return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path supports num_columns in {1, 2, 4, 8, 16}");
+  const int gamma = (int)num_columns;
+  c->gamma = gamma;
+  memcpy(c->w_seed, w_seed, 32);
+  c->P.gamma = gamma;
+  for (int r = 0; r < 2; r++) {
+    const uint64_t qm = c->params.crt_moduli[r];
+    const uint64_t r96 = (uint64_t)(((u128)1 << 96) % qm);
+    const uint64_t k = (uint64_t)((u128)((u128)inv_prime(gamma, qm) * inv_prime(N, qm) % qm) * r96 % qm);
+    c->P.r[r].e_scale = (uint32_t)k;
+    c->P.r[r].e_scale_p = shoup(k, qm);
+  }
+  // w_mask = generate_mask_from_seed(w_seed) (inspiring2.rs:816-835): next_u64 % q, CRT split
+  std::vector<uint32_t> wm((size_t)ELL * 2 * N);
+  HostChaCha rng(w_seed);
+  for (int k = 0; k < ELL; k++)
+    for (int i = 0; i < N; i++) {
+      const uint64_t v = rng.next_u64() % c->q;
+      wm[((size_t)k * 2 + 0) * N + i] = (uint32_t)(v % c->params.crt_moduli[0]);
+      wm[((size_t)k * 2 + 1) * N + i] = (uint32_t)(v % c->params.crt_moduli[1]);
+    }
+  DevMem dwm;
+  CUDA_TRY(dwm.ensure(wm.size() * sizeof(uint32_t)));
+  CUDA_TRY(cudaMemcpy(dwm.p, wm.data(), wm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(c->what.ensure(sizeof(uint32_t) * (size_t)std::max(1, (gamma - 1) * ELL) * 2 * N));
+  CUDA_TRY(launch_crs_what(c->P, dwm.as<uint32_t>(), c->what.as<uint32_t>(), c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // key tables of registered clients were built for the previous gamma
+  for (size_t i = 0; i < c->clients.size(); i++) release_keys(c, (int32_t)i);
+  c->has_crs = true;
+  return INSPIRE_OK;
+}
+
+int inspire_db_create(inspire_ctx* c, const uint8_t* raw, uint64_t n_entries, uint32_t entry_size,
+                      inspire_db** out) {
+  if (!c || !out || (!raw && n_entries && entry_size)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  *out = nullptr;
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (int rc = set_device(c)) return rc;
+  inspire_db* db = new inspire_db();
+  db->ctx = c;
+  db->n_entries = n_entries;
+  db->entry_size = entry_size;
+  // encode_database returns no shard for an empty database (encode_db.rs:112-114)
+  const uint64_t nshards64 = (entry_size == 0 || n_entries == 0) ? 0 : (n_entries + N - 1) / N;
+  if (nshards64 > 0x7fffffffULL) {
+    delete db;
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "too many shards");
+  }
+  db->nshards = (int)nshards64;
+  const int gamma = entry_size ? (int)((entry_size * 8 + 15) / 16) : c->gamma;
+  if (db->nshards > 0 && gamma != c->gamma) {
+    delete db;
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ceil(entry_size/2) must equal the CRS num_columns");
+  }
+  db->gamma = c->gamma;
+  if (db->nshards > 0) {
+    const size_t hbytes = sizeof(uint16_t) * (size_t)db->nshards * gamma * N;
+    const size_t ebytes = sizeof(uint32_t) * (size_t)db->nshards * 2 * ELL * gamma * N;
+    cudaError_t e = db->H.ensure(hbytes);
+    if (e == cudaSuccess) e = db->E.ensure(ebytes);
+    if (e != cudaSuccess) {
+      delete db;
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, "database allocation failed");
+    }
+    // raw bytes in chunks of whole shards
+    const uint64_t shards_per_chunk = std::max<uint64_t>(1, (256ULL << 20) / ((uint64_t)N * entry_size));
+    DevMem stage;
+    for (uint64_t s0 = 0; s0 < (uint64_t)db->nshards; s0 += shards_per_chunk) {
+      const uint64_t s1 = std::min<uint64_t>(db->nshards, s0 + shards_per_chunk);
+      const uint64_t e0 = s0 * N, e1 = std::min<uint64_t>(n_entries, s1 * N);
+      const size_t bytes = (size_t)(e1 - e0) * entry_size;
+      cudaError_t ce = stage.ensure(std::max<size_t>(bytes, 1));
+      if (ce == cudaSuccess) ce = cudaMemcpy(stage.p, raw + e0 * entry_size, bytes, cudaMemcpyHostToDevice);
+      if (ce == cudaSuccess)
+        ce = launch_columns_from_raw(stage.as<uint8_t>(), e1 - e0, (int)entry_size, gamma, (int)(s1 - s0),
+                                     db->H.as<uint16_t>() + s0 * gamma * N, c->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+      if (ce != cudaSuccess) {
+        delete db;
+        return fail(INSPIRE_ERR_CUDA, std::string("database upload: ") + cudaGetErrorString(ce));
+      }
+    }
+    cudaError_t ce = launch_encode_E(c->P, db->H.as<uint16_t>(), db->nshards, db->E.as<uint32_t>(), c->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+    if (ce != cudaSuccess) {
+      delete db;
+      return fail(INSPIRE_ERR_CUDA, std::string("database encode: ") + cudaGetErrorString(ce));
+    }
+  }
+  *out = db;
+  return INSPIRE_OK;
+}
+
+void inspire_db_destroy(inspire_db* db) {
+  if (!db) return;
+  cudaSetDevice(db->ctx->device);
+  delete db;
+}
+
+uint32_t inspire_db_num_shards(const inspire_db* db) { return db ? (uint32_t)db->nshards : 0; }
+
+uint64_t inspire_db_device_bytes(const inspire_db* db) { return db ? (uint64_t)(db->H.bytes + db->E.bytes) : 0; }
+
+int inspire_client_register(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all, int32_t* id) {
+  if (!c || !id) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (int rc = set_device(c)) return rc;
+  return register_keys(c, y_body, y_all, id);
+}
+
+int inspire_client_release(inspire_ctx* c, int32_t id) {
+  if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (id < 0 || (size_t)id >= c->clients.size() || !c->clients[id])
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "unknown client id");
+  if (int rc = set_device(c)) return rc;
+  release_keys(c, id);
+  return INSPIRE_OK;
+}
+
+int inspire_respond_seeded_inspiring(inspire_ctx* c, const inspire_db* db, const inspire_seeded_query* qy,
+                                     uint64_t* out_ct) {
+  if (!c || !qy) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!qy->seeds || !qy->b_rows) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null query rows");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (int rc = set_device(c)) return rc;
+  return single_query(c, db, qy->shard_id, qy->seeds, nullptr, qy->b_rows, qy->has_packing_keys, qy->y_body,
+                      qy->y_all, out_ct);
+}
+
+int inspire_respond_inspiring(inspire_ctx* c, const inspire_db* db, const inspire_query* qy, uint64_t* out_ct) {
+  if (!c || !qy) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!qy->rgsw) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null query rows");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (int rc = set_device(c)) return rc;
+  return single_query(c, db, qy->shard_id, nullptr, qy->rgsw, nullptr, qy->has_packing_keys, qy->y_body,
+                      qy->y_all, out_ct);
+}
+
+int inspire_respond_seeded_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,
+                                 const uint8_t* seeds, const uint64_t* b_rows, const int32_t* client_ids,
+                                 uint64_t* out_ct) {
+  if (!c || !db || (n && (!shard_ids || !seeds || !b_rows || !client_ids || !out_ct)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (int rc = set_device(c)) return rc;
+  for (uint32_t i = 0; i < n; i++) {
+    if (shard_ids[i] >= (uint32_t)db->nshards)
+      return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(shard_ids[i]) + " not found");
+    const int32_t id = client_ids[i];
+    if (id < 0 || (size_t)id >= c->clients.size() || !c->clients[id])
+      return fail(INSPIRE_ERR_KEYS_MISSING, "InspiRING client packing keys missing from query");
+  }
+  return run_batch(c, db, n, shard_ids, seeds + 32 * ELL, (size_t)64 * ELL, nullptr, b_rows + (size_t)ELL * poly_words(),
+                   2 * ELL, client_ids, out_ct);
+}
+
+int inspire_respond_seeded_batch_device(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* d_shard_ids,
+                                        const uint8_t* d_seeds, const uint64_t* d_b_rows, const int32_t* d_client_ids,
+                                        uint64_t* d_out_ct, int32_t* d_status, void* stream) {
+  if (!c || !db || (n && (!d_shard_ids || !d_seeds || !d_b_rows || !d_client_ids || !d_out_ct || !d_status)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (int rc = set_device(c)) return rc;
+  if (int rc = sync_client_table(c)) return rc;
+  RespondArgs a{};
+  a.P = c->P;
+  a.nq = (int)n;
+  a.shard = d_shard_ids;
+  a.seeds = d_seeds;
+  a.arows = nullptr;
+  a.brows = d_b_rows;
+  a.client = d_client_ids;
+  a.yhat_table = c->client_table.as<const uint32_t*>();
+  a.nclients = (int)c->client_ptrs.size();
+  a.nshards = db->nshards;
+  a.E = db->E.as<uint32_t>();
+  a.H = db->H.as<uint16_t>();
+  a.what = c->what.as<uint32_t>();
+  a.out = d_out_ct;
+  a.status = d_status;
+  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_ntt_forward_device(inspire_ctx* c, uint32_t* d_polys, uint32_t npolys, void* stream) {
+  if (!c || (npolys && !d_polys)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (int rc = set_device(c)) return rc;
+  CUDA_TRY(launch_ntt_ref(c->P, d_polys, (int)npolys, false, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_ntt_inverse_device(inspire_ctx* c, uint32_t* d_polys, uint32_t npolys, void* stream) {
+  if (!c || (npolys && !d_polys)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (int rc = set_device(c)) return rc;
+  CUDA_TRY(launch_ntt_ref(c->P, d_polys, (int)npolys, true, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_external_product_device(inspire_ctx* c, const uint32_t* d_ct, const uint32_t* d_rgsw, uint32_t* d_out,
+                                    uint32_t npairs, void* stream) {
+  if (!c || (npairs && (!d_ct || !d_rgsw || !d_out))) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (int rc = set_device(c)) return rc;
+  CUDA_TRY(launch_external_product(c->P, d_ct, d_rgsw, d_out, (int)npairs, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+}  // extern "C"

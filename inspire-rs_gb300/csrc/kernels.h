@@ -1,0 +1,52 @@
+// kernels.h -- launch interfaces of the InsPIRe GB300 kernels (internal).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace ig {
+
+constexpr int ERR_EXPAND = 1;  // seeded expansion exceeded its iteration bound
+constexpr int ERR_INDEX = 2;   // shard or client id out of range
+
+struct RespondArgs {
+  DevParams P;
+  int nq;
+  const uint32_t* shard;         // [nq] shard index (validated by the host)
+  const uint8_t* seeds;          // [nq][ELL][32]   seeds of RGSW rows ELL..2ELL-1
+  const uint64_t* arows;         // [nq][ELL][2][N] a-polys of rows ELL..2ELL-1 (unseeded queries) or null
+  const uint64_t* brows;         // [nq][ELL][2][N] b-polys of rows ELL..2ELL-1
+  const int32_t* client;         // [nq] client id
+  const uint32_t* const* yhat_table;  // [nclients] -> key table [(gamma-1)][ELL][2][N]
+  int nclients, nshards;
+  const uint32_t* E;             // [nshards][2][ELL][gamma][N] contracted database
+  const uint16_t* H;             // [nshards][gamma][N] raw 16-bit columns
+  const uint32_t* what;          // [(gamma-1)][ELL][2][N] rotated w_mask (CRS)
+  uint64_t* out;                 // [nq][2][2][N] response (a_hat, b) residues
+  int* status;                   // [nq]
+};
+
+size_t respond_smem_bytes(int mode);
+cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st);
+
+// setup-time kernels
+cudaError_t launch_columns_from_raw(const uint8_t* raw, uint64_t n_entries, int entry_size,
+                                    int gamma, int nshards, uint16_t* H, cudaStream_t st);
+cudaError_t launch_encode_E(const DevParams& P, const uint16_t* H, int nshards, uint32_t* E,
+                            cudaStream_t st);
+cudaError_t launch_crs_what(const DevParams& P, const uint32_t* wmask, uint32_t* what,
+                            cudaStream_t st);
+cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat,
+                                     cudaStream_t st);
+cudaError_t launch_client_from_yall(const DevParams& P, const uint64_t* yall, uint32_t* yhat,
+                                    cudaStream_t st);
+
+// kernel-level operations
+cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool inverse,
+                           cudaStream_t st);
+cudaError_t launch_external_product(const DevParams& P, const uint32_t* ct, const uint32_t* rgsw,
+                                    uint32_t* out, int npairs, cudaStream_t st);
+
+}  // namespace ig

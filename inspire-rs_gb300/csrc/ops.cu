@@ -1,0 +1,116 @@
+// ops.cu -- kernel-level operations with the reference's own data semantics:
+// batched NttContext::forward / inverse (src/math/ntt.rs:223-325, NTT-domain
+// values in Montgomery form with R = 2^64) and the general RLWE x RGSW external
+// product (src/rgsw/external_product.rs:88-150).
+#include "kernels.h"
+
+namespace ig {
+
+namespace {
+
+// One polynomial (both residues) per CTA; group g transforms residue g.
+// Layout: polys[p][r][N] u32.  Forward: coefficients -> reference NTT slots
+// (times 2^64).  Inverse: reference NTT slots -> coefficients.
+template <bool INVERSE>
+__global__ void __launch_bounds__(BLOCK) ntt_ref_kernel(const DevParams P, uint32_t* __restrict__ polys) {
+  __shared__ uint32_t SC[2][NTT_SCRATCH];
+  const int p = blockIdx.x, tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const ResidueConsts& C = P.r[g];
+  const uint32_t q = C.q;
+  uint32_t* a = polys + ((size_t)p * 2 + g) * N;
+  uint32_t v[16];
+  if (!INVERSE) {
+#pragma unroll
+    for (int r = 0; r < 16; r++) v[r] = mul_shoup(a[x + 128 * r], C.r64, C.r64_p, q);
+    ntt_fwd(v, SC[g], fwd_tw(C), q, x, 1 + g);
+    uint4* d = reinterpret_cast<uint4*>(a + 16 * x);
+#pragma unroll
+    for (int r = 0; r < 4; r++) d[r] = make_uint4(v[4 * r], v[4 * r + 1], v[4 * r + 2], v[4 * r + 3]);
+  } else {
+    const uint4* s = reinterpret_cast<const uint4*>(a + 16 * x);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      uint4 t = s[r];
+      v[4 * r] = t.x; v[4 * r + 1] = t.y; v[4 * r + 2] = t.z; v[4 * r + 3] = t.w;
+    }
+    ntt_inv_noscale(v, SC[g], inv_tw(C), q, x, 1 + g);
+#pragma unroll
+    for (int r = 0; r < 16; r++) a[x + 128 * r] = mul_shoup(v[r], C.ref_inv_scale, C.ref_inv_scale_p, q);
+  }
+}
+
+// external_product(rlwe, rgsw): result = sum_i g^-1(a)_i * C[i] + g^-1(b)_i * C[ELL+i].
+// ct[p][2 (a,b)][2][N]; rgsw[p][2*ELL rows][2 (a,b)][2][N]; out[p][2][2][N].
+__global__ void __launch_bounds__(BLOCK) external_product_kernel(const DevParams P, const uint32_t* __restrict__ ct,
+                                                                 const uint32_t* __restrict__ rgsw,
+                                                                 uint32_t* __restrict__ out) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint32_t* dig = smem;                   // [2*ELL][N]: digits of a (rows 0..ELL-1), of b (ELL..)
+  uint32_t* SC = dig + 2 * ELL * N;       // [2][NTT_SCRATCH]
+  const int p = blockIdx.x, tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const uint32_t* c = ct + (size_t)p * 4 * N;
+  for (int j = tid; j < 2 * N; j += BLOCK) {
+    const int part = j >> LOGN, jj = j & (N - 1);
+    const uint64_t v = crt_compose(P, c[(part * 2 + 0) * N + jj], c[(part * 2 + 1) * N + jj]);
+#pragma unroll
+    for (int i = 0; i < ELL; i++) dig[(part * ELL + i) * N + jj] = (uint32_t)(v >> (ZBITS * i)) & ((1u << ZBITS) - 1);
+  }
+  __syncthreads();
+  const ResidueConsts& C = P.r[g];
+  const uint32_t q = C.q, qinv = C.qinv, q2 = 2 * q;
+  uint32_t accA[16], accB[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) accA[r] = accB[r] = 0;
+  const uint32_t* rows = rgsw + (size_t)p * 2 * ELL * 4 * N;
+  for (int d = 0; d < 2 * ELL; d++) {
+    uint32_t dh[16], v[16];
+#pragma unroll
+    for (int r = 0; r < 16; r++) dh[r] = dig[d * N + x + 128 * r];
+    ntt_fwd(dh, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+    // row d: (a, b) of residue g
+    for (int part = 0; part < 2; part++) {
+      const uint32_t* rp = rows + ((size_t)(d * 2 + part) * 2 + g) * N;
+#pragma unroll
+      for (int r = 0; r < 16; r++) v[r] = rp[x + 128 * r];
+      ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+#pragma unroll
+      for (int r = 0; r < 16; r++) {
+        const uint32_t pr = redc_lazy((uint64_t)dh[r] * v[r], q, qinv);
+        if (part == 0) accA[r] = acc_2q(accA[r], pr, q2);
+        else accB[r] = acc_2q(accB[r], pr, q2);
+      }
+    }
+  }
+  uint32_t* o = out + (size_t)p * 4 * N;
+#pragma unroll
+  for (int r = 0; r < 16; r++) accA[r] = reduce_2q(accA[r], q);
+  ntt_inv_noscale(accA, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);
+#pragma unroll
+  for (int r = 0; r < 16; r++) o[(0 * 2 + g) * N + x + 128 * r] = mul_shoup(accA[r], C.ninv_mont, C.ninv_mont_p, q);
+#pragma unroll
+  for (int r = 0; r < 16; r++) accB[r] = reduce_2q(accB[r], q);
+  ntt_inv_noscale(accB, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);
+#pragma unroll
+  for (int r = 0; r < 16; r++) o[(1 * 2 + g) * N + x + 128 * r] = mul_shoup(accB[r], C.ninv_mont, C.ninv_mont_p, q);
+}
+
+}  // namespace
+
+cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool inverse, cudaStream_t st) {
+  if (npolys <= 0) return cudaSuccess;
+  if (inverse) ntt_ref_kernel<true><<<npolys, BLOCK, 0, st>>>(P, polys);
+  else ntt_ref_kernel<false><<<npolys, BLOCK, 0, st>>>(P, polys);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_external_product(const DevParams& P, const uint32_t* ct, const uint32_t* rgsw, uint32_t* out,
+                                    int npairs, cudaStream_t st) {
+  if (npairs <= 0) return cudaSuccess;
+  const size_t smem = sizeof(uint32_t) * ((size_t)2 * ELL * N + 2 * NTT_SCRATCH);
+  cudaError_t e = cudaFuncSetAttribute(external_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  external_product_kernel<<<npairs, BLOCK, smem, st>>>(P, ct, rgsw, out);
+  return cudaGetLastError();
+}
+
+}  // namespace ig

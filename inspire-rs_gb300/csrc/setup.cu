@@ -1,0 +1,203 @@
+// setup.cu -- setup-time GPU kernels: resident database, CRS key table and
+// per-client key tables.  All outputs stay in HBM for the lifetime of their
+// handles; Respond then reads them without further preprocessing.
+#include "kernels.h"
+
+namespace ig {
+
+namespace {
+
+// encode_database (src/pir/encode_db.rs:106-181): shard s holds entries
+// [s*N, s*N + N); column c, coefficient i = little-endian u16 of bytes
+// (2c, 2c+1) of that entry (a lone trailing byte is the value itself).
+__global__ void columns_from_raw_kernel(const uint8_t* __restrict__ raw, uint64_t n_entries,
+                                        int entry_size, int gamma, int nshards,
+                                        uint16_t* __restrict__ H) {
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t total = (uint64_t)nshards * N;
+  if (idx >= total) return;
+  const uint64_t s = idx >> LOGN, i = idx & (N - 1);
+  const uint64_t e = idx;  // global entry index = s * N + i
+  for (int c = 0; c < gamma; c++) {
+    uint16_t v = 0;
+    if (e < n_entries) {
+      const uint8_t* ent = raw + e * (uint64_t)entry_size;
+      const int bo = 2 * c;
+      if (bo + 1 < entry_size) v = (uint16_t)(ent[bo] | (ent[bo + 1] << 8));
+      else if (bo < entry_size) v = ent[bo];
+    }
+    H[(s * gamma + c) * N + i] = v;
+  }
+}
+
+// E[s][r][t][k][u] = K * sum_j zeta^(k j) * omega_u^j * NTT(d_t(Delta h_j))[u]
+// with omega_u = psi^(2brv(u)+1), zeta = psi^(2n/gamma), K = gamma^-1 n^-1
+// 2^32 (Montgomery form, n^-1 pre-applied for the unscaled inverse NTTs of
+// the Respond kernel).  Grid: (shard, residue, digit t).
+__global__ void __launch_bounds__(BLOCK) encode_E_kernel(const DevParams P, const uint16_t* __restrict__ H,
+                                                         uint32_t* __restrict__ E) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  const int gamma = P.gamma;
+  uint32_t* Dh = smem;                  // [gamma][N]
+  uint32_t* SC = Dh + gamma * N;        // [2][NTT_SCRATCH]
+  uint32_t* zp = SC + 2 * NTT_SCRATCH;  // [gamma] powers of zeta
+  const int s = blockIdx.x, r = blockIdx.y, t = blockIdx.z;
+  const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const ResidueConsts& C = P.r[r];
+  const uint32_t q = C.q, qinv = C.qinv;
+  if (tid < gamma) zp[tid] = C.psi_pow[((2 * N / gamma) * tid) & (2 * N - 1)];
+  for (int j = g; j < gamma; j += 2) {
+    const uint16_t* h = H + ((size_t)s * gamma + j) * N;
+    uint32_t v[16];
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++) {
+      const uint64_t xv = P.delta * (uint64_t)h[x + 128 * rr];
+      v[rr] = (uint32_t)(xv >> (ZBITS * t)) & ((1u << ZBITS) - 1);  // digit t < 2^20 < q
+    }
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+    uint4* dst = reinterpret_cast<uint4*>(Dh + j * N + 16 * x);
+#pragma unroll
+    for (int rr = 0; rr < 4; rr++) dst[rr] = make_uint4(v[4 * rr], v[4 * rr + 1], v[4 * rr + 2], v[4 * rr + 3]);
+  }
+  __syncthreads();
+  uint32_t* Eo = E + ((((size_t)s * 2 + r) * ELL + t) * gamma) * N;
+  for (int v = 0; v < N / BLOCK; v++) {
+    const int u = tid + BLOCK * v;
+    const uint32_t e = 2 * brv11(u) + 1;
+    uint32_t c[MAX_GAMMA];
+#pragma unroll
+    for (int j = 0; j < MAX_GAMMA; j++)
+      if (j < gamma) c[j] = mont_mul(Dh[j * N + u], __ldg(C.psi_pow + ((e * j) & (2 * N - 1))), q, qinv);
+    for (int k = 0; k < gamma; k++) {
+      uint64_t T = 0;
+#pragma unroll
+      for (int j = 0; j < MAX_GAMMA; j++)
+        if (j < gamma) T += (uint64_t)zp[(k * j) & (gamma - 1)] * c[j];
+      // the two REDCs divided by 2^64; e_scale = gamma^-1 n^-1 2^96 leaves
+      // the factor 2^32 gamma^-1 n^-1
+      Eo[(size_t)k * N + u] = mul_shoup(redc(T, q, qinv), C.e_scale, C.e_scale_p, q);
+    }
+  }
+}
+
+// OfflinePackingKeys::generate (inspiring2.rs:448-506): w_all_ntt[i][k] =
+// NTT-domain automorphism tau_{g^i} of NTT(w_mask[k]) for i < gamma-1, with the
+// reference's residue-1 behaviour in compat mode.  Stored times n^-1 2^32.
+__global__ void __launch_bounds__(BLOCK) crs_what_kernel(const DevParams P, const uint32_t* __restrict__ wmask,
+                                                         uint32_t* __restrict__ what) {
+  __shared__ __align__(16) uint32_t W[2][N];
+  __shared__ uint32_t SC[2][NTT_SCRATCH];
+  const int k = blockIdx.x, tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const int gamma = P.gamma;
+  {
+    const ResidueConsts& C = P.r[g];
+    uint32_t v[16];
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++) v[rr] = wmask[((size_t)k * 2 + g) * N + x + 128 * rr];
+    ntt_fwd(v, SC[g], fwd_tw(C), C.q, x, 1 + g);
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++) W[g][16 * x + rr] = v[rr];
+  }
+  __syncthreads();
+  for (int i = 0; i + 1 < gamma; i++) {
+    const uint32_t tg = gen_pow(gamma, i);
+    for (int v = 0; v < N / BLOCK; v++) {
+      const int s = tid + BLOCK * v;
+      const uint32_t es = 2 * brv11(s) + 1;
+      const int u = brv11(((tg * es) & (2 * N - 1)) >> 1);  // table_{g^i}[s]
+      uint32_t v0 = W[0][u];
+      uint32_t v1 = P.mode == MODE_COMPAT ? compat_residue1(P, v0) : W[1][u];
+      v0 = mul_shoup(v0, P.r[0].ninv_mont, P.r[0].ninv_mont_p, P.r[0].q);
+      v1 = mul_shoup(v1, P.r[1].ninv_mont, P.r[1].ninv_mont_p, P.r[1].q);
+      what[(((size_t)i * ELL + k) * 2 + 0) * N + s] = v0;
+      what[(((size_t)i * ELL + k) * 2 + 1) * N + s] = v1;
+    }
+  }
+}
+
+// Client key table from y_body: generate_rotations (inspiring2.rs:1309-1323)
+// followed by the forward NTT of packing_online (:1199-1213).  tau in the
+// coefficient domain is the slot permutation in the NTT domain on both
+// residues.  Stored times n^-1 2^32.
+__global__ void __launch_bounds__(BLOCK) client_ybody_kernel(const DevParams P, const uint64_t* __restrict__ yb,
+                                                             uint32_t* __restrict__ yhat) {
+  __shared__ __align__(16) uint32_t W[2][N];
+  __shared__ uint32_t SC[2][NTT_SCRATCH];
+  const int k = blockIdx.x, tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const int gamma = P.gamma;
+  const ResidueConsts& C = P.r[g];
+  {
+    uint32_t v[16];
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++) v[rr] = (uint32_t)yb[((size_t)k * 2 + g) * N + x + 128 * rr];
+    ntt_fwd(v, SC[g], fwd_tw(C), C.q, x, 1 + g);
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++) W[g][16 * x + rr] = mul_shoup(v[rr], C.ninv_mont, C.ninv_mont_p, C.q);
+  }
+  __syncthreads();
+  for (int i = 0; i + 1 < gamma; i++) {
+    const uint32_t tg = gen_pow(gamma, i);
+    for (int v = 0; v < N / BLOCK; v++) {
+      const int s = tid + BLOCK * v;
+      const uint32_t es = 2 * brv11(s) + 1;
+      const int u = brv11(((tg * es) & (2 * N - 1)) >> 1);
+      yhat[(((size_t)i * ELL + k) * 2 + 0) * N + s] = W[0][u];
+      yhat[(((size_t)i * ELL + k) * 2 + 1) * N + s] = W[1][u];
+    }
+  }
+}
+
+// Client key table from an explicit y_all ((gamma-1)*ELL coefficient polys).
+__global__ void __launch_bounds__(BLOCK) client_yall_kernel(const DevParams P, const uint64_t* __restrict__ ya,
+                                                            uint32_t* __restrict__ yhat) {
+  __shared__ uint32_t SC[2][NTT_SCRATCH];
+  const int p = blockIdx.x, tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const ResidueConsts& C = P.r[g];
+  uint32_t v[16];
+#pragma unroll
+  for (int rr = 0; rr < 16; rr++) v[rr] = (uint32_t)ya[((size_t)p * 2 + g) * N + x + 128 * rr];
+  ntt_fwd(v, SC[g], fwd_tw(C), C.q, x, 1 + g);
+#pragma unroll
+  for (int rr = 0; rr < 16; rr++)
+    yhat[((size_t)p * 2 + g) * N + 16 * x + rr] = mul_shoup(v[rr], C.ninv_mont, C.ninv_mont_p, C.q);
+}
+
+}  // namespace
+
+cudaError_t launch_columns_from_raw(const uint8_t* raw, uint64_t n_entries, int entry_size, int gamma,
+                                    int nshards, uint16_t* H, cudaStream_t st) {
+  const uint64_t total = (uint64_t)nshards * N;
+  const unsigned blocks = (unsigned)((total + 255) / 256);
+  if (blocks) columns_from_raw_kernel<<<blocks, 256, 0, st>>>(raw, n_entries, entry_size, gamma, nshards, H);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_encode_E(const DevParams& P, const uint16_t* H, int nshards, uint32_t* E, cudaStream_t st) {
+  if (nshards <= 0) return cudaSuccess;
+  const size_t smem = sizeof(uint32_t) * ((size_t)P.gamma * N + 2 * NTT_SCRATCH + MAX_GAMMA);
+  cudaError_t e = cudaFuncSetAttribute(encode_E_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  // grid.x is limited to 2^31-1 shards; y = residue, z = digit
+  encode_E_kernel<<<dim3(nshards, 2, ELL), BLOCK, smem, st>>>(P, H, E);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_crs_what(const DevParams& P, const uint32_t* wmask, uint32_t* what, cudaStream_t st) {
+  if (P.gamma < 2) return cudaSuccess;
+  crs_what_kernel<<<ELL, BLOCK, 0, st>>>(P, wmask, what);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat, cudaStream_t st) {
+  if (P.gamma < 2) return cudaSuccess;
+  client_ybody_kernel<<<ELL, BLOCK, 0, st>>>(P, ybody, yhat);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_client_from_yall(const DevParams& P, const uint64_t* yall, uint32_t* yhat, cudaStream_t st) {
+  if (P.gamma < 2) return cudaSuccess;
+  client_yall_kernel<<<(P.gamma - 1) * ELL, BLOCK, 0, st>>>(P, yall, yhat);
+  return cudaGetLastError();
+}
+
+}  // namespace ig

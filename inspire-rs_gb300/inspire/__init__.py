@@ -1,0 +1,24 @@
+"""GB300-native InsPIRe server Respond path (drop-in for igor53627/inspire-rs).
+
+The package mirrors the crate's Respond API (`inspire::pir`) over the C ABI of
+include/inspire_gpu.h; all arithmetic runs in the CUDA kernels of csrc/.
+"""
+from .params import InspireParams, InspireVariant, num_columns  # noqa: F401
+from .pir import (  # noqa: F401
+    ClientPackingKeys,
+    ClientQuery,
+    EncodedDatabase,
+    PirError,
+    RlweCiphertext,
+    SeededClientQuery,
+    ServerCrs,
+    ServerResponse,
+    external_product_device,
+    ntt_forward_device,
+    ntt_inverse_device,
+    respond_inspiring,
+    respond_seeded_batch,
+    respond_seeded_batch_device,
+    respond_seeded_inspiring,
+    respond_seeded_with_variant,
+)

@@ -1,0 +1,115 @@
+"""ctypes binding of libinspire_gpu.so (the C ABI in include/inspire_gpu.h).
+
+The library is built in-tree by inspire-rs_gb300/build_lib.py.  There is no
+CPU implementation behind this module: if the library is missing or cannot be
+loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libinspire_gpu.so")
+HEADER = os.path.join(os.path.dirname(PKG_ROOT), "include", "inspire_gpu.h")
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_SHARD_NOT_FOUND = 2
+ERR_KEYS_MISSING = 3
+ERR_KEYS_INVALID = 4
+ERR_UNSUPPORTED = 5
+ERR_CUDA = 6
+ERR_OUT_OF_MEMORY = 7
+ERR_NO_CRS = 8
+ERR_DEVICE_STATUS = 9
+
+MODE_COMPAT = 0
+MODE_CRT_FIXED = 1
+
+
+class InspireParamsC(C.Structure):
+    _fields_ = [
+        ("ring_dim", C.c_uint32),
+        ("crt_count", C.c_uint32),
+        ("crt_moduli", C.c_uint64 * 2),
+        ("p", C.c_uint64),
+        ("sigma", C.c_double),
+        ("gadget_base", C.c_uint64),
+        ("gadget_len", C.c_uint32),
+    ]
+
+
+class SeededQueryC(C.Structure):
+    _fields_ = [
+        ("shard_id", C.c_uint32),
+        ("seeds", C.c_void_p),
+        ("b_rows", C.c_void_p),
+        ("has_packing_keys", C.c_int32),
+        ("y_body", C.c_void_p),
+        ("y_all", C.c_void_p),
+    ]
+
+
+class QueryC(C.Structure):
+    _fields_ = [
+        ("shard_id", C.c_uint32),
+        ("rgsw", C.c_void_p),
+        ("has_packing_keys", C.c_int32),
+        ("y_body", C.c_void_p),
+        ("y_all", C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the native library (raises OSError if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"libinspire_gpu.so not built: {path} (run inspire-rs_gb300/build_lib.py)")
+    L = C.CDLL(path)
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32
+    sig = {
+        "inspire_last_error": (C.c_char_p, []),
+        "inspire_version": (C.c_char_p, []),
+        "inspire_params_default": (None, [C.POINTER(InspireParamsC)]),
+        "inspire_ctx_create": (C.c_int, [C.POINTER(InspireParamsC), C.c_int, C.c_int, C.POINTER(vp)]),
+        "inspire_ctx_destroy": (None, [vp]),
+        "inspire_crs_load": (C.c_int, [vp, vp, u32]),
+        "inspire_db_create": (C.c_int, [vp, vp, u64, u32, C.POINTER(vp)]),
+        "inspire_db_destroy": (None, [vp]),
+        "inspire_db_num_shards": (u32, [vp]),
+        "inspire_db_device_bytes": (u64, [vp]),
+        "inspire_client_register": (C.c_int, [vp, vp, vp, C.POINTER(i32)]),
+        "inspire_client_release": (C.c_int, [vp, i32]),
+        "inspire_respond_seeded_inspiring": (C.c_int, [vp, vp, C.POINTER(SeededQueryC), vp]),
+        "inspire_respond_inspiring": (C.c_int, [vp, vp, C.POINTER(QueryC), vp]),
+        "inspire_respond_seeded_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp]),
+        "inspire_respond_seeded_batch_device": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp]),
+        "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),
+        "inspire_ntt_inverse_device": (C.c_int, [vp, vp, u32, vp]),
+        "inspire_external_product_device": (C.c_int, [vp, vp, vp, vp, u32, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().inspire_last_error().decode()
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Names of the functions declared in include/inspire_gpu.h."""
+    import re
+
+    text = open(header).read()
+    return sorted(set(re.findall(r"\b(inspire_[a-z0-9_]+)\s*\(", text)))

@@ -1,0 +1,275 @@
+"""Server Respond API of the InsPIRe PIR protocol on one GB300.
+
+Mirrors the Respond surface of the Rust crate igor53627/inspire-rs v0.1.2
+(src/pir/mod.rs:57-71): `respond_seeded_inspiring`, `respond_inspiring`,
+`respond_seeded_with_variant`, the query/response types and `PirError`, with
+the same argument meaning and error texts.  Every call goes through the C ABI
+of include/inspire_gpu.h; responses are computed by the CUDA kernels.
+
+Polynomials are numpy uint64 arrays of shape (crt_count * ring_dim,), residue
+major, canonical: the layout of the crate's `Poly::coeffs` (poly.rs:64-77).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native as nat
+from .params import InspireParams, InspireVariant
+
+
+class PirError(Exception):
+    """PirError(String) of src/pir/error.rs:13 (plus the native status code)."""
+
+    def __init__(self, message: str, status: int = 0):
+        super().__init__(message)
+        self.status = status
+
+
+def _check(rc: int) -> None:
+    if rc != nat.OK:
+        raise PirError(nat.last_error(), rc)
+
+
+def _u64(a, shape=None) -> np.ndarray:
+    arr = np.ascontiguousarray(a, dtype=np.uint64)
+    if shape is not None and arr.shape != shape:
+        arr = arr.reshape(shape)
+    return arr
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class ClientPackingKeys:
+    """ClientPackingKeys (inspiring2.rs:604-628): y_body (gadget_len polys)
+    and/or the in-process y_all ((num_columns-1)*gadget_len polys)."""
+
+    y_body: Optional[np.ndarray] = None
+    y_all: Optional[np.ndarray] = None
+
+
+@dataclass
+class SeededClientQuery:
+    """SeededClientQuery (query.rs:138-150): seeds (2*ell, 32) uint8 and
+    b_rows (2*ell, crt*n) uint64 of the SeededRgswCiphertext."""
+
+    shard_id: int
+    seeds: np.ndarray
+    b_rows: np.ndarray
+    packing_mode: str = "inspiring"
+    inspiring_packing_keys: Optional[ClientPackingKeys] = None
+
+
+@dataclass
+class ClientQuery:
+    """ClientQuery (query.rs:119-132): rgsw = (2*ell, 2, crt*n) rows (a, b)."""
+
+    shard_id: int
+    rgsw: np.ndarray
+    packing_mode: str = "inspiring"
+    inspiring_packing_keys: Optional[ClientPackingKeys] = None
+
+
+@dataclass
+class RlweCiphertext:
+    a: np.ndarray
+    b: np.ndarray
+
+
+@dataclass
+class ServerResponse:
+    """ServerResponse (respond.rs:31-37)."""
+
+    ciphertext: RlweCiphertext
+    column_ciphertexts: list = field(default_factory=list)
+
+
+class ServerCrs:
+    """The InspiRING part of ServerCrs (setup.rs:52-87) bound to one GPU.
+
+    Holds the device context (NTT tables, constants) and the rotated w_mask
+    table built once from `inspiring_w_seed` for `inspiring_num_columns`.
+    `mode` selects the NTT-domain automorphism semantics: "compat" reproduces
+    the crate bit for bit; "crt_fixed" applies the permutation to both CRT
+    residues (the responses decrypt)."""
+
+    def __init__(self, params: InspireParams, inspiring_w_seed: bytes, inspiring_num_columns: int,
+                 mode: str = "crt_fixed", device: int = 0):
+        self.L = nat.load()
+        self.params = params
+        self.inspiring_w_seed = bytes(inspiring_w_seed)
+        self.inspiring_num_columns = int(inspiring_num_columns)
+        self.mode = mode
+        if mode not in ("compat", "crt_fixed"):
+            raise ValueError("mode must be 'compat' or 'crt_fixed'")
+        pc = params.to_c()
+        h = C.c_void_p()
+        _check(self.L.inspire_ctx_create(C.byref(pc), device, nat.MODE_COMPAT if mode == "compat" else nat.MODE_CRT_FIXED,
+                                         C.byref(h)))
+        self.h = h
+        seed = (C.c_uint8 * 32).from_buffer_copy(self.inspiring_w_seed)
+        _check(self.L.inspire_crs_load(self.h, C.cast(seed, C.c_void_p), self.inspiring_num_columns))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.inspire_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ring_dim(self) -> int:
+        return self.params.ring_dim
+
+    def modulus(self) -> int:
+        return self.params.q
+
+    # ---- client key residency (serving) ----
+    def register_client(self, keys: ClientPackingKeys) -> int:
+        yb = None if keys.y_body is None else _u64(keys.y_body)
+        ya = None if keys.y_all is None else _u64(keys.y_all)
+        cid = C.c_int32()
+        _check(self.L.inspire_client_register(self.h, _ptr(yb), _ptr(ya), C.byref(cid)))
+        return cid.value
+
+    def release_client(self, client_id: int) -> None:
+        _check(self.L.inspire_client_release(self.h, client_id))
+
+
+class EncodedDatabase:
+    """EncodedDatabase (setup.rs:104-120) resident in HBM: shards of ring_dim
+    entries, 16-bit columns (encode_db.rs:106-181), plus the contracted form
+    the Respond kernel reads."""
+
+    def __init__(self, crs: ServerCrs, database: bytes | np.ndarray, entry_size: int):
+        self.crs = crs
+        self.L = crs.L
+        raw = np.frombuffer(database, dtype=np.uint8) if isinstance(database, (bytes, bytearray)) else \
+            np.ascontiguousarray(database, dtype=np.uint8).reshape(-1)
+        self.entry_size = int(entry_size)
+        self.total_entries = raw.size // self.entry_size if self.entry_size else 0
+        h = C.c_void_p()
+        _check(self.L.inspire_db_create(crs.h, raw.ctypes.data_as(C.c_void_p), self.total_entries, self.entry_size,
+                                        C.byref(h)))
+        self.h = h
+
+    @property
+    def num_shards(self) -> int:
+        return int(self.L.inspire_db_num_shards(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.L.inspire_db_device_bytes(self.h))
+
+    def index_to_shard(self, global_idx: int):
+        """ShardConfig::index_to_shard (params.rs:553-558)."""
+        n = self.crs.params.ring_dim
+        return global_idx // n, global_idx % n
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.inspire_db_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _response(out: np.ndarray, plen: int) -> ServerResponse:
+    return ServerResponse(RlweCiphertext(out[:plen].copy(), out[plen:].copy()), [])
+
+
+def respond_seeded_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery) -> ServerResponse:
+    """respond_seeded_inspiring (respond.rs:391-398)."""
+    plen = crs.params.plen
+    ell = crs.params.gadget_len
+    seeds = np.ascontiguousarray(query.seeds, dtype=np.uint8).reshape(2 * ell, 32)
+    b_rows = _u64(query.b_rows).reshape(2 * ell, plen)
+    keys = query.inspiring_packing_keys
+    yb = None if keys is None or keys.y_body is None else _u64(keys.y_body)
+    ya = None if keys is None or keys.y_all is None else _u64(keys.y_all)
+    q = nat.SeededQueryC(query.shard_id, seeds.ctypes.data_as(C.c_void_p), b_rows.ctypes.data_as(C.c_void_p),
+                         1 if keys is not None else 0, _ptr(yb), _ptr(ya))
+    out = np.zeros(2 * plen, dtype=np.uint64)
+    _check(crs.L.inspire_respond_seeded_inspiring(crs.h, encoded_db.h, C.byref(q), _ptr(out)))
+    return _response(out, plen)
+
+
+def respond_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery) -> ServerResponse:
+    """respond_inspiring (respond.rs:284-386)."""
+    plen = crs.params.plen
+    ell = crs.params.gadget_len
+    rgsw = _u64(query.rgsw).reshape(2 * ell, 2, plen)
+    keys = query.inspiring_packing_keys
+    yb = None if keys is None or keys.y_body is None else _u64(keys.y_body)
+    ya = None if keys is None or keys.y_all is None else _u64(keys.y_all)
+    q = nat.QueryC(query.shard_id, rgsw.ctypes.data_as(C.c_void_p), 1 if keys is not None else 0, _ptr(yb), _ptr(ya))
+    out = np.zeros(2 * plen, dtype=np.uint64)
+    _check(crs.L.inspire_respond_inspiring(crs.h, encoded_db.h, C.byref(q), _ptr(out)))
+    return _response(out, plen)
+
+
+def respond_seeded_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery,
+                                variant: InspireVariant) -> ServerResponse:
+    """respond_seeded_with_variant (respond.rs:161-183): the InspiRING branch
+    runs on the GPU; NoPacking and tree packing are not part of this path."""
+    if variant == InspireVariant.NoPacking or query.packing_mode == "tree":
+        raise PirError("NoPacking / tree packing are not implemented on the GPU path", nat.ERR_UNSUPPORTED)
+    if query.inspiring_packing_keys is None:
+        raise PirError("InspiRING packing keys missing (set packing_mode=tree to use tree packing)",
+                       nat.ERR_KEYS_MISSING)
+    return respond_seeded_inspiring(crs, encoded_db, query)
+
+
+def respond_seeded_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int], seeds: np.ndarray,
+                         b_rows: np.ndarray, client_ids: Sequence[int]) -> np.ndarray:
+    """Batched respond_seeded_inspiring with registered client keys.
+
+    seeds (n, 2*ell, 32) uint8; b_rows (n, 2*ell, plen) uint64; returns
+    (n, 2, plen) uint64 = the (a, b) of each response."""
+    n = len(shard_ids)
+    plen = crs.params.plen
+    sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+    cid = np.ascontiguousarray(client_ids, dtype=np.int32)
+    sd = np.ascontiguousarray(seeds, dtype=np.uint8)
+    br = _u64(b_rows)
+    out = np.zeros((n, 2, plen), dtype=np.uint64)
+    _check(crs.L.inspire_respond_seeded_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br), _ptr(cid),
+                                              _ptr(out)))
+    return out
+
+
+def respond_seeded_batch_device(crs: ServerCrs, encoded_db: EncodedDatabase, n: int, d_shard_ids: int, d_seeds: int,
+                                d_b_rows: int, d_client_ids: int, d_out: int, d_status: int, stream: int) -> None:
+    """Device-buffer batch (raw device pointers as ints); asynchronous."""
+    v = C.c_void_p
+    _check(crs.L.inspire_respond_seeded_batch_device(crs.h, encoded_db.h, n, v(d_shard_ids), v(d_seeds), v(d_b_rows),
+                                                     v(d_client_ids), v(d_out), v(d_status), v(stream)))
+
+
+def ntt_forward_device(crs: ServerCrs, d_polys: int, npolys: int, stream: int) -> None:
+    """Batched NttContext::forward (ntt.rs:223-246) on device u32 data."""
+    _check(crs.L.inspire_ntt_forward_device(crs.h, C.c_void_p(d_polys), npolys, C.c_void_p(stream)))
+
+
+def ntt_inverse_device(crs: ServerCrs, d_polys: int, npolys: int, stream: int) -> None:
+    """Batched NttContext::inverse (ntt.rs:308-325) on device u32 data."""
+    _check(crs.L.inspire_ntt_inverse_device(crs.h, C.c_void_p(d_polys), npolys, C.c_void_p(stream)))
+
+
+def external_product_device(crs: ServerCrs, d_ct: int, d_rgsw: int, d_out: int, npairs: int, stream: int) -> None:
+    """Batched external_product (external_product.rs:88-150) on device u32 data."""
+    _check(crs.L.inspire_external_product_device(crs.h, C.c_void_p(d_ct), C.c_void_p(d_rgsw), C.c_void_p(d_out),
+                                                 npairs, C.c_void_p(stream)))

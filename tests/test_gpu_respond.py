@@ -1,0 +1,206 @@
+"""GPU parity of the Respond path through the C ABI, bit-exact against the
+oracle restatement of respond_seeded_inspiring / respond_inspiring
+(src/pir/respond.rs:284-398), in both automorphism modes, plus the crate's
+error behaviour and end-to-end extraction (tests/e2e_pir.rs:464-535)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 2048
+ENTRY = 32
+W_SEED = bytes(range(7, 39))
+
+
+@pytest.fixture(scope="module")
+def world(oracle_mod):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import inspire
+
+    O = oracle_mod
+    rng = np.random.default_rng(2024)
+    n_entries = 2 * N + 900  # three shards, the last one partial
+    db = rng.integers(0, 256, size=n_entries * ENTRY, dtype=np.uint8)
+    ctx = O.Ctx()
+    client = O.Client(ctx, seed=0, rng_seed=17)
+    w = {}
+    for mode, omode in (("crt_fixed", O.MODE_CRT_FIXED), ("compat", O.MODE_COMPAT)):
+        crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode=mode)
+        edb = inspire.EncodedDatabase(crs, db, ENTRY)
+        pack = O.Pack(ctx, 16, W_SEED, mode=omode)
+        w[mode] = (crs, edb, pack, omode)
+    shards = [ctx.encode_shard(db, ENTRY, s) for s in range(3)]
+    return dict(O=O, inspire=inspire, ctx=ctx, client=client, db=db, w=w, shards=shards, n_entries=n_entries)
+
+
+def oracle_response(W, mode, shard_id, rgsw, y_body=None, y_all=None):
+    crs, edb, pack, omode = W["w"][mode]
+    return W["ctx"].respond_inspiring(W["shards"][shard_id], rgsw, W_SEED, mode=omode, pack=pack,
+                                      y_body=y_body, y_all=y_all)
+
+
+@pytest.mark.parametrize("mode", ["crt_fixed", "compat"])
+@pytest.mark.parametrize("index", [0, 1, 2047, 2048, 4096 + 899])
+def test_seeded_respond_bit_exact(world, mode, index):
+    W = world
+    inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
+    crs, edb, pack, omode = W["w"][mode]
+    sid, local = divmod(index, N)
+    seeds, b_rows = client.query_seeded(local)
+    y_body, _ = client.packing_keys(pack)
+    want = oracle_response(W, mode, sid, ctx.expand_rgsw(seeds, b_rows), y_body=y_body)
+    q = inspire.SeededClientQuery(sid, seeds, b_rows, inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body))
+    resp = inspire.respond_seeded_inspiring(crs, edb, q)
+    assert resp.column_ciphertexts == []
+    assert np.array_equal(resp.ciphertext.a, want[0])
+    assert np.array_equal(resp.ciphertext.b, want[1])
+    got_entry = client.extract_inspiring(want, ENTRY)
+    expect = W["db"][index * ENTRY:(index + 1) * ENTRY]
+    if mode == "crt_fixed":
+        assert np.array_equal(got_entry, expect)
+
+
+@pytest.mark.parametrize("mode", ["crt_fixed", "compat"])
+def test_in_process_y_all_keys(world, mode):
+    """Queries built in-process carry y_all (inspiring2.rs:670-695); respond
+    uses it instead of rotating y_body (respond.rs:365-377)."""
+    W = world
+    inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
+    crs, edb, pack, omode = W["w"][mode]
+    seeds, b_rows = client.query_seeded(321)
+    y_body, y_all = client.packing_keys(pack)
+    want = oracle_response(W, mode, 1, ctx.expand_rgsw(seeds, b_rows), y_all=y_all)
+    q = inspire.SeededClientQuery(1, seeds, b_rows,
+                                  inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body, y_all=y_all))
+    resp = inspire.respond_seeded_inspiring(crs, edb, q)
+    assert np.array_equal(np.stack([resp.ciphertext.a, resp.ciphertext.b]), want)
+
+
+@pytest.mark.parametrize("mode", ["crt_fixed", "compat"])
+def test_unseeded_respond_inspiring(world, mode):
+    W = world
+    inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
+    crs, edb, pack, omode = W["w"][mode]
+    seeds, b_rows = client.query_seeded(1000)
+    rgsw = ctx.expand_rgsw(seeds, b_rows)
+    y_body, _ = client.packing_keys(pack)
+    want = oracle_response(W, mode, 2, rgsw, y_body=y_body)
+    q = inspire.ClientQuery(2, rgsw, inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body))
+    resp = inspire.respond_inspiring(crs, edb, q)
+    assert np.array_equal(np.stack([resp.ciphertext.a, resp.ciphertext.b]), want)
+
+
+@pytest.mark.parametrize("mode", ["crt_fixed", "compat"])
+def test_batch_equals_single(world, mode):
+    """A batch mixing shards and clients returns, per query, the single-query
+    response."""
+    W = world
+    inspire, ctx, O = W["inspire"], W["ctx"], W["O"]
+    crs, edb, pack, omode = W["w"][mode]
+    clients = [O.Client(ctx, seed=s, rng_seed=100 + s) for s in range(3)]
+    ids, keys = [], []
+    for c in clients:
+        yb, _ = c.packing_keys(pack)
+        keys.append(yb)
+        ids.append(crs.register_client(inspire.ClientPackingKeys(y_body=yb)))
+    idxs = [5, 2050, 4100, 77, 4995, 2047]
+    seeds = np.zeros((len(idxs), 6, 32), dtype=np.uint8)
+    brows = np.zeros((len(idxs), 6, 2 * N), dtype=np.uint64)
+    sids, cids = [], []
+    for k, ix in enumerate(idxs):
+        c = k % 3
+        s, b = clients[c].query_seeded(ix % N)
+        seeds[k], brows[k] = s, b
+        sids.append(ix // N)
+        cids.append(ids[c])
+    out = inspire.respond_seeded_batch(crs, edb, sids, seeds, brows, cids)
+    for k in range(len(idxs)):
+        q = inspire.SeededClientQuery(sids[k], seeds[k], brows[k],
+                                      inspiring_packing_keys=inspire.ClientPackingKeys(y_body=keys[k % 3]))
+        r = inspire.respond_seeded_inspiring(crs, edb, q)
+        assert np.array_equal(out[k], np.stack([r.ciphertext.a, r.ciphertext.b]))
+    want0 = oracle_response(W, mode, sids[0], ctx.expand_rgsw(seeds[0], brows[0]), y_body=keys[0])
+    assert np.array_equal(out[0], want0)
+    for i in ids:
+        crs.release_client(i)
+
+
+def test_errors_follow_reference(world):
+    W = world
+    inspire, client = W["inspire"], W["client"]
+    crs, edb, pack, _ = W["w"]["crt_fixed"]
+    seeds, b_rows = client.query_seeded(3)
+    y_body, _ = client.packing_keys(pack)
+    keys = inspire.ClientPackingKeys(y_body=y_body)
+    with pytest.raises(inspire.PirError, match="Shard 3 not found"):
+        inspire.respond_seeded_inspiring(crs, edb, inspire.SeededClientQuery(3, seeds, b_rows, inspiring_packing_keys=keys))
+    with pytest.raises(inspire.PirError, match="InspiRING client packing keys missing from query"):
+        inspire.respond_seeded_inspiring(crs, edb, inspire.SeededClientQuery(0, seeds, b_rows))
+    with pytest.raises(inspire.PirError, match="y_all and y_body are both empty"):
+        inspire.respond_seeded_inspiring(crs, edb, inspire.SeededClientQuery(
+            0, seeds, b_rows, inspiring_packing_keys=inspire.ClientPackingKeys()))
+    # keys-missing is checked before the shard lookup (respond.rs:296-305)
+    with pytest.raises(inspire.PirError, match="keys missing"):
+        inspire.respond_seeded_inspiring(crs, edb, inspire.SeededClientQuery(99, seeds, b_rows))
+
+
+@pytest.mark.parametrize("entry_size,gamma", [(2, 1), (8, 4), (16, 8)])
+def test_other_column_counts(oracle_mod, entry_size, gamma):
+    torch = pytest.importorskip("torch")
+    import inspire
+
+    O = oracle_mod
+    rng = np.random.default_rng(entry_size)
+    n_entries = 1500
+    db = rng.integers(0, 256, size=n_entries * entry_size, dtype=np.uint8)
+    ctx = O.Ctx()
+    client = O.Client(ctx, seed=1, rng_seed=entry_size)
+    for mode, omode in (("crt_fixed", O.MODE_CRT_FIXED), ("compat", O.MODE_COMPAT)):
+        crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, gamma, mode=mode)
+        edb = inspire.EncodedDatabase(crs, db, entry_size)
+        pack = O.Pack(ctx, gamma, W_SEED, mode=omode)
+        seeds, b_rows = client.query_seeded(1234)
+        y_body, _ = client.packing_keys(pack)
+        want = ctx.respond_inspiring(ctx.encode_shard(db, entry_size, 0), ctx.expand_rgsw(seeds, b_rows), W_SEED,
+                                     mode=omode, pack=pack, y_body=y_body)
+        q = inspire.SeededClientQuery(0, seeds, b_rows, inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body))
+        r = inspire.respond_seeded_inspiring(crs, edb, q)
+        assert np.array_equal(np.stack([r.ciphertext.a, r.ciphertext.b]), want), mode
+        if mode == "crt_fixed":
+            assert np.array_equal(client.extract_inspiring(want, entry_size),
+                                  db[1234 * entry_size:1235 * entry_size])
+
+
+def test_full_size_database_extracts(oracle_mod):
+    """2^20 entries x 32 B resident (512 shards): sampled queries decrypt to
+    their entries (crt_fixed) and the first matches the oracle bit for bit."""
+    torch = pytest.importorskip("torch")
+    import inspire
+
+    O = oracle_mod
+    rng = np.random.default_rng(20)
+    n_entries = 1 << 20
+    db = rng.integers(0, 256, size=n_entries * ENTRY, dtype=np.uint8)
+    ctx = O.Ctx()
+    client = O.Client(ctx, seed=2, rng_seed=21)
+    crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
+    edb = inspire.EncodedDatabase(crs, db, ENTRY)
+    assert edb.num_shards == 512
+    pack = O.Pack(ctx, 16, W_SEED, mode=O.MODE_CRT_FIXED)
+    y_body, _ = client.packing_keys(pack)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    idxs = rng.integers(0, n_entries, size=24)
+    seeds = np.zeros((len(idxs), 6, 32), dtype=np.uint8)
+    brows = np.zeros((len(idxs), 6, 2 * N), dtype=np.uint64)
+    for k, ix in enumerate(idxs):
+        seeds[k], brows[k] = client.query_seeded(int(ix) % N)
+    out = inspire.respond_seeded_batch(crs, edb, [int(i) // N for i in idxs], seeds, brows, [cid] * len(idxs))
+    for k, ix in enumerate(idxs):
+        ix = int(ix)
+        assert np.array_equal(client.extract_inspiring(out[k], ENTRY), db[ix * ENTRY:(ix + 1) * ENTRY])
+    ix = int(idxs[0])
+    want = ctx.respond_inspiring(ctx.encode_shard(db, ENTRY, ix // N), ctx.expand_rgsw(seeds[0], brows[0]), W_SEED,
+                                 mode=O.MODE_CRT_FIXED, pack=pack, y_body=y_body)
+    assert np.array_equal(out[0], want)
