@@ -36,12 +36,17 @@ ENTRY = 32
 GAMMA = 16
 LOG2_ENTRIES = 24
 BATCH = 128
+LAUNCHES_PER_STEP = 16  # one step answers LAUNCHES_PER_STEP * BATCH queries
+POOL_BATCHES = 32       # distinct staged batches, cycled
+REFERENCE_BUDGET_S = 150.0
 W_SEED = bytes(range(100, 132))
 METRIC = "Respond queries/s (batched InsPIRe^2, seeded queries, InspiRING packing)"
 # algorithmic bytes per query (raw shard 64 KiB + query b-rows 48 KiB + y_body 48 KiB + response 32 KiB)
 ALG_BYTES_PER_QUERY = 192 * 1024
 # exact modular multiplies per query (transform butterflies + pointwise products), see the design doc
 MULMODS_PER_QUERY = 3.4e6
+# resident database bytes one query reads: contracted form 768 KiB + raw columns 64 KiB
+DB_BYTES_PER_QUERY = (768 + 64) * 1024
 
 
 def dist_env():
@@ -66,7 +71,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -158,29 +163,35 @@ def reference_arm(args):
     rng = np.random.default_rng(1)
     shard_db = rng.integers(0, 256, size=N * ENTRY, dtype=np.uint8)
     shard = ctx.encode_shard(shard_db, ENTRY, 0)
+    # one faithful query takes seconds (PackParams::new searches 2048 tables by
+    # brute force), so the run stops at REFERENCE_BUDGET_S and reports the
+    # number of steps it timed
     times = []
-    for step in range(args.warmup + args.steps):
+    budget_t0 = time.perf_counter()
+    for step in range(min(args.warmup, 1) + args.steps):
         k = step % len(locals_)
         t0 = time.perf_counter()
         rgsw = ctx.expand_rgsw(seeds[k], brows[k])
         ctx.respond_inspiring(shard, rgsw, W_SEED, mode=O.MODE_COMPAT, pack=None, y_body=y_body)
         dt = time.perf_counter() - t0
-        if step >= args.warmup:
+        if step >= min(args.warmup, 1):
             times.append(dt)
+        if time.perf_counter() - budget_t0 > REFERENCE_BUDGET_S and times:
+            break
     total = sum(times)
     qps = len(times) / total
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "steps": len(times), "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64 modular integer",
         "data": "synthetic",
         "config": {"workload": "InsPIRe^2 respond, d=2048 CRT [268369921,249561089], p=2^16, 32-B entries, "
                                "one seeded query per step (the crate answers one query per call)",
                    "mode": "compat (the crate's own semantics)"},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} queries, one per step, PackParams::new + OfflinePackingKeys "
-                                   "rebuilt per query as respond.rs:360-361 do"},
+                         "sample": f"{len(times)} queries, one per step (time-budgeted to {REFERENCE_BUDGET_S:.0f} s), "
+                                   "PackParams::new + OfflinePackingKeys rebuilt per query as respond.rs:360-361 do"},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -189,8 +200,9 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--launches-per-step", type=int, default=LAUNCHES_PER_STEP)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--log2-entries", type=int, default=LOG2_ENTRIES)
@@ -243,40 +255,45 @@ def main():
     client, locals_, seeds, brows, y_body = pool
     cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
 
-    steps_total = args.warmup + args.steps
+    L = args.launches_per_step
+    nb = POOL_BATCHES
     qrng = np.random.default_rng(5 + rank)
-    pool_idx = qrng.integers(0, len(locals_), size=(steps_total, B))
-    shard_ids = qrng.integers(0, nshards, size=(steps_total, B)).astype(np.uint32)
+    pool_idx = qrng.integers(0, len(locals_), size=(nb, B))
+    shard_ids = qrng.integers(0, nshards, size=(nb, B)).astype(np.uint32)
 
-    # device-resident inputs for every step (rows ELL..2ELL-1 only)
+    # device-resident inputs of nb distinct batches (rows ELL..2ELL-1 only)
     d_seeds = torch.from_numpy(np.ascontiguousarray(seeds[pool_idx][:, :, 3:6, :])).to(dev)
     d_brows = torch.from_numpy(np.ascontiguousarray(brows[pool_idx][:, :, 3:6, :]).view(np.int64)).to(dev)
     d_shard = torch.from_numpy(shard_ids.view(np.int32)).to(dev)
-    d_client = torch.full((steps_total, B), cid, dtype=torch.int32, device=dev)
-    d_out = torch.zeros((steps_total, B, 2, 2 * N), dtype=torch.int64, device=dev)
-    d_status = torch.zeros((steps_total, B), dtype=torch.int32, device=dev)
+    d_client = torch.full((nb, B), cid, dtype=torch.int32, device=dev)
+    d_out = torch.zeros((nb, B, 2, 2 * N), dtype=torch.int64, device=dev)
+    d_status = torch.zeros((nb, B), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
 
     def launch(s, n=B):
+        s %= nb
         inspire.respond_seeded_batch_device(crs, edb, n, d_shard[s].data_ptr(), d_seeds[s].data_ptr(),
                                             d_brows[s].data_ptr(), d_client[s].data_ptr(), d_out[s].data_ptr(),
                                             d_status[s].data_ptr(), sp)
 
     for s in range(args.warmup):
-        launch(s)
+        for j in range(L):
+            launch(s * L + j)
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(local) as clk:
+        time.sleep(0.3)
         torch.cuda.synchronize()
         wall0 = time.perf_counter()
         for k in range(args.steps):
             flush.fill_(k & 0xFF)  # evict the previous step's shards from L2 (untimed)
             evs[k][0].record(stream)
-            launch(args.warmup + k)
+            for j in range(L):
+                launch(k * L + j)
             evs[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
@@ -288,14 +305,14 @@ def main():
         t = torch.tensor([kern_s], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         kern_s = float(t.item())
-    value = ws * B * args.steps / kern_s
+    value = ws * B * L * args.steps / kern_s
 
     # correctness of what was timed: status and client-side extraction on samples
-    status = d_status[args.warmup:].cpu().numpy()
+    status = d_status.cpu().numpy()
     assert not status.any(), "respond kernel reported a nonzero status"
-    outs = d_out[-1].cpu().numpy().view(np.uint64)
+    s = (args.steps * L - 1) % nb
+    outs = d_out[s].cpu().numpy().view(np.uint64)
     for j in range(0, B, max(1, B // 8)):
-        s = steps_total - 1
         gi = int(shard_ids[s, j]) * N + int(locals_[pool_idx[s, j]])
         got = client.extract_inspiring(outs[j], ENTRY)
         if args.mode == "crt_fixed":
@@ -311,7 +328,7 @@ def main():
         reps = 20 if bs < 32 else 5
         e0.record(stream)
         for r in range(reps):
-            launch(args.warmup + (r % args.steps), bs)
+            launch(r, bs)
         e1.record(stream)
         torch.cuda.synchronize()
         sweep[str(bs)] = bs * reps / (e0.elapsed_time(e1) / 1e3)
@@ -323,7 +340,7 @@ def main():
     hs, hb, ho = h_seeds.numpy(), h_brows.numpy().view(np.uint64), h_out.numpy().view(np.uint64)
     e2e_times = []
     for k in range(args.warmup + args.steps):
-        s = k % steps_total
+        s = k % nb
         hs[:] = seeds[pool_idx[s]]
         hb[:] = brows[pool_idx[s]]
         t0 = time.perf_counter()
@@ -336,14 +353,14 @@ def main():
         t = torch.tensor([e2e_s], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_value = ws * B * args.steps / e2e_s
+    e2e_value = ws * B * args.steps / e2e_s  # e2e step = one host-buffer call of B queries
     h2d = B * (4 + 4 + 32 * 3 + 3 * 2 * N * 8)
     d2h = B * (2 * 2 * N * 8 + 4)
 
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    mean_kernel_s = kern_s / args.steps
+    mean_kernel_s = kern_s / (args.steps * L)
     achieved_gbs = ALG_BYTES_PER_QUERY * B / mean_kernel_s / 1e9
     resident_bytes = edb.device_bytes
 
@@ -360,6 +377,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "u32 modular integer (exact)", "data": "synthetic",
             "config": {"workload": f"batched InsPIRe^2 respond: 2^{args.log2_entries} entries x 32 B resident "
                                    f"({nshards} shards), B={B} seeded queries per launch, uniform shard ids",
+                       "step": f"{L} launches x {B} queries; e2e step = one host-buffer call of {B} queries",
                        "mode": args.mode, "global_batch": B * ws, "ring_dim": N,
                        "crt_moduli": [268369921, 249561089], "p": 65536,
                        "l2": "flushed between timed steps (256 MiB write); resident DB 6.5 GiB > L2",
@@ -370,7 +388,8 @@ def main():
                          "note": "algorithmic bytes 192 KiB/query; the kernel is integer-issue bound, see DESIGN.md"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * L,
+            "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
             "plain_single_query_qps": sweep.get("1"),
             "wall_s_timed_region": wall,

@@ -183,7 +183,8 @@ struct inspire_ctx {
 };
 
 struct inspire_db {
-  inspire_ctx* ctx = nullptr;
+  inspire_ctx* ctx = nullptr;  // never dereferenced after creation
+  int device = 0;
   int gamma = 0;
   uint64_t n_entries = 0;
   uint32_t entry_size = 0;
@@ -541,6 +542,7 @@ int inspire_db_create(inspire_ctx* c, const uint8_t* raw, uint64_t n_entries, ui
   if (int rc = set_device(c)) return rc;
   inspire_db* db = new inspire_db();
   db->ctx = c;
+  db->device = c->device;
   db->n_entries = n_entries;
   db->entry_size = entry_size;
   // encode_database returns no shard for an empty database (encode_db.rs:112-114)
@@ -596,7 +598,7 @@ int inspire_db_create(inspire_ctx* c, const uint8_t* raw, uint64_t n_entries, ui
 
 void inspire_db_destroy(inspire_db* db) {
   if (!db) return;
-  cudaSetDevice(db->ctx->device);
+  cudaSetDevice(db->device);
   delete db;
 }
 

@@ -22,9 +22,11 @@
 //    interleaved: each T[i][k] NTT is multiplied into R[i] with the CRS key
 //    w_all and into the b accumulator with the client key y_all.
 //
-// Layout: 256 threads = two groups of 128; group g owns CRT residue g for
-// every transform.  All intermediate state lives in shared memory and
-// registers; the kernel uses no global scratch.
+// Layout: 768 threads = six groups of 128, group g = 3 r + k owns CRT residue
+// r and gadget digit k.  Per recursion step, groups (r,0) run the inverse NTT
+// while groups (r,1),(r,2) scatter the query-only term R_i; then the three
+// digit NTTs of each residue run concurrently.  All intermediate state lives
+// in shared memory and registers; the kernel uses no global scratch.
 #include "chacha.cuh"
 #include "kernels.h"
 
@@ -32,9 +34,19 @@ namespace ig {
 
 namespace {
 
-// Exclusive scan over the 256 threads of the block; ws needs 16 ints.
-__device__ __forceinline__ int block_scan_excl(int v, int* ws, int& total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+constexpr int RG = 6;                 // NTT groups per CTA
+constexpr int RBLOCK = RG * NTT_GT;   // 768 threads
+constexpr int SUB = 256;              // threads of one expansion sub-block
+constexpr int NWARP = RBLOCK / 32;
+
+__device__ __forceinline__ void named_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Exclusive scan over one 256-thread sub-block (lt = thread index in it);
+// ws needs 17 ints.
+__device__ __forceinline__ int sub_scan_excl(int v, int* ws, int& total, int bar, int lt) {
+  const int lane = lt & 31, warp = lt >> 5;
   int incl = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -42,7 +54,7 @@ __device__ __forceinline__ int block_scan_excl(int v, int* ws, int& total) {
     if (lane >= o) incl += t;
   }
   if (lane == 31) ws[warp] = incl;
-  __syncthreads();
+  named_sync(bar, SUB);
   if (warp == 0) {
     int wv = lane < 8 ? ws[lane] : 0;
 #pragma unroll
@@ -52,63 +64,62 @@ __device__ __forceinline__ int block_scan_excl(int v, int* ws, int& total) {
     }
     if (lane < 8) ws[8 + lane] = wv;
   }
-  __syncthreads();
+  named_sync(bar, SUB);
   total = ws[15];
   const int base = warp ? ws[8 + warp - 1] : 0;
   const int r = base + incl - v;
-  __syncthreads();
+  named_sync(bar, SUB);
   return r;
 }
 
-// Poly::from_seed_moduli (poly.rs:251-281): residue 0 takes the first N
-// accepted draws of gen_range(0..q0), residue 1 the next N of gen_range(0..q1).
-// NR = 1 stops after residue 0.  Writes a0[N], a1[N]; returns false if the
-// iteration bound was hit (never for a working ChaCha stream).
+// Poly::from_seed_moduli (poly.rs:251-281) by one 256-thread sub-block:
+// residue 0 takes the first N accepted draws of gen_range(0..q0), residue 1
+// the next N of gen_range(0..q1); NR = 1 stops after residue 0.  Returns false
+// if the iteration bound was hit (never for a working ChaCha stream).
 template <int NR>
-__device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict__ seed,
-                                  uint64_t* cand, uint32_t* a0, uint32_t* a1, int* ws) {
+__device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict__ seed, uint64_t* cand,
+                                  uint32_t* a0, uint32_t* a1, int* ws, int bar, int lt) {
   uint32_t key[8];
 #pragma unroll
   for (int i = 0; i < 8; i++)
-    key[i] = (uint32_t)seed[4 * i] | ((uint32_t)seed[4 * i + 1] << 8) |
-             ((uint32_t)seed[4 * i + 2] << 16) | ((uint32_t)seed[4 * i + 3] << 24);
-  const int tid = threadIdx.x;
+    key[i] = (uint32_t)seed[4 * i] | ((uint32_t)seed[4 * i + 1] << 8) | ((uint32_t)seed[4 * i + 2] << 16) |
+             ((uint32_t)seed[4 * i + 3] << 24);
   int pos0 = 0, pos1 = 0, res = 0;
   uint64_t blk = 0;
   for (int it = 0; it < 64; it++) {
     const int need = res == 0 ? (N - pos0) + (NR == 2 ? N : 0) : (N - pos1);
-    const int nblk = min(BLOCK, (need * 9) / 64 + 3);
-    if (tid < nblk) {
+    const int nblk = min(SUB, (need * 9) / 64 + 3);
+    if (lt < nblk) {
       uint32_t w[16];
-      chacha20_block(key, blk + tid, w);
+      chacha20_block(key, blk + lt, w);
 #pragma unroll
-      for (int k = 0; k < 8; k++) cand[8 * tid + k] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
+      for (int k = 0; k < 8; k++) cand[8 * lt + k] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
     }
     blk += nblk;
-    __syncthreads();
+    named_sync(bar, SUB);
     int start = 0;
     if (res == 0) {
       uint32_t vals[8];
       unsigned fl = 0;
       int cnt = 0;
-      if (tid < nblk) {
+      if (lt < nblk) {
 #pragma unroll
         for (int k = 0; k < 8; k++)
-          if (uniform_accept(cand[8 * tid + k], P.r[0].q, P.r[0].zone, vals[k])) {
+          if (uniform_accept(cand[8 * lt + k], P.r[0].q, P.r[0].zone, vals[k])) {
             fl |= 1u << k;
             cnt++;
           }
       }
       int total;
-      int p = pos0 + block_scan_excl(cnt, ws, total);
+      int p = pos0 + sub_scan_excl(cnt, ws, total, bar, lt);
 #pragma unroll
       for (int k = 0; k < 8; k++)
         if ((fl >> k) & 1u) {
           if (p < N) a0[p] = vals[k];
-          if (p == N - 1) ws[16] = 8 * tid + k;
+          if (p == N - 1) ws[16] = 8 * lt + k;
           p++;
         }
-      __syncthreads();
+      named_sync(bar, SUB);
       if (pos0 + total >= N) {
         start = ws[16] + 1;
         res = 1;
@@ -117,23 +128,23 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
         pos0 += total;
         start = nblk * 8;
       }
-      __syncthreads();
+      named_sync(bar, SUB);
       if (NR == 1 && res == 1) return true;
     }
     if (NR == 2 && res == 1) {
       uint32_t vals[8];
       unsigned fl = 0;
       int cnt = 0;
-      if (tid < nblk) {
+      if (lt < nblk) {
 #pragma unroll
         for (int k = 0; k < 8; k++)
-          if (8 * tid + k >= start && uniform_accept(cand[8 * tid + k], P.r[1].q, P.r[1].zone, vals[k])) {
+          if (8 * lt + k >= start && uniform_accept(cand[8 * lt + k], P.r[1].q, P.r[1].zone, vals[k])) {
             fl |= 1u << k;
             cnt++;
           }
       }
       int total;
-      int p = pos1 + block_scan_excl(cnt, ws, total);
+      int p = pos1 + sub_scan_excl(cnt, ws, total, bar, lt);
 #pragma unroll
       for (int k = 0; k < 8; k++)
         if ((fl >> k) & 1u) {
@@ -143,18 +154,17 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
       pos1 += total;
       if (pos1 >= N) return true;
     }
-    __syncthreads();
+    named_sync(bar, SUB);
   }
   return false;
 }
 
-// b0_c for every column c and residue (see file comment).  bp (6N words) is
-// scratch; bpoly[r * 16 + c] receives the result.
-__device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H,
-                          const uint64_t* __restrict__ brows, uint32_t* bp, uint64_t* red,
-                          uint32_t* bpoly) {
+// b0_c for every column c and residue (see file comment).  bp (6N words) and
+// red (NWARP*16*2 u64) are scratch; bpoly[r * 16 + c] receives the result.
+__device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* __restrict__ brows,
+                          uint32_t* bp, uint64_t* red, uint32_t* bpoly) {
   const int tid = threadIdx.x, gamma = P.gamma;
-  for (int idx = tid; idx < ELL * 2 * N; idx += BLOCK) {
+  for (int idx = tid; idx < ELL * 2 * N; idx += RBLOCK) {
     const int i = idx & (N - 1), tr = idx >> LOGN, r = tr & 1;
     const uint64_t* row = brows + (size_t)tr * N;
     uint32_t v = (uint32_t)(i == 0 ? row[0] : row[N - i]);
@@ -165,12 +175,9 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H,
   const int lane = tid & 31, warp = tid >> 5;
   for (int c = 0; c < gamma; c++) {
     uint64_t acc0 = 0, acc1 = 0;
-#pragma unroll 4
-    for (int v = 0; v < N / BLOCK; v++) {
-      const int i = tid + BLOCK * v;
+    for (int i = tid; i < N; i += RBLOCK) {
       const uint64_t xv = P.delta * (uint64_t)H[c * N + i];
-      const uint32_t d0 = (uint32_t)xv & 0xFFFFFu, d1 = (uint32_t)(xv >> 20) & 0xFFFFFu,
-                     d2 = (uint32_t)(xv >> 40);
+      const uint32_t d0 = (uint32_t)xv & 0xFFFFFu, d1 = (uint32_t)(xv >> 20) & 0xFFFFFu, d2 = (uint32_t)(xv >> 40);
       acc0 += (uint64_t)d0 * bp[0 * N + i] + (uint64_t)d1 * bp[2 * N + i] + (uint64_t)d2 * bp[4 * N + i];
       acc1 += (uint64_t)d0 * bp[1 * N + i] + (uint64_t)d1 * bp[3 * N + i] + (uint64_t)d2 * bp[5 * N + i];
     }
@@ -180,58 +187,89 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H,
       acc1 += __shfl_down_sync(0xffffffffu, acc1, o);
     }
     if (lane == 0) {
-      red[(c * 8 + warp) * 2 + 0] = acc0;
-      red[(c * 8 + warp) * 2 + 1] = acc1;
+      red[(c * NWARP + warp) * 2 + 0] = acc0;
+      red[(c * NWARP + warp) * 2 + 1] = acc1;
     }
   }
   __syncthreads();
   if (tid < 2 * gamma) {
     const int c = tid >> 1, r = tid & 1;
     uint64_t s = 0;
-    for (int w = 0; w < 8; w++) s += red[(c * 8 + w) * 2 + r];
+    for (int w = 0; w < NWARP; w++) s += red[(c * NWARP + w) * 2 + r];
     bpoly[r * 16 + c] = (uint32_t)(s % P.r[r].q);
   }
   __syncthreads();
 }
 
-// R_i (NTT domain, scaled by n^-1) of packing_offline step 1 for residue g,
+// R_i (NTT domain, scaled by n^-1) of packing_offline step 1 for one residue,
 // scattered to dst[slot]: source slot u contributes to slot s with
 // 2brv(s)+1 = h_i (2brv(u)+1) mod 2n, where h_i = g^-i
-// (inspiring2.rs:952-981 with the tables of :208-263).
-__device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint32_t* __restrict__ Eg,
-                                          const uint32_t* Ag, int astride, uint32_t* dst, int x,
-                                          uint32_t q, uint32_t qinv) {
+// (inspiring2.rs:952-981 with the tables of :208-263).  Threads p in
+// [0, nthr) handle u = p + nthr * v.
+__device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint32_t* __restrict__ Eg, const uint32_t* Ag,
+                                          int astride, uint32_t* dst, int p, int nthr, uint32_t q, uint32_t qinv) {
   const int gamma = P.gamma;
   const uint32_t mi = (uint32_t)(gamma - i) & (uint32_t)(gamma - 1);
   const uint32_t hi = (1u + (uint32_t)(2 * N / gamma) * mi) & (2 * N - 1);
 #pragma unroll 4
-  for (int v = 0; v < 16; v++) {
-    const int u = x + 128 * v;
+  for (int u = p; u < N; u += nthr) {
     const uint32_t e = 2 * brv11(u) + 1;
     const uint32_t k = (e * mi) & (uint32_t)(gamma - 1);
     const uint32_t* ek = Eg + (size_t)k * N + u;
-    uint64_t T = (uint64_t)__ldg(ek) * Ag[u] + (uint64_t)__ldg(ek + (size_t)gamma * N) * Ag[astride + u] +
-                 (uint64_t)__ldg(ek + (size_t)2 * gamma * N) * Ag[2 * astride + u];
+    const uint64_t T = (uint64_t)__ldg(ek) * Ag[u] + (uint64_t)__ldg(ek + (size_t)gamma * N) * Ag[astride + u] +
+                       (uint64_t)__ldg(ek + (size_t)2 * gamma * N) * Ag[2 * astride + u];
     const uint32_t s = brv11(((hi * e) & (2 * N - 1)) >> 1);
     dst[s] = redc(T, q, qinv);
   }
 }
 
+__device__ __forceinline__ void load16(const uint32_t* __restrict__ src, uint32_t v[16]) {
+  const uint4* s4 = reinterpret_cast<const uint4*>(src);
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const uint4 t = s4[r];
+    v[4 * r] = t.x;
+    v[4 * r + 1] = t.y;
+    v[4 * r + 2] = t.z;
+    v[4 * r + 3] = t.w;
+  }
+}
+
+__device__ __forceinline__ void store16(uint32_t* dst, const uint32_t v[16]) {
+  uint4* d4 = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+  for (int r = 0; r < 4; r++) d4[r] = make_uint4(v[4 * r], v[4 * r + 1], v[4 * r + 2], v[4 * r + 3]);
+}
+
+// Shared-memory layout in u32 words (NR = residues of the a side).
+template <int NR>
+struct Smem {
+  static constexpr int AHAT = 0;                           // [ELL][NR][N]
+  static constexpr int SC = AHAT + ELL * NR * N;           // [RG][NTT_SCRATCH]
+  static constexpr int T = SC + RG * NTT_SCRATCH;          // [3][N] digits (T0/T1 also hold the INTT output)
+  static constexpr int SCAT = T + 3 * N;                   // [2][2][N] R_i, double buffered
+  static constexpr int PB = SCAT + 4 * N;                  // [2][2][N] partial products of digits 1, 2
+  static constexpr int MISC = PB + 4 * N;                  // bpoly[32], ws[3][20]
+  static constexpr int TOTAL = MISC + 128;
+};
+
 template <int MODE, bool SEEDED>
-__global__ void __launch_bounds__(BLOCK, 2) respond_kernel(const RespondArgs A) {
-  constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;  // residues needed on the a side
+__global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A) {
+  constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
+  using L = Smem<NR>;
   extern __shared__ __align__(16) uint32_t smem[];
-  uint32_t* Ahat = smem;                        // [ELL][NR][N]
-  uint32_t* SC = Ahat + ELL * NR * N;           // [2][NTT_SCRATCH]
-  uint32_t* RT = SC + 2 * NTT_SCRATCH;          // [3][N]
-  uint32_t* misc = RT + 3 * N;
-  uint32_t* bpoly = misc;                       // [2][16]
-  int* ws = (int*)(misc + 32);                  // [17]
-  uint64_t* red = (uint64_t*)(misc + 64);       // [16][8][2]
+  uint32_t* Ahat = smem + L::AHAT;
+  uint32_t* SC = smem + L::SC;
+  uint32_t* T = smem + L::T;
+  uint32_t* SCAT = smem + L::SCAT;
+  uint32_t* PB = smem + L::PB;
+  uint32_t* bpoly = smem + L::MISC;
+  int* wsb = (int*)(smem + L::MISC + 32);
 
   const DevParams& P = A.P;
   const int qi = blockIdx.x;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const int r = g / 3, kd = g - 3 * r;  // residue, gadget digit of this group
   const int gamma = P.gamma;
   const uint32_t shard = A.shard[qi];
   const int32_t cid = A.client[qi];
@@ -243,81 +281,88 @@ __global__ void __launch_bounds__(BLOCK, 2) respond_kernel(const RespondArgs A) 
   const uint32_t* E = A.E + (size_t)shard * 2 * ELL * gamma * N;
   const uint16_t* H = A.H + (size_t)shard * gamma * N;
   const uint32_t* Y = A.yhat_table[cid];
-  const uint32_t q = P.r[g].q, qinv = P.r[g].qinv, q2 = 2 * q;
+  const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
 
-  column_b0(P, H, A.brows + (size_t)qi * ELL * 2 * N, smem, red, bpoly);
+  // ---- b part of the column products (bp aliases SCAT+PB, red aliases T) ----
+  column_b0(P, H, A.brows + (size_t)qi * ELL * 2 * N, SCAT, (uint64_t*)T, bpoly);
 
-  // ---- rows ELL..2ELL-1: a-polys, forward NTT ----
-  for (int t = 0; t < ELL; t++) {
-    __syncthreads();
-    uint32_t* a0 = SC;
-    uint32_t* a1 = SC + NTT_SCRATCH;
+  // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
+  {
+    const int t = tid >> 8, lt = tid & 255;
+    uint64_t* cand = reinterpret_cast<uint64_t*>(SC) + t * N;  // 3 x 16 KiB within SC
+    uint32_t* a0 = T + t * 2 * N;                               // 3 x 16 KiB within T..PB
+    uint32_t* a1 = a0 + N;
     if (SEEDED) {
-      bool ok = expand_seeded_row<NR>(P, A.seeds + ((size_t)qi * ELL + t) * 32, (uint64_t*)RT, a0, a1, ws);
-      if (!ok && tid == 0) A.status[qi] = ERR_EXPAND;
+      const bool ok = expand_seeded_row<NR>(P, A.seeds + ((size_t)qi * ELL + t) * 32, cand, a0, a1, wsb + 20 * t,
+                                            7 + t, lt);
+      if (!ok && lt == 0) A.status[qi] = ERR_EXPAND;
     } else {
       const uint64_t* ar = A.arows + ((size_t)qi * ELL + t) * 2 * N;
-      for (int j = tid; j < NR * N; j += BLOCK) (j < N ? a0 : a1)[j & (N - 1)] = (uint32_t)ar[j];
-    }
-    __syncthreads();
-    if (g < NR) {
-      uint32_t v[16];
-      const uint32_t* src = g ? a1 : a0;
-#pragma unroll
-      for (int r = 0; r < 16; r++) v[r] = src[x + 128 * r];
-      ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
-      uint4* dst = reinterpret_cast<uint4*>(Ahat + (t * NR + g) * N + 16 * x);
-#pragma unroll
-      for (int r = 0; r < 4; r++) dst[r] = make_uint4(v[4 * r], v[4 * r + 1], v[4 * r + 2], v[4 * r + 3]);
+      for (int j = lt; j < NR * N; j += SUB) a0[j] = (uint32_t)ar[j];  // a1 follows a0
     }
   }
   __syncthreads();
-
-  const bool scat = (MODE == MODE_CRT_FIXED) || g == 0;
-  const uint32_t* Eg = E + (size_t)g * ELL * gamma * N;
-  const uint32_t* Ag = Ahat + (MODE == MODE_CRT_FIXED ? g : 0) * N;
-  uint32_t* dst = RT + (MODE == MODE_CRT_FIXED ? g : 0) * N;
-
-  uint32_t vR[16], acc[16], accb[16];
+  if (r < NR) {  // group (r, t=kd) transforms row kd, residue r
+    uint32_t v[16];
+    const uint32_t* src = T + kd * 2 * N + r * N;
 #pragma unroll
-  for (int r = 0; r < 16; r++) accb[r] = 0;
+    for (int j = 0; j < 16; j++) v[j] = src[x + 128 * j];
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    store16(Ahat + (kd * NR + r) * N + 16 * x, v);
+  }
+  __syncthreads();
+
+  // scatter roles: fixed mode -> groups (r,1),(r,2) do residue r;
+  // compat -> groups with digit 1, 2 of both residues do residue 0
+  const int sres = MODE == MODE_CRT_FIXED ? r : 0;
+  const int sp = MODE == MODE_CRT_FIXED ? (kd - 1) * NTT_GT + x : ((r * 2 + (kd - 1)) * NTT_GT + x);
+  const int snthr = MODE == MODE_CRT_FIXED ? 2 * NTT_GT : 4 * NTT_GT;
+  const bool scatters = kd != 0;
+  const uint32_t* Eg = E + (size_t)sres * ELL * gamma * N;
+  const uint32_t* Ag = Ahat + sres * N;
+  const uint32_t sq = P.r[sres].q, sqinv = P.r[sres].qinv;
+
+  uint32_t vR[16], accb[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) accb[j] = 0;
 
   // R_{gamma-1}
-  if (scat) scatter_r(P, gamma - 1, Eg, Ag, NR * N, dst, x, q, qinv);
+  if (scatters) scatter_r(P, gamma - 1, Eg, Ag, NR * N, SCAT + (((gamma - 1) & 1) * 2 + sres) * N, sp, snthr, sq, sqinv);
   __syncthreads();
+  if (kd == 0) {
+    const uint32_t* src = SCAT + (((gamma - 1) & 1) * 2 + (MODE == MODE_CRT_FIXED ? r : 0)) * N + 16 * x;
+    load16(src, vR);
+    if (MODE == MODE_COMPAT && r == 1)
 #pragma unroll
-  for (int r = 0; r < 16; r++) {
-    const uint32_t w = dst[16 * x + r];
-    vR[r] = (MODE == MODE_COMPAT && g == 1) ? compat_residue1_ninv(P, w) : w;
+      for (int j = 0; j < 16; j++) vR[j] = compat_residue1_ninv(P, vR[j]);
   }
 
-  const uint32_t* Wg = A.what;
   for (int i = gamma - 2; i >= 0; i--) {
-    // INTT(R_{i+1}) -> coefficients (values already carry n^-1)
-    ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[g]), q, x, 1 + g);
-    __syncthreads();
+    // [A] INTT(R_{i+1}) by groups (r,0); scatter of R_i by the others
+    if (kd == 0) {
+      ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
-    for (int r = 0; r < 16; r++) RT[g * N + x + 128 * r] = vR[r];
-    __syncthreads();
-    // gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37)
-#pragma unroll 2
-    for (int v = 0; v < N / BLOCK; v++) {
-      const int j = tid + BLOCK * v;
-      const uint64_t c = crt_compose(P, RT[j], RT[N + j]);
-      RT[j] = (uint32_t)c & 0xFFFFFu;
-      RT[N + j] = (uint32_t)(c >> 20) & 0xFFFFFu;
-      RT[2 * N + j] = (uint32_t)(c >> 40);
+      for (int j = 0; j < 16; j++) T[r * N + x + 128 * j] = vR[j];
+    } else {
+      scatter_r(P, i, Eg, Ag, NR * N, SCAT + ((i & 1) * 2 + sres) * N, sp, snthr, sq, sqinv);
     }
     __syncthreads();
+    // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37)
+    for (int j = tid; j < N; j += RBLOCK) {
+      const uint64_t c = crt_compose(P, T[j], T[N + j]);
+      T[j] = (uint32_t)c & 0xFFFFFu;
+      T[N + j] = (uint32_t)(c >> 20) & 0xFFFFFu;
+      T[2 * N + j] = (uint32_t)(c >> 40);
+    }
+    __syncthreads();
+    // [C] group (r,k): NTT of digit k mod q_r, products with w_all[i][k] and y_all[i][k]
+    uint32_t v[16], acc[16];
 #pragma unroll
-    for (int r = 0; r < 16; r++) acc[r] = 0;
-    for (int k = 0; k < ELL; k++) {
-      uint32_t v[16];
-#pragma unroll
-      for (int r = 0; r < 16; r++) v[r] = RT[k * N + x + 128 * r];
-      ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
-      const size_t off = ((size_t)(i * ELL + k) * 2 + g) * N + 16 * x;
-      const uint4* w4 = reinterpret_cast<const uint4*>(Wg + off);
+    for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    {
+      const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
+      const uint4* w4 = reinterpret_cast<const uint4*>(A.what + off);
       const uint4* y4 = reinterpret_cast<const uint4*>(Y + off);
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
@@ -325,51 +370,71 @@ __global__ void __launch_bounds__(BLOCK, 2) respond_kernel(const RespondArgs A) 
         const uint32_t ww[4] = {wv.x, wv.y, wv.z, wv.w}, yy[4] = {yv.x, yv.y, yv.z, yv.w};
 #pragma unroll
         for (int e = 0; e < 4; e++) {
-          const int r = 4 * r4 + e;
-          acc[r] = acc_2q(acc[r], redc_lazy((uint64_t)v[r] * ww[e], q, qinv), q2);
-          accb[r] = acc_2q(accb[r], redc_lazy((uint64_t)v[r] * yy[e], q, qinv), q2);
+          const int j = 4 * r4 + e;
+          acc[j] = redc_lazy((uint64_t)v[j] * ww[e], q, qinv);
+          accb[j] = acc_2q(accb[j], redc_lazy((uint64_t)v[j] * yy[e], q, qinv), q2);
         }
       }
     }
+    if (kd != 0) store16(PB + (r * 2 + kd - 1) * N + 16 * x, acc);
     __syncthreads();
-    if (scat) scatter_r(P, i, Eg, Ag, NR * N, dst, x, q, qinv);
-    __syncthreads();
+    // [D] R_i = scatter + sum_k products, by groups (r,0)
+    if (kd == 0) {
+      uint32_t rh[16], p1[16], p2[16];
+      load16(SCAT + ((i & 1) * 2 + (MODE == MODE_CRT_FIXED ? r : 0)) * N + 16 * x, rh);
+      load16(PB + (r * 2 + 0) * N + 16 * x, p1);
+      load16(PB + (r * 2 + 1) * N + 16 * x, p2);
 #pragma unroll
-    for (int r = 0; r < 16; r++) {
-      const uint32_t w = dst[16 * x + r];
-      const uint32_t rh = (MODE == MODE_COMPAT && g == 1) ? compat_residue1_ninv(P, w) : w;
-      vR[r] = add_mod(rh, reduce_2q(acc[r], q), q);
+      for (int j = 0; j < 16; j++) {
+        uint32_t h = (MODE == MODE_COMPAT && r == 1) ? compat_residue1_ninv(P, rh[j]) : rh[j];
+        uint32_t s = h + acc[j] + p1[j] + p2[j];  // < 7q < 2^31
+        s = min(s, s - 4 * q);
+        s = min(s, s - 2 * q);
+        vR[j] = min(s, s - q);
+      }
     }
   }
 
-  // a_hat = INTT(R_0) (inspiring2.rs:1027-1029)
+  // ---- outputs: a_hat = INTT(R_0) (inspiring2.rs:1027-1029),
+  //      b = b_poly + INTT(sum y_all * bold_t) (inspiring2.rs:1217-1221) ----
+  __syncthreads();  // groups (r,0) have finished reading PB in the last step
+  if (kd != 1) store16(PB + (r * 2 + (kd == 0 ? 0 : 1)) * N + 16 * x, accb);
+  __syncthreads();
   uint64_t* out = A.out + (size_t)qi * 4 * N;
-  ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[g]), q, x, 1 + g);
+  if (kd == 0) {
+    ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
-  for (int r = 0; r < 16; r++) out[g * N + x + 128 * r] = vR[r];
-  // b = b_poly + INTT(sum y_all * bold_t) (inspiring2.rs:1217-1221)
+    for (int j = 0; j < 16; j++) out[r * N + x + 128 * j] = vR[j];
+  } else if (kd == 1) {
+    uint32_t p0[16], p2[16];
+    load16(PB + (r * 2 + 0) * N + 16 * x, p0);
+    load16(PB + (r * 2 + 1) * N + 16 * x, p2);
 #pragma unroll
-  for (int r = 0; r < 16; r++) accb[r] = reduce_2q(accb[r], q);
-  ntt_inv_noscale(accb, SC + g * NTT_SCRATCH, inv_tw(P.r[g]), q, x, 1 + g);
-  if (x < gamma) accb[0] = add_mod(accb[0], bpoly[g * 16 + x], q);
+    for (int j = 0; j < 16; j++) {
+      uint32_t s = accb[j] + p0[j] + p2[j];  // < 6q
+      s = min(s, s - 4 * q);
+      s = min(s, s - 2 * q);
+      accb[j] = min(s, s - q);
+    }
+    ntt_inv_noscale(accb, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
+    if (x < gamma) accb[0] = add_mod(accb[0], bpoly[r * 16 + x], q);
 #pragma unroll
-  for (int r = 0; r < 16; r++) out[2 * N + g * N + x + 128 * r] = accb[r];
+    for (int j = 0; j < 16; j++) out[2 * N + r * N + x + 128 * j] = accb[j];
+  }
 }
 
 }  // namespace
 
 size_t respond_smem_bytes(int mode) {
-  const int nr = mode == MODE_COMPAT ? 1 : 2;
-  return sizeof(uint32_t) * ((size_t)ELL * nr * N + 2 * NTT_SCRATCH + 3 * N + 1024);
+  return sizeof(uint32_t) * (mode == MODE_COMPAT ? Smem<1>::TOTAL : Smem<2>::TOTAL);
 }
 
 template <int MODE, bool SEEDED>
 static cudaError_t launch_one(const RespondArgs& a, cudaStream_t st) {
   const size_t smem = respond_smem_bytes(MODE);
-  cudaError_t e = cudaFuncSetAttribute(respond_kernel<MODE, SEEDED>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(respond_kernel<MODE, SEEDED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  respond_kernel<MODE, SEEDED><<<a.nq, BLOCK, smem, st>>>(a);
+  respond_kernel<MODE, SEEDED><<<a.nq, RBLOCK, smem, st>>>(a);
   return cudaGetLastError();
 }
 

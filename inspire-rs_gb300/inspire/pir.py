@@ -11,7 +11,9 @@ major, canonical: the layout of the crate's `Poly::coeffs` (poly.rs:64-77).
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import weakref
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
@@ -19,6 +21,20 @@ import numpy as np
 
 from . import _native as nat
 from .params import InspireParams, InspireVariant
+
+
+# Live native handles, closed databases-first at interpreter exit (before the
+# CUDA runtime tears down) whatever order the garbage collector would pick.
+_LIVE_DBS: "weakref.WeakSet" = weakref.WeakSet()
+_LIVE_CRS: "weakref.WeakSet" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all() -> None:
+    for db in list(_LIVE_DBS):
+        db.close()
+    for crs in list(_LIVE_CRS):
+        crs.close()
 
 
 class PirError(Exception):
@@ -113,11 +129,15 @@ class ServerCrs:
         _check(self.L.inspire_ctx_create(C.byref(pc), device, nat.MODE_COMPAT if mode == "compat" else nat.MODE_CRT_FIXED,
                                          C.byref(h)))
         self.h = h
+        _LIVE_CRS.add(self)
         seed = (C.c_uint8 * 32).from_buffer_copy(self.inspiring_w_seed)
         _check(self.L.inspire_crs_load(self.h, C.cast(seed, C.c_void_p), self.inspiring_num_columns))
 
     def close(self):
         if getattr(self, "h", None):
+            for db in list(_LIVE_DBS):
+                if db.crs is self:
+                    db.close()
             self.L.inspire_ctx_destroy(self.h)
             self.h = None
 
@@ -161,6 +181,7 @@ class EncodedDatabase:
         _check(self.L.inspire_db_create(crs.h, raw.ctypes.data_as(C.c_void_p), self.total_entries, self.entry_size,
                                         C.byref(h)))
         self.h = h
+        _LIVE_DBS.add(self)
 
     @property
     def num_shards(self) -> int:

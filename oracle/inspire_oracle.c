@@ -633,6 +633,7 @@ void io_automorph_table_brute(const io_ctx *c, int t, io_rng *g,
 
 struct io_pack {
   const io_ctx *c;
+  int n;  /* ring dimension, kept so io_pack_free never touches c */
   int gamma, gen, mode;
   uint8_t w_seed[32];
   int32_t *gen_pows;       /* n */
@@ -673,6 +674,7 @@ io_pack *io_pack_new(const io_ctx *c, int gamma, const uint8_t w_seed[32],
   if (gamma < 1) return NULL;
   io_pack *pk = (io_pack *)calloc(1, sizeof(io_pack));
   pk->c = c;
+  pk->n = n;
   pk->gamma = gamma;
   pk->mode = mode;
   memcpy(pk->w_seed, w_seed, 32);
@@ -743,7 +745,7 @@ io_pack *io_pack_new(const io_ctx *c, int gamma, const uint8_t w_seed[32],
 
 void io_pack_free(io_pack *pk) {
   if (!pk) return;
-  for (int i = 0; i < pk->c->n; i++) free(pk->tables[i]);
+  for (int i = 0; i < pk->n; i++) free(pk->tables[i]);
   free(pk->tables);
   free(pk->gen_pows);
   free(pk->mod_inv_ntt);
