@@ -147,6 +147,44 @@ def cpu_baseline(ctx, pack, db_raw, pool, budget_s=12.0, max_queries=200):
     return done / dt, done, dt
 
 
+def kernel_microbench(inspire, crs, torch, dev, reps=20):
+    """Kernel microbenchmark configuration: batched NTT / inverse NTT over both
+    CRT moduli on 4096 seeded uniform polynomials (u32), and RGSW x RLWE
+    external products on 1024 seeded pairs, in the crate's data semantics."""
+    q = crs.params.crt_moduli
+    g = torch.Generator(device="cpu").manual_seed(4)
+    polys = torch.stack([torch.randint(0, q[0], (4096, N), generator=g, dtype=torch.int64),
+                         torch.randint(0, q[1], (4096, N), generator=g, dtype=torch.int64)], 1).to(torch.int32).to(dev)
+    cts = torch.stack([torch.randint(0, q[0], (1024, 2, N), generator=g, dtype=torch.int64),
+                       torch.randint(0, q[1], (1024, 2, N), generator=g, dtype=torch.int64)], 2).to(torch.int32).to(dev)
+    rg = torch.stack([torch.randint(0, q[0], (1024, 6, 2, N), generator=g, dtype=torch.int64),
+                      torch.randint(0, q[1], (1024, 6, 2, N), generator=g, dtype=torch.int64)], 3).to(torch.int32).to(dev)
+    out = torch.empty_like(cts)
+    st = torch.cuda.current_stream(dev)
+    sp = st.cuda_stream
+    res = {}
+    for name, fn in (("ntt_forward_4096x2", lambda: inspire.ntt_forward_device(crs, polys.data_ptr(), 4096, sp)),
+                     ("ntt_inverse_4096x2", lambda: inspire.ntt_inverse_device(crs, polys.data_ptr(), 4096, sp)),
+                     ("external_product_1024", lambda: inspire.external_product_device(
+                         crs, cts.data_ptr(), rg.data_ptr(), out.data_ptr(), 1024, sp))):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        res[name + "_us"] = e0.elapsed_time(e1) * 1e3 / reps
+    # bytes moved per NTT launch: read + write of 4096 x 2 x 2048 u32
+    byts = 2 * 4096 * 2 * N * 4
+    res["ntt_forward_gbs"] = byts / (res["ntt_forward_4096x2_us"] * 1e-6) / 1e9
+    res["transforms_per_s"] = 8192 / (res["ntt_forward_4096x2_us"] * 1e-6)
+    res["external_products_per_s"] = 1024 / (res["external_product_1024_us"] * 1e-6)
+    return res
+
+
 def reference_arm(args):
     """The crate's Respond path restated on the host cores: respond_seeded_inspiring
     exactly as respond.rs:391-398 runs it, including PackParams::new (brute-force
@@ -333,6 +371,8 @@ def main():
         torch.cuda.synchronize()
         sweep[str(bs)] = bs * reps / (e0.elapsed_time(e1) / 1e3)
 
+    micro = kernel_microbench(inspire, crs, torch, dev)
+
     # end to end through the host-buffer C ABI call, pinned host memory
     h_seeds = torch.empty((B, 6, 32), dtype=torch.uint8, pin_memory=True)
     h_brows = torch.empty((B, 6, 2 * N), dtype=torch.int64, pin_memory=True)
@@ -392,6 +432,7 @@ def main():
             "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
             "plain_single_query_qps": sweep.get("1"),
+            "kernel_microbench": micro,
             "wall_s_timed_region": wall,
         }
         print(json.dumps(line), flush=True)

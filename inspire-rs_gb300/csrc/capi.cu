@@ -411,7 +411,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     delete c;
     return fail(INSPIRE_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
   }
-  // tables per residue: fwd_w, fwd_wp, inv_w, inv_wp (N each), psi_pow (2N)
+  // tables per residue: fwd pairs (2N words), inv pairs (2N words), psi_pow (2N)
   const size_t per = 6 * (size_t)N;
   std::vector<uint32_t> host(2 * per);
   DevParams& P = c->P;
@@ -422,10 +422,10 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     const uint64_t psi = find_psi(2 * N, qm), psi_inv = inv_prime(psi, qm);
     for (int k = 1; k < N; k++) {
       const uint64_t w = powmod(psi, brv(k, LOGN), qm), wi = powmod(psi_inv, brv(k, LOGN), qm);
-      t[k] = (uint32_t)w;
-      t[N + k] = shoup(w, qm);
-      t[2 * N + k] = (uint32_t)wi;
-      t[3 * N + k] = shoup(wi, qm);
+      t[2 * k] = (uint32_t)w;
+      t[2 * k + 1] = shoup(w, qm);
+      t[2 * N + 2 * k] = (uint32_t)wi;
+      t[2 * N + 2 * k + 1] = shoup(wi, qm);
     }
     uint64_t pw = 1;
     for (int k = 0; k < 2 * N; k++) {
@@ -479,10 +479,8 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
   }
   for (int r = 0; r < 2; r++) {
     const uint32_t* base = c->tables.as<uint32_t>() + r * per;
-    P.r[r].fwd_w = base;
-    P.r[r].fwd_wp = base + N;
-    P.r[r].inv_w = base + 2 * N;
-    P.r[r].inv_wp = base + 3 * N;
+    P.r[r].fwd = reinterpret_cast<const uint2*>(base);
+    P.r[r].inv = reinterpret_cast<const uint2*>(base + 2 * N);
     P.r[r].psi_pow = base + 4 * N;
   }
   *out = c;

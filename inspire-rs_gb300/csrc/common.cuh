@@ -22,10 +22,8 @@ constexpr int MODE_CRT_FIXED = 1;  // permutation applied to both residues
 
 struct ResidueConsts {
   uint32_t q, qinv;                  // qinv = -q^-1 mod 2^32
-  const uint32_t* fwd_w;             // psi^brv(k), k in [1, n)
-  const uint32_t* fwd_wp;
-  const uint32_t* inv_w;             // psi^-brv(k)
-  const uint32_t* inv_wp;
+  const uint2* fwd;                  // {psi^brv(k), Shoup companion}, k in [1, n)
+  const uint2* inv;                  // {psi^-brv(k), Shoup companion}
   const uint32_t* psi_pow;           // psi^e, e in [0, 2n)
   uint32_t r64, r64_p;               // 2^64 mod q: reference Montgomery factor
   uint32_t ref_inv_scale, ref_inv_scale_p;  // n^-1 * 2^-64 mod q
@@ -47,8 +45,8 @@ struct DevParams {
   int mode;
 };
 
-__device__ __forceinline__ TwiddleRef fwd_tw(const ResidueConsts& c) { return {c.fwd_w, c.fwd_wp}; }
-__device__ __forceinline__ TwiddleRef inv_tw(const ResidueConsts& c) { return {c.inv_w, c.inv_wp}; }
+__device__ __forceinline__ TwiddleRef fwd_tw(const ResidueConsts& c) { return {c.fwd}; }
+__device__ __forceinline__ TwiddleRef inv_tw(const ResidueConsts& c) { return {c.inv}; }
 
 __device__ __forceinline__ uint32_t brv11(uint32_t x) { return __brev(x) >> (32 - LOGN); }
 

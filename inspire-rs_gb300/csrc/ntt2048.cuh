@@ -6,14 +6,21 @@
 // primitive 2n-th root (first g >= 2 with g^((q-1)/2n) of order 2n,
 // ntt.rs:525-538); the inverse is its exact inverse.  Values here are plain
 // residues (no Montgomery factor); callers fold constant factors (R = 2^64 of
-// the reference form, n^-1) into loads or twiddle-free scalings.
+// the reference form, n^-1) into loads or scalings.
+//
+// Butterflies keep values lazily reduced (Harvey's bounds, q < 2^30): the
+// forward transform takes inputs in [0, 4q) and returns values in [0, 4q); the
+// inverse takes [0, 2q) and returns [0, 2q).  canon4 / canon2 bring them to
+// [0, q).  Twiddles are read as {w, floor(w * 2^32 / q)} pairs (one 64-bit
+// load).
 //
 // Data layout per thread x (0..127) of the group:
 //   "coefficient layout" (forward input, inverse output): v[r] = a[x + 128 r]
 //   "slot layout" (forward output, inverse input):        v[r] = A[16 x + r]
-// Stages 0-3 and 8-10 run in registers; two exchanges through a per-group
-// shared-memory scratch of NTT_SCRATCH words re-pair the values for stages
-// 4-7 and 8-10.  The two padded index maps keep every exchange free of bank
+// Stages 0-3, 4-7 and 8-10 run in registers, each reading its thread's run
+// of consecutive twiddle pairs with 128-bit loads; two exchanges through a
+// per-group shared-memory scratch of NTT_SCRATCH words re-pair the values
+// between the phases.  Both padded index maps keep the exchanges free of bank
 // conflicts.
 #pragma once
 #include <cstdint>
@@ -23,7 +30,7 @@
 namespace ig {
 
 constexpr int NTT_N = 2048;
-constexpr int NTT_GT = 128;   // threads per group
+constexpr int NTT_GT = 128;  // threads per group
 constexpr int NTT_SCRATCH = NTT_N + 128;
 
 __device__ __forceinline__ int pad_a(int j) { return j + ((j >> 7) << 3); }
@@ -35,41 +42,89 @@ __device__ __forceinline__ void group_sync(int id) {
 }
 
 struct TwiddleRef {
-  const uint32_t* __restrict__ w;   // w[k] = psi^(+-brv(k)), k in [1, n)
-  const uint32_t* __restrict__ wp;  // Shoup companions floor(w * 2^32 / q)
+  const uint2* __restrict__ w;  // w[k] = {psi^(+-brv(k)), floor(w * 2^32 / q)}, k in [1, n)
 };
 
-__device__ __forceinline__ void ct_bfly(uint32_t& a, uint32_t& b, uint32_t w, uint32_t wp,
-                                        uint32_t q) {
-  uint32_t t = mul_shoup(b, w, wp, q);
-  uint32_t u = a;
-  a = add_mod(u, t, q);
-  b = sub_mod(u, t, q);
+// a * w mod q up to one q: result in [0, 2q) for any a < 2^32.
+__device__ __forceinline__ uint32_t mul_shoup_lazy(uint32_t a, uint2 w, uint32_t q) {
+  const uint32_t h = __umulhi(a, w.y);
+  return a * w.x - h * q;
 }
 
-__device__ __forceinline__ void gs_bfly(uint32_t& a, uint32_t& b, uint32_t w, uint32_t wp,
-                                        uint32_t q) {
-  uint32_t u = a, v = b;
-  a = add_mod(u, v, q);
-  b = mul_shoup(sub_mod(u, v, q), w, wp, q);
+// Cooley-Tukey butterfly, inputs and outputs in [0, 4q).
+__device__ __forceinline__ void ct_bfly(uint32_t& a, uint32_t& b, uint2 w, uint32_t q, uint32_t q2) {
+  const uint32_t x = min(a, a - q2);
+  const uint32_t t = mul_shoup_lazy(b, w, q);
+  a = x + t;
+  b = x - t + q2;
 }
 
-// Forward transform (Cooley-Tukey, decimation in time), coefficient layout in,
-// slot layout out.  `sc` is this group's scratch; `bar` its barrier id.
-__device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef tw, uint32_t q,
-                                        int x, int bar) {
-  // stages 0..3: element r is a[x + 128 r]; pair distance 8 >> s in r
+// Gentleman-Sande butterfly, inputs and outputs in [0, 2q).
+__device__ __forceinline__ void gs_bfly(uint32_t& a, uint32_t& b, uint2 w, uint32_t q, uint32_t q2) {
+  const uint32_t u = a, v = b;
+  const uint32_t s = u + v;
+  a = min(s, s - q2);
+  b = mul_shoup_lazy(u - v + q2, w, q);
+}
+
+__device__ __forceinline__ uint32_t canon4(uint32_t x, uint32_t q) {
+  x = min(x, x - 2 * q);
+  return min(x, x - q);
+}
+
+__device__ __forceinline__ uint32_t canon2(uint32_t x, uint32_t q) { return min(x, x - q); }
+
+// Load the CNT contiguous twiddle pairs w[k0 .. k0+CNT) (k0 * 8 bytes is a
+// multiple of 16 when CNT >= 2) with 128-bit loads.
+template <int CNT>
+__device__ __forceinline__ void tw_run(TwiddleRef t, int k0, uint2 (&w)[CNT]) {
+  if (CNT == 1) {
+    w[0] = __ldg(t.w + k0);
+  } else {
+    const uint4* p = reinterpret_cast<const uint4*>(t.w + k0);
 #pragma unroll
-  for (int s = 0; s < 4; s++) {
-    const int h = 8 >> s;
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-      if ((r & h) == 0) {
-        const int k = (1 << s) + (r >> (4 - s));
-        ct_bfly(v[r], v[r + h], __ldg(tw.w + k), __ldg(tw.wp + k), q);
-      }
+    for (int i = 0; i < CNT / 2; i++) {
+      const uint4 v = __ldg(p + i);
+      w[2 * i] = make_uint2(v.x, v.y);
+      w[2 * i + 1] = make_uint2(v.z, v.w);
     }
   }
+}
+
+// One register stage.  Element r pairs with r + H when (r & H) == 0 and uses
+// twiddle run[r >> SH].
+template <int H, int SH, int CNT, bool FWD>
+__device__ __forceinline__ void reg_stage(uint32_t v[16], const uint2 (&run)[CNT], uint32_t q, uint32_t q2) {
+#pragma unroll
+  for (int r = 0; r < 16; r++) {
+    if ((r & H) == 0) {
+      if (FWD) ct_bfly(v[r], v[r + H], run[r >> SH], q, q2);
+      else gs_bfly(v[r], v[r + H], run[r >> SH], q, q2);
+    }
+  }
+}
+
+// Stage S of a register phase: element r uses twiddle (1 << S) + first +
+// (r >> SHIFT), i.e. a run of 16 >> SHIFT consecutive pairs per thread.
+template <int S, int SHIFT, bool FWD>
+__device__ __forceinline__ void stage(uint32_t v[16], TwiddleRef tw, int first, uint32_t q, uint32_t q2) {
+  constexpr int CNT = 16 >> SHIFT;
+  constexpr int H = (S < 4) ? (8 >> S) : (S < 8 ? (8 >> (S - 4)) : (4 >> (S - 8)));
+  uint2 run[CNT];
+  tw_run<CNT>(tw, (1 << S) + first, run);
+  reg_stage<H, SHIFT, CNT, FWD>(v, run, q, q2);
+}
+
+// Forward transform (Cooley-Tukey, decimation in time), coefficient layout in
+// ([0, 4q)), slot layout out ([0, 4q)).  `sc` is this group's scratch; `bar`
+// its barrier id.
+__device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef tw, uint32_t q, int x, int bar) {
+  const uint32_t q2 = 2 * q;
+  // stages 0..3: element r is a[x + 128 r]; twiddle (1 << s) + (r >> (4 - s))
+  stage<0, 4, true>(v, tw, 0, q, q2);
+  stage<1, 3, true>(v, tw, 0, q, q2);
+  stage<2, 2, true>(v, tw, 0, q, q2);
+  stage<3, 1, true>(v, tw, 0, q, q2);
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) sc[pad_a(x + 128 * r)] = v[r];
@@ -77,53 +132,31 @@ __device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef
   const int b = x >> 3, y = x & 7;
 #pragma unroll
   for (int r = 0; r < 16; r++) v[r] = sc[pad_a(128 * b + y + 8 * r)];
-  // stages 4..7: element r is a[128 b + y + 8 r]
-#pragma unroll
-  for (int s = 4; s < 8; s++) {
-    const int h = 8 >> (s - 4);
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-      if ((r & h) == 0) {
-        const int k = (1 << s) + (b << (s - 4)) + (r >> (8 - s));
-        ct_bfly(v[r], v[r + h], __ldg(tw.w + k), __ldg(tw.wp + k), q);
-      }
-    }
-  }
+  // stages 4..7: element r is a[128 b + y + 8 r]; twiddle (1 << s) + (b << (s - 4)) + (r >> (8 - s))
+  stage<4, 4, true>(v, tw, b, q, q2);
+  stage<5, 3, true>(v, tw, b << 1, q, q2);
+  stage<6, 2, true>(v, tw, b << 2, q, q2);
+  stage<7, 1, true>(v, tw, b << 3, q, q2);
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) sc[pad_b(128 * b + y + 8 * r)] = v[r];
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) v[r] = sc[pad_b(16 * x + r)];
-  // stages 8..10: element r is a[16 x + r]
-#pragma unroll
-  for (int s = 8; s < 11; s++) {
-    const int h = 4 >> (s - 8);
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-      if ((r & h) == 0) {
-        const int k = (1 << s) + (x << (s - 7)) + (r >> (11 - s));
-        ct_bfly(v[r], v[r + h], __ldg(tw.w + k), __ldg(tw.wp + k), q);
-      }
-    }
-  }
+  // stages 8..10: element r is a[16 x + r]; twiddle (1 << s) + (x << (s - 7)) + (r >> (11 - s))
+  stage<8, 3, true>(v, tw, x << 1, q, q2);
+  stage<9, 2, true>(v, tw, x << 2, q, q2);
+  stage<10, 1, true>(v, tw, x << 3, q, q2);
 }
 
 // Inverse transform without the n^-1 factor (Gentleman-Sande, decimation in
-// frequency), slot layout in, coefficient layout out.
-__device__ __forceinline__ void ntt_inv_noscale(uint32_t v[16], uint32_t* sc, TwiddleRef tw,
-                                                uint32_t q, int x, int bar) {
-#pragma unroll
-  for (int s = 10; s >= 8; s--) {
-    const int h = 4 >> (s - 8);
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-      if ((r & h) == 0) {
-        const int k = (1 << s) + (x << (s - 7)) + (r >> (11 - s));
-        gs_bfly(v[r], v[r + h], __ldg(tw.w + k), __ldg(tw.wp + k), q);
-      }
-    }
-  }
+// frequency), slot layout in ([0, 2q)), coefficient layout out ([0, 2q)).
+__device__ __forceinline__ void ntt_inv_noscale(uint32_t v[16], uint32_t* sc, TwiddleRef tw, uint32_t q, int x,
+                                                int bar) {
+  const uint32_t q2 = 2 * q;
+  stage<10, 1, false>(v, tw, x << 3, q, q2);
+  stage<9, 2, false>(v, tw, x << 2, q, q2);
+  stage<8, 3, false>(v, tw, x << 1, q, q2);
   const int b = x >> 3, y = x & 7;
   group_sync(bar);
 #pragma unroll
@@ -131,34 +164,46 @@ __device__ __forceinline__ void ntt_inv_noscale(uint32_t v[16], uint32_t* sc, Tw
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) v[r] = sc[pad_b(128 * b + y + 8 * r)];
-#pragma unroll
-  for (int s = 7; s >= 4; s--) {
-    const int h = 8 >> (s - 4);
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-      if ((r & h) == 0) {
-        const int k = (1 << s) + (b << (s - 4)) + (r >> (8 - s));
-        gs_bfly(v[r], v[r + h], __ldg(tw.w + k), __ldg(tw.wp + k), q);
-      }
-    }
-  }
+  stage<7, 1, false>(v, tw, b << 3, q, q2);
+  stage<6, 2, false>(v, tw, b << 2, q, q2);
+  stage<5, 3, false>(v, tw, b << 1, q, q2);
+  stage<4, 4, false>(v, tw, b, q, q2);
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) sc[pad_a(128 * b + y + 8 * r)] = v[r];
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) v[r] = sc[pad_a(x + 128 * r)];
+  stage<3, 1, false>(v, tw, 0, q, q2);
+  stage<2, 2, false>(v, tw, 0, q, q2);
+  stage<1, 3, false>(v, tw, 0, q, q2);
+  stage<0, 4, false>(v, tw, 0, q, q2);
+}
+
+// Slot-layout arrays in shared memory are stored with this XOR swizzle, which
+// moves 4-word chunks inside each 16-word block so that the 128-bit accesses
+// of load16/store16 (thread x: words 16x..16x+15) hit eight distinct bank
+// groups per quarter warp, while single-word accesses of 32 consecutive slots
+// stay conflict-free.
+__device__ __forceinline__ int swz(int s) { return s ^ (((s >> 5) & 3) << 2); }
+
+__device__ __forceinline__ void load16(const uint32_t* base, int x, uint32_t v[16]) {
+  const int f = (x >> 1) & 3;
 #pragma unroll
-  for (int s = 3; s >= 0; s--) {
-    const int h = 8 >> s;
-#pragma unroll
-    for (int r = 0; r < 16; r++) {
-      if ((r & h) == 0) {
-        const int k = (1 << s) + (r >> (4 - s));
-        gs_bfly(v[r], v[r + h], __ldg(tw.w + k), __ldg(tw.wp + k), q);
-      }
-    }
+  for (int r4 = 0; r4 < 4; r4++) {
+    const uint4 t = *reinterpret_cast<const uint4*>(base + 16 * x + 4 * (r4 ^ f));
+    v[4 * r4] = t.x;
+    v[4 * r4 + 1] = t.y;
+    v[4 * r4 + 2] = t.z;
+    v[4 * r4 + 3] = t.w;
   }
+}
+
+__device__ __forceinline__ void store16(uint32_t* base, int x, const uint32_t v[16]) {
+  const int f = (x >> 1) & 3;
+#pragma unroll
+  for (int r4 = 0; r4 < 4; r4++)
+    *reinterpret_cast<uint4*>(base + 16 * x + 4 * (r4 ^ f)) = make_uint4(v[4 * r4], v[4 * r4 + 1], v[4 * r4 + 2], v[4 * r4 + 3]);
 }
 
 }  // namespace ig

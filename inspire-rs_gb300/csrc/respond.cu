@@ -93,7 +93,7 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
       uint32_t w[16];
       chacha20_block(key, blk + lt, w);
 #pragma unroll
-      for (int k = 0; k < 8; k++) cand[8 * lt + k] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
+      for (int k = 0; k < 8; k++) cand[k * SUB + lt] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
     }
     blk += nblk;
     named_sync(bar, SUB);
@@ -105,7 +105,7 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
       if (lt < nblk) {
 #pragma unroll
         for (int k = 0; k < 8; k++)
-          if (uniform_accept(cand[8 * lt + k], P.r[0].q, P.r[0].zone, vals[k])) {
+          if (uniform_accept(cand[k * SUB + lt], P.r[0].q, P.r[0].zone, vals[k])) {
             fl |= 1u << k;
             cnt++;
           }
@@ -138,7 +138,7 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
       if (lt < nblk) {
 #pragma unroll
         for (int k = 0; k < 8; k++)
-          if (8 * lt + k >= start && uniform_accept(cand[8 * lt + k], P.r[1].q, P.r[1].zone, vals[k])) {
+          if (8 * lt + k >= start && uniform_accept(cand[k * SUB + lt], P.r[1].q, P.r[1].zone, vals[k])) {
             fl |= 1u << k;
             cnt++;
           }
@@ -159,27 +159,41 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
   return false;
 }
 
-// b0_c for every column c and residue (see file comment).  bp (6N words) and
-// red (NWARP*16*2 u64) are scratch; bpoly[r * 16 + c] receives the result.
+// b0_c for every column c and residue (see file comment).  bp (6N words) is
+// scratch; bpoly[r * 16 + c] receives the result.  Warp c handles column c:
+// each lane reads its 64 coefficients with eight 128-bit loads issued up
+// front, so the shard's raw column is fetched with one memory latency.
 __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* __restrict__ brows,
-                          uint32_t* bp, uint64_t* red, uint32_t* bpoly) {
+                          uint32_t* bp, uint32_t* bpoly) {
   const int tid = threadIdx.x, gamma = P.gamma;
+#pragma unroll 8
   for (int idx = tid; idx < ELL * 2 * N; idx += RBLOCK) {
     const int i = idx & (N - 1), tr = idx >> LOGN, r = tr & 1;
     const uint64_t* row = brows + (size_t)tr * N;
-    uint32_t v = (uint32_t)(i == 0 ? row[0] : row[N - i]);
+    uint32_t v = (uint32_t)__ldg(row + (i == 0 ? 0 : N - i));
     if (i != 0 && v != 0) v = P.r[r].q - v;
     bp[idx] = v;
   }
   __syncthreads();
-  const int lane = tid & 31, warp = tid >> 5;
-  for (int c = 0; c < gamma; c++) {
+  const int lane = tid & 31, c = tid >> 5;
+  if (c < gamma) {
+    const uint4* h4 = reinterpret_cast<const uint4*>(H + (size_t)c * N);
+    uint4 hv[8];
+#pragma unroll
+    for (int m = 0; m < 8; m++) hv[m] = __ldg(h4 + lane + 32 * m);
     uint64_t acc0 = 0, acc1 = 0;
-    for (int i = tid; i < N; i += RBLOCK) {
-      const uint64_t xv = P.delta * (uint64_t)H[c * N + i];
-      const uint32_t d0 = (uint32_t)xv & 0xFFFFFu, d1 = (uint32_t)(xv >> 20) & 0xFFFFFu, d2 = (uint32_t)(xv >> 40);
-      acc0 += (uint64_t)d0 * bp[0 * N + i] + (uint64_t)d1 * bp[2 * N + i] + (uint64_t)d2 * bp[4 * N + i];
-      acc1 += (uint64_t)d0 * bp[1 * N + i] + (uint64_t)d1 * bp[3 * N + i] + (uint64_t)d2 * bp[5 * N + i];
+#pragma unroll
+    for (int m = 0; m < 8; m++) {
+      const uint32_t hw[4] = {hv[m].x, hv[m].y, hv[m].z, hv[m].w};
+      const int i0 = 8 * (lane + 32 * m);
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const int i = i0 + e;
+        const uint64_t xv = P.delta * (uint64_t)((hw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);
+        const uint32_t d0 = (uint32_t)xv & 0xFFFFFu, d1 = (uint32_t)(xv >> 20) & 0xFFFFFu, d2 = (uint32_t)(xv >> 40);
+        acc0 += (uint64_t)d0 * bp[0 * N + i] + (uint64_t)d1 * bp[2 * N + i] + (uint64_t)d2 * bp[4 * N + i];
+        acc1 += (uint64_t)d0 * bp[1 * N + i] + (uint64_t)d1 * bp[3 * N + i] + (uint64_t)d2 * bp[5 * N + i];
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -187,18 +201,20 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
       acc1 += __shfl_down_sync(0xffffffffu, acc1, o);
     }
     if (lane == 0) {
-      red[(c * NWARP + warp) * 2 + 0] = acc0;
-      red[(c * NWARP + warp) * 2 + 1] = acc1;
+      bpoly[c] = (uint32_t)(acc0 % P.r[0].q);
+      bpoly[16 + c] = (uint32_t)(acc1 % P.r[1].q);
     }
   }
   __syncthreads();
-  if (tid < 2 * gamma) {
-    const int c = tid >> 1, r = tid & 1;
-    uint64_t s = 0;
-    for (int w = 0; w < NWARP; w++) s += red[(c * NWARP + w) * 2 + r];
-    bpoly[r * 16 + c] = (uint32_t)(s % P.r[r].q);
+}
+
+// L2 prefetch of a contiguous device range with bulk (TMA) prefetches.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+  const char* c = static_cast<const char*>(p);
+  for (size_t off = 0; off < bytes; off += 65536) {
+    const uint32_t sz = (uint32_t)(bytes - off < 65536 ? bytes - off : 65536);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(c + off), "r"(sz) : "memory");
   }
-  __syncthreads();
 }
 
 // R_i (NTT domain, scaled by n^-1) of packing_offline step 1 for one residue,
@@ -216,29 +232,12 @@ __device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint3
     const uint32_t e = 2 * brv11(u) + 1;
     const uint32_t k = (e * mi) & (uint32_t)(gamma - 1);
     const uint32_t* ek = Eg + (size_t)k * N + u;
-    const uint64_t T = (uint64_t)__ldg(ek) * Ag[u] + (uint64_t)__ldg(ek + (size_t)gamma * N) * Ag[astride + u] +
-                       (uint64_t)__ldg(ek + (size_t)2 * gamma * N) * Ag[2 * astride + u];
+    const int us = swz(u);
+    const uint64_t T = (uint64_t)__ldg(ek) * Ag[us] + (uint64_t)__ldg(ek + (size_t)gamma * N) * Ag[astride + us] +
+                       (uint64_t)__ldg(ek + (size_t)2 * gamma * N) * Ag[2 * astride + us];
     const uint32_t s = brv11(((hi * e) & (2 * N - 1)) >> 1);
-    dst[s] = redc(T, q, qinv);
+    dst[swz(s)] = redc(T, q, qinv);
   }
-}
-
-__device__ __forceinline__ void load16(const uint32_t* __restrict__ src, uint32_t v[16]) {
-  const uint4* s4 = reinterpret_cast<const uint4*>(src);
-#pragma unroll
-  for (int r = 0; r < 4; r++) {
-    const uint4 t = s4[r];
-    v[4 * r] = t.x;
-    v[4 * r + 1] = t.y;
-    v[4 * r + 2] = t.z;
-    v[4 * r + 3] = t.w;
-  }
-}
-
-__device__ __forceinline__ void store16(uint32_t* dst, const uint32_t v[16]) {
-  uint4* d4 = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-  for (int r = 0; r < 4; r++) d4[r] = make_uint4(v[4 * r], v[4 * r + 1], v[4 * r + 2], v[4 * r + 3]);
 }
 
 // Shared-memory layout in u32 words (NR = residues of the a side).
@@ -247,14 +246,15 @@ struct Smem {
   static constexpr int AHAT = 0;                           // [ELL][NR][N]
   static constexpr int SC = AHAT + ELL * NR * N;           // [RG][NTT_SCRATCH]
   static constexpr int T = SC + RG * NTT_SCRATCH;          // [3][N] digits (T0/T1 also hold the INTT output)
-  static constexpr int SCAT = T + 3 * N;                   // [2][2][N] R_i, double buffered
-  static constexpr int PB = SCAT + 4 * N;                  // [2][2][N] partial products of digits 1, 2
-  static constexpr int MISC = PB + 4 * N;                  // bpoly[32], ws[3][20]
+  static constexpr int SCAT = T + 3 * N;                   // [2][N] R_i (slot layout, swizzled)
+  static constexpr int PB = SCAT + 2 * N;                  // [2][2][N] partial products of digits 1, 2
+  static constexpr int ACC = PB + 4 * N;                   // [RG][N] per-group b accumulators
+  static constexpr int MISC = ACC + RG * N;                // bpoly[32], ws[3][20]
   static constexpr int TOTAL = MISC + 128;
 };
 
 template <int MODE, bool SEEDED>
-__global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A) {
+__global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constant__ RespondArgs A) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
   using L = Smem<NR>;
   extern __shared__ __align__(16) uint32_t smem[];
@@ -270,6 +270,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A)
   const int qi = blockIdx.x;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
   const int r = g / 3, kd = g - 3 * r;  // residue, gadget digit of this group
+  uint32_t* ACC = smem + L::ACC + g * N;  // this group's b accumulator
   const int gamma = P.gamma;
   const uint32_t shard = A.shard[qi];
   const int32_t cid = A.client[qi];
@@ -283,8 +284,16 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A)
   const uint32_t* Y = A.yhat_table[cid];
   const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
 
-  // ---- b part of the column products (bp aliases SCAT+PB, red aliases T) ----
-  column_b0(P, H, A.brows + (size_t)qi * ELL * 2 * N, SCAT, (uint64_t*)T, bpoly);
+  // stream this query's shard (contracted form of the a side, raw columns)
+  // and client key table into L2 while the prologue runs
+  if (tid == 0) {
+    prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
+    prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
+    if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
+  }
+
+  // ---- b part of the column products (bp aliases SCAT+PB) ----
+  column_b0(P, H, A.brows + (size_t)qi * ELL * 2 * N, SCAT, bpoly);
 
   // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
   {
@@ -308,7 +317,9 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A)
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = src[x + 128 * j];
     ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
-    store16(Ahat + (kd * NR + r) * N + 16 * x, v);
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = canon4(v[j], q);
+    store16(Ahat + (kd * NR + r) * N, x, v);
   }
   __syncthreads();
 
@@ -322,29 +333,31 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A)
   const uint32_t* Ag = Ahat + sres * N;
   const uint32_t sq = P.r[sres].q, sqinv = P.r[sres].qinv;
 
-  uint32_t vR[16], accb[16];
-#pragma unroll
-  for (int j = 0; j < 16; j++) accb[j] = 0;
+  uint32_t vR[16];
+  {
+    const uint32_t zero[16] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    store16(ACC, x, zero);
+  }
 
   // R_{gamma-1}
-  if (scatters) scatter_r(P, gamma - 1, Eg, Ag, NR * N, SCAT + (((gamma - 1) & 1) * 2 + sres) * N, sp, snthr, sq, sqinv);
+  if (scatters) scatter_r(P, gamma - 1, Eg, Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
   __syncthreads();
   if (kd == 0) {
-    const uint32_t* src = SCAT + (((gamma - 1) & 1) * 2 + (MODE == MODE_CRT_FIXED ? r : 0)) * N + 16 * x;
-    load16(src, vR);
+    load16(SCAT + (MODE == MODE_CRT_FIXED ? r : 0) * N, x, vR);
     if (MODE == MODE_COMPAT && r == 1)
 #pragma unroll
       for (int j = 0; j < 16; j++) vR[j] = compat_residue1_ninv(P, vR[j]);
   }
+  __syncthreads();  // the scatter buffer is reused by the first step
 
   for (int i = gamma - 2; i >= 0; i--) {
     // [A] INTT(R_{i+1}) by groups (r,0); scatter of R_i by the others
     if (kd == 0) {
       ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
-      for (int j = 0; j < 16; j++) T[r * N + x + 128 * j] = vR[j];
+      for (int j = 0; j < 16; j++) T[r * N + x + 128 * j] = canon2(vR[j], q);
     } else {
-      scatter_r(P, i, Eg, Ag, NR * N, SCAT + ((i & 1) * 2 + sres) * N, sp, snthr, sq, sqinv);
+      scatter_r(P, i, Eg, Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
     }
     __syncthreads();
     // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37)
@@ -355,71 +368,106 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const RespondArgs A)
       T[2 * N + j] = (uint32_t)(c >> 40);
     }
     __syncthreads();
-    // [C] group (r,k): NTT of digit k mod q_r, products with w_all[i][k] and y_all[i][k]
-    uint32_t v[16], acc[16];
-#pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
-    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    // [C] group (r,k): NTT of digit k mod q_r, products with w_all[i][k]
+    //     (R_i accumulator) and y_all[i][k] (b accumulator)
+    uint32_t v[16];
+    const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
+    // the key slices of this step are fetched before the transform so their
+    // L2 latency overlaps it
+    uint4 wv[4], yv[4];
     {
-      const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
       const uint4* w4 = reinterpret_cast<const uint4*>(A.what + off);
       const uint4* y4 = reinterpret_cast<const uint4*>(Y + off);
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
-        const uint4 wv = __ldg(w4 + r4), yv = __ldg(y4 + r4);
-        const uint32_t ww[4] = {wv.x, wv.y, wv.z, wv.w}, yy[4] = {yv.x, yv.y, yv.z, yv.w};
+        wv[r4] = __ldg(w4 + r4);
+        yv[r4] = __ldg(y4 + r4);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    {
+      const int f = (x >> 1) & 3;
+      uint32_t* accp = ACC + 16 * x;
+      const uint32_t* sb = SCAT + (MODE == MODE_CRT_FIXED ? r : 0) * N + 16 * x;
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        const uint32_t ww[4] = {wv[r4].x, wv[r4].y, wv[r4].z, wv[r4].w};
+        const uint32_t yy[4] = {yv[r4].x, yv[r4].y, yv[r4].z, yv[r4].w};
+        uint4* ap = reinterpret_cast<uint4*>(accp + 4 * (r4 ^ f));
+        const uint4 a4 = *ap;
+        uint32_t ab[4] = {a4.x, a4.y, a4.z, a4.w};
+        uint32_t hh[4] = {0, 0, 0, 0};
+        if (kd == 0) {
+          const uint4 h4 = *reinterpret_cast<const uint4*>(sb + 4 * (r4 ^ f));
+          hh[0] = h4.x; hh[1] = h4.y; hh[2] = h4.z; hh[3] = h4.w;
+        }
 #pragma unroll
         for (int e = 0; e < 4; e++) {
           const int j = 4 * r4 + e;
-          acc[j] = redc_lazy((uint64_t)v[j] * ww[e], q, qinv);
-          accb[j] = acc_2q(accb[j], redc_lazy((uint64_t)v[j] * yy[e], q, qinv), q2);
+          ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v[j] * yy[e], q, qinv), q2);
+          uint32_t pr = redc_lazy((uint64_t)v[j] * ww[e], q, qinv);  // [0, 2q)
+          if (kd == 0) {
+            const uint32_t h = (MODE == MODE_COMPAT && r == 1) ? compat_residue1_ninv(P, hh[e]) : hh[e];
+            pr += h;  // [0, 3q)
+          }
+          v[j] = pr;
         }
+        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
       }
     }
-    if (kd != 0) store16(PB + (r * 2 + kd - 1) * N + 16 * x, acc);
+    if (kd != 0) store16(PB + (r * 2 + kd - 1) * N, x, v);
     __syncthreads();
     // [D] R_i = scatter + sum_k products, by groups (r,0)
     if (kd == 0) {
-      uint32_t rh[16], p1[16], p2[16];
-      load16(SCAT + ((i & 1) * 2 + (MODE == MODE_CRT_FIXED ? r : 0)) * N + 16 * x, rh);
-      load16(PB + (r * 2 + 0) * N + 16 * x, p1);
-      load16(PB + (r * 2 + 1) * N + 16 * x, p2);
+      const int f = (x >> 1) & 3;
+      const uint32_t* pb0 = PB + (r * 2 + 0) * N + 16 * x;
+      const uint32_t* pb1 = PB + (r * 2 + 1) * N + 16 * x;
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        uint32_t h = (MODE == MODE_COMPAT && r == 1) ? compat_residue1_ninv(P, rh[j]) : rh[j];
-        uint32_t s = h + acc[j] + p1[j] + p2[j];  // < 7q < 2^31
-        s = min(s, s - 4 * q);
-        s = min(s, s - 2 * q);
-        vR[j] = min(s, s - q);
+      for (int r4 = 0; r4 < 4; r4++) {
+        const int o = 4 * (r4 ^ f);
+        const uint4 a4 = *reinterpret_cast<const uint4*>(pb0 + o);
+        const uint4 b4 = *reinterpret_cast<const uint4*>(pb1 + o);
+        const uint32_t aa[4] = {a4.x, a4.y, a4.z, a4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int j = 4 * r4 + e;
+          uint32_t sum = v[j] + aa[e] + bb[e];  // < 7q < 2^31
+          sum = min(sum, sum - 4 * q);
+          sum = min(sum, sum - 2 * q);
+          vR[j] = min(sum, sum - q);
+        }
       }
     }
   }
 
   // ---- outputs: a_hat = INTT(R_0) (inspiring2.rs:1027-1029),
   //      b = b_poly + INTT(sum y_all * bold_t) (inspiring2.rs:1217-1221) ----
-  __syncthreads();  // groups (r,0) have finished reading PB in the last step
-  if (kd != 1) store16(PB + (r * 2 + (kd == 0 ? 0 : 1)) * N + 16 * x, accb);
-  __syncthreads();
+  // (the b accumulators were last written before the final barrier)
   uint64_t* out = A.out + (size_t)qi * 4 * N;
   if (kd == 0) {
     ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
-    for (int j = 0; j < 16; j++) out[r * N + x + 128 * j] = vR[j];
+    for (int j = 0; j < 16; j++) out[r * N + x + 128 * j] = canon2(vR[j], q);
   } else if (kd == 1) {
-    uint32_t p0[16], p2[16];
-    load16(PB + (r * 2 + 0) * N + 16 * x, p0);
-    load16(PB + (r * 2 + 1) * N + 16 * x, p2);
+    uint32_t b0[16], b1[16], b2[16];
+    load16(smem + L::ACC + (3 * r + 0) * N, x, b0);
+    load16(smem + L::ACC + (3 * r + 1) * N, x, b1);
+    load16(smem + L::ACC + (3 * r + 2) * N, x, b2);
 #pragma unroll
     for (int j = 0; j < 16; j++) {
-      uint32_t s = accb[j] + p0[j] + p2[j];  // < 6q
-      s = min(s, s - 4 * q);
-      s = min(s, s - 2 * q);
-      accb[j] = min(s, s - q);
+      uint32_t s2 = b0[j] + b1[j] + b2[j];  // < 6q
+      s2 = min(s2, s2 - 4 * q);
+      s2 = min(s2, s2 - 2 * q);
+      b0[j] = min(s2, s2 - q);
     }
-    ntt_inv_noscale(accb, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
-    if (x < gamma) accb[0] = add_mod(accb[0], bpoly[r * 16 + x], q);
+    ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
-    for (int j = 0; j < 16; j++) out[2 * N + r * N + x + 128 * j] = accb[j];
+    for (int j = 0; j < 16; j++) b0[j] = canon2(b0[j], q);
+    if (x < gamma) b0[0] = add_mod(b0[0], bpoly[r * 16 + x], q);
+#pragma unroll
+    for (int j = 0; j < 16; j++) out[2 * N + r * N + x + 128 * j] = b0[j];
   }
 }
 
