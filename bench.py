@@ -47,6 +47,9 @@ ALG_BYTES_PER_QUERY = 192 * 1024
 MULMODS_PER_QUERY = 3.4e6
 # resident database bytes one query reads: contracted form 768 KiB + raw columns 64 KiB
 DB_BYTES_PER_QUERY = (768 + 64) * 1024
+# dram__bytes_read.sum + dram__bytes_write.sum of one B=128 respond launch, from the
+# ncu capture summarised in profiles/respond_kernel_b128.md
+NCU_TRAFFIC_PER_LAUNCH_B128 = 122.9e6
 
 
 def dist_env():
@@ -424,7 +427,8 @@ def main():
                        "db_setup_s": setup_s, "db_device_bytes": resident_bytes},
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved_gbs / hbm_peak, "traffic": None,
+                         "frac": achieved_gbs / hbm_peak,
+                         "traffic": NCU_TRAFFIC_PER_LAUNCH_B128 if B == 128 else None,
                          "note": "algorithmic bytes 192 KiB/query; the kernel is integer-issue bound, see DESIGN.md"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
