@@ -143,6 +143,27 @@ int inspire_respond_seeded_inspiring(inspire_ctx *ctx, const inspire_db *db, con
 int inspire_respond_inspiring(inspire_ctx *ctx, const inspire_db *db, const inspire_query *query,
                               uint64_t *out_ct);
 
+/* respond (src/pir/respond.rs:71-115), the NoPacking variant: one external
+ * product of trivial_encrypt(column) with the query's RGSW per shard column.
+ * out_ct receives ServerResponse.ciphertext (the sum of the column
+ * ciphertexts) as [a poly, b poly]; out_columns, if not NULL, receives
+ * column_ciphertexts as [num_columns][a, b][poly].  Packing keys in the query
+ * are ignored, as in the crate. */
+int inspire_respond(inspire_ctx *ctx, const inspire_db *db, const inspire_query *query, uint64_t *out_ct,
+                    uint64_t *out_columns);
+
+/* respond_seeded (src/pir/respond.rs:408-415): SeededClientQuery::expand then
+ * respond. */
+int inspire_respond_seeded(inspire_ctx *ctx, const inspire_db *db, const inspire_seeded_query *query,
+                           uint64_t *out_ct, uint64_t *out_columns);
+
+/* Batched respond_seeded (combined ciphertexts only), host buffers laid out
+ * as for inspire_respond_seeded_batch: shard_ids[n], seeds[n][2*gadget_len][32],
+ * b_rows[n][2*gadget_len][poly], out_ct[n][2][poly]. */
+int inspire_respond_seeded_nopacking_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n,
+                                           const uint32_t *shard_ids, const uint8_t *seeds, const uint64_t *b_rows,
+                                           uint64_t *out_ct);
+
 /* Batched respond_seeded_inspiring over n queries with registered client
  * keys, host buffers: shard_ids[n], seeds[n][2*gadget_len][32],
  * b_rows[n][2*gadget_len][poly], client_ids[n], out_ct[n][2][poly].  Queries

@@ -173,7 +173,7 @@ struct inspire_ctx {
   bool client_table_dirty = true;
   // staging for host-buffer calls
   cudaStream_t stream = nullptr;
-  DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_status, d_keys;
+  DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys;
   std::vector<int32_t> h_status;
 
   ~inspire_ctx() {
@@ -316,6 +316,60 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
     if (c->h_status[i] != 0)
       return fail(INSPIRE_ERR_DEVICE_STATUS,
                   "respond kernel status " + std::to_string(c->h_status[i]) + " for query " + std::to_string(i));
+  return INSPIRE_OK;
+}
+
+// Stage n NoPacking queries (same row layout as run_batch) and run the
+// NoPacking kernel; out_columns may be null.
+int run_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
+                  size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
+                  uint64_t* out_ct, uint64_t* out_columns) {
+  if (n == 0) return INSPIRE_OK;
+  const size_t pw = poly_words();
+  const size_t col_words = (size_t)db->gamma * 2 * pw;
+  CUDA_TRY(c->d_shard.ensure(sizeof(uint32_t) * n));
+  CUDA_TRY(c->d_brows.ensure(sizeof(uint64_t) * n * ELL * pw));
+  CUDA_TRY(c->d_out.ensure(sizeof(uint64_t) * n * 2 * pw));
+  if (out_columns) CUDA_TRY(c->d_cols.ensure(sizeof(uint64_t) * n * col_words));
+  CUDA_TRY(c->d_status.ensure(sizeof(int32_t) * n));
+  CUDA_TRY(cudaMemcpyAsync(c->d_shard.p, shard_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpy2DAsync(c->d_brows.p, sizeof(uint64_t) * ELL * pw, b_rows, sizeof(uint64_t) * stride_polys * pw,
+                             sizeof(uint64_t) * ELL * pw, n, cudaMemcpyHostToDevice, c->stream));
+  const bool seeded = seeds != nullptr;
+  if (seeded) {
+    CUDA_TRY(c->d_seeds.ensure((size_t)32 * ELL * n));
+    CUDA_TRY(cudaMemcpy2DAsync(c->d_seeds.p, (size_t)32 * ELL, seeds, seed_stride, (size_t)32 * ELL, n,
+                               cudaMemcpyHostToDevice, c->stream));
+  } else {
+    CUDA_TRY(c->d_arows.ensure(sizeof(uint64_t) * n * ELL * pw));
+    CUDA_TRY(cudaMemcpy2DAsync(c->d_arows.p, sizeof(uint64_t) * ELL * pw, a_rows, sizeof(uint64_t) * stride_polys * pw,
+                               sizeof(uint64_t) * ELL * pw, n, cudaMemcpyHostToDevice, c->stream));
+  }
+  NoPackingArgs a{};
+  a.P = c->P;
+  a.nq = (int)n;
+  a.shard = c->d_shard.as<uint32_t>();
+  a.seeds = seeded ? c->d_seeds.as<uint8_t>() : nullptr;
+  a.arows = seeded ? nullptr : c->d_arows.as<uint64_t>();
+  a.brows = c->d_brows.as<uint64_t>();
+  a.nshards = db->nshards;
+  a.H = db->H.as<uint16_t>();
+  a.out = c->d_out.as<uint64_t>();
+  a.out_columns = out_columns ? c->d_cols.as<uint64_t>() : nullptr;
+  a.status = c->d_status.as<int>();
+  CUDA_TRY(launch_nopacking(a, seeded, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(out_ct, c->d_out.p, sizeof(uint64_t) * n * 2 * pw, cudaMemcpyDeviceToHost, c->stream));
+  if (out_columns)
+    CUDA_TRY(cudaMemcpyAsync(out_columns, c->d_cols.p, sizeof(uint64_t) * n * col_words, cudaMemcpyDeviceToHost,
+                             c->stream));
+  c->h_status.resize(n);
+  CUDA_TRY(cudaMemcpyAsync(c->h_status.data(), c->d_status.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                           c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (uint32_t i = 0; i < n; i++)
+    if (c->h_status[i] != 0)
+      return fail(INSPIRE_ERR_DEVICE_STATUS,
+                  "nopacking kernel status " + std::to_string(c->h_status[i]) + " for query " + std::to_string(i));
   return INSPIRE_OK;
 }
 
@@ -639,6 +693,53 @@ int inspire_respond_inspiring(inspire_ctx* c, const inspire_db* db, const inspir
   if (int rc = set_device(c)) return rc;
   return single_query(c, db, qy->shard_id, nullptr, qy->rgsw, nullptr, qy->has_packing_keys, qy->y_body,
                       qy->y_all, out_ct);
+}
+
+int inspire_respond_seeded(inspire_ctx* c, const inspire_db* db, const inspire_seeded_query* qy, uint64_t* out_ct,
+                           uint64_t* out_columns) {
+  if (!c || !db || !qy || !out_ct) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!qy->seeds || !qy->b_rows) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null query rows");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (qy->shard_id >= (uint32_t)db->nshards)
+    return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(qy->shard_id) + " not found");
+  if (int rc = set_device(c)) return rc;
+  return run_nopacking(c, db, 1, &qy->shard_id, qy->seeds + 32 * ELL, (size_t)64 * ELL, nullptr,
+                       qy->b_rows + (size_t)ELL * poly_words(), 2 * ELL, out_ct, out_columns);
+}
+
+int inspire_respond(inspire_ctx* c, const inspire_db* db, const inspire_query* qy, uint64_t* out_ct,
+                    uint64_t* out_columns) {
+  if (!c || !db || !qy || !out_ct) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!qy->rgsw) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null query rows");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (qy->shard_id >= (uint32_t)db->nshards)
+    return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(qy->shard_id) + " not found");
+  if (int rc = set_device(c)) return rc;
+  // rgsw holds 2*ELL rows of (a, b): row r's a is poly 2r, its b poly 2r+1
+  const size_t pw = poly_words();
+  std::vector<uint64_t> ar((size_t)ELL * pw), br((size_t)ELL * pw);
+  for (int t = 0; t < ELL; t++) {
+    memcpy(ar.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t)) * pw, pw * sizeof(uint64_t));
+    memcpy(br.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t) + 1) * pw, pw * sizeof(uint64_t));
+  }
+  return run_nopacking(c, db, 1, &qy->shard_id, nullptr, 0, ar.data(), br.data(), ELL, out_ct, out_columns);
+}
+
+int inspire_respond_seeded_nopacking_batch(inspire_ctx* c, const inspire_db* db, uint32_t n,
+                                           const uint32_t* shard_ids, const uint8_t* seeds, const uint64_t* b_rows,
+                                           uint64_t* out_ct) {
+  if (!c || !db || (n && (!shard_ids || !seeds || !b_rows || !out_ct)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  for (uint32_t i = 0; i < n; i++)
+    if (shard_ids[i] >= (uint32_t)db->nshards)
+      return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(shard_ids[i]) + " not found");
+  if (int rc = set_device(c)) return rc;
+  return run_nopacking(c, db, n, shard_ids, seeds + 32 * ELL, (size_t)64 * ELL, nullptr,
+                       b_rows + (size_t)ELL * poly_words(), 2 * ELL, out_ct, nullptr);
 }
 
 int inspire_respond_seeded_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,

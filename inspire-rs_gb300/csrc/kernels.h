@@ -28,6 +28,26 @@ struct RespondArgs {
   int* status;                   // [nq]
 };
 
+// NoPacking respond (respond.rs:71-115): per query the combined ciphertext
+// out[nq][2][2][N] and, if out_columns is set, every column ciphertext
+// out_columns[nq][gamma][2][2][N].
+struct NoPackingArgs {
+  DevParams P;
+  int nq;
+  const uint32_t* shard;
+  const uint8_t* seeds;          // [nq][ELL][32] or null
+  const uint64_t* arows;         // [nq][ELL][2][N] or null
+  const uint64_t* brows;         // [nq][ELL][2][N]
+  int nshards;
+  const uint16_t* H;             // [nshards][gamma][N]
+  uint64_t* out;
+  uint64_t* out_columns;
+  int* status;
+};
+
+size_t nopacking_smem_bytes();
+cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);
+
 size_t respond_smem_bytes(int mode);
 cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st);
 

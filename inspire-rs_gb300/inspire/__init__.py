@@ -16,9 +16,13 @@ from .pir import (  # noqa: F401
     external_product_device,
     ntt_forward_device,
     ntt_inverse_device,
+    respond,
     respond_inspiring,
+    respond_seeded,
     respond_seeded_batch,
     respond_seeded_batch_device,
     respond_seeded_inspiring,
+    respond_seeded_nopacking_batch,
     respond_seeded_with_variant,
+    respond_with_variant,
 )

@@ -89,6 +89,9 @@ def load(path: str = LIB_PATH):
         "inspire_client_release": (C.c_int, [vp, i32]),
         "inspire_respond_seeded_inspiring": (C.c_int, [vp, vp, C.POINTER(SeededQueryC), vp]),
         "inspire_respond_inspiring": (C.c_int, [vp, vp, C.POINTER(QueryC), vp]),
+        "inspire_respond": (C.c_int, [vp, vp, C.POINTER(QueryC), vp, vp]),
+        "inspire_respond_seeded": (C.c_int, [vp, vp, C.POINTER(SeededQueryC), vp, vp]),
+        "inspire_respond_seeded_nopacking_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
         "inspire_respond_seeded_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp]),
         "inspire_respond_seeded_batch_device": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp]),
         "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),

@@ -242,12 +242,77 @@ def respond_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query: Client
     return _response(out, plen)
 
 
+def _nopacking_response(out: np.ndarray, cols: Optional[np.ndarray], plen: int) -> ServerResponse:
+    columns = [] if cols is None else [RlweCiphertext(c[0].copy(), c[1].copy()) for c in cols]
+    return ServerResponse(RlweCiphertext(out[:plen].copy(), out[plen:].copy()), columns)
+
+
+def respond(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery,
+            with_columns: bool = True) -> ServerResponse:
+    """respond (respond.rs:71-115), the NoPacking variant: column_ciphertexts
+    holds one RLWE ciphertext per shard column (skipped when with_columns is
+    False), ciphertext their sum."""
+    plen = crs.params.plen
+    ell = crs.params.gadget_len
+    rgsw = _u64(query.rgsw).reshape(2 * ell, 2, plen)
+    q = nat.QueryC(query.shard_id, rgsw.ctypes.data_as(C.c_void_p), 0, None, None)
+    out = np.zeros(2 * plen, dtype=np.uint64)
+    cols = np.zeros((crs.inspiring_num_columns, 2, plen), dtype=np.uint64) if with_columns else None
+    _check(crs.L.inspire_respond(crs.h, encoded_db.h, C.byref(q), _ptr(out), _ptr(cols)))
+    return _nopacking_response(out, cols, plen)
+
+
+def respond_seeded(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery,
+                   with_columns: bool = True) -> ServerResponse:
+    """respond_seeded (respond.rs:408-415): expand, then NoPacking respond."""
+    plen = crs.params.plen
+    ell = crs.params.gadget_len
+    seeds = np.ascontiguousarray(query.seeds, dtype=np.uint8).reshape(2 * ell, 32)
+    b_rows = _u64(query.b_rows).reshape(2 * ell, plen)
+    q = nat.SeededQueryC(query.shard_id, seeds.ctypes.data_as(C.c_void_p), b_rows.ctypes.data_as(C.c_void_p),
+                         0, None, None)
+    out = np.zeros(2 * plen, dtype=np.uint64)
+    cols = np.zeros((crs.inspiring_num_columns, 2, plen), dtype=np.uint64) if with_columns else None
+    _check(crs.L.inspire_respond_seeded(crs.h, encoded_db.h, C.byref(q), _ptr(out), _ptr(cols)))
+    return _nopacking_response(out, cols, plen)
+
+
+def respond_seeded_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int],
+                                   seeds: np.ndarray, b_rows: np.ndarray) -> np.ndarray:
+    """Batched respond_seeded: (n, 2, plen) combined ciphertexts."""
+    n = len(shard_ids)
+    plen = crs.params.plen
+    sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+    sd = np.ascontiguousarray(seeds, dtype=np.uint8)
+    br = _u64(b_rows)
+    out = np.zeros((n, 2, plen), dtype=np.uint64)
+    _check(crs.L.inspire_respond_seeded_nopacking_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br),
+                                                        _ptr(out)))
+    return out
+
+
+def respond_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery,
+                         variant: InspireVariant) -> ServerResponse:
+    """respond_with_variant (respond.rs:129-151).  Tree packing
+    (respond_one_packing) is not part of the GPU path."""
+    if variant == InspireVariant.NoPacking:
+        return respond(crs, encoded_db, query)
+    if query.packing_mode == "tree":
+        raise PirError("tree packing is not implemented on the GPU path", nat.ERR_UNSUPPORTED)
+    if query.inspiring_packing_keys is None:
+        raise PirError("InspiRING packing keys missing (set packing_mode=tree to use tree packing)",
+                       nat.ERR_KEYS_MISSING)
+    return respond_inspiring(crs, encoded_db, query)
+
+
 def respond_seeded_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery,
                                 variant: InspireVariant) -> ServerResponse:
-    """respond_seeded_with_variant (respond.rs:161-183): the InspiRING branch
-    runs on the GPU; NoPacking and tree packing are not part of this path."""
-    if variant == InspireVariant.NoPacking or query.packing_mode == "tree":
-        raise PirError("NoPacking / tree packing are not implemented on the GPU path", nat.ERR_UNSUPPORTED)
+    """respond_seeded_with_variant (respond.rs:161-183).  Tree packing
+    (respond_seeded_packed) is not part of the GPU path."""
+    if variant == InspireVariant.NoPacking:
+        return respond_seeded(crs, encoded_db, query)
+    if query.packing_mode == "tree":
+        raise PirError("tree packing is not implemented on the GPU path", nat.ERR_UNSUPPORTED)
     if query.inspiring_packing_keys is None:
         raise PirError("InspiRING packing keys missing (set packing_mode=tree to use tree packing)",
                        nat.ERR_KEYS_MISSING)
