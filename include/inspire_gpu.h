@@ -37,11 +37,13 @@ typedef enum {
   INSPIRE_ERR_SHARD_NOT_FOUND = 2,  /* "Shard {id} not found" (respond.rs:301-305) */
   INSPIRE_ERR_KEYS_MISSING = 3,     /* "InspiRING client packing keys missing from query" (respond.rs:296-299) */
   INSPIRE_ERR_KEYS_INVALID = 4,     /* "InspiRING packing keys invalid: y_all and y_body are both empty" (respond.rs:365-370) */
-  INSPIRE_ERR_UNSUPPORTED = 5,      /* parameters outside the GPU path */
+  INSPIRE_ERR_UNSUPPORTED = 5,      /* parameters outside the GPU path (ring_dim 2048, two CRT primes, gadget 2^20 x 3, num_columns <= 16) */
   INSPIRE_ERR_CUDA = 6,
   INSPIRE_ERR_OUT_OF_MEMORY = 7,
   INSPIRE_ERR_NO_CRS = 8,
-  INSPIRE_ERR_DEVICE_STATUS = 9     /* a kernel reported a failed bounded loop or a bad index */
+  INSPIRE_ERR_DEVICE_STATUS = 9,    /* a kernel reported a failed bounded loop or a bad index */
+  INSPIRE_PENDING = 10,             /* serving loop: the ticket's response is not ready yet */
+  INSPIRE_ERR_BUSY = 11             /* serving loop: no free query slot; retry after polling */
 } inspire_status;
 
 /* NTT-domain automorphism semantics of InspiRING packing
@@ -181,6 +183,64 @@ int inspire_respond_seeded_batch_device(inspire_ctx *ctx, const inspire_db *db, 
                                         const uint32_t *d_shard_ids, const uint8_t *d_seeds,
                                         const uint64_t *d_b_rows, const int32_t *d_client_ids, uint64_t *d_out_ct,
                                         int32_t *d_status, void *stream);
+
+/* ---- Serving loop ----
+ * The crate serves each HTTP request with one synchronous respond call on a
+ * tokio worker (src/bin/server.rs:179-236).  The serving loop replaces that
+ * with continuous batching on the GPU: queries are submitted from any thread
+ * and admitted into pinned query slots; a dispatcher thread launches each
+ * batch of pending queries (up to max_batch, any shards, any registered
+ * clients, any databases of this context) on one of max_inflight CUDA streams
+ * as soon as a stream is free, so batches overlap on the device; the GPU reads
+ * the queries and writes the responses in pinned host memory directly.  Each
+ * response equals respond_seeded_inspiring of that query alone. */
+typedef struct inspire_server inspire_server;
+
+typedef struct {
+  uint32_t max_batch;     /* queries per launch (1..1024) */
+  uint32_t max_inflight;  /* batches on the device at once, one stream each */
+  uint32_t capacity;      /* queries submitted and not yet polled, at most */
+  uint64_t device_budget; /* device bytes for in-flight batches; 0 = no limit.
+                             Fewer streams are used if max_inflight batches do not fit. */
+} inspire_server_config;
+
+typedef struct {
+  uint64_t submitted, completed, batches; /* totals since creation */
+  uint32_t pending, inflight_batches;     /* now */
+  uint32_t streams;                       /* streams in use (after the device budget) */
+} inspire_server_stats;
+
+/* max_batch 128, max_inflight 4, capacity 4096, device_budget 0. */
+void inspire_server_config_default(inspire_server_config *cfg);
+int inspire_server_create(inspire_ctx *ctx, const inspire_server_config *cfg, inspire_server **out);
+/* Waits for batches in flight, then frees the loop.  Unpolled tickets die. */
+void inspire_server_destroy(inspire_server *srv);
+
+/* Submit n seeded InspiRING queries against `db`, laid out as for
+ * inspire_respond_seeded_batch (full 2*gadget_len-row seeds and b_rows; the
+ * needed rows are copied, so the buffers are free on return).  arrival_ns
+ * (may be NULL: the submit time) stamps each query for latency accounting on
+ * the inspire_now_ns clock.  tickets[n] receive one ticket per accepted query.
+ * Validation as inspire_respond_seeded_batch ("Shard {id} not found", keys
+ * missing); queries are accepted in order until the first invalid one (its
+ * error is returned) or until capacity is reached (INSPIRE_ERR_BUSY);
+ * *accepted counts the accepted ones. */
+int inspire_server_submit(inspire_server *srv, const inspire_db *db, uint32_t n, const uint32_t *shard_ids,
+                          const uint8_t *seeds, const uint64_t *b_rows, const int32_t *client_ids,
+                          const int64_t *arrival_ns, uint64_t *tickets, uint32_t *accepted);
+
+/* Collect a ticket: waits up to timeout_us (0 = do not wait, < 0 = no
+ * limit).  INSPIRE_OK: out_ct (may be NULL) receives [a poly, b poly],
+ * done_ns (may be NULL) the completion time, and the ticket is consumed.
+ * INSPIRE_PENDING: not ready.  Unknown or consumed tickets:
+ * INSPIRE_ERR_INVALID_ARGUMENT. */
+int inspire_server_poll(inspire_server *srv, uint64_t ticket, uint64_t *out_ct, int64_t *done_ns,
+                        int32_t timeout_us);
+
+int inspire_server_get_stats(inspire_server *srv, inspire_server_stats *out);
+
+/* Monotonic clock of the serving loop's timestamps (CLOCK_MONOTONIC, ns). */
+int64_t inspire_now_ns(void);
 
 /* Batched NttContext::forward / inverse (src/math/ntt.rs:223-325) on device
  * data polys[npolys][2][ring_dim] (u32 residues), in place.  Forward outputs

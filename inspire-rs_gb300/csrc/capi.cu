@@ -13,28 +13,13 @@
 #include <string>
 #include <vector>
 
-#include "inspire_gpu.h"
-#include "kernels.h"
+#include "host.h"
 
 using u128 = unsigned __int128;
 using namespace ig;
+using namespace ighost;
 
 namespace {
-
-thread_local std::string g_last_error;
-
-int fail(int code, const std::string& msg) {
-  g_last_error = msg;
-  return code;
-}
-
-#define CUDA_TRY(expr)                                                                    \
-  do {                                                                                    \
-    cudaError_t _e = (expr);                                                              \
-    if (_e != cudaSuccess)                                                                \
-      return fail(_e == cudaErrorMemoryAllocation ? INSPIRE_ERR_OUT_OF_MEMORY : INSPIRE_ERR_CUDA, \
-                  std::string(#expr) + ": " + cudaGetErrorString(_e));                   \
-  } while (0)
 
 uint64_t powmod(uint64_t b, uint64_t e, uint64_t m) {
   uint64_t r = 1;
@@ -73,31 +58,6 @@ uint64_t find_psi(uint64_t two_n, uint64_t q) {
   }
   return 0;
 }
-
-struct DevMem {
-  void* p = nullptr;
-  size_t bytes = 0;
-  DevMem() = default;
-  DevMem(const DevMem&) = delete;
-  DevMem& operator=(const DevMem&) = delete;
-  ~DevMem() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  cudaError_t ensure(size_t want) {
-    if (want <= bytes) return cudaSuccess;
-    release();
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e == cudaSuccess) bytes = want;
-    return e;
-  }
-  template <class T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
 
 // ChaCha20Rng::from_seed + next_u64 for generate_mask_from_seed
 // (src/inspiring/inspiring2.rs:816-835), host side.
@@ -153,64 +113,7 @@ struct HostChaCha {
 
 }  // namespace
 
-struct inspire_ctx {
-  std::mutex mu;
-  int device = 0;
-  int mode = 0;
-  inspire_params params{};
-  uint64_t q = 0;  // composite modulus
-  DevParams P{};
-  DevMem tables;
-  // CRS
-  bool has_crs = false;
-  int gamma = 0;
-  uint8_t w_seed[32] = {};
-  DevMem what;
-  // clients
-  std::vector<DevMem*> clients;
-  std::vector<const uint32_t*> client_ptrs;
-  DevMem client_table;  // device copy of client_ptrs
-  bool client_table_dirty = true;
-  // staging for host-buffer calls
-  cudaStream_t stream = nullptr;
-  DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys;
-  std::vector<int32_t> h_status;
-
-  ~inspire_ctx() {
-    for (DevMem* m : clients) delete m;
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
-
-struct inspire_db {
-  inspire_ctx* ctx = nullptr;  // never dereferenced after creation
-  int device = 0;
-  int gamma = 0;
-  uint64_t n_entries = 0;
-  uint32_t entry_size = 0;
-  int nshards = 0;
-  DevMem H, E;
-};
-
 namespace {
-
-size_t poly_words() { return (size_t)2 * N; }
-
-int sync_client_table(inspire_ctx* c) {
-  if (!c->client_table_dirty) return INSPIRE_OK;
-  const size_t bytes = sizeof(uint32_t*) * (c->client_ptrs.size() + 1);
-  CUDA_TRY(c->client_table.ensure(bytes));
-  if (!c->client_ptrs.empty())
-    CUDA_TRY(cudaMemcpy(c->client_table.p, c->client_ptrs.data(), sizeof(uint32_t*) * c->client_ptrs.size(),
-                        cudaMemcpyHostToDevice));
-  c->client_table_dirty = false;
-  return INSPIRE_OK;
-}
-
-int set_device(inspire_ctx* c) {
-  CUDA_TRY(cudaSetDevice(c->device));
-  return INSPIRE_OK;
-}
 
 int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all, int32_t* id) {
   if (!y_body && !y_all)

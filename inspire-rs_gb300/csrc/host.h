@@ -1,0 +1,121 @@
+// host.h -- host-side objects shared by the C ABI translation units
+// (capi.cu, serve.cu): error reporting, device buffers, and the context and
+// database handles.  Internal; not part of the public header.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "inspire_gpu.h"
+#include "kernels.h"
+
+namespace ighost {
+
+using namespace ig;
+
+inline thread_local std::string g_last_error;
+
+inline int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                    \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess)                                                                \
+      return fail(_e == cudaErrorMemoryAllocation ? INSPIRE_ERR_OUT_OF_MEMORY : INSPIRE_ERR_CUDA, \
+                  std::string(#expr) + ": " + cudaGetErrorString(_e));                   \
+  } while (0)
+
+struct DevMem {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevMem() = default;
+  DevMem(const DevMem&) = delete;
+  DevMem& operator=(const DevMem&) = delete;
+  ~DevMem() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+}  // namespace ighost
+
+struct inspire_ctx {
+  std::mutex mu;
+  int device = 0;
+  int mode = 0;
+  inspire_params params{};
+  uint64_t q = 0;  // composite modulus
+  ig::DevParams P{};
+  ighost::DevMem tables;
+  // CRS
+  bool has_crs = false;
+  int gamma = 0;
+  uint8_t w_seed[32] = {};
+  ighost::DevMem what;
+  // clients
+  std::vector<ighost::DevMem*> clients;
+  std::vector<const uint32_t*> client_ptrs;
+  ighost::DevMem client_table;  // device copy of client_ptrs
+  bool client_table_dirty = true;
+  // staging for host-buffer calls
+  cudaStream_t stream = nullptr;
+  ighost::DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys;
+  std::vector<int32_t> h_status;
+
+  ~inspire_ctx() {
+    for (ighost::DevMem* m : clients) delete m;
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct inspire_db {
+  inspire_ctx* ctx = nullptr;  // never dereferenced after creation
+  int device = 0;
+  int gamma = 0;
+  uint64_t n_entries = 0;
+  uint32_t entry_size = 0;
+  int nshards = 0;
+  ighost::DevMem H, E;
+};
+
+namespace ighost {
+
+inline size_t poly_words() { return (size_t)2 * N; }
+
+inline int sync_client_table(inspire_ctx* c) {
+  if (!c->client_table_dirty) return INSPIRE_OK;
+  // grown in steps of 256 entries: a reallocation (which waits for the
+  // device) is rare while a serving loop has batches in flight
+  const size_t bytes = sizeof(uint32_t*) * ((c->client_ptrs.size() + 256) & ~(size_t)255);
+  CUDA_TRY(c->client_table.ensure(bytes));
+  if (!c->client_ptrs.empty())
+    CUDA_TRY(cudaMemcpy(c->client_table.p, c->client_ptrs.data(), sizeof(uint32_t*) * c->client_ptrs.size(),
+                        cudaMemcpyHostToDevice));
+  c->client_table_dirty = false;
+  return INSPIRE_OK;
+}
+
+inline int set_device(inspire_ctx* c) {
+  CUDA_TRY(cudaSetDevice(c->device));
+  return INSPIRE_OK;
+}
+
+}  // namespace ighost

@@ -11,6 +11,14 @@ namespace ig {
 constexpr int ERR_EXPAND = 1;  // seeded expansion exceeded its iteration bound
 constexpr int ERR_INDEX = 2;   // shard or client id out of range
 
+// One resident database as the Respond kernel sees it.
+struct DbView {
+  const uint32_t* E;  // [nshards][2][ELL][gamma][N] contracted database
+  const uint16_t* H;  // [nshards][gamma][N] raw 16-bit columns
+  int nshards;
+  int pad;
+};
+
 struct RespondArgs {
   DevParams P;
   int nq;
@@ -26,6 +34,7 @@ struct RespondArgs {
   const uint32_t* what;          // [(gamma-1)][ELL][2][N] rotated w_mask (CRS)
   uint64_t* out;                 // [nq][2][2][N] response (a_hat, b) residues
   int* status;                   // [nq]
+  const DbView* qdb;             // [nq] per-query database (overrides E/H/nshards) or null
 };
 
 // NoPacking respond (respond.rs:71-115): per query the combined ciphertext
@@ -44,6 +53,24 @@ struct NoPackingArgs {
   uint64_t* out_columns;
   int* status;
 };
+
+// One admitted query of the serving loop, in pinned host memory that the
+// device reads and writes directly (no staging copies on the host).
+struct QueryDesc {
+  const uint8_t* seeds;   // [ELL][32] seeds of rows ELL..2ELL-1
+  const uint64_t* brows;  // [ELL][2][N] b-polys of rows ELL..2ELL-1 (16-byte aligned)
+  uint64_t* out;          // [2][2][N] response destination (16-byte aligned)
+  int32_t* status;        // kernel status destination
+  DbView db;
+  uint32_t shard;
+  int32_t client;
+};
+
+// Gather the batch's query rows from the descriptors into device buffers
+// laid out as RespondArgs expects; scatter responses and statuses back.
+cudaError_t launch_gather(const QueryDesc* d, int nq, uint8_t* seeds, uint64_t* brows, uint32_t* shard,
+                          int32_t* client, DbView* qdb, cudaStream_t st);
+cudaError_t launch_scatter(const QueryDesc* d, int nq, const uint64_t* out, const int* status, cudaStream_t st);
 
 size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);

@@ -149,12 +149,20 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const int gamma = P.gamma;
   const uint32_t shard = A.shard[qi];
   const int32_t cid = A.client[qi];
-  if (shard >= (uint32_t)A.nshards || cid < 0 || cid >= A.nclients || A.yhat_table[cid] == nullptr) {
+  const uint32_t* Ebase = A.E;
+  const uint16_t* Hbase = A.H;
+  int nshards = A.nshards;
+  if (A.qdb) {
+    Ebase = A.qdb[qi].E;
+    Hbase = A.qdb[qi].H;
+    nshards = A.qdb[qi].nshards;
+  }
+  if (shard >= (uint32_t)nshards || cid < 0 || cid >= A.nclients || A.yhat_table[cid] == nullptr) {
     if (tid == 0) A.status[qi] = ERR_INDEX;
     return;  // uniform over the CTA
   }
-  const uint32_t* E = A.E + (size_t)shard * 2 * ELL * gamma * N;
-  const uint16_t* H = A.H + (size_t)shard * gamma * N;
+  const uint32_t* E = Ebase + (size_t)shard * 2 * ELL * gamma * N;
+  const uint16_t* H = Hbase + (size_t)shard * gamma * N;
   const uint32_t* Y = A.yhat_table[cid];
   const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
 

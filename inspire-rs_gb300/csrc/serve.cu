@@ -1,0 +1,472 @@
+// serve.cu -- the serving loop: continuous batching of seeded InspiRING
+// queries over several CUDA streams.
+//
+// Submitted queries are copied into records of a pinned, device-mapped pool
+// (rows ELL..2ELL-1 only: seeds and b-polys).  A dispatcher thread takes up to
+// max_batch pending queries whenever one of its streams is free, writes one
+// QueryDesc per query into that stream's pinned descriptor array, and issues
+// gather -> respond -> scatter -> event on the stream.  The gather and scatter
+// kernels read the query rows from, and write the responses to, the pool over
+// the host link directly (NVLink-C2C on a Grace-Blackwell node), so no host
+// thread copies a batch.  Batches on different streams overlap on the device,
+// which also fills the SMs a single batch leaves idle.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <thread>
+
+#include "host.h"
+
+using namespace ig;
+using namespace ighost;
+
+namespace ig {
+namespace {
+
+constexpr int IO_THREADS = 256;
+static_assert(sizeof(QueryDesc) == 64, "QueryDesc is read as four 16-byte words");
+
+// Descriptors live in pinned host memory rewritten between batches: read them
+// with cache-volatile loads.
+__device__ __forceinline__ void load_desc(const QueryDesc* d, QueryDesc& q) {
+  const uint4* s = reinterpret_cast<const uint4*>(d);
+  uint4* t = reinterpret_cast<uint4*>(&q);
+#pragma unroll
+  for (int i = 0; i < 4; i++) t[i] = __ldcv(s + i);
+}
+
+// Query rows: pool -> device buffers in the layout RespondArgs expects.
+__global__ void __launch_bounds__(IO_THREADS) gather_kernel(const QueryDesc* __restrict__ d, uint8_t* seeds,
+                                                            uint64_t* brows, uint32_t* shard, int32_t* client,
+                                                            DbView* qdb) {
+  __shared__ __align__(16) QueryDesc q;
+  const int qi = blockIdx.x, tid = threadIdx.x;
+  if (tid == 0) load_desc(d + qi, q);
+  __syncthreads();
+  const uint4* src = reinterpret_cast<const uint4*>(q.brows);
+  uint4* dst = reinterpret_cast<uint4*>(brows + (size_t)qi * ELL * 2 * N);
+  for (int i = tid; i < ELL * N; i += IO_THREADS) dst[i] = __ldcv(src + i);  // ELL * 2N u64
+  if (tid < ELL * 32) seeds[(size_t)qi * ELL * 32 + tid] = __ldcv(q.seeds + tid);
+  if (tid == 0) {
+    shard[qi] = q.shard;
+    client[qi] = q.client;
+    qdb[qi] = q.db;
+  }
+}
+
+// Responses and statuses: device buffers -> pool.
+__global__ void __launch_bounds__(IO_THREADS) scatter_kernel(const QueryDesc* __restrict__ d, const uint64_t* out,
+                                                             const int* status) {
+  __shared__ __align__(16) QueryDesc q;
+  const int qi = blockIdx.x, tid = threadIdx.x;
+  if (tid == 0) load_desc(d + qi, q);
+  __syncthreads();
+  const uint4* src = reinterpret_cast<const uint4*>(out + (size_t)qi * 4 * N);
+  uint4* dst = reinterpret_cast<uint4*>(q.out);
+  for (int i = tid; i < 2 * N; i += IO_THREADS) dst[i] = src[i];  // 4N u64
+  if (tid == 0) *q.status = status[qi];
+}
+
+}  // namespace
+
+cudaError_t launch_gather(const QueryDesc* d, int nq, uint8_t* seeds, uint64_t* brows, uint32_t* shard,
+                          int32_t* client, DbView* qdb, cudaStream_t st) {
+  if (nq <= 0) return cudaSuccess;
+  gather_kernel<<<nq, IO_THREADS, 0, st>>>(d, seeds, brows, shard, client, qdb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const QueryDesc* d, int nq, const uint64_t* out, const int* status, cudaStream_t st) {
+  if (nq <= 0) return cudaSuccess;
+  scatter_kernel<<<nq, IO_THREADS, 0, st>>>(d, out, status);
+  return cudaGetLastError();
+}
+
+}  // namespace ig
+
+namespace {
+
+int64_t now_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// Pool record: [seeds ELL*32 (padded to 128)][b rows ELL*2N u64][out 4N u64][status]
+constexpr size_t REC_SEEDS = 0;
+constexpr size_t REC_BROWS = 128;
+constexpr size_t REC_OUT = REC_BROWS + sizeof(uint64_t) * ELL * 2 * N;
+constexpr size_t REC_STATUS = REC_OUT + sizeof(uint64_t) * 4 * N;
+constexpr size_t REC_BYTES = (REC_STATUS + 16 + 255) & ~(size_t)255;
+constexpr int TICKET_IDX_BITS = 24;
+
+// Device bytes one query of a batch holds.
+constexpr size_t SLOT_BYTES_PER_QUERY = 32 * ELL + sizeof(uint64_t) * ELL * 2 * N + sizeof(uint64_t) * 4 * N +
+                                        sizeof(uint32_t) + sizeof(int32_t) + sizeof(DbView) + sizeof(int);
+
+enum RecState { FREE = 0, PENDING = 1, INFLIGHT = 2, DONE = 3, COLLECTING = 4 };
+
+struct Rec {
+  uint64_t gen = 1;
+  RecState state = FREE;
+  const inspire_db* db = nullptr;
+  uint32_t shard = 0;
+  int32_t client = 0;
+  int64_t t_arrival = 0, t_done = 0;
+  int cuda_error = 0;  // nonzero: the batch failed on the host side
+};
+
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  QueryDesc* desc = nullptr;  // pinned, mapped
+  DevMem seeds, brows, shard, client, qdb, out, status;
+  std::vector<int> recs;
+  bool busy = false;
+};
+
+}  // namespace
+
+struct inspire_server {
+  inspire_ctx* ctx = nullptr;
+  inspire_server_config cfg{};
+  uint8_t* pool = nullptr;  // pinned, mapped; capacity records
+  std::vector<Rec> recs;
+  std::deque<int> free_list, pending;
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  bool stop = false;
+  std::thread worker;
+  uint64_t n_submitted = 0, n_completed = 0, n_batches = 0;
+  std::string worker_error;
+
+  uint8_t* rec_ptr(int i) const { return pool + (size_t)i * REC_BYTES; }
+  uint64_t ticket(int i) const { return (recs[i].gen << TICKET_IDX_BITS) | (uint64_t)i; }
+  void run();
+  int launch(Slot& s, const std::vector<int>& batch);
+};
+
+// Issue gather -> respond -> scatter -> event for `batch` on slot `s`.
+int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
+  const int n = (int)batch.size();
+  for (int k = 0; k < n; k++) {
+    const Rec& r = recs[batch[k]];
+    uint8_t* p = rec_ptr(batch[k]);
+    QueryDesc& d = s.desc[k];
+    d.seeds = p + REC_SEEDS;
+    d.brows = reinterpret_cast<const uint64_t*>(p + REC_BROWS);
+    d.out = reinterpret_cast<uint64_t*>(p + REC_OUT);
+    d.status = reinterpret_cast<int32_t*>(p + REC_STATUS);
+    d.db = DbView{r.db->E.as<uint32_t>(), r.db->H.as<uint16_t>(), r.db->nshards, 0};
+    d.shard = r.shard;
+    d.client = r.client;
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (int rc = sync_client_table(ctx)) return rc;
+  CUDA_TRY(launch_gather(s.desc, n, s.seeds.as<uint8_t>(), s.brows.as<uint64_t>(), s.shard.as<uint32_t>(),
+                         s.client.as<int32_t>(), s.qdb.as<DbView>(), s.st));
+  RespondArgs a{};
+  a.P = ctx->P;
+  a.nq = n;
+  a.shard = s.shard.as<uint32_t>();
+  a.seeds = s.seeds.as<uint8_t>();
+  a.arows = nullptr;
+  a.brows = s.brows.as<uint64_t>();
+  a.client = s.client.as<int32_t>();
+  a.yhat_table = ctx->client_table.as<const uint32_t*>();
+  a.nclients = (int)ctx->client_ptrs.size();
+  a.nshards = 0;
+  a.E = nullptr;
+  a.H = nullptr;
+  a.what = ctx->what.as<uint32_t>();
+  a.out = s.out.as<uint64_t>();
+  a.status = s.status.as<int>();
+  a.qdb = s.qdb.as<DbView>();
+  CUDA_TRY(launch_respond(a, true, s.st));
+  CUDA_TRY(launch_scatter(s.desc, n, s.out.as<uint64_t>(), s.status.as<int>(), s.st));
+  CUDA_TRY(cudaEventRecord(s.ev, s.st));
+  return INSPIRE_OK;
+}
+
+void inspire_server::run() {
+  cudaSetDevice(ctx->device);
+  std::vector<int> batch;
+  batch.reserve(cfg.max_batch);
+  std::unique_lock<std::mutex> lk(mu);
+  for (;;) {
+    bool progressed = false;
+    // completions
+    for (auto& sp : slots) {
+      Slot& s = *sp;
+      if (!s.busy) continue;
+      const cudaError_t e = cudaEventQuery(s.ev);
+      if (e == cudaErrorNotReady) continue;
+      const int64_t t = now_ns();
+      for (int i : s.recs) {
+        recs[i].state = DONE;
+        recs[i].t_done = t;
+        recs[i].cuda_error = e == cudaSuccess ? 0 : (int)e;
+      }
+      if (e != cudaSuccess) worker_error = std::string("serving batch: ") + cudaGetErrorString(e);
+      n_completed += s.recs.size();
+      s.recs.clear();
+      s.busy = false;
+      progressed = true;
+    }
+    if (progressed) cv_done.notify_all();
+    // dispatch
+    for (auto& sp : slots) {
+      Slot& s = *sp;
+      if (s.busy || pending.empty()) continue;
+      batch.clear();
+      while (!pending.empty() && batch.size() < cfg.max_batch) {
+        const int i = pending.front();
+        pending.pop_front();
+        recs[i].state = INFLIGHT;
+        batch.push_back(i);
+      }
+      s.recs = batch;
+      s.busy = true;
+      n_batches++;
+      lk.unlock();
+      const int rc = launch(s, batch);
+      lk.lock();
+      if (rc != INSPIRE_OK) {  // fail the batch's queries; the loop keeps serving
+        cudaStreamSynchronize(s.st);
+        worker_error = g_last_error;
+        const int64_t t = now_ns();
+        for (int i : s.recs) {
+          recs[i].state = DONE;
+          recs[i].t_done = t;
+          recs[i].cuda_error = rc;
+        }
+        n_completed += s.recs.size();
+        s.recs.clear();
+        s.busy = false;
+        cv_done.notify_all();
+      }
+      progressed = true;
+    }
+    bool any_busy = false;
+    for (const auto& sp : slots) any_busy |= sp->busy;
+    if (stop && !any_busy && pending.empty()) break;
+    if (progressed) continue;
+    if (any_busy) {  // batches in flight: poll their events
+      lk.unlock();
+      std::this_thread::yield();
+      lk.lock();
+    } else {
+      cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+    }
+  }
+}
+
+extern "C" {
+
+void inspire_server_config_default(inspire_server_config* cfg) {
+  if (!cfg) return;
+  cfg->max_batch = 128;
+  cfg->max_inflight = 4;
+  cfg->capacity = 4096;
+  cfg->device_budget = 0;
+}
+
+int64_t inspire_now_ns(void) { return now_ns(); }
+
+int inspire_server_create(inspire_ctx* c, const inspire_server_config* cfg, inspire_server** out) {
+  if (!c || !cfg || !out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (cfg->max_batch < 1 || cfg->max_batch > 1024 || cfg->max_inflight < 1 || cfg->max_inflight > 64 ||
+      cfg->capacity < cfg->max_batch || cfg->capacity >= (1u << TICKET_IDX_BITS))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "server config out of range");
+  uint32_t streams = cfg->max_inflight;
+  const size_t slot_bytes = SLOT_BYTES_PER_QUERY * cfg->max_batch;
+  if (cfg->device_budget) {
+    const uint64_t fit = cfg->device_budget / slot_bytes;
+    if (fit == 0) return fail(INSPIRE_ERR_OUT_OF_MEMORY, "device_budget is below one batch");
+    if (fit < streams) streams = (uint32_t)fit;
+  }
+  if (int rc = set_device(c)) return rc;
+  inspire_server* s = new inspire_server();
+  s->ctx = c;
+  s->cfg = *cfg;
+  auto bail = [&](int rc) {
+    inspire_server_destroy(s);
+    return rc;
+  };
+  cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&s->pool), REC_BYTES * cfg->capacity,
+                                cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    s->pool = nullptr;
+    return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, std::string("pinned query pool: ") + cudaGetErrorString(e)));
+  }
+  s->recs.resize(cfg->capacity);
+  for (uint32_t i = 0; i < cfg->capacity; i++) s->free_list.push_back((int)i);
+  for (uint32_t i = 0; i < streams; i++) s->slots.push_back(std::make_unique<Slot>());
+  const size_t B = cfg->max_batch;
+  for (auto& slp : s->slots) {
+    Slot& sl = *slp;
+    if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaHostAlloc(reinterpret_cast<void**>(&sl.desc), sizeof(QueryDesc) * B, cudaHostAllocMapped) != cudaSuccess)
+      return bail(fail(INSPIRE_ERR_CUDA, "serving stream setup failed"));
+    if (sl.seeds.ensure(32 * ELL * B) || sl.brows.ensure(sizeof(uint64_t) * ELL * 2 * N * B) ||
+        sl.shard.ensure(sizeof(uint32_t) * B) || sl.client.ensure(sizeof(int32_t) * B) ||
+        sl.qdb.ensure(sizeof(DbView) * B) || sl.out.ensure(sizeof(uint64_t) * 4 * N * B) ||
+        sl.status.ensure(sizeof(int) * B))
+      return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, "serving slot buffers"));
+  }
+  s->worker = std::thread([s] { s->run(); });
+  *out = s;
+  return INSPIRE_OK;
+}
+
+void inspire_server_destroy(inspire_server* s) {
+  if (!s) return;
+  if (s->worker.joinable()) {
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stop = true;
+      s->pending.clear();  // queries never launched die with the loop
+    }
+    s->cv_work.notify_all();
+    s->worker.join();
+  }
+  cudaSetDevice(s->ctx->device);
+  for (auto& slp : s->slots) {
+    Slot& sl = *slp;
+    if (sl.st) cudaStreamSynchronize(sl.st);
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.st) cudaStreamDestroy(sl.st);
+    if (sl.desc) cudaFreeHost(sl.desc);
+  }
+  if (s->pool) cudaFreeHost(s->pool);
+  delete s;
+}
+
+int inspire_server_submit(inspire_server* s, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,
+                          const uint8_t* seeds, const uint64_t* b_rows, const int32_t* client_ids,
+                          const int64_t* arrival_ns, uint64_t* tickets, uint32_t* accepted) {
+  if (accepted) *accepted = 0;
+  if (!s || !db || !accepted || (n && (!shard_ids || !seeds || !b_rows || !client_ids || !tickets)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (db->device != s->ctx->device) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "database lives on another device");
+  const int64_t t_submit = now_ns();
+  // validate in order; the first invalid query ends the accepted prefix
+  uint32_t valid = n;
+  int vrc = INSPIRE_OK;
+  std::string vmsg;
+  {
+    std::lock_guard<std::mutex> lk(s->ctx->mu);
+    for (uint32_t i = 0; i < n; i++) {
+      if (shard_ids[i] >= (uint32_t)db->nshards) {
+        valid = i;
+        vrc = INSPIRE_ERR_SHARD_NOT_FOUND;
+        vmsg = "Shard " + std::to_string(shard_ids[i]) + " not found";
+        break;
+      }
+      const int32_t id = client_ids[i];
+      if (id < 0 || (size_t)id >= s->ctx->clients.size() || !s->ctx->clients[id]) {
+        valid = i;
+        vrc = INSPIRE_ERR_KEYS_MISSING;
+        vmsg = "InspiRING client packing keys missing from query";
+        break;
+      }
+    }
+  }
+  // reserve records
+  std::vector<int> got;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "server is shutting down");
+    while (got.size() < valid && !s->free_list.empty()) {
+      got.push_back(s->free_list.front());
+      s->free_list.pop_front();
+    }
+  }
+  // copy rows ELL..2ELL-1 of each query into its record (no lock held)
+  const size_t pw = poly_words();
+  for (size_t k = 0; k < got.size(); k++) {
+    uint8_t* p = s->rec_ptr(got[k]);
+    memcpy(p + REC_SEEDS, seeds + (size_t)k * 64 * ELL + 32 * ELL, 32 * ELL);
+    memcpy(p + REC_BROWS, b_rows + ((size_t)k * 2 * ELL + ELL) * pw, sizeof(uint64_t) * ELL * pw);
+    Rec& r = s->recs[got[k]];
+    r.db = db;
+    r.shard = shard_ids[k];
+    r.client = client_ids[k];
+    r.t_arrival = arrival_ns ? arrival_ns[k] : t_submit;
+    r.cuda_error = 0;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (size_t k = 0; k < got.size(); k++) {
+      s->recs[got[k]].state = PENDING;
+      s->pending.push_back(got[k]);
+      tickets[k] = s->ticket(got[k]);
+    }
+    s->n_submitted += got.size();
+  }
+  if (!got.empty()) s->cv_work.notify_one();
+  *accepted = (uint32_t)got.size();
+  if (got.size() < valid) return fail(INSPIRE_ERR_BUSY, "serving loop at capacity");
+  if (vrc != INSPIRE_OK) return fail(vrc, vmsg);
+  return INSPIRE_OK;
+}
+
+int inspire_server_poll(inspire_server* s, uint64_t ticket, uint64_t* out_ct, int64_t* done_ns, int32_t timeout_us) {
+  if (!s) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  const uint64_t idx = ticket & ((1ull << TICKET_IDX_BITS) - 1);
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (idx >= s->recs.size() || s->recs[idx].gen != (ticket >> TICKET_IDX_BITS) || s->recs[idx].state == FREE)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "unknown ticket");
+  Rec& r = s->recs[idx];
+  const uint64_t gen = r.gen;
+  auto ready = [&] { return r.gen != gen || r.state == DONE || r.state == COLLECTING; };
+  if (!ready()) {
+    if (timeout_us == 0) return INSPIRE_PENDING;
+    if (timeout_us < 0) {
+      s->cv_done.wait(lk, ready);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), ready)) {
+      return INSPIRE_PENDING;
+    }
+  }
+  if (r.gen != gen || r.state != DONE) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ticket already collected");
+  r.state = COLLECTING;  // this caller owns the record until it frees it
+  const int cuda_error = r.cuda_error;
+  const int64_t t_done = r.t_done;
+  lk.unlock();
+  const uint8_t* p = s->rec_ptr((int)idx);
+  const int32_t kstatus = *reinterpret_cast<const volatile int32_t*>(p + REC_STATUS);
+  if (out_ct && !cuda_error && !kstatus) memcpy(out_ct, p + REC_OUT, sizeof(uint64_t) * 4 * N);
+  if (done_ns) *done_ns = t_done;
+  lk.lock();
+  r.gen++;
+  r.state = FREE;
+  s->free_list.push_back((int)idx);
+  const std::string werr = s->worker_error;
+  lk.unlock();
+  if (cuda_error) return fail(INSPIRE_ERR_CUDA, werr.empty() ? "serving batch failed" : werr);
+  if (kstatus)
+    return fail(INSPIRE_ERR_DEVICE_STATUS, "respond kernel status " + std::to_string(kstatus) + " for ticket " +
+                                               std::to_string(ticket));
+  return INSPIRE_OK;
+}
+
+int inspire_server_get_stats(inspire_server* s, inspire_server_stats* out) {
+  if (!s || !out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  out->submitted = s->n_submitted;
+  out->completed = s->n_completed;
+  out->batches = s->n_batches;
+  out->pending = (uint32_t)s->pending.size();
+  uint32_t busy = 0;
+  for (const auto& sl : s->slots) busy += sl->busy;
+  out->inflight_batches = busy;
+  out->streams = (uint32_t)s->slots.size();
+  return INSPIRE_OK;
+}
+
+}  // extern "C"

@@ -11,9 +11,11 @@ from .pir import (  # noqa: F401
     PirError,
     RlweCiphertext,
     SeededClientQuery,
+    Server,
     ServerCrs,
     ServerResponse,
     external_product_device,
+    now_ns,
     ntt_forward_device,
     ntt_inverse_device,
     respond,

@@ -24,6 +24,8 @@ ERR_CUDA = 6
 ERR_OUT_OF_MEMORY = 7
 ERR_NO_CRS = 8
 ERR_DEVICE_STATUS = 9
+PENDING = 10
+ERR_BUSY = 11
 
 MODE_COMPAT = 0
 MODE_CRT_FIXED = 1
@@ -62,6 +64,26 @@ class QueryC(C.Structure):
     ]
 
 
+class ServerConfigC(C.Structure):
+    _fields_ = [
+        ("max_batch", C.c_uint32),
+        ("max_inflight", C.c_uint32),
+        ("capacity", C.c_uint32),
+        ("device_budget", C.c_uint64),
+    ]
+
+
+class ServerStatsC(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_uint64),
+        ("completed", C.c_uint64),
+        ("batches", C.c_uint64),
+        ("pending", C.c_uint32),
+        ("inflight_batches", C.c_uint32),
+        ("streams", C.c_uint32),
+    ]
+
+
 _lib = None
 
 
@@ -94,6 +116,13 @@ def load(path: str = LIB_PATH):
         "inspire_respond_seeded_nopacking_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
         "inspire_respond_seeded_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp]),
         "inspire_respond_seeded_batch_device": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp]),
+        "inspire_server_config_default": (None, [C.POINTER(ServerConfigC)]),
+        "inspire_server_create": (C.c_int, [vp, C.POINTER(ServerConfigC), C.POINTER(vp)]),
+        "inspire_server_destroy": (None, [vp]),
+        "inspire_server_submit": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, C.POINTER(u32)]),
+        "inspire_server_poll": (C.c_int, [vp, u64, vp, C.POINTER(C.c_int64), i32]),
+        "inspire_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStatsC)]),
+        "inspire_now_ns": (C.c_int64, []),
         "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),
         "inspire_ntt_inverse_device": (C.c_int, [vp, vp, u32, vp]),
         "inspire_external_product_device": (C.c_int, [vp, vp, vp, vp, u32, vp]),

@@ -27,10 +27,13 @@ from .params import InspireParams, InspireVariant
 # CUDA runtime tears down) whatever order the garbage collector would pick.
 _LIVE_DBS: "weakref.WeakSet" = weakref.WeakSet()
 _LIVE_CRS: "weakref.WeakSet" = weakref.WeakSet()
+_LIVE_SERVERS: "weakref.WeakSet" = weakref.WeakSet()
 
 
 @atexit.register
 def _close_all() -> None:
+    for srv in list(_LIVE_SERVERS):
+        srv.close()
     for db in list(_LIVE_DBS):
         db.close()
     for crs in list(_LIVE_CRS):
@@ -359,3 +362,80 @@ def external_product_device(crs: ServerCrs, d_ct: int, d_rgsw: int, d_out: int, 
     """Batched external_product (external_product.rs:88-150) on device u32 data."""
     _check(crs.L.inspire_external_product_device(crs.h, C.c_void_p(d_ct), C.c_void_p(d_rgsw), C.c_void_p(d_out),
                                                  npairs, C.c_void_p(stream)))
+
+
+def now_ns() -> int:
+    """The serving loop's clock (CLOCK_MONOTONIC, ns)."""
+    return int(nat.load().inspire_now_ns())
+
+
+class Server:
+    """Serving loop over one ServerCrs: continuous batching of seeded
+    InspiRING queries (the GPU replacement of the crate's per-request
+    respond call in src/bin/server.rs:179-236).
+
+    submit() copies each query's rows into a pinned slot and returns tickets;
+    a native dispatcher launches pending queries in batches of up to
+    max_batch on max_inflight streams as they free up; poll() collects a
+    response.  Client keys are those registered with
+    ServerCrs.register_client; queries may name any database of the CRS."""
+
+    def __init__(self, crs: ServerCrs, max_batch: int = 128, max_inflight: int = 4, capacity: int = 4096,
+                 device_budget: int = 0):
+        self.crs = crs
+        self.L = crs.L
+        cfg = nat.ServerConfigC()
+        self.L.inspire_server_config_default(C.byref(cfg))
+        cfg.max_batch, cfg.max_inflight, cfg.capacity, cfg.device_budget = max_batch, max_inflight, capacity, \
+            device_budget
+        h = C.c_void_p()
+        _check(self.L.inspire_server_create(crs.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.plen = crs.params.plen
+        _LIVE_SERVERS.add(self)
+
+    def submit(self, encoded_db: EncodedDatabase, shard_ids, seeds: np.ndarray, b_rows: np.ndarray, client_ids,
+               arrival_ns: Optional[np.ndarray] = None):
+        """Submit n queries (seeds (n, 2*ell, 32), b_rows (n, 2*ell, plen)).
+        Returns (tickets, status): tickets of the accepted prefix, status 0,
+        ERR_BUSY (capacity reached) or the error of the first invalid query
+        (raised as PirError when nothing was accepted)."""
+        sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+        n = sid.size
+        cid = np.ascontiguousarray(client_ids, dtype=np.int32)
+        sd = np.ascontiguousarray(seeds, dtype=np.uint8)
+        br = _u64(b_rows)
+        arr = None if arrival_ns is None else np.ascontiguousarray(arrival_ns, dtype=np.int64)
+        tickets = np.zeros(n, dtype=np.uint64)
+        acc = C.c_uint32(0)
+        rc = self.L.inspire_server_submit(self.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br), _ptr(cid),
+                                          _ptr(arr), _ptr(tickets), C.byref(acc))
+        if rc not in (nat.OK, nat.ERR_BUSY) and acc.value == 0:
+            raise PirError(nat.last_error(), rc)
+        return tickets[:acc.value], rc
+
+    def poll(self, ticket: int, out: Optional[np.ndarray] = None, timeout_us: int = -1):
+        """Collect one ticket.  Returns done_ns when ready (out, if given,
+        receives (2, plen) uint64), None if still pending after timeout_us."""
+        done = C.c_int64(0)
+        rc = self.L.inspire_server_poll(self.h, int(ticket), _ptr(out), C.byref(done), int(timeout_us))
+        if rc == nat.PENDING:
+            return None
+        _check(rc)
+        return int(done.value)
+
+    def stats(self) -> dict:
+        st = nat.ServerStatsC()
+        _check(self.L.inspire_server_get_stats(self.h, C.byref(st)))
+        return {k: int(getattr(st, k)) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.inspire_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

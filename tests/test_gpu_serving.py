@@ -1,0 +1,187 @@
+"""The serving loop (continuous batching over several streams, mixed
+databases, shards and clients): every response equals the one the same
+query gets alone, and the oracle's for sampled queries; backpressure, ticket
+and error behaviour."""
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 2048
+ENTRY = 32
+W_SEED = bytes(range(11, 43))
+
+
+@pytest.fixture(scope="module")
+def world(oracle_mod):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import inspire
+
+    O = oracle_mod
+    rng = np.random.default_rng(99)
+    ctx = O.Ctx()
+    crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
+    pack = O.Pack(ctx, 16, W_SEED, mode=O.MODE_CRT_FIXED)
+    sizes = [2 * N + 700, N // 2, 4 * N]  # databases of different sizes
+    raws = [rng.integers(0, 256, size=s * ENTRY, dtype=np.uint8) for s in sizes]
+    dbs = [inspire.EncodedDatabase(crs, r, ENTRY) for r in raws]
+    clients = [O.Client(ctx, seed=s, rng_seed=200 + s) for s in range(3)]
+    ids, ybodies = [], []
+    for c in clients:
+        yb, _ = c.packing_keys(pack)
+        ybodies.append(yb)
+        ids.append(crs.register_client(inspire.ClientPackingKeys(y_body=yb)))
+    return dict(O=O, inspire=inspire, ctx=ctx, crs=crs, pack=pack, raws=raws, dbs=dbs, sizes=sizes,
+                clients=clients, ids=ids, ybodies=ybodies, rng=rng)
+
+
+def make_queries(W, n):
+    rng = W["rng"]
+    qs = []
+    for _ in range(n):
+        d = int(rng.integers(0, len(W["dbs"])))
+        idx = int(rng.integers(0, W["sizes"][d]))
+        c = int(rng.integers(0, len(W["clients"])))
+        seeds, b_rows = W["clients"][c].query_seeded(idx % N)
+        qs.append(dict(db=d, shard=idx // N, idx=idx, client=c, seeds=seeds, b_rows=b_rows))
+    return qs
+
+
+def alone(W, q):
+    inspire = W["inspire"]
+    return inspire.respond_seeded_batch(W["crs"], W["dbs"][q["db"]], [q["shard"]], q["seeds"][None],
+                                        q["b_rows"][None], [W["ids"][q["client"]]])[0]
+
+
+def test_served_equals_alone_under_concurrency(world):
+    W = world
+    inspire = W["inspire"]
+    qs = make_queries(W, 240)
+    want = [alone(W, q) for q in qs]
+    srv = inspire.Server(W["crs"], max_batch=32, max_inflight=3, capacity=96)
+    tickets = [None] * len(qs)
+    errors = []
+
+    def submitter(part):
+        rng = np.random.default_rng(part)
+        order = list(range(part, len(qs), 3))
+        k = 0
+        while k < len(order):
+            burst = order[k:k + int(rng.integers(1, 24))]
+            # one call per database (a submit names one database)
+            by_db = {}
+            for i in burst:
+                by_db.setdefault(qs[i]["db"], []).append(i)
+            for d, idxs in by_db.items():
+                pos = 0
+                while pos < len(idxs):
+                    sub = idxs[pos:]
+                    t, rc = srv.submit(W["dbs"][d], [qs[i]["shard"] for i in sub],
+                                       np.stack([qs[i]["seeds"] for i in sub]),
+                                       np.stack([qs[i]["b_rows"] for i in sub]),
+                                       [W["ids"][qs[i]["client"]] for i in sub])
+                    for j, tk in enumerate(t):
+                        tickets[sub[j]] = int(tk)
+                    pos += len(t)
+                    if rc == inspire.pir.nat.ERR_BUSY:
+                        threading.Event().wait(0.001)  # capacity reached: let the collector drain
+                    elif rc != 0:
+                        errors.append(rc)
+                        return
+            k += len(burst)
+
+    got = [None] * len(qs)
+
+    def collector():
+        remaining = set(range(len(qs)))
+        while remaining:
+            for i in sorted(remaining):
+                if tickets[i] is None:
+                    continue
+                out = np.zeros((2, 2 * N), dtype=np.uint64)
+                if srv.poll(tickets[i], out, timeout_us=200) is not None:
+                    got[i] = out
+                    remaining.discard(i)
+
+    threads = [threading.Thread(target=submitter, args=(p,)) for p in range(3)]
+    col = threading.Thread(target=collector)
+    for t in threads:
+        t.start()
+    col.start()
+    for t in threads:
+        t.join(120)
+    col.join(120)
+    assert not errors
+    assert not col.is_alive()
+    for i in range(len(qs)):
+        assert np.array_equal(got[i], want[i]), f"query {i} differs from its alone response"
+    st = srv.stats()
+    assert st["completed"] == len(qs) and st["submitted"] == len(qs)
+    assert st["batches"] >= len(qs) // 32 and st["streams"] == 3
+    srv.close()
+
+
+def test_served_matches_oracle_and_decrypts(world):
+    W = world
+    inspire, ctx = W["inspire"], W["ctx"]
+    srv = inspire.Server(W["crs"], max_batch=8, max_inflight=2, capacity=16)
+    for q in make_queries(W, 3):
+        t, rc = srv.submit(W["dbs"][q["db"]], [q["shard"]], q["seeds"][None], q["b_rows"][None],
+                           [W["ids"][q["client"]]])
+        assert rc == 0 and len(t) == 1
+        out = np.zeros((2, 2 * N), dtype=np.uint64)
+        assert srv.poll(int(t[0]), out) is not None
+        shard = ctx.encode_shard(W["raws"][q["db"]], ENTRY, q["shard"])
+        want = ctx.respond_inspiring(shard, ctx.expand_rgsw(q["seeds"], q["b_rows"]), W_SEED,
+                                     mode=W["O"].MODE_CRT_FIXED, pack=W["pack"], y_body=W["ybodies"][q["client"]])
+        assert np.array_equal(out, want)
+        entry = W["clients"][q["client"]].extract_inspiring(out, ENTRY)
+        assert np.array_equal(entry, W["raws"][q["db"]][q["idx"] * ENTRY:(q["idx"] + 1) * ENTRY])
+    srv.close()
+
+
+def test_serving_errors_and_tickets(world):
+    W = world
+    inspire = W["inspire"]
+    srv = inspire.Server(W["crs"], max_batch=4, max_inflight=1, capacity=4)
+    q = make_queries(W, 1)[0]
+    seeds = np.stack([q["seeds"]] * 2)
+    brows = np.stack([q["b_rows"]] * 2)
+    db = W["dbs"][0]
+    # the first query is accepted, the second names a missing shard
+    t, rc = srv.submit(db, [0, 9], seeds, brows, [W["ids"][0]] * 2)
+    assert len(t) == 1 and rc == inspire.pir.nat.ERR_SHARD_NOT_FOUND
+    with pytest.raises(inspire.PirError, match="Shard 9 not found"):
+        srv.submit(db, [9], seeds[:1], brows[:1], [W["ids"][0]])
+    with pytest.raises(inspire.PirError, match="keys missing"):
+        srv.submit(db, [0], seeds[:1], brows[:1], [77])
+    assert srv.poll(int(t[0])) is not None
+    with pytest.raises(inspire.PirError, match="ticket"):
+        srv.poll(int(t[0]))  # consumed
+    # capacity: 4 accepted, the fifth is refused with BUSY until polled
+    five = np.stack([q["seeds"]] * 5), np.stack([q["b_rows"]] * 5)
+    t, rc = srv.submit(db, [0] * 5, five[0], five[1], [W["ids"][1]] * 5)
+    assert len(t) == 4 and rc == inspire.pir.nat.ERR_BUSY
+    outs = []
+    for tk in t:
+        o = np.zeros((2, 2 * N), dtype=np.uint64)
+        assert srv.poll(int(tk), o) is not None
+        outs.append(o)
+    assert all(np.array_equal(outs[0], o) for o in outs)
+    assert srv.stats()["pending"] == 0
+    srv.close()
+
+
+def test_device_budget_limits_streams(world):
+    W = world
+    inspire = W["inspire"]
+    one_batch = 8 * (96 + 6 * 2048 * 8 + 4 * 2048 * 8 + 40)
+    srv = inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=2 * one_batch + 100)
+    assert srv.stats()["streams"] == 2
+    srv.close()
+    with pytest.raises(inspire.PirError, match="below one batch"):
+        inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=1000)
