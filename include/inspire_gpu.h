@@ -216,18 +216,29 @@ int inspire_server_create(inspire_ctx *ctx, const inspire_server_config *cfg, in
 /* Waits for batches in flight, then frees the loop.  Unpolled tickets die. */
 void inspire_server_destroy(inspire_server *srv);
 
-/* Submit n seeded InspiRING queries against `db`, laid out as for
- * inspire_respond_seeded_batch (full 2*gadget_len-row seeds and b_rows; the
- * needed rows are copied, so the buffers are free on return).  arrival_ns
+/* Submission flag: read the query rows in place instead of copying them.
+ * seeds and b_rows must then lie in page-locked host memory (for instance
+ * from inspire_pinned_alloc) with b_rows 16-byte aligned, and must stay
+ * unchanged until every ticket of the call has been collected. */
+#define INSPIRE_SUBMIT_BORROW 1u
+
+/* Submit n seeded InspiRING queries; query i asks database dbs[i] (any
+ * database of this context), laid out as for inspire_respond_seeded_batch
+ * (full 2*gadget_len-row seeds and b_rows).  Without INSPIRE_SUBMIT_BORROW
+ * the needed rows are copied, so the buffers are free on return.  arrival_ns
  * (may be NULL: the submit time) stamps each query for latency accounting on
  * the inspire_now_ns clock.  tickets[n] receive one ticket per accepted query.
  * Validation as inspire_respond_seeded_batch ("Shard {id} not found", keys
  * missing); queries are accepted in order until the first invalid one (its
  * error is returned) or until capacity is reached (INSPIRE_ERR_BUSY);
  * *accepted counts the accepted ones. */
-int inspire_server_submit(inspire_server *srv, const inspire_db *db, uint32_t n, const uint32_t *shard_ids,
+int inspire_server_submit(inspire_server *srv, uint32_t n, const inspire_db *const *dbs, const uint32_t *shard_ids,
                           const uint8_t *seeds, const uint64_t *b_rows, const int32_t *client_ids,
-                          const int64_t *arrival_ns, uint64_t *tickets, uint32_t *accepted);
+                          const int64_t *arrival_ns, uint32_t flags, uint64_t *tickets, uint32_t *accepted);
+
+/* Page-locked, device-mapped host memory for borrowed submissions. */
+int inspire_pinned_alloc(size_t bytes, void **out);
+void inspire_pinned_free(void *p);
 
 /* Collect a ticket: waits up to timeout_us (0 = do not wait, < 0 = no
  * limit).  INSPIRE_OK: out_ct (may be NULL) receives [a poly, b poly],
@@ -236,6 +247,14 @@ int inspire_server_submit(inspire_server *srv, const inspire_db *db, uint32_t n,
  * INSPIRE_ERR_INVALID_ARGUMENT. */
 int inspire_server_poll(inspire_server *srv, uint64_t ticket, uint64_t *out_ct, int64_t *done_ns,
                         int32_t timeout_us);
+
+/* Collect tickets[0..n) in order, as inspire_server_poll each (out_ct, may
+ * be NULL, receives n responses of [a poly, b poly]; done_ns, may be NULL, n
+ * times), waiting for all of them up to timeout_us in total.  Stops at the
+ * first ticket still pending (INSPIRE_PENDING) or failing (its error);
+ * *collected counts the tickets consumed. */
+int inspire_server_poll_batch(inspire_server *srv, uint32_t n, const uint64_t *tickets, uint64_t *out_ct,
+                              int64_t *done_ns, int32_t timeout_us, uint32_t *collected);
 
 int inspire_server_get_stats(inspire_server *srv, inspire_server_stats *out);
 

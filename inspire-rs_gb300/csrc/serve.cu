@@ -10,7 +10,9 @@
 // the host link directly (NVLink-C2C on a Grace-Blackwell node), so no host
 // thread copies a batch.  Batches on different streams overlap on the device,
 // which also fills the SMs a single batch leaves idle.
+#include <algorithm>
 #include <chrono>
+#include <climits>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -110,6 +112,8 @@ enum RecState { FREE = 0, PENDING = 1, INFLIGHT = 2, DONE = 3, COLLECTING = 4 };
 struct Rec {
   uint64_t gen = 1;
   RecState state = FREE;
+  const uint8_t* seeds = nullptr;   // device-accessible rows: the pool record's or borrowed
+  const uint64_t* brows = nullptr;
   const inspire_db* db = nullptr;
   uint32_t shard = 0;
   int32_t client = 0;
@@ -120,7 +124,8 @@ struct Rec {
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
-  QueryDesc* desc = nullptr;  // pinned, mapped
+  QueryDesc* desc = nullptr;   // pinned, mapped (host address)
+  QueryDesc* ddesc = nullptr;  // its device address
   DevMem seeds, brows, shard, client, qdb, out, status;
   std::vector<int> recs;
   bool busy = false;
@@ -132,6 +137,7 @@ struct inspire_server {
   inspire_ctx* ctx = nullptr;
   inspire_server_config cfg{};
   uint8_t* pool = nullptr;  // pinned, mapped; capacity records
+  uint8_t* dpool = nullptr;  // the pool's device address
   std::vector<Rec> recs;
   std::deque<int> free_list, pending;
   std::vector<std::unique_ptr<Slot>> slots;
@@ -143,6 +149,7 @@ struct inspire_server {
   std::string worker_error;
 
   uint8_t* rec_ptr(int i) const { return pool + (size_t)i * REC_BYTES; }
+  uint8_t* dev_rec_ptr(int i) const { return dpool + (size_t)i * REC_BYTES; }
   uint64_t ticket(int i) const { return (recs[i].gen << TICKET_IDX_BITS) | (uint64_t)i; }
   void run();
   int launch(Slot& s, const std::vector<int>& batch);
@@ -153,10 +160,10 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   const int n = (int)batch.size();
   for (int k = 0; k < n; k++) {
     const Rec& r = recs[batch[k]];
-    uint8_t* p = rec_ptr(batch[k]);
+    uint8_t* p = dev_rec_ptr(batch[k]);
     QueryDesc& d = s.desc[k];
-    d.seeds = p + REC_SEEDS;
-    d.brows = reinterpret_cast<const uint64_t*>(p + REC_BROWS);
+    d.seeds = r.seeds;
+    d.brows = r.brows;
     d.out = reinterpret_cast<uint64_t*>(p + REC_OUT);
     d.status = reinterpret_cast<int32_t*>(p + REC_STATUS);
     d.db = DbView{r.db->E.as<uint32_t>(), r.db->H.as<uint16_t>(), r.db->nshards, 0};
@@ -165,7 +172,7 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   }
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (int rc = sync_client_table(ctx)) return rc;
-  CUDA_TRY(launch_gather(s.desc, n, s.seeds.as<uint8_t>(), s.brows.as<uint64_t>(), s.shard.as<uint32_t>(),
+  CUDA_TRY(launch_gather(s.ddesc, n, s.seeds.as<uint8_t>(), s.brows.as<uint64_t>(), s.shard.as<uint32_t>(),
                          s.client.as<int32_t>(), s.qdb.as<DbView>(), s.st));
   RespondArgs a{};
   a.P = ctx->P;
@@ -185,56 +192,74 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   a.status = s.status.as<int>();
   a.qdb = s.qdb.as<DbView>();
   CUDA_TRY(launch_respond(a, true, s.st));
-  CUDA_TRY(launch_scatter(s.desc, n, s.out.as<uint64_t>(), s.status.as<int>(), s.st));
+  CUDA_TRY(launch_scatter(s.ddesc, n, s.out.as<uint64_t>(), s.status.as<int>(), s.st));
   CUDA_TRY(cudaEventRecord(s.ev, s.st));
   return INSPIRE_OK;
 }
 
+// The dispatcher.  Events are queried and batches launched without holding
+// `mu` (only this thread changes a slot's batch), so submitters and pollers
+// only ever wait for the short bookkeeping sections.
 void inspire_server::run() {
   cudaSetDevice(ctx->device);
-  std::vector<int> batch;
-  batch.reserve(cfg.max_batch);
-  std::unique_lock<std::mutex> lk(mu);
+  std::vector<Slot*> finished, to_launch;
+  std::vector<cudaError_t> fin_err;
   for (;;) {
-    bool progressed = false;
-    // completions
+    finished.clear();
+    fin_err.clear();
     for (auto& sp : slots) {
-      Slot& s = *sp;
-      if (!s.busy) continue;
-      const cudaError_t e = cudaEventQuery(s.ev);
+      if (!sp->busy) continue;
+      const cudaError_t e = cudaEventQuery(sp->ev);
       if (e == cudaErrorNotReady) continue;
-      const int64_t t = now_ns();
-      for (int i : s.recs) {
-        recs[i].state = DONE;
-        recs[i].t_done = t;
-        recs[i].cuda_error = e == cudaSuccess ? 0 : (int)e;
-      }
-      if (e != cudaSuccess) worker_error = std::string("serving batch: ") + cudaGetErrorString(e);
-      n_completed += s.recs.size();
-      s.recs.clear();
-      s.busy = false;
-      progressed = true;
+      finished.push_back(sp.get());
+      fin_err.push_back(e);
     }
-    if (progressed) cv_done.notify_all();
-    // dispatch
-    for (auto& sp : slots) {
-      Slot& s = *sp;
-      if (s.busy || pending.empty()) continue;
-      batch.clear();
-      while (!pending.empty() && batch.size() < cfg.max_batch) {
-        const int i = pending.front();
-        pending.pop_front();
-        recs[i].state = INFLIGHT;
-        batch.push_back(i);
+    to_launch.clear();
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      const int64_t t = now_ns();
+      for (size_t k = 0; k < finished.size(); k++) {
+        Slot& s = *finished[k];
+        const cudaError_t e = fin_err[k];
+        for (int i : s.recs) {
+          recs[i].state = DONE;
+          recs[i].t_done = t;
+          recs[i].cuda_error = e == cudaSuccess ? 0 : (int)e;
+        }
+        if (e != cudaSuccess) worker_error = std::string("serving batch: ") + cudaGetErrorString(e);
+        n_completed += s.recs.size();
+        s.recs.clear();
+        s.busy = false;
       }
-      s.recs = batch;
-      s.busy = true;
-      n_batches++;
-      lk.unlock();
-      const int rc = launch(s, batch);
-      lk.lock();
+      for (auto& sp : slots) {
+        if (sp->busy || pending.empty()) continue;
+        Slot& s = *sp;
+        s.recs.clear();
+        while (!pending.empty() && s.recs.size() < cfg.max_batch) {
+          const int i = pending.front();
+          pending.pop_front();
+          recs[i].state = INFLIGHT;
+          s.recs.push_back(i);
+        }
+        s.busy = true;
+        n_batches++;
+        to_launch.push_back(&s);
+      }
+      bool any_busy = false;
+      for (const auto& sp : slots) any_busy |= sp->busy;
+      if (stop && !any_busy && pending.empty()) break;
+      if (finished.empty() && to_launch.empty() && !any_busy) {
+        cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+        continue;
+      }
+    }
+    if (!finished.empty()) cv_done.notify_all();
+    for (Slot* sp : to_launch) {
+      Slot& s = *sp;
+      const int rc = launch(s, s.recs);
       if (rc != INSPIRE_OK) {  // fail the batch's queries; the loop keeps serving
         cudaStreamSynchronize(s.st);
+        std::lock_guard<std::mutex> lk(mu);
         worker_error = g_last_error;
         const int64_t t = now_ns();
         for (int i : s.recs) {
@@ -247,19 +272,8 @@ void inspire_server::run() {
         s.busy = false;
         cv_done.notify_all();
       }
-      progressed = true;
     }
-    bool any_busy = false;
-    for (const auto& sp : slots) any_busy |= sp->busy;
-    if (stop && !any_busy && pending.empty()) break;
-    if (progressed) continue;
-    if (any_busy) {  // batches in flight: poll their events
-      lk.unlock();
-      std::this_thread::yield();
-      lk.lock();
-    } else {
-      cv_work.wait(lk, [&] { return stop || !pending.empty(); });
-    }
+    if (finished.empty() && to_launch.empty()) std::this_thread::yield();  // batches in flight
   }
 }
 
@@ -303,6 +317,8 @@ int inspire_server_create(inspire_ctx* c, const inspire_server_config* cfg, insp
     s->pool = nullptr;
     return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, std::string("pinned query pool: ") + cudaGetErrorString(e)));
   }
+  if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->dpool), s->pool, 0) != cudaSuccess)
+    return bail(fail(INSPIRE_ERR_CUDA, "pinned query pool is not device-mapped"));
   s->recs.resize(cfg->capacity);
   for (uint32_t i = 0; i < cfg->capacity; i++) s->free_list.push_back((int)i);
   for (uint32_t i = 0; i < streams; i++) s->slots.push_back(std::make_unique<Slot>());
@@ -311,7 +327,8 @@ int inspire_server_create(inspire_ctx* c, const inspire_server_config* cfg, insp
     Slot& sl = *slp;
     if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
-        cudaHostAlloc(reinterpret_cast<void**>(&sl.desc), sizeof(QueryDesc) * B, cudaHostAllocMapped) != cudaSuccess)
+        cudaHostAlloc(reinterpret_cast<void**>(&sl.desc), sizeof(QueryDesc) * B, cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(reinterpret_cast<void**>(&sl.ddesc), sl.desc, 0) != cudaSuccess)
       return bail(fail(INSPIRE_ERR_CUDA, "serving stream setup failed"));
     if (sl.seeds.ensure(32 * ELL * B) || sl.brows.ensure(sizeof(uint64_t) * ELL * 2 * N * B) ||
         sl.shard.ensure(sizeof(uint32_t) * B) || sl.client.ensure(sizeof(int32_t) * B) ||
@@ -347,13 +364,43 @@ void inspire_server_destroy(inspire_server* s) {
   delete s;
 }
 
-int inspire_server_submit(inspire_server* s, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,
+// Device address of a page-locked host range [p, p + bytes), or null.
+static const uint8_t* mapped_range(const void* p, size_t bytes) {
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const uint8_t* last = static_cast<const uint8_t*>(p) + bytes - 1;
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess || b.type != cudaMemoryTypeHost || !b.devicePointer ||
+      static_cast<const uint8_t*>(b.devicePointer) != static_cast<const uint8_t*>(a.devicePointer) + (bytes - 1)) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return static_cast<const uint8_t*>(a.devicePointer);
+}
+
+int inspire_server_submit(inspire_server* s, uint32_t n, const inspire_db* const* dbs, const uint32_t* shard_ids,
                           const uint8_t* seeds, const uint64_t* b_rows, const int32_t* client_ids,
-                          const int64_t* arrival_ns, uint64_t* tickets, uint32_t* accepted) {
+                          const int64_t* arrival_ns, uint32_t flags, uint64_t* tickets, uint32_t* accepted) {
   if (accepted) *accepted = 0;
-  if (!s || !db || !accepted || (n && (!shard_ids || !seeds || !b_rows || !client_ids || !tickets)))
+  if (!s || !accepted || (n && (!dbs || !shard_ids || !seeds || !b_rows || !client_ids || !tickets)))
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
-  if (db->device != s->ctx->device) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "database lives on another device");
+  if (flags & ~INSPIRE_SUBMIT_BORROW) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "unknown submit flags");
+  const bool borrow = flags & INSPIRE_SUBMIT_BORROW;
+  const size_t pw = poly_words();
+  const uint8_t* d_seeds = nullptr;
+  const uint8_t* d_brows = nullptr;
+  if (borrow && n) {
+    // pointer attributes are looked up in this thread's current context
+    if (int rc = set_device(s->ctx)) return rc;
+    if (reinterpret_cast<uintptr_t>(b_rows) % 16)
+      return fail(INSPIRE_ERR_INVALID_ARGUMENT, "borrowed b_rows must be 16-byte aligned");
+    d_seeds = mapped_range(seeds, (size_t)n * 64 * ELL);
+    d_brows = mapped_range(b_rows, sizeof(uint64_t) * (size_t)n * 2 * ELL * pw);
+    if (!d_seeds || !d_brows)
+      return fail(INSPIRE_ERR_INVALID_ARGUMENT, "borrowed query rows must lie in page-locked host memory");
+  }
   const int64_t t_submit = now_ns();
   // validate in order; the first invalid query ends the accepted prefix
   uint32_t valid = n;
@@ -362,6 +409,13 @@ int inspire_server_submit(inspire_server* s, const inspire_db* db, uint32_t n, c
   {
     std::lock_guard<std::mutex> lk(s->ctx->mu);
     for (uint32_t i = 0; i < n; i++) {
+      const inspire_db* db = dbs[i];
+      if (!db || db->device != s->ctx->device) {
+        valid = i;
+        vrc = INSPIRE_ERR_INVALID_ARGUMENT;
+        vmsg = "query " + std::to_string(i) + ": null database or database of another device";
+        break;
+      }
       if (shard_ids[i] >= (uint32_t)db->nshards) {
         valid = i;
         vrc = INSPIRE_ERR_SHARD_NOT_FOUND;
@@ -379,6 +433,7 @@ int inspire_server_submit(inspire_server* s, const inspire_db* db, uint32_t n, c
   }
   // reserve records
   std::vector<int> got;
+  got.reserve(valid);
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "server is shutting down");
@@ -387,14 +442,22 @@ int inspire_server_submit(inspire_server* s, const inspire_db* db, uint32_t n, c
       s->free_list.pop_front();
     }
   }
-  // copy rows ELL..2ELL-1 of each query into its record (no lock held)
-  const size_t pw = poly_words();
+  // rows ELL..2ELL-1 of each query: copied into its record, or borrowed in place
   for (size_t k = 0; k < got.size(); k++) {
-    uint8_t* p = s->rec_ptr(got[k]);
-    memcpy(p + REC_SEEDS, seeds + (size_t)k * 64 * ELL + 32 * ELL, 32 * ELL);
-    memcpy(p + REC_BROWS, b_rows + ((size_t)k * 2 * ELL + ELL) * pw, sizeof(uint64_t) * ELL * pw);
     Rec& r = s->recs[got[k]];
-    r.db = db;
+    const size_t so = (size_t)k * 64 * ELL + 32 * ELL;                        // bytes into seeds
+    const size_t bo = sizeof(uint64_t) * ((size_t)k * 2 * ELL + ELL) * pw;    // bytes into b_rows
+    if (borrow) {
+      r.seeds = d_seeds + so;
+      r.brows = reinterpret_cast<const uint64_t*>(d_brows + bo);
+    } else {
+      uint8_t* p = s->rec_ptr(got[k]);
+      memcpy(p + REC_SEEDS, seeds + so, 32 * ELL);
+      memcpy(p + REC_BROWS, reinterpret_cast<const uint8_t*>(b_rows) + bo, sizeof(uint64_t) * ELL * pw);
+      r.seeds = s->dev_rec_ptr(got[k]) + REC_SEEDS;
+      r.brows = reinterpret_cast<const uint64_t*>(s->dev_rec_ptr(got[k]) + REC_BROWS);
+    }
+    r.db = dbs[k];
     r.shard = shard_ids[k];
     r.client = client_ids[k];
     r.t_arrival = arrival_ns ? arrival_ns[k] : t_submit;
@@ -414,6 +477,18 @@ int inspire_server_submit(inspire_server* s, const inspire_db* db, uint32_t n, c
   if (got.size() < valid) return fail(INSPIRE_ERR_BUSY, "serving loop at capacity");
   if (vrc != INSPIRE_OK) return fail(vrc, vmsg);
   return INSPIRE_OK;
+}
+
+int inspire_pinned_alloc(size_t bytes, void** out) {
+  if (!out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (bytes == 0) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "zero-size allocation");
+  CUDA_TRY(cudaHostAlloc(out, bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+  return INSPIRE_OK;
+}
+
+void inspire_pinned_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 int inspire_server_poll(inspire_server* s, uint64_t ticket, uint64_t* out_ct, int64_t* done_ns, int32_t timeout_us) {
@@ -452,6 +527,28 @@ int inspire_server_poll(inspire_server* s, uint64_t ticket, uint64_t* out_ct, in
   if (kstatus)
     return fail(INSPIRE_ERR_DEVICE_STATUS, "respond kernel status " + std::to_string(kstatus) + " for ticket " +
                                                std::to_string(ticket));
+  return INSPIRE_OK;
+}
+
+int inspire_server_poll_batch(inspire_server* s, uint32_t n, const uint64_t* tickets, uint64_t* out_ct,
+                              int64_t* done_ns, int32_t timeout_us, uint32_t* collected) {
+  if (collected) *collected = 0;
+  if (!s || !collected || (n && !tickets)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  const int64_t deadline = timeout_us < 0 ? INT64_MAX : now_ns() + (int64_t)timeout_us * 1000;
+  const size_t pw = poly_words();
+  for (uint32_t k = 0; k < n; k++) {
+    int32_t left = 0;
+    if (timeout_us < 0) {
+      left = -1;
+    } else {
+      const int64_t rem = deadline - now_ns();
+      left = rem > 0 ? (int32_t)std::min<int64_t>(rem / 1000, INT32_MAX) : 0;
+    }
+    const int rc = inspire_server_poll(s, tickets[k], out_ct ? out_ct + (size_t)k * 2 * pw : nullptr,
+                                       done_ns ? done_ns + k : nullptr, left);
+    if (rc != INSPIRE_OK) return rc;
+    *collected = k + 1;
+  }
   return INSPIRE_OK;
 }
 

@@ -8,6 +8,7 @@ from .pir import (  # noqa: F401
     ClientPackingKeys,
     ClientQuery,
     EncodedDatabase,
+    PinnedBuffer,
     PirError,
     RlweCiphertext,
     SeededClientQuery,

@@ -26,6 +26,7 @@ ERR_NO_CRS = 8
 ERR_DEVICE_STATUS = 9
 PENDING = 10
 ERR_BUSY = 11
+SUBMIT_BORROW = 1
 
 MODE_COMPAT = 0
 MODE_CRT_FIXED = 1
@@ -119,8 +120,11 @@ def load(path: str = LIB_PATH):
         "inspire_server_config_default": (None, [C.POINTER(ServerConfigC)]),
         "inspire_server_create": (C.c_int, [vp, C.POINTER(ServerConfigC), C.POINTER(vp)]),
         "inspire_server_destroy": (None, [vp]),
-        "inspire_server_submit": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, C.POINTER(u32)]),
+        "inspire_server_submit": (C.c_int, [vp, u32, vp, vp, vp, vp, vp, vp, u32, vp, C.POINTER(u32)]),
+        "inspire_pinned_alloc": (C.c_int, [C.c_size_t, C.POINTER(vp)]),
+        "inspire_pinned_free": (None, [vp]),
         "inspire_server_poll": (C.c_int, [vp, u64, vp, C.POINTER(C.c_int64), i32]),
+        "inspire_server_poll_batch": (C.c_int, [vp, u32, vp, vp, vp, i32, C.POINTER(u32)]),
         "inspire_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStatsC)]),
         "inspire_now_ns": (C.c_int64, []),
         "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),

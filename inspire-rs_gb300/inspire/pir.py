@@ -28,12 +28,15 @@ from .params import InspireParams, InspireVariant
 _LIVE_DBS: "weakref.WeakSet" = weakref.WeakSet()
 _LIVE_CRS: "weakref.WeakSet" = weakref.WeakSet()
 _LIVE_SERVERS: "weakref.WeakSet" = weakref.WeakSet()
+_LIVE_PINNED: "weakref.WeakSet" = weakref.WeakSet()
 
 
 @atexit.register
 def _close_all() -> None:
     for srv in list(_LIVE_SERVERS):
         srv.close()
+    for buf in list(_LIVE_PINNED):
+        buf.close()
     for db in list(_LIVE_DBS):
         db.close()
     for crs in list(_LIVE_CRS):
@@ -394,25 +397,47 @@ class Server:
         self.plen = crs.params.plen
         _LIVE_SERVERS.add(self)
 
-    def submit(self, encoded_db: EncodedDatabase, shard_ids, seeds: np.ndarray, b_rows: np.ndarray, client_ids,
-               arrival_ns: Optional[np.ndarray] = None):
-        """Submit n queries (seeds (n, 2*ell, 32), b_rows (n, 2*ell, plen)).
-        Returns (tickets, status): tickets of the accepted prefix, status 0,
-        ERR_BUSY (capacity reached) or the error of the first invalid query
-        (raised as PirError when nothing was accepted)."""
+    def submit(self, encoded_db, shard_ids, seeds: np.ndarray, b_rows: np.ndarray, client_ids,
+               arrival_ns: Optional[np.ndarray] = None, borrow: bool = False):
+        """Submit n queries (seeds (n, 2*ell, 32), b_rows (n, 2*ell, plen));
+        encoded_db is one EncodedDatabase for all of them or a sequence of n.
+        borrow=True reads the rows in place (they must lie in PinnedBuffer
+        memory and stay unchanged until collected).  Returns (tickets,
+        status): tickets of the accepted prefix, status 0, ERR_BUSY (capacity
+        reached) or the error of the first invalid query (raised as PirError
+        when nothing was accepted)."""
         sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
         n = sid.size
+        if isinstance(encoded_db, EncodedDatabase):
+            dbs = np.full(n, encoded_db.h.value, dtype=np.uint64)
+        elif isinstance(encoded_db, np.ndarray):  # handle values (Server.handle_of)
+            dbs = np.ascontiguousarray(encoded_db, dtype=np.uint64)
+        else:
+            dbs = np.array([d.h.value for d in encoded_db], dtype=np.uint64)
+        if dbs.size != n:
+            raise ValueError("one database per query")
         cid = np.ascontiguousarray(client_ids, dtype=np.int32)
-        sd = np.ascontiguousarray(seeds, dtype=np.uint8)
-        br = _u64(b_rows)
+        if borrow:
+            sd, br = seeds, b_rows
+            if not (sd.flags.c_contiguous and br.flags.c_contiguous and sd.dtype == np.uint8 and
+                    br.dtype == np.uint64):
+                raise ValueError("borrowed rows must be C-contiguous uint8 seeds / uint64 b_rows")
+        else:
+            sd = np.ascontiguousarray(seeds, dtype=np.uint8)
+            br = _u64(b_rows)
         arr = None if arrival_ns is None else np.ascontiguousarray(arrival_ns, dtype=np.int64)
         tickets = np.zeros(n, dtype=np.uint64)
         acc = C.c_uint32(0)
-        rc = self.L.inspire_server_submit(self.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br), _ptr(cid),
-                                          _ptr(arr), _ptr(tickets), C.byref(acc))
+        rc = self.L.inspire_server_submit(self.h, n, _ptr(dbs), _ptr(sid), _ptr(sd), _ptr(br), _ptr(cid), _ptr(arr),
+                                          nat.SUBMIT_BORROW if borrow else 0, _ptr(tickets), C.byref(acc))
         if rc not in (nat.OK, nat.ERR_BUSY) and acc.value == 0:
             raise PirError(nat.last_error(), rc)
         return tickets[:acc.value], rc
+
+    @staticmethod
+    def handle_of(encoded_db: EncodedDatabase) -> int:
+        """The native handle value submit() accepts in a uint64 array."""
+        return int(encoded_db.h.value)
 
     def poll(self, ticket: int, out: Optional[np.ndarray] = None, timeout_us: int = -1):
         """Collect one ticket.  Returns done_ns when ready (out, if given,
@@ -424,6 +449,19 @@ class Server:
         _check(rc)
         return int(done.value)
 
+    def poll_batch(self, tickets: np.ndarray, out: Optional[np.ndarray] = None, timeout_us: int = -1):
+        """Collect tickets in order (out, if given: (n, 2, plen) uint64).
+        Returns done_ns of the collected prefix (shorter than tickets if one
+        is still pending after timeout_us)."""
+        tk = np.ascontiguousarray(tickets, dtype=np.uint64)
+        done = np.zeros(tk.size, dtype=np.int64)
+        got = C.c_uint32(0)
+        rc = self.L.inspire_server_poll_batch(self.h, tk.size, _ptr(tk), _ptr(out), _ptr(done), int(timeout_us),
+                                              C.byref(got))
+        if rc not in (nat.OK, nat.PENDING):
+            raise PirError(nat.last_error(), rc)
+        return done[:got.value]
+
     def stats(self) -> dict:
         st = nat.ServerStatsC()
         _check(self.L.inspire_server_get_stats(self.h, C.byref(st)))
@@ -433,6 +471,35 @@ class Server:
         if getattr(self, "h", None):
             self.L.inspire_server_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked, device-mapped host memory (inspire_pinned_alloc) viewed
+    as a numpy array; the serving loop can read borrowed query rows from it
+    in place."""
+
+    def __init__(self, shape, dtype):
+        self.L = nat.load()
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        p = C.c_void_p()
+        _check(self.L.inspire_pinned_alloc(nbytes, C.byref(p)))
+        self.p = p
+        raw = (C.c_uint8 * nbytes).from_address(p.value)
+        self.array = np.frombuffer(raw, dtype=np.uint8).view(dt).reshape(shape)
+        _LIVE_PINNED.add(self)
+
+    def close(self):
+        if getattr(self, "p", None):
+            self.array = None
+            self.L.inspire_pinned_free(self.p)
+            self.p = None
 
     def __del__(self):
         try:

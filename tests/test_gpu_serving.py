@@ -185,3 +185,32 @@ def test_device_budget_limits_streams(world):
     srv.close()
     with pytest.raises(inspire.PirError, match="below one batch"):
         inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=1000)
+
+
+def test_borrowed_rows_mixed_databases_one_call(world):
+    """One submit naming three databases, rows read in place from pinned
+    memory (no host copy): each response equals the query's alone response."""
+    W = world
+    inspire = W["inspire"]
+    qs = make_queries(W, 40)
+    want = [alone(W, q) for q in qs]
+    sb = inspire.PinnedBuffer((len(qs), 6, 32), np.uint8)
+    bb = inspire.PinnedBuffer((len(qs), 6, 2 * N), np.uint64)
+    for i, q in enumerate(qs):
+        sb.array[i], bb.array[i] = q["seeds"], q["b_rows"]
+    srv = inspire.Server(W["crs"], max_batch=16, max_inflight=2, capacity=64)
+    t, rc = srv.submit([W["dbs"][q["db"]] for q in qs], [q["shard"] for q in qs], sb.array, bb.array,
+                       [W["ids"][q["client"]] for q in qs], borrow=True)
+    assert rc == 0 and len(t) == len(qs)
+    out = np.zeros((len(qs), 2, 2 * N), dtype=np.uint64)
+    done = srv.poll_batch(t, out)
+    assert len(done) == len(qs)
+    for i in range(len(qs)):
+        assert np.array_equal(out[i], want[i])
+    # borrowing pageable memory is refused
+    with pytest.raises(inspire.PirError, match="page-locked"):
+        srv.submit(W["dbs"][0], [0], np.zeros((1, 6, 32), np.uint8), np.zeros((1, 6, 2 * N), np.uint64),
+                   [W["ids"][0]], borrow=True)
+    srv.close()
+    sb.close()
+    bb.close()

@@ -31,7 +31,7 @@ def test_binding_covers_header(lib_path):
 
     L = _native.load(lib_path)
     for s in _native.declared_symbols():
-        assert getattr(L, s).restype is not None or s.endswith(("destroy", "default")), s
+        assert getattr(L, s).argtypes is not None, s  # every declared entry point has a signature
     assert L.inspire_version().decode().startswith("inspire-gb300")
 
 
