@@ -192,6 +192,18 @@ def kernel_microbench(inspire, crs, torch, dev, reps=20):
         e1.record(st)
         torch.cuda.synchronize()
         res[name + "_us"] = e0.elapsed_time(e1) * 1e3 / reps
+    # exact modular-multiply rate probe: the integer roofline denominator
+    sink = torch.empty(152 * 8 * 256, dtype=torch.int32, device=dev)
+    best = None
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        nmm = inspire.pir.mulmod_rate_device(crs, 152 * 8, 4096, sink.data_ptr(), sp)
+        e1.record(st)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) / 1e3
+        best = dt if best is None else min(best, dt)
+    res["mulmod_rate_tps"] = nmm / best / 1e12  # 10^12 modular multiplies per second
     # bytes moved per NTT launch: read + write of 4096 x 2 x 2048 u32
     byts = 2 * 4096 * 2 * N * 4
     res["ntt_forward_gbs"] = byts / (res["ntt_forward_4096x2_us"] * 1e-6) / 1e9
@@ -490,6 +502,11 @@ def main():
                          "frac": achieved_gbs / hbm_peak,
                          "traffic": NCU_TRAFFIC_PER_LAUNCH_B128 if B == 128 else None,
                          "note": "algorithmic bytes 192 KiB/query; the kernel is integer-issue bound, see DESIGN.md"},
+            "int_roofline": {"bound": "integer pipes", "achieved": value * MULMODS_PER_QUERY / 1e12,
+                             "peak": micro["mulmod_rate_tps"], "unit": "10^12 modular multiplies/s",
+                             "frac": value * MULMODS_PER_QUERY / 1e12 / micro["mulmod_rate_tps"],
+                             "note": "algorithmic 3.4 M exact 28-bit modular multiplies per query; peak = the "
+                                     "rate probe (independent lazy Shoup multiply chains, all SMs)"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": args.steps * L,

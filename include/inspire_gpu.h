@@ -274,6 +274,13 @@ int inspire_ntt_inverse_device(inspire_ctx *ctx, uint32_t *d_polys, uint32_t npo
 int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, const uint32_t *d_rgsw,
                                     uint32_t *d_out, uint32_t npairs, void *stream);
 
+/* Rate probe with no crate counterpart: blocks x 256 threads x 8
+ * independent chains x iters exact 28-bit modular multiplies (Shoup's
+ * method, the operation the transforms and products are built from) on
+ * `stream`; d_sink receives blocks * 256 u32.  Timing it gives the integer
+ * roofline denominator of the integer-bound kernels. */
+int inspire_mulmod_rate_device(inspire_ctx *ctx, uint32_t blocks, uint32_t iters, uint32_t *d_sink, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -707,6 +707,13 @@ int inspire_ntt_inverse_device(inspire_ctx* c, uint32_t* d_polys, uint32_t npoly
   return INSPIRE_OK;
 }
 
+int inspire_mulmod_rate_device(inspire_ctx* c, uint32_t blocks, uint32_t iters, uint32_t* d_sink, void* stream) {
+  if (!c || (blocks && !d_sink)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (int rc = set_device(c)) return rc;
+  CUDA_TRY(launch_mulmod_rate(c->P, (int)blocks, (int)iters, d_sink, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
 int inspire_external_product_device(inspire_ctx* c, const uint32_t* d_ct, const uint32_t* d_rgsw, uint32_t* d_out,
                                     uint32_t npairs, void* stream) {
   if (!c || (npairs && (!d_ct || !d_rgsw || !d_out))) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");

@@ -91,6 +91,8 @@ cudaError_t launch_client_from_yall(const DevParams& P, const uint64_t* yall, ui
                                     cudaStream_t st);
 
 // kernel-level operations
+// blocks x 256 threads x 8 chains x iters lazy Shoup multiplies; sink[blocks * 256].
+cudaError_t launch_mulmod_rate(const DevParams& P, int blocks, int iters, uint32_t* sink, cudaStream_t st);
 cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool inverse,
                            cudaStream_t st);
 cudaError_t launch_external_product(const DevParams& P, const uint32_t* ct, const uint32_t* rgsw,

@@ -98,7 +98,40 @@ __global__ void __launch_bounds__(BLOCK) external_product_kernel(const DevParams
   for (int r = 0; r < 16; r++) o[(1 * 2 + g) * N + x + 128 * r] = mul_shoup(accB[r], C.ninv_mont, C.ninv_mont_p, q);
 }
 
+// Throughput probe of the exact modular multiply the transforms are built
+// from (a * w mod q by Shoup's method, lazily reduced to [0, 2q)): every
+// thread runs MM_CHAINS independent chains of `iters` dependent multiplies;
+// the xor of the chain ends is stored so nothing is dead code.
+constexpr int MM_CHAINS = 8;
+constexpr int MM_BLOCK = 256;
+
+__global__ void __launch_bounds__(MM_BLOCK) mulmod_rate_kernel(uint32_t q, uint32_t w, uint32_t wp, int iters,
+                                                               uint32_t* __restrict__ sink) {
+  uint32_t x[MM_CHAINS];
+  const uint32_t t = blockIdx.x * MM_BLOCK + threadIdx.x;
+#pragma unroll
+  for (int c = 0; c < MM_CHAINS; c++) x[c] = (t * 2654435761u + c) % q;
+  const uint2 wv = make_uint2(w, wp);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < MM_CHAINS; c++) x[c] = mul_shoup_lazy(x[c], wv, q);
+  }
+  uint32_t acc = 0;
+#pragma unroll
+  for (int c = 0; c < MM_CHAINS; c++) acc ^= x[c];
+  sink[t] = acc;
+}
+
 }  // namespace
+
+cudaError_t launch_mulmod_rate(const DevParams& P, int blocks, int iters, uint32_t* sink, cudaStream_t st) {
+  if (blocks <= 0 || iters <= 0) return cudaSuccess;
+  const uint32_t q = P.r[0].q;
+  const uint32_t w = 123456789u % q;
+  const uint32_t wp = (uint32_t)(((uint64_t)w << 32) / q);
+  mulmod_rate_kernel<<<blocks, MM_BLOCK, 0, st>>>(q, w, wp, iters, sink);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool inverse, cudaStream_t st) {
   if (npolys <= 0) return cudaSuccess;

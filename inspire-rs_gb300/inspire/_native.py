@@ -127,6 +127,7 @@ def load(path: str = LIB_PATH):
         "inspire_server_poll_batch": (C.c_int, [vp, u32, vp, vp, vp, i32, C.POINTER(u32)]),
         "inspire_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStatsC)]),
         "inspire_now_ns": (C.c_int64, []),
+        "inspire_mulmod_rate_device": (C.c_int, [vp, u32, u32, vp, vp]),
         "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),
         "inspire_ntt_inverse_device": (C.c_int, [vp, vp, u32, vp]),
         "inspire_external_product_device": (C.c_int, [vp, vp, vp, vp, u32, vp]),

@@ -361,6 +361,12 @@ def ntt_inverse_device(crs: ServerCrs, d_polys: int, npolys: int, stream: int) -
     _check(crs.L.inspire_ntt_inverse_device(crs.h, C.c_void_p(d_polys), npolys, C.c_void_p(stream)))
 
 
+def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, stream: int) -> int:
+    """Launch the modular-multiply rate probe; returns the multiplies issued."""
+    _check(crs.L.inspire_mulmod_rate_device(crs.h, blocks, iters, C.c_void_p(d_sink), C.c_void_p(stream)))
+    return blocks * 256 * 8 * iters
+
+
 def external_product_device(crs: ServerCrs, d_ct: int, d_rgsw: int, d_out: int, npairs: int, stream: int) -> None:
     """Batched external_product (external_product.rs:88-150) on device u32 data."""
     _check(crs.L.inspire_external_product_device(crs.h, C.c_void_p(d_ct), C.c_void_p(d_rgsw), C.c_void_p(d_out),
