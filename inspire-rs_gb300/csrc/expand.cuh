@@ -48,7 +48,7 @@ __device__ __forceinline__ int sub_scan_excl(int v, int* ws, int& total, int bar
 // the next N of gen_range(0..q1); NR = 1 stops after residue 0.  Returns false
 // if the iteration bound was hit (never for a working ChaCha stream).
 template <int NR>
-__device__ __forceinline__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict__ seed, uint64_t* cand,
+__device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict__ seed, uint64_t* cand,
                                   uint32_t* a0, uint32_t* a1, int* ws, int bar, int lt) {
   uint32_t key[8];
 #pragma unroll

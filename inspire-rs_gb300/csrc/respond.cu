@@ -36,8 +36,10 @@ namespace {
 
 // b0_c for every column c and residue (see file comment).  bp (6N words) is
 // scratch; bpoly[r * 16 + c] receives the result.  Warp c handles column c:
-// each lane reads its 64 coefficients with eight 128-bit loads issued up
-// front, so the shard's raw column is fetched with one memory latency.
+// lane l takes the coefficient pairs i = 2 (l + 32 m) + {0, 1}, reading the
+// raw column as u32 pairs (four loads in flight) and the staged rows as
+// 64-bit words, so every shared-memory read of a warp covers 256 contiguous
+// bytes (no bank conflicts).
 __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* __restrict__ brows,
                           uint32_t* bp, uint32_t* bpoly) {
   const int tid = threadIdx.x, gamma = P.gamma;
@@ -52,22 +54,30 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
   __syncthreads();
   const int lane = tid & 31, c = tid >> 5;
   if (c < gamma) {
-    const uint4* h4 = reinterpret_cast<const uint4*>(H + (size_t)c * N);
-    uint4 hv[8];
-#pragma unroll
-    for (int m = 0; m < 8; m++) hv[m] = __ldg(h4 + lane + 32 * m);
+    const uint32_t* h2 = reinterpret_cast<const uint32_t*>(H + (size_t)c * N);
+    const uint2* b2 = reinterpret_cast<const uint2*>(bp);
     uint64_t acc0 = 0, acc1 = 0;
+#pragma unroll 1
+    for (int m0 = 0; m0 < N / 64; m0 += 4) {
+      uint32_t hw[4];
 #pragma unroll
-    for (int m = 0; m < 8; m++) {
-      const uint32_t hw[4] = {hv[m].x, hv[m].y, hv[m].z, hv[m].w};
-      const int i0 = 8 * (lane + 32 * m);
+      for (int m = 0; m < 4; m++) hw[m] = __ldg(h2 + lane + 32 * (m0 + m));
 #pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const int i = i0 + e;
-        const uint64_t xv = P.delta * (uint64_t)((hw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);
-        const uint32_t d0 = (uint32_t)xv & 0xFFFFFu, d1 = (uint32_t)(xv >> 20) & 0xFFFFFu, d2 = (uint32_t)(xv >> 40);
-        acc0 += (uint64_t)d0 * bp[0 * N + i] + (uint64_t)d1 * bp[2 * N + i] + (uint64_t)d2 * bp[4 * N + i];
-        acc1 += (uint64_t)d0 * bp[1 * N + i] + (uint64_t)d1 * bp[3 * N + i] + (uint64_t)d2 * bp[5 * N + i];
+      for (int m = 0; m < 4; m++) {
+        const int j = lane + 32 * (m0 + m);  // pair index: coefficients 2j, 2j + 1
+        const uint2 b00 = b2[0 * (N / 2) + j], b01 = b2[1 * (N / 2) + j];  // digit 0: residue 0, 1
+        const uint2 b10 = b2[2 * (N / 2) + j], b11 = b2[3 * (N / 2) + j];  // digit 1
+        const uint2 b20 = b2[4 * (N / 2) + j], b21 = b2[5 * (N / 2) + j];  // digit 2
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const uint64_t xv = P.delta * (uint64_t)((hw[m] >> (16 * e)) & 0xFFFFu);
+          const uint32_t d0 = (uint32_t)xv & 0xFFFFFu, d1 = (uint32_t)(xv >> 20) & 0xFFFFFu,
+                         d2 = (uint32_t)(xv >> 40);
+          acc0 += (uint64_t)d0 * (e ? b00.y : b00.x) + (uint64_t)d1 * (e ? b10.y : b10.x) +
+                  (uint64_t)d2 * (e ? b20.y : b20.x);
+          acc1 += (uint64_t)d0 * (e ? b01.y : b01.x) + (uint64_t)d1 * (e ? b11.y : b11.x) +
+                  (uint64_t)d2 * (e ? b21.y : b21.x);
+        }
       }
     }
 #pragma unroll
@@ -81,6 +91,15 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
     }
   }
   __syncthreads();
+}
+
+// A 64-bit load the compiler may neither hoist nor keep in a register: used
+// to re-read a query's database base pointer where it is needed instead of
+// holding it through the kernel.
+__device__ __forceinline__ const uint32_t* reload_ptr(const uint32_t* const* p) {
+  uint64_t v;
+  asm volatile("ld.global.nc.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return reinterpret_cast<const uint32_t*>(v);
 }
 
 // L2 prefetch of a contiguous device range with bulk (TMA) prefetches.
@@ -128,7 +147,7 @@ struct Smem {
   static constexpr int TOTAL = MISC + 128;
 };
 
-template <int MODE, bool SEEDED>
+template <int MODE, bool SEEDED, bool QDB>
 __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constant__ RespondArgs A) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
   using L = Smem<NR>;
@@ -149,14 +168,10 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const int gamma = P.gamma;
   const uint32_t shard = A.shard[qi];
   const int32_t cid = A.client[qi];
-  const uint32_t* Ebase = A.E;
-  const uint16_t* Hbase = A.H;
-  int nshards = A.nshards;
-  if (A.qdb) {
-    Ebase = A.qdb[qi].E;
-    Hbase = A.qdb[qi].H;
-    nshards = A.qdb[qi].nshards;
-  }
+  // QDB: the query names its database (serving loop); otherwise the launch's
+  const uint32_t* Ebase = QDB ? A.qdb[qi].E : A.E;
+  const uint16_t* Hbase = QDB ? A.qdb[qi].H : A.H;
+  const int nshards = QDB ? A.qdb[qi].nshards : A.nshards;
   if (shard >= (uint32_t)nshards || cid < 0 || cid >= A.nclients || A.yhat_table[cid] == nullptr) {
     if (tid == 0) A.status[qi] = ERR_INDEX;
     return;  // uniform over the CTA
@@ -213,7 +228,14 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const int sp = MODE == MODE_CRT_FIXED ? (kd - 1) * NTT_GT + x : ((r * 2 + (kd - 1)) * NTT_GT + x);
   const int snthr = MODE == MODE_CRT_FIXED ? 2 * NTT_GT : 4 * NTT_GT;
   const bool scatters = kd != 0;
-  const uint32_t* Eg = E + (size_t)sres * ELL * gamma * N;
+  // Eg: this group's residue of the contracted shard; with per-query
+  // databases it is re-derived at each use from the query's view
+  const uint32_t* Eg_fixed = QDB ? nullptr : E + (size_t)sres * ELL * gamma * N;
+  auto Eg_at = [&]() -> const uint32_t* {
+    if (!QDB) return Eg_fixed;
+    const uint32_t sh = *reinterpret_cast<const volatile uint32_t*>(A.shard + qi);
+    return reload_ptr(&A.qdb[qi].E) + ((size_t)sh * 2 * ELL + (size_t)sres * ELL) * gamma * N;
+  };
   const uint32_t* Ag = Ahat + sres * N;
   const uint32_t sq = P.r[sres].q, sqinv = P.r[sres].qinv;
 
@@ -224,7 +246,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   }
 
   // R_{gamma-1}
-  if (scatters) scatter_r(P, gamma - 1, Eg, Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
+  if (scatters) scatter_r(P, gamma - 1, Eg_at(), Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
   __syncthreads();
   if (kd == 0) {
     load16(SCAT + (MODE == MODE_CRT_FIXED ? r : 0) * N, x, vR);
@@ -241,7 +263,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
 #pragma unroll
       for (int j = 0; j < 16; j++) T[r * N + x + 128 * j] = canon2(vR[j], q);
     } else {
-      scatter_r(P, i, Eg, Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
+      scatter_r(P, i, Eg_at(), Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
     }
     __syncthreads();
     // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37)
@@ -361,20 +383,25 @@ size_t respond_smem_bytes(int mode) {
   return sizeof(uint32_t) * (mode == MODE_COMPAT ? Smem<1>::TOTAL : Smem<2>::TOTAL);
 }
 
-template <int MODE, bool SEEDED>
+template <int MODE, bool SEEDED, bool QDB>
 static cudaError_t launch_one(const RespondArgs& a, cudaStream_t st) {
   const size_t smem = respond_smem_bytes(MODE);
-  cudaError_t e = cudaFuncSetAttribute(respond_kernel<MODE, SEEDED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e =
+      cudaFuncSetAttribute(respond_kernel<MODE, SEEDED, QDB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  respond_kernel<MODE, SEEDED><<<a.nq, RBLOCK, smem, st>>>(a);
+  respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_mode(const RespondArgs& a, bool seeded, cudaStream_t st) {
+  if (a.qdb) return seeded ? launch_one<MODE, true, true>(a, st) : launch_one<MODE, false, true>(a, st);
+  return seeded ? launch_one<MODE, true, false>(a, st) : launch_one<MODE, false, false>(a, st);
 }
 
 cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st) {
   if (a.nq <= 0) return cudaSuccess;
-  if (a.P.mode == MODE_COMPAT)
-    return seeded ? launch_one<MODE_COMPAT, true>(a, st) : launch_one<MODE_COMPAT, false>(a, st);
-  return seeded ? launch_one<MODE_CRT_FIXED, true>(a, st) : launch_one<MODE_CRT_FIXED, false>(a, st);
+  return a.P.mode == MODE_COMPAT ? launch_mode<MODE_COMPAT>(a, seeded, st) : launch_mode<MODE_CRT_FIXED>(a, seeded, st);
 }
 
 }  // namespace ig
