@@ -61,7 +61,7 @@ MULMODS_PER_QUERY = 3.4e6
 DB_BYTES_PER_QUERY = (768 + 64) * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one B=128 respond launch, from the
 # ncu capture summarised in profiles/respond_kernel_b128.md
-NCU_TRAFFIC_PER_LAUNCH_B128 = 122.9e6
+NCU_TRAFFIC_PER_LAUNCH_B128 = 114.9e6
 
 
 def dist_env():

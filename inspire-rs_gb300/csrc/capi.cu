@@ -428,6 +428,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
   }
   P.delta = q / prm->p;
   P.mode = mode;
+  P.one = 1;
   e = c->tables.ensure(host.size() * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemcpy(c->tables.p, host.data(), host.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {

@@ -13,14 +13,19 @@ namespace ig {
 
 __device__ __forceinline__ uint32_t rotl32(uint32_t x, int k) { return __funnelshift_l(x, x, k); }
 
-#define IG_QR(a, b, c, d)                 \
-  a += b; d ^= a; d = rotl32(d, 16);      \
-  c += d; b ^= c; b = rotl32(b, 12);      \
-  a += b; d ^= a; d = rotl32(d, 8);       \
-  c += d; b ^= c; b = rotl32(b, 7);
+// The quarter round's additions are written as multiply-adds by `one` (a
+// runtime 1 the compiler cannot fold), which puts them on the integer
+// multiply-add pipe while the xors and rotates use the ALU pipe: the block
+// function is otherwise limited by the ALU pipe alone.
+#define IG_QR(a, b, c, d)                       \
+  a = a * one + b; d ^= a; d = rotl32(d, 16);   \
+  c = c * one + d; b ^= c; b = rotl32(b, 12);   \
+  a = a * one + b; d ^= a; d = rotl32(d, 8);    \
+  c = c * one + d; b ^= c; b = rotl32(b, 7);
 
-// Block `ctr` of the keystream keyed by key[8]; writes 16 words.
-__device__ __forceinline__ void chacha20_block(const uint32_t key[8], uint64_t ctr,
+// Block `ctr` of the keystream keyed by key[8]; writes 16 words.  `one`
+// must be 1.
+__device__ __forceinline__ void chacha20_block(const uint32_t key[8], uint64_t ctr, uint32_t one,
                                                uint32_t out[16]) {
   uint32_t x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
   uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];

@@ -43,6 +43,7 @@ struct DevParams {
   uint64_t delta;                    // floor(q / p)
   int gamma;                         // packed columns (num_to_pack)
   int mode;
+  uint32_t one;                      // 1 (a value the compiler cannot fold)
 };
 
 __device__ __forceinline__ TwiddleRef fwd_tw(const ResidueConsts& c) { return {c.fwd}; }

@@ -62,7 +62,7 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
     const int nblk = min(SUB, (need * 9) / 64 + 3);
     if (lt < nblk) {
       uint32_t w[16];
-      chacha20_block(key, blk + lt, w);
+      chacha20_block(key, blk + lt, P.one, w);
 #pragma unroll
       for (int k = 0; k < 8; k++) cand[k * SUB + lt] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
     }

@@ -181,18 +181,23 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const uint32_t* Y = A.yhat_table[cid];
   const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
 
-  // stream this query's shard (contracted form of the a side, raw columns)
-  // and client key table into L2 while the prologue runs
+  // stream what the b side reads (raw columns, query b rows) into L2 first;
+  // the contracted shard and the client key table follow once the b side is
+  // done, during the compute-bound row expansion, so that the burst of a
+  // whole launch's prefetches does not delay the b side's loads
   if (tid == 0) {
     prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
-    prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
-    if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
+    prefetch_l2(A.brows + (size_t)qi * ELL * 2 * N, sizeof(uint64_t) * (size_t)ELL * 2 * N);
   }
 
   // ---- b part of the column products (bp aliases SCAT+PB) ----
   column_b0(P, H, A.brows + (size_t)qi * ELL * 2 * N, SCAT, bpoly);
 
   // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
+  if (tid == 0) {
+    prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
+    if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
+  }
   {
     const int t = tid >> 8, lt = tid & 255;
     uint64_t* cand = reinterpret_cast<uint64_t*>(SC) + t * N;  // 3 x 16 KiB within SC
