@@ -532,8 +532,15 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
     and the mixed served workload over 8 databases of 2^18..2^26 entries."""
     from inspire import serving as sv
 
-    pool = sv.QueryPool(seeds, brows, locals_, pinned=True)
-    srv = inspire.Server(crs, max_batch=B, max_inflight=4, capacity=8192)
+    # the 32 real queries tiled to 256 pinned rows, so that one submit call
+    # can carry up to 256 queries (each still names its own shard)
+    reps = 256 // len(locals_)
+    pool = sv.QueryPool(np.tile(seeds, (reps, 1, 1)), np.tile(brows, (reps, 1, 1)), np.tile(locals_, reps),
+                        pinned=True)
+    main = [sv.Target(edb, nshards, 1.0)]
+    tuned = sv.autotune(lambda **kw: inspire.Server(crs, capacity=8192, **kw), main, pool, cid)
+    cfg = tuned["best"]
+    srv = inspire.Server(crs, capacity=8192, **cfg)
 
     def check(samples, raws, targets_nshards):
         for d, shard, pidx, out in samples[:16]:
@@ -542,22 +549,55 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
             if args.mode == "crt_fixed":
                 assert np.array_equal(got, raws[d][gi * ENTRY:(gi + 1) * ENTRY]), "served response failed to decrypt"
 
-    main = [sv.Target(edb, nshards, 1.0)]
     sv.run(srv, main, pool, cid, rate=None, n_queries=8192, n_threads=4)  # warm-up
-    closed = sv.run(srv, main, pool, cid, rate=None, n_queries=1 << 17, n_threads=4, keep_outputs=True)
+
+    def closed_run(server, targets, n_threads):
+        st0 = server.stats()
+        res = sv.run(server, targets, pool, cid, rate=None, n_queries=1 << 17, n_threads=n_threads, keep_outputs=True,
+                     closed_chunk=256)
+        st1 = server.stats()
+        res["mean_batch"] = (st1["completed"] - st0["completed"]) / max(1, st1["batches"] - st0["batches"])
+        res["submitter_threads"] = n_threads
+        return res
+
+    def burst_run(server, n=8192):
+        """One thread submits n queries back to back (pool-sized calls, rows
+        borrowed), then collects them: the loop's rate without per-call
+        Python overhead on the collection side."""
+        from inspire.pir import now_ns
+
+        rng = np.random.default_rng(3)
+        sh = rng.integers(0, nshards, size=n).astype(np.uint32)
+        cids = np.full(pool.q, cid, np.int32)
+        tickets = []
+        t0 = now_ns()
+        k = 0
+        while k < n:
+            m = min(pool.q, n - k)
+            t, rc = server.submit(edb, sh[k:k + m], pool.seeds[:m], pool.b_rows[:m], cids[:m], borrow=True)
+            tickets.append(t)
+            k += len(t)
+        done = server.poll_batch(np.concatenate(tickets))
+        return {"n": n, "achieved_qps": n / ((done.max() - t0) / 1e9)}
+
+    burst_run(srv)  # warm-up
+    burst = burst_run(srv)
+    closed = max((closed_run(srv, main, t) for t in (4, 8)), key=lambda r: r["achieved_qps"])
     check(closed.pop("samples"), [db_raw], None)
     cap = closed["achieved_qps"]
+    sv.run(srv, main, pool, cid, rate=0.25 * cap, duration_s=0.5, n_threads=4, seed=10)  # open-loop warm-up
     sweep = []
     for frac in SERVE_RATE_FRACS:
         r = sv.run(srv, main, pool, cid, rate=frac * cap, duration_s=SERVE_DURATION_S, n_threads=4, seed=11)
         r["load_frac"] = frac
         sweep.append(r)
     head = next((r for r in sweep if r["load_frac"] == 0.75), sweep[-1])
-    out = {"config": {"max_batch": B, "streams": 4, "capacity": 8192, "submitter_threads": 4,
+    out = {"config": {**cfg, "capacity": 8192, "submitter_threads": closed["submitter_threads"],
+                      "autotune": tuned["table"],
                       "query_rows": "pinned host memory, borrowed (read in place by the GPU)",
                       "arrivals": "Poisson, offered rate = fraction x saturated closed-loop rate",
                       "database": f"{nshards * N} entries x 32 B"},
-           "closed_loop": closed, "open_loop": sweep,
+           "closed_loop": closed, "burst": burst, "open_loop": sweep,
            "headline": {"p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"], "offered_qps": head["offered_qps"],
                         "achieved_qps": head["achieved_qps"], "load_frac": head["load_frac"]}}
     srv.close()
@@ -574,11 +614,12 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
             targets.append(sv.Target(db, (1 << lg) // N, float(1 << lg)))
         torch.cuda.synchronize()
         setup = time.perf_counter() - t0
-        srv = inspire.Server(crs, max_batch=B, max_inflight=4, capacity=8192)
+        srv = inspire.Server(crs, capacity=8192, **cfg)
         sv.run(srv, targets, pool, cid, rate=None, n_queries=8192, n_threads=4)  # warm-up
-        mclosed = sv.run(srv, targets, pool, cid, rate=None, n_queries=1 << 17, n_threads=4, keep_outputs=True)
+        mclosed = closed_run(srv, targets, closed["submitter_threads"])
         check(mclosed.pop("samples"), raws, None)
         mcap = mclosed["achieved_qps"]
+        sv.run(srv, targets, pool, cid, rate=0.25 * mcap, duration_s=0.5, n_threads=4, seed=10)  # warm-up
         msweep = []
         for frac in (0.5, 0.75, 0.9):
             r = sv.run(srv, targets, pool, cid, rate=frac * mcap, duration_s=SERVE_DURATION_S, n_threads=4, seed=12)

@@ -202,6 +202,8 @@ typedef struct {
   uint32_t capacity;      /* queries submitted and not yet polled, at most */
   uint64_t device_budget; /* device bytes for in-flight batches; 0 = no limit.
                              Fewer streams are used if max_inflight batches do not fit. */
+  uint32_t batch_wait_us; /* while at least one query per SM is in flight, a free
+                             stream waits up to this long for a full batch */
 } inspire_server_config;
 
 typedef struct {
@@ -210,7 +212,7 @@ typedef struct {
   uint32_t streams;                       /* streams in use (after the device budget) */
 } inspire_server_stats;
 
-/* max_batch 128, max_inflight 4, capacity 4096, device_budget 0. */
+/* max_batch 128, max_inflight 4, capacity 4096, device_budget 0, batch_wait_us 100. */
 void inspire_server_config_default(inspire_server_config *cfg);
 int inspire_server_create(inspire_ctx *ctx, const inspire_server_config *cfg, inspire_server **out);
 /* Waits for batches in flight, then frees the loop.  Unpolled tickets die. */

@@ -118,6 +118,7 @@ struct Rec {
   uint32_t shard = 0;
   int32_t client = 0;
   int64_t t_arrival = 0, t_done = 0;
+  int64_t t_enqueue = 0;  // when the query became pending
   int cuda_error = 0;  // nonzero: the batch failed on the host side
 };
 
@@ -146,6 +147,7 @@ struct inspire_server {
   bool stop = false;
   std::thread worker;
   uint64_t n_submitted = 0, n_completed = 0, n_batches = 0;
+  int sm_count = 0;
   std::string worker_error;
 
   uint8_t* rec_ptr(int i) const { return pool + (size_t)i * REC_BYTES; }
@@ -231,8 +233,16 @@ void inspire_server::run() {
         s.recs.clear();
         s.busy = false;
       }
+      size_t inflight_q = 0;
+      for (const auto& sp : slots) inflight_q += sp->busy ? sp->recs.size() : 0;
       for (auto& sp : slots) {
         if (sp->busy || pending.empty()) continue;
+        // Batch formation: a full batch goes at once; a partial one goes at
+        // once while the GPU has idle SMs, else when its oldest query has
+        // waited batch_wait_us (the batches in flight keep the GPU busy).
+        if (pending.size() < cfg.max_batch && inflight_q >= (size_t)sm_count &&
+            now_ns() - recs[pending.front()].t_enqueue < (int64_t)cfg.batch_wait_us * 1000)
+          break;
         Slot& s = *sp;
         s.recs.clear();
         while (!pending.empty() && s.recs.size() < cfg.max_batch) {
@@ -243,11 +253,13 @@ void inspire_server::run() {
         }
         s.busy = true;
         n_batches++;
+        inflight_q += s.recs.size();
         to_launch.push_back(&s);
       }
       bool any_busy = false;
       for (const auto& sp : slots) any_busy |= sp->busy;
       if (stop && !any_busy && pending.empty()) break;
+      // nothing in flight: pending queries (if any) were launched above
       if (finished.empty() && to_launch.empty() && !any_busy) {
         cv_work.wait(lk, [&] { return stop || !pending.empty(); });
         continue;
@@ -285,6 +297,7 @@ void inspire_server_config_default(inspire_server_config* cfg) {
   cfg->max_inflight = 4;
   cfg->capacity = 4096;
   cfg->device_budget = 0;
+  cfg->batch_wait_us = 100;
 }
 
 int64_t inspire_now_ns(void) { return now_ns(); }
@@ -304,9 +317,13 @@ int inspire_server_create(inspire_ctx* c, const inspire_server_config* cfg, insp
     if (fit < streams) streams = (uint32_t)fit;
   }
   if (int rc = set_device(c)) return rc;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || sms <= 0)
+    return fail(INSPIRE_ERR_CUDA, "cannot read the SM count");
   inspire_server* s = new inspire_server();
   s->ctx = c;
   s->cfg = *cfg;
+  s->sm_count = sms;
   auto bail = [&](int rc) {
     inspire_server_destroy(s);
     return rc;
@@ -465,8 +482,10 @@ int inspire_server_submit(inspire_server* s, uint32_t n, const inspire_db* const
   }
   {
     std::lock_guard<std::mutex> lk(s->mu);
+    const int64_t t_enq = now_ns();
     for (size_t k = 0; k < got.size(); k++) {
       s->recs[got[k]].state = PENDING;
+      s->recs[got[k]].t_enqueue = t_enq;
       s->pending.push_back(got[k]);
       tickets[k] = s->ticket(got[k]);
     }

@@ -71,6 +71,7 @@ class ServerConfigC(C.Structure):
         ("max_inflight", C.c_uint32),
         ("capacity", C.c_uint32),
         ("device_budget", C.c_uint64),
+        ("batch_wait_us", C.c_uint32),
     ]
 
 

@@ -390,13 +390,14 @@ class Server:
     ServerCrs.register_client; queries may name any database of the CRS."""
 
     def __init__(self, crs: ServerCrs, max_batch: int = 128, max_inflight: int = 4, capacity: int = 4096,
-                 device_budget: int = 0):
+                 device_budget: int = 0, batch_wait_us: int = 100):
         self.crs = crs
         self.L = crs.L
         cfg = nat.ServerConfigC()
         self.L.inspire_server_config_default(C.byref(cfg))
         cfg.max_batch, cfg.max_inflight, cfg.capacity, cfg.device_budget = max_batch, max_inflight, capacity, \
             device_budget
+        cfg.batch_wait_us = batch_wait_us
         h = C.c_void_p()
         _check(self.L.inspire_server_create(crs.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -14,6 +14,7 @@ index is uniform over all entries.
 """
 from __future__ import annotations
 
+import gc
 import threading
 import time
 from collections import deque
@@ -231,16 +232,24 @@ def run(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate:
     t0 = now_ns() + 20_000_000
     lanes = [_Lane(server, handles, pool, client_id, None if offs is None else t0 + offs, dbi, shards,
                    max_burst if rate is not None else closed_chunk, keep_outputs) for offs, dbi, shards in plans]
-    wall0 = time.perf_counter()
-    ths = []
-    for ln in lanes:
-        ths.append(threading.Thread(target=ln.submitter))
-        ths.append(threading.Thread(target=ln.collector))
-    for th in ths:
-        th.start()
-    for th in ths:
-        th.join()
-    wall = time.perf_counter() - wall0
+    # the cyclic garbage collector stops every load-generator thread while it
+    # runs (tens of ms in a large process); it stays off during the run
+    gc_was_enabled = gc.isenabled()
+    gc.disable()
+    try:
+        wall0 = time.perf_counter()
+        ths = []
+        for ln in lanes:
+            ths.append(threading.Thread(target=ln.submitter))
+            ths.append(threading.Thread(target=ln.collector))
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        wall = time.perf_counter() - wall0
+    finally:
+        if gc_was_enabled:
+            gc.enable()
     for ln in lanes:
         if ln.error is not None:
             raise ln.error
@@ -257,3 +266,28 @@ def run(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate:
     if keep_outputs:
         res["samples"] = [s for ln in lanes for s in ln.samples]
     return res
+
+
+def autotune(make_server, targets: List[Target], pool: QueryPool, client_id: int, *,
+             batches=(128, 152, 256), inflight=(4, 8), waits_us=(100,), n_queries: int = 1 << 15,
+             n_threads: int = 4) -> dict:
+    """Pick the serving configuration (max_batch, max_inflight,
+    batch_wait_us) with the highest saturated closed-loop rate.
+    make_server(max_batch=, max_inflight=, batch_wait_us=) builds a server;
+    each candidate gets a warm-up run, then a timed run of n_queries.
+    Returns {"best": config, "table": [config + rate, ...]}."""
+    table = []
+    for mb in batches:
+        for mi in inflight:
+            for w in waits_us:
+                srv = make_server(max_batch=mb, max_inflight=mi, batch_wait_us=w)
+                try:
+                    run(srv, targets, pool, client_id, rate=None, n_queries=n_queries // 4, n_threads=n_threads)
+                    r = run(srv, targets, pool, client_id, rate=None, n_queries=n_queries, n_threads=n_threads,
+                            closed_chunk=min(pool.q, 256))
+                finally:
+                    srv.close()
+                table.append({"max_batch": mb, "max_inflight": mi, "batch_wait_us": w,
+                              "qps": r["achieved_qps"], "p50_ms": r["p50_ms"]})
+    best = max(table, key=lambda t: t["qps"])
+    return {"best": {k: best[k] for k in ("max_batch", "max_inflight", "batch_wait_us")}, "table": table}
