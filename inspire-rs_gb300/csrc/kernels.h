@@ -19,6 +19,19 @@ struct DbView {
   int pad;
 };
 
+// One admitted query of the serving loop.  The descriptor itself is copied to
+// device memory per batch; the rows and the response live in pinned host
+// memory that the Respond kernel reads and writes directly.
+struct QueryDesc {
+  const uint8_t* seeds;   // [ELL][32] seeds of rows ELL..2ELL-1
+  const uint64_t* brows;  // [ELL][2][N] b-polys of rows ELL..2ELL-1 (16-byte aligned)
+  uint64_t* out;          // [2][2][N] response destination (16-byte aligned)
+  int32_t* status;        // kernel status destination
+  DbView db;
+  uint32_t shard;
+  int32_t client;
+};
+
 struct RespondArgs {
   DevParams P;
   int nq;
@@ -34,7 +47,10 @@ struct RespondArgs {
   const uint32_t* what;          // [(gamma-1)][ELL][2][N] rotated w_mask (CRS)
   uint64_t* out;                 // [nq][2][2][N] response (a_hat, b) residues
   int* status;                   // [nq]
-  const DbView* qdb;             // [nq] per-query database (overrides E/H/nshards) or null
+  // Serving loop: per-query descriptors in device memory (override shard,
+  // client, seeds, brows, E/H/nshards, out and status; rows are read from and
+  // responses written to the pinned host memory they point at), or null.
+  const struct QueryDesc* qdesc;
 };
 
 // NoPacking respond (respond.rs:71-115): per query the combined ciphertext
@@ -53,24 +69,6 @@ struct NoPackingArgs {
   uint64_t* out_columns;
   int* status;
 };
-
-// One admitted query of the serving loop, in pinned host memory that the
-// device reads and writes directly (no staging copies on the host).
-struct QueryDesc {
-  const uint8_t* seeds;   // [ELL][32] seeds of rows ELL..2ELL-1
-  const uint64_t* brows;  // [ELL][2][N] b-polys of rows ELL..2ELL-1 (16-byte aligned)
-  uint64_t* out;          // [2][2][N] response destination (16-byte aligned)
-  int32_t* status;        // kernel status destination
-  DbView db;
-  uint32_t shard;
-  int32_t client;
-};
-
-// Gather the batch's query rows from the descriptors into device buffers
-// laid out as RespondArgs expects; scatter responses and statuses back.
-cudaError_t launch_gather(const QueryDesc* d, int nq, uint8_t* seeds, uint64_t* brows, uint32_t* shard,
-                          int32_t* client, DbView* qdb, cudaStream_t st);
-cudaError_t launch_scatter(const QueryDesc* d, int nq, const uint64_t* out, const int* status, cudaStream_t st);
 
 size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);

@@ -47,7 +47,7 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
   for (int idx = tid; idx < ELL * 2 * N; idx += RBLOCK) {
     const int i = idx & (N - 1), tr = idx >> LOGN, r = tr & 1;
     const uint64_t* row = brows + (size_t)tr * N;
-    uint32_t v = (uint32_t)__ldg(row + (i == 0 ? 0 : N - i));
+    uint32_t v = (uint32_t)__ldcg(row + (i == 0 ? 0 : N - i));  // rows may be in host memory
     if (i != 0 && v != 0) v = P.r[r].q - v;
     bp[idx] = v;
   }
@@ -96,10 +96,11 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
 // A 64-bit load the compiler may neither hoist nor keep in a register: used
 // to re-read a query's database base pointer where it is needed instead of
 // holding it through the kernel.
-__device__ __forceinline__ const uint32_t* reload_ptr(const uint32_t* const* p) {
+template <class T>
+__device__ __forceinline__ T* reload_ptr(T* const* p) {
   uint64_t v;
   asm volatile("ld.global.nc.u64 %0, [%1];" : "=l"(v) : "l"(p));
-  return reinterpret_cast<const uint32_t*>(v);
+  return reinterpret_cast<T*>(v);
 }
 
 // L2 prefetch of a contiguous device range with bulk (TMA) prefetches.
@@ -143,7 +144,7 @@ struct Smem {
   static constexpr int SCAT = T + 3 * N;                   // [2][N] R_i (slot layout, swizzled)
   static constexpr int PB = SCAT + 2 * N;                  // [2][2][N] partial products of digits 1, 2
   static constexpr int ACC = PB + 4 * N;                   // [RG][N] per-group b accumulators
-  static constexpr int MISC = ACC + RG * N;                // bpoly[32], ws[3][20]
+  static constexpr int MISC = ACC + RG * N;                // bpoly[32], ws[3][20], staged seeds (96 B)
   static constexpr int TOTAL = MISC + 128;
 };
 
@@ -166,32 +167,45 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const int r = g / 3, kd = g - 3 * r;  // residue, gadget digit of this group
   uint32_t* ACC = smem + L::ACC + g * N;  // this group's b accumulator
   const int gamma = P.gamma;
-  const uint32_t shard = A.shard[qi];
-  const int32_t cid = A.client[qi];
-  // QDB: the query names its database (serving loop); otherwise the launch's
-  const uint32_t* Ebase = QDB ? A.qdb[qi].E : A.E;
-  const uint16_t* Hbase = QDB ? A.qdb[qi].H : A.H;
-  const int nshards = QDB ? A.qdb[qi].nshards : A.nshards;
+  // QDB (serving loop): this query's fields come from its descriptor in
+  // device memory, its rows and response from / to pinned host memory;
+  // otherwise from the launch's arrays.  Descriptor fields are re-read where
+  // used (reload_*) rather than held in registers.
+  const QueryDesc* D = QDB ? A.qdesc + qi : nullptr;
+  const uint32_t shard = QDB ? D->shard : A.shard[qi];
+  const int32_t cid = QDB ? D->client : A.client[qi];
+  const uint32_t* Ebase = QDB ? D->db.E : A.E;
+  const uint16_t* Hbase = QDB ? D->db.H : A.H;
+  const int nshards = QDB ? D->db.nshards : A.nshards;
+  auto status_ptr = [&]() -> int32_t* {
+    return QDB ? reload_ptr(&D->status) : A.status + qi;
+  };
   if (shard >= (uint32_t)nshards || cid < 0 || cid >= A.nclients || A.yhat_table[cid] == nullptr) {
-    if (tid == 0) A.status[qi] = ERR_INDEX;
+    if (tid == 0) *status_ptr() = ERR_INDEX;
     return;  // uniform over the CTA
   }
   const uint32_t* E = Ebase + (size_t)shard * 2 * ELL * gamma * N;
   const uint16_t* H = Hbase + (size_t)shard * gamma * N;
   const uint32_t* Y = A.yhat_table[cid];
   const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
+  const uint64_t* brows = QDB ? D->brows : A.brows + (size_t)qi * ELL * 2 * N;
 
   // stream what the b side reads (raw columns, query b rows) into L2 first;
   // the contracted shard and the client key table follow once the b side is
   // done, during the compute-bound row expansion, so that the burst of a
-  // whole launch's prefetches does not delay the b side's loads
+  // whole launch's prefetches does not delay the b side's loads.  (Rows in
+  // host memory are not prefetched.)
   if (tid == 0) {
     prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
-    prefetch_l2(A.brows + (size_t)qi * ELL * 2 * N, sizeof(uint64_t) * (size_t)ELL * 2 * N);
+    if (!QDB) prefetch_l2(brows, sizeof(uint64_t) * (size_t)ELL * 2 * N);
   }
+  // seeds in host memory: staged into shared memory (ordered before the
+  // expansion by the b side's barriers)
+  uint8_t* seed_sm = reinterpret_cast<uint8_t*>(smem + L::MISC + 96);
+  if (QDB && tid < ELL * 32) seed_sm[tid] = __ldcv(D->seeds + tid);
 
   // ---- b part of the column products (bp aliases SCAT+PB) ----
-  column_b0(P, H, A.brows + (size_t)qi * ELL * 2 * N, SCAT, bpoly);
+  column_b0(P, H, brows, SCAT, bpoly);
 
   // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
   if (tid == 0) {
@@ -204,8 +218,8 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
     uint32_t* a0 = T + t * 2 * N;                               // 3 x 16 KiB within T..PB
     uint32_t* a1 = a0 + N;
     if (SEEDED) {
-      const bool ok = expand_seeded_row<NR>(P, A.seeds + ((size_t)qi * ELL + t) * 32, cand, a0, a1, wsb + 20 * t,
-                                            7 + t, lt);
+      const uint8_t* seed = QDB ? seed_sm + 32 * t : A.seeds + ((size_t)qi * ELL + t) * 32;
+      const bool ok = expand_seeded_row<NR>(P, seed, cand, a0, a1, wsb + 20 * t, 7 + t, lt);
       if (lt == 0) wsb[20 * t + 17] = ok;
     } else {
       const uint64_t* ar = A.arows + ((size_t)qi * ELL + t) * 2 * N;
@@ -214,7 +228,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   }
   __syncthreads();
   // the query's status is written once, by one thread
-  if (tid == 0) A.status[qi] = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
+  if (tid == 0) *status_ptr() = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
   if (r < NR) {  // group (r, t=kd) transforms row kd, residue r
     uint32_t v[16];
     const uint32_t* src = T + kd * 2 * N + r * N;
@@ -238,8 +252,8 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const uint32_t* Eg_fixed = QDB ? nullptr : E + (size_t)sres * ELL * gamma * N;
   auto Eg_at = [&]() -> const uint32_t* {
     if (!QDB) return Eg_fixed;
-    const uint32_t sh = *reinterpret_cast<const volatile uint32_t*>(A.shard + qi);
-    return reload_ptr(&A.qdb[qi].E) + ((size_t)sh * 2 * ELL + (size_t)sres * ELL) * gamma * N;
+    const uint32_t sh = *reinterpret_cast<const volatile uint32_t*>(&D->shard);
+    return reload_ptr(&D->db.E) + ((size_t)sh * 2 * ELL + (size_t)sres * ELL) * gamma * N;
   };
   const uint32_t* Ag = Ahat + sres * N;
   const uint32_t sq = P.r[sres].q, sqinv = P.r[sres].qinv;
@@ -356,7 +370,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   // ---- outputs: a_hat = INTT(R_0) (inspiring2.rs:1027-1029),
   //      b = b_poly + INTT(sum y_all * bold_t) (inspiring2.rs:1217-1221) ----
   // (the b accumulators were last written before the final barrier)
-  uint64_t* out = A.out + (size_t)qi * 4 * N;
+  uint64_t* out = QDB ? reload_ptr(&D->out) : A.out + (size_t)qi * 4 * N;
   if (kd == 0) {
     ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
@@ -400,7 +414,7 @@ static cudaError_t launch_one(const RespondArgs& a, cudaStream_t st) {
 
 template <int MODE>
 static cudaError_t launch_mode(const RespondArgs& a, bool seeded, cudaStream_t st) {
-  if (a.qdb) return seeded ? launch_one<MODE, true, true>(a, st) : launch_one<MODE, false, true>(a, st);
+  if (a.qdesc) return seeded ? launch_one<MODE, true, true>(a, st) : launch_one<MODE, false, true>(a, st);
   return seeded ? launch_one<MODE, true, false>(a, st) : launch_one<MODE, false, false>(a, st);
 }
 

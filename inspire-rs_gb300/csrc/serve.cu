@@ -2,14 +2,15 @@
 // queries over several CUDA streams.
 //
 // Submitted queries are copied into records of a pinned, device-mapped pool
-// (rows ELL..2ELL-1 only: seeds and b-polys).  A dispatcher thread takes up to
-// max_batch pending queries whenever one of its streams is free, writes one
-// QueryDesc per query into that stream's pinned descriptor array, and issues
-// gather -> respond -> scatter -> event on the stream.  The gather and scatter
-// kernels read the query rows from, and write the responses to, the pool over
-// the host link directly (NVLink-C2C on a Grace-Blackwell node), so no host
-// thread copies a batch.  Batches on different streams overlap on the device,
-// which also fills the SMs a single batch leaves idle.
+// (rows ELL..2ELL-1 only: seeds and b-polys), or borrowed in place.  A
+// dispatcher thread takes up to max_batch pending queries whenever one of its
+// streams is free, writes one QueryDesc per query into that stream's pinned
+// descriptor array, and issues descriptor copy -> respond -> event on the
+// stream.  The Respond kernel reads each query's rows from, and writes its
+// response to, pinned host memory over the host link (NVLink-C2C on a
+// Grace-Blackwell node), so no host thread copies a batch and no extra
+// kernel runs.  Batches on different streams overlap on the device, which
+// also fills the SMs a single batch leaves idle.
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -23,70 +24,6 @@
 
 using namespace ig;
 using namespace ighost;
-
-namespace ig {
-namespace {
-
-constexpr int IO_THREADS = 256;
-static_assert(sizeof(QueryDesc) == 64, "QueryDesc is read as four 16-byte words");
-
-// Descriptors live in pinned host memory rewritten between batches: read them
-// with cache-volatile loads.
-__device__ __forceinline__ void load_desc(const QueryDesc* d, QueryDesc& q) {
-  const uint4* s = reinterpret_cast<const uint4*>(d);
-  uint4* t = reinterpret_cast<uint4*>(&q);
-#pragma unroll
-  for (int i = 0; i < 4; i++) t[i] = __ldcv(s + i);
-}
-
-// Query rows: pool -> device buffers in the layout RespondArgs expects.
-__global__ void __launch_bounds__(IO_THREADS) gather_kernel(const QueryDesc* __restrict__ d, uint8_t* seeds,
-                                                            uint64_t* brows, uint32_t* shard, int32_t* client,
-                                                            DbView* qdb) {
-  __shared__ __align__(16) QueryDesc q;
-  const int qi = blockIdx.x, tid = threadIdx.x;
-  if (tid == 0) load_desc(d + qi, q);
-  __syncthreads();
-  const uint4* src = reinterpret_cast<const uint4*>(q.brows);
-  uint4* dst = reinterpret_cast<uint4*>(brows + (size_t)qi * ELL * 2 * N);
-  for (int i = tid; i < ELL * N; i += IO_THREADS) dst[i] = __ldcv(src + i);  // ELL * 2N u64
-  if (tid < ELL * 32) seeds[(size_t)qi * ELL * 32 + tid] = __ldcv(q.seeds + tid);
-  if (tid == 0) {
-    shard[qi] = q.shard;
-    client[qi] = q.client;
-    qdb[qi] = q.db;
-  }
-}
-
-// Responses and statuses: device buffers -> pool.
-__global__ void __launch_bounds__(IO_THREADS) scatter_kernel(const QueryDesc* __restrict__ d, const uint64_t* out,
-                                                             const int* status) {
-  __shared__ __align__(16) QueryDesc q;
-  const int qi = blockIdx.x, tid = threadIdx.x;
-  if (tid == 0) load_desc(d + qi, q);
-  __syncthreads();
-  const uint4* src = reinterpret_cast<const uint4*>(out + (size_t)qi * 4 * N);
-  uint4* dst = reinterpret_cast<uint4*>(q.out);
-  for (int i = tid; i < 2 * N; i += IO_THREADS) dst[i] = src[i];  // 4N u64
-  if (tid == 0) *q.status = status[qi];
-}
-
-}  // namespace
-
-cudaError_t launch_gather(const QueryDesc* d, int nq, uint8_t* seeds, uint64_t* brows, uint32_t* shard,
-                          int32_t* client, DbView* qdb, cudaStream_t st) {
-  if (nq <= 0) return cudaSuccess;
-  gather_kernel<<<nq, IO_THREADS, 0, st>>>(d, seeds, brows, shard, client, qdb);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_scatter(const QueryDesc* d, int nq, const uint64_t* out, const int* status, cudaStream_t st) {
-  if (nq <= 0) return cudaSuccess;
-  scatter_kernel<<<nq, IO_THREADS, 0, st>>>(d, out, status);
-  return cudaGetLastError();
-}
-
-}  // namespace ig
 
 namespace {
 
@@ -103,9 +40,8 @@ constexpr size_t REC_STATUS = REC_OUT + sizeof(uint64_t) * 4 * N;
 constexpr size_t REC_BYTES = (REC_STATUS + 16 + 255) & ~(size_t)255;
 constexpr int TICKET_IDX_BITS = 24;
 
-// Device bytes one query of a batch holds.
-constexpr size_t SLOT_BYTES_PER_QUERY = 32 * ELL + sizeof(uint64_t) * ELL * 2 * N + sizeof(uint64_t) * 4 * N +
-                                        sizeof(uint32_t) + sizeof(int32_t) + sizeof(DbView) + sizeof(int);
+// Device bytes one query of a batch holds (its descriptor).
+constexpr size_t SLOT_BYTES_PER_QUERY = sizeof(QueryDesc);
 
 enum RecState { FREE = 0, PENDING = 1, INFLIGHT = 2, DONE = 3, COLLECTING = 4 };
 
@@ -125,9 +61,8 @@ struct Rec {
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
-  QueryDesc* desc = nullptr;   // pinned, mapped (host address)
-  QueryDesc* ddesc = nullptr;  // its device address
-  DevMem seeds, brows, shard, client, qdb, out, status;
+  QueryDesc* desc = nullptr;  // pinned (host)
+  DevMem ddesc;               // the batch's descriptors in device memory
   std::vector<int> recs;
   bool busy = false;
 };
@@ -157,7 +92,7 @@ struct inspire_server {
   int launch(Slot& s, const std::vector<int>& batch);
 };
 
-// Issue gather -> respond -> scatter -> event for `batch` on slot `s`.
+// Issue descriptor copy -> respond -> event for `batch` on slot `s`.
 int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   const int n = (int)batch.size();
   for (int k = 0; k < n; k++) {
@@ -174,27 +109,15 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   }
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (int rc = sync_client_table(ctx)) return rc;
-  CUDA_TRY(launch_gather(s.ddesc, n, s.seeds.as<uint8_t>(), s.brows.as<uint64_t>(), s.shard.as<uint32_t>(),
-                         s.client.as<int32_t>(), s.qdb.as<DbView>(), s.st));
+  CUDA_TRY(cudaMemcpyAsync(s.ddesc.p, s.desc, sizeof(QueryDesc) * n, cudaMemcpyHostToDevice, s.st));
   RespondArgs a{};
   a.P = ctx->P;
   a.nq = n;
-  a.shard = s.shard.as<uint32_t>();
-  a.seeds = s.seeds.as<uint8_t>();
-  a.arows = nullptr;
-  a.brows = s.brows.as<uint64_t>();
-  a.client = s.client.as<int32_t>();
   a.yhat_table = ctx->client_table.as<const uint32_t*>();
   a.nclients = (int)ctx->client_ptrs.size();
-  a.nshards = 0;
-  a.E = nullptr;
-  a.H = nullptr;
   a.what = ctx->what.as<uint32_t>();
-  a.out = s.out.as<uint64_t>();
-  a.status = s.status.as<int>();
-  a.qdb = s.qdb.as<DbView>();
+  a.qdesc = s.ddesc.as<QueryDesc>();
   CUDA_TRY(launch_respond(a, true, s.st));
-  CUDA_TRY(launch_scatter(s.ddesc, n, s.out.as<uint64_t>(), s.status.as<int>(), s.st));
   CUDA_TRY(cudaEventRecord(s.ev, s.st));
   return INSPIRE_OK;
 }
@@ -344,14 +267,9 @@ int inspire_server_create(inspire_ctx* c, const inspire_server_config* cfg, insp
     Slot& sl = *slp;
     if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
-        cudaHostAlloc(reinterpret_cast<void**>(&sl.desc), sizeof(QueryDesc) * B, cudaHostAllocMapped) != cudaSuccess ||
-        cudaHostGetDevicePointer(reinterpret_cast<void**>(&sl.ddesc), sl.desc, 0) != cudaSuccess)
+        cudaHostAlloc(reinterpret_cast<void**>(&sl.desc), sizeof(QueryDesc) * B, cudaHostAllocDefault) != cudaSuccess)
       return bail(fail(INSPIRE_ERR_CUDA, "serving stream setup failed"));
-    if (sl.seeds.ensure(32 * ELL * B) || sl.brows.ensure(sizeof(uint64_t) * ELL * 2 * N * B) ||
-        sl.shard.ensure(sizeof(uint32_t) * B) || sl.client.ensure(sizeof(int32_t) * B) ||
-        sl.qdb.ensure(sizeof(DbView) * B) || sl.out.ensure(sizeof(uint64_t) * 4 * N * B) ||
-        sl.status.ensure(sizeof(int) * B))
-      return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, "serving slot buffers"));
+    if (sl.ddesc.ensure(sizeof(QueryDesc) * B)) return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, "serving slot buffers"));
   }
   s->worker = std::thread([s] { s->run(); });
   *out = s;

@@ -179,12 +179,14 @@ def test_serving_errors_and_tickets(world):
 def test_device_budget_limits_streams(world):
     W = world
     inspire = W["inspire"]
-    one_batch = 8 * (96 + 6 * 2048 * 8 + 4 * 2048 * 8 + 40)
-    srv = inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=2 * one_batch + 100)
+    # in-flight device memory per batch: one 64-byte descriptor per query (the
+    # rows and responses stay in pinned host memory)
+    one_batch = 8 * 64
+    srv = inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=2 * one_batch + 10)
     assert srv.stats()["streams"] == 2
     srv.close()
     with pytest.raises(inspire.PirError, match="below one batch"):
-        inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=1000)
+        inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=one_batch - 1)
 
 
 def test_borrowed_rows_mixed_databases_one_call(world):
