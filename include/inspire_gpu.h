@@ -100,6 +100,20 @@ int inspire_crs_load(inspire_ctx *ctx, const uint8_t w_seed[32], uint32_t num_co
 int inspire_db_create(inspire_ctx *ctx, const uint8_t *raw, uint64_t n_entries, uint32_t entry_size,
                       inspire_db **out);
 void inspire_db_destroy(inspire_db *db);
+
+/* Load the crate's binary shard files from `dir` straight into HBM:
+ * save_shards_binary's format (src/pir/mmap.rs:19-53, shard-{id:04}.bin),
+ * read as MmapDatabase::open / get_shard / load_shard_binary read it
+ * (mmap.rs:56-122): every "shard-*" file is one shard and ids 0..n-1 must all
+ * exist ("Shard {id} not found" otherwise).  Each shard must hold num_columns
+ * encoded 16-bit column polynomials over this context's moduli.  The result
+ * equals inspire_db_create on the raw entries the files encode. */
+int inspire_db_load_shards(inspire_ctx *ctx, const char *dir, inspire_db **out);
+
+/* Write a resident database as the crate's binary shard files into `dir`
+ * (which must exist), in save_shards_binary's format, with the moduli of
+ * `params`. */
+int inspire_db_save_shards(const inspire_db *db, const inspire_params *params, const char *dir);
 uint32_t inspire_db_num_shards(const inspire_db *db);
 /* Device bytes held by the database. */
 uint64_t inspire_db_device_bytes(const inspire_db *db);

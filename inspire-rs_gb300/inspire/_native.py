@@ -107,6 +107,8 @@ def load(path: str = LIB_PATH):
         "inspire_crs_load": (C.c_int, [vp, vp, u32]),
         "inspire_db_create": (C.c_int, [vp, vp, u64, u32, C.POINTER(vp)]),
         "inspire_db_destroy": (None, [vp]),
+        "inspire_db_load_shards": (C.c_int, [vp, C.c_char_p, C.POINTER(vp)]),
+        "inspire_db_save_shards": (C.c_int, [vp, C.POINTER(InspireParamsC), C.c_char_p]),
         "inspire_db_num_shards": (u32, [vp]),
         "inspire_db_device_bytes": (u64, [vp]),
         "inspire_client_register": (C.c_int, [vp, vp, vp, C.POINTER(i32)]),

@@ -176,18 +176,36 @@ class EncodedDatabase:
     entries, 16-bit columns (encode_db.rs:106-181), plus the contracted form
     the Respond kernel reads."""
 
-    def __init__(self, crs: ServerCrs, database: bytes | np.ndarray, entry_size: int):
+    def __init__(self, crs: ServerCrs, database: bytes | np.ndarray, entry_size: int, _handle=None):
         self.crs = crs
         self.L = crs.L
+        self.entry_size = int(entry_size)
+        if _handle is not None:
+            self.h = _handle
+            self.total_entries = self.num_shards * crs.params.ring_dim
+            _LIVE_DBS.add(self)
+            return
         raw = np.frombuffer(database, dtype=np.uint8) if isinstance(database, (bytes, bytearray)) else \
             np.ascontiguousarray(database, dtype=np.uint8).reshape(-1)
-        self.entry_size = int(entry_size)
         self.total_entries = raw.size // self.entry_size if self.entry_size else 0
         h = C.c_void_p()
         _check(self.L.inspire_db_create(crs.h, raw.ctypes.data_as(C.c_void_p), self.total_entries, self.entry_size,
                                         C.byref(h)))
         self.h = h
         _LIVE_DBS.add(self)
+
+    @classmethod
+    def load_shards(cls, crs: ServerCrs, directory: str) -> "EncodedDatabase":
+        """Load the crate's binary shard files (save_shards_binary,
+        mmap.rs:19-53) from `directory` straight into HBM."""
+        h = C.c_void_p()
+        _check(crs.L.inspire_db_load_shards(crs.h, str(directory).encode(), C.byref(h)))
+        return cls(crs, b"", 2 * crs.inspiring_num_columns, _handle=h)
+
+    def save_shards(self, directory: str) -> None:
+        """Write this database as the crate's binary shard files."""
+        pc = self.crs.params.to_c()
+        _check(self.L.inspire_db_save_shards(self.h, C.byref(pc), str(directory).encode()))
 
     @property
     def num_shards(self) -> int:
