@@ -413,6 +413,8 @@ def main():
         sweep[str(bs)] = bs * reps / (e0.elapsed_time(e1) / 1e3)
 
     micro = kernel_microbench(inspire, crs, torch, dev)
+    codec = wire_bench(inspire, crs, seeds[0], brows[0], y_body, d_out[0, 0].cpu().numpy().view(np.uint64)
+                       .reshape(2, 2 * N))
 
     # end to end through the host-buffer C ABI call, pinned host memory
     h_seeds = torch.empty((B, 6, 32), dtype=torch.uint8, pin_memory=True)
@@ -519,6 +521,7 @@ def main():
             "p99_ms": None if serving is None else serving["headline"]["p99_ms"],
             "serving": serving,
             "kernel_microbench": micro,
+            "wire_codec": codec,
             "wall_s_timed_region": wall,
         }
         print(json.dumps(line), flush=True)
@@ -634,6 +637,42 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
             d.close()
     pool.close()
     return out
+
+
+def wire_bench(inspire, crs, seeds, brows, y_body, out_ct, reps=50):
+    """Host cost of the HTTP wire formats through the native codecs: parse a
+    real SeededClientQuery JSON body (with y_body keys), write the JSON reply
+    and the bincode ServerResponse of a real response (one core)."""
+    import json as _json
+
+    from inspire import wire
+
+    P = crs.params
+    q = crs.params.crt_moduli
+
+    def poly(c):
+        return {"coeffs": [int(x) for x in c], "moduli": list(q), "q": q[0] * q[1], "dim": N,
+                "crt_q0_inv_mod_q1": pow(q[0], q[1] - 2, q[1]), "is_ntt": False}
+
+    body = _json.dumps({"shard_id": 7, "rgsw_ciphertext": {
+        "rows": [{"seed": [int(b) for b in seeds[i]], "b": poly(brows[i])} for i in range(6)],
+        "gadget": {"base": 1 << 20, "len": 3, "q": q[0] * q[1]}}, "packing_mode": "inspiring",
+        "inspiring_packing_keys": {"y_body": [poly(p) for p in y_body], "full_key": False, "num_to_pack": 16}},
+        separators=(",", ":")).encode()
+    resp = inspire.ServerResponse(inspire.RlweCiphertext(out_ct[0], out_ct[1]), [])
+    res = {"query_json_bytes": len(body)}
+    for name, fn in (("parse_query_json", lambda: wire.seeded_query_from_json(P, body)),
+                     ("write_response_json", lambda: wire.query_response_to_json(P, resp, 1)),
+                     ("write_response_bincode", lambda: wire.server_response_to_bincode(P, resp))):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        res[name + "_us"] = (time.perf_counter() - t0) / reps * 1e6
+    res["response_json_bytes"] = len(wire.query_response_to_json(P, resp, 1))
+    res["response_bincode_bytes"] = len(wire.server_response_to_bincode(P, resp))
+    res["parse_query_json_mb_s"] = len(body) / res["parse_query_json_us"]
+    return res
 
 
 def _respond_into(crs, edb, shard_ids, seeds, brows, client_ids, out):

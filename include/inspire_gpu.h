@@ -277,6 +277,36 @@ int inspire_server_get_stats(inspire_server *srv, inspire_server_stats *out);
 /* Monotonic clock of the serving loop's timestamps (CLOCK_MONOTONIC, ns). */
 int64_t inspire_now_ns(void);
 
+/* ---- Wire codecs (host only; need no GPU) ----
+ * JSON as serde_json writes the crate's derived layouts (Poly,
+ * src/math/poly.rs:63-77; SeededRlweCiphertext, rlwe/types.rs:165-171;
+ * SeededRgswCiphertext + GadgetVector, rgsw/types.rs:37-45, 225-231;
+ * ClientPackingKeys, inspiring/inspiring2.rs:603-628; SeededClientQuery,
+ * pir/query.rs:138-150; ServerResponse, pir/respond.rs:31-37; the server's
+ * QueryResponse, src/bin/server.rs:88-92); bincode 1.3's default encoding for
+ * ServerResponse::to_binary (pir/respond.rs:43-50). */
+
+/* Parse a SeededClientQuery JSON body (the /query/seeded request) into the
+ * inspire_seeded_query layout: seeds[2*gadget_len][32],
+ * b_rows[2*gadget_len][poly], *packing_mode 0 = inspiring / 1 = tree,
+ * *has_keys = whether inspiring_packing_keys is present, y_body[gadget_len][poly]
+ * (may be NULL to skip).  Polynomials must be in coefficient form over the
+ * parameters' moduli. */
+int inspire_seeded_query_from_json(const inspire_params *params, const char *json, size_t len, uint32_t *shard_id,
+                                   uint8_t *seeds, uint64_t *b_rows, int32_t *packing_mode, int32_t *has_keys,
+                                   uint64_t *y_body);
+
+/* The server's JSON reply {"response": ServerResponse, "processing_time_ms": t}
+ * for ciphertext ct[2][poly] and n_columns column ciphertexts
+ * columns[n][2][poly].  buf NULL: *len receives the size only. */
+int inspire_query_response_to_json(const inspire_params *params, const uint64_t *ct, uint32_t n_columns,
+                                   const uint64_t *columns, uint64_t processing_time_ms, char *buf, size_t cap,
+                                   size_t *len);
+
+/* ServerResponse::to_binary (bincode) of the same response. */
+int inspire_server_response_to_bincode(const inspire_params *params, const uint64_t *ct, uint32_t n_columns,
+                                       const uint64_t *columns, uint8_t *buf, size_t cap, size_t *len);
+
 /* Batched NttContext::forward / inverse (src/math/ntt.rs:223-325) on device
  * data polys[npolys][2][ring_dim] (u32 residues), in place.  Forward outputs
  * the crate's NTT-domain values (Montgomery form, R = 2^64, bit-reversed slot

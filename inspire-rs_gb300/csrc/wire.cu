@@ -1,0 +1,487 @@
+// wire.cu -- native codecs for the crate's wire formats (host code only).
+//
+// JSON follows serde's derived layouts with serde_json's compact output:
+//   Poly (src/math/poly.rs:63-77)
+//     {"coeffs":[..],"moduli":[..],"q":Q,"dim":D,"crt_q0_inv_mod_q1":I,"is_ntt":false}
+//   SeededRlweCiphertext (rlwe/types.rs:165-171) {"seed":[32 bytes],"b":Poly}
+//   GadgetVector (rgsw/types.rs:37-45) {"base":B,"len":L,"q":Q}
+//   SeededRgswCiphertext (rgsw/types.rs:225-231) {"rows":[..],"gadget":G}
+//   ClientPackingKeys (inspiring/inspiring2.rs:603-628)
+//     {"y_body":[..],"z_body":[..] (omitted when empty),"full_key":b,"num_to_pack":n}
+//   SeededClientQuery (pir/query.rs:138-150)
+//     {"shard_id":s,"rgsw_ciphertext":R,"packing_mode":"inspiring"|"tree",
+//      "inspiring_packing_keys":K (omitted when None)}
+//   RlweCiphertext {"a":Poly,"b":Poly}; ServerResponse (pir/respond.rs:31-37)
+//     {"ciphertext":C,"column_ciphertexts":[..]}
+//   the server's QueryResponse (src/bin/server.rs:88-92)
+//     {"response":ServerResponse,"processing_time_ms":t}
+// bincode 1.3's default encoding (fixed-width little-endian integers, u64
+// sequence lengths, bool as one byte) for ServerResponse::to_binary
+// (pir/respond.rs:43-50).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host.h"
+
+using namespace ighost;
+
+namespace {
+
+// ---------------------------------------------------------------- parser
+struct Json {
+  const char* p;
+  const char* end;
+  std::string err;
+
+  bool fail(const std::string& m) {
+    if (err.empty()) err = m + " at byte " + std::to_string(pos());
+    return false;
+  }
+  size_t pos() const { return (size_t)(p - begin); }
+  const char* begin;
+
+  void ws() {
+    while (p < end && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) p++;
+  }
+  bool eat(char c) {
+    ws();
+    if (p < end && *p == c) {
+      p++;
+      return true;
+    }
+    return false;
+  }
+  bool expect(char c) { return eat(c) || fail(std::string("expected '") + c + "'"); }
+  bool str(std::string& out) {
+    ws();
+    if (p >= end || *p != '"') return fail("expected a string");
+    p++;
+    out.clear();
+    while (p < end && *p != '"') {
+      if (*p == '\\') {
+        if (p + 1 >= end) return fail("bad escape");
+        p++;
+        const char c = *p;
+        out.push_back(c == 'n' ? '\n' : c == 't' ? '\t' : c == 'r' ? '\r' : c);  // keys here are plain ASCII
+        p++;
+        continue;
+      }
+      out.push_back(*p++);
+    }
+    if (p >= end) return fail("unterminated string");
+    p++;
+    return true;
+  }
+  bool u64(uint64_t& v) {
+    ws();
+    const char* q = p;
+    uint64_t x = 0;
+    // up to 19 digits cannot overflow; a 20th is checked
+    int n = 0;
+    while (q < end && (unsigned)(*q - '0') < 10u && n < 19) {
+      x = x * 10 + (uint64_t)(*q - '0');
+      q++;
+      n++;
+    }
+    if (n == 0) return fail("expected an unsigned integer");
+    if (q < end && (unsigned)(*q - '0') < 10u) {
+      const uint64_t d = (uint64_t)(*q - '0');
+      if (x > (UINT64_MAX - d) / 10) return fail("integer overflow");
+      x = x * 10 + d;
+      q++;
+      if (q < end && (unsigned)(*q - '0') < 10u) return fail("integer overflow");
+    }
+    p = q;
+    if (p < end && (*p == '.' || *p == 'e' || *p == 'E')) return fail("expected an integer");
+    v = x;
+    return true;
+  }
+  // array of at most cap u64 into out; *n receives the count
+  bool u64_array_into(uint64_t* out, size_t cap, size_t* n) {
+    *n = 0;
+    if (!expect('[')) return false;
+    if (eat(']')) return true;
+    do {
+      uint64_t v;
+      if (!u64(v)) return false;
+      if (*n >= cap) return fail("array too long");
+      out[(*n)++] = v;
+    } while (eat(','));
+    return expect(']');
+  }
+  bool boolean(bool& b) {
+    ws();
+    if (end - p >= 4 && memcmp(p, "true", 4) == 0) {
+      p += 4;
+      b = true;
+      return true;
+    }
+    if (end - p >= 5 && memcmp(p, "false", 5) == 0) {
+      p += 5;
+      b = false;
+      return true;
+    }
+    return fail("expected a boolean");
+  }
+  // skip any JSON value (unknown fields)
+  bool skip() {
+    ws();
+    if (p >= end) return fail("unexpected end");
+    if (*p == '"') {
+      std::string s;
+      return str(s);
+    }
+    if (*p == '{' || *p == '[') {
+      const char open = *p, close = open == '{' ? '}' : ']';
+      p++;
+      if (eat(close)) return true;
+      do {
+        if (open == '{') {
+          std::string k;
+          if (!str(k) || !expect(':')) return false;
+        }
+        if (!skip()) return false;
+      } while (eat(','));
+      return expect(close);
+    }
+    if (*p == 't' || *p == 'f') {
+      bool b;
+      return boolean(b);
+    }
+    if (end - p >= 4 && memcmp(p, "null", 4) == 0) {
+      p += 4;
+      return true;
+    }
+    // number (possibly signed / fractional)
+    const char* s = p;
+    while (p < end && (strchr("+-.eE", *p) || (*p >= '0' && *p <= '9'))) p++;
+    return p > s || fail("unexpected character");
+  }
+  bool null() {
+    ws();
+    if (end - p >= 4 && memcmp(p, "null", 4) == 0) {
+      p += 4;
+      return true;
+    }
+    return false;
+  }
+  // array of u64 into out (cleared)
+  bool u64_array(std::vector<uint64_t>& out) {
+    out.clear();
+    if (!expect('[')) return false;
+    if (eat(']')) return true;
+    do {
+      uint64_t v;
+      if (!u64(v)) return false;
+      out.push_back(v);
+    } while (eat(','));
+    return expect(']');
+  }
+  // object: calls field(key) for each key; field consumes the value
+  template <class F>
+  bool object(F&& field) {
+    if (!expect('{')) return false;
+    if (eat('}')) return true;
+    do {
+      std::string k;
+      if (!str(k) || !expect(':')) return false;
+      if (!field(k)) return false;
+    } while (eat(','));
+    return expect('}');
+  }
+  template <class F>
+  bool array(F&& elem) {
+    if (!expect('[')) return false;
+    if (eat(']')) return true;
+    size_t i = 0;
+    do {
+      if (!elem(i++)) return false;
+    } while (eat(','));
+    return expect(']');
+  }
+};
+
+// Poly in coefficient form over the context's moduli, into dst[2N].
+bool parse_poly(Json& j, const inspire_params& P, uint64_t* dst, const std::string& what) {
+  const size_t plen = 2 * (size_t)P.ring_dim;
+  uint64_t moduli[3] = {0, 0, 0};
+  size_t ncoeffs = 0, nmod = 0;
+  uint64_t dim = 0;
+  bool is_ntt = false, have_coeffs = false, have_moduli = false;
+  const bool ok = j.object([&](const std::string& k) {
+    if (k == "coeffs") {
+      have_coeffs = true;
+      return j.u64_array_into(dst, plen, &ncoeffs);  // parsed in place, checked below
+    }
+    if (k == "moduli") {
+      have_moduli = true;
+      return j.u64_array_into(moduli, 3, &nmod);
+    }
+    if (k == "dim") return j.u64(dim);
+    if (k == "is_ntt") return j.boolean(is_ntt);
+    return j.skip();  // q, crt_q0_inv_mod_q1 are derived from the moduli
+  });
+  if (!ok) return false;
+  if (!have_coeffs || !have_moduli) return j.fail(what + ": missing coeffs or moduli");
+  if (nmod != 2 || moduli[0] != P.crt_moduli[0] || moduli[1] != P.crt_moduli[1])
+    return j.fail(what + ": moduli differ from the context");
+  if (dim != P.ring_dim || ncoeffs != plen) return j.fail(what + ": dimension mismatch");
+  if (is_ntt) return j.fail(what + ": expected coefficient form (is_ntt false)");
+  for (size_t i = 0; i < plen; i++)
+    if (dst[i] >= moduli[i / P.ring_dim]) return j.fail(what + ": residue not reduced");
+  return true;
+}
+
+// ---------------------------------------------------------------- writer
+struct Out {
+  std::string s;
+  size_t n = 0;  // bytes used in s (s is grown ahead of the writes)
+  void room(size_t k) {
+    if (n + k > s.size()) s.resize(std::max(s.size() * 2, n + k + 4096));
+  }
+  void ch(char c) {
+    room(1);
+    s[n++] = c;
+  }
+  void lit(const char* x) {
+    const size_t k = strlen(x);
+    room(k);
+    memcpy(&s[n], x, k);
+    n += k;
+  }
+  void num(uint64_t v) {
+    room(20);
+    char b[20];
+    int k = 0;
+    do {
+      b[k++] = (char)('0' + v % 10);
+      v /= 10;
+    } while (v);
+    while (k) s[n++] = b[--k];
+  }
+  std::string done() {
+    s.resize(n);
+    return std::move(s);
+  }
+};
+
+uint64_t q0_inv_q1(uint64_t q0, uint64_t q1) {
+  // Poly::init_moduli's cached q0^-1 mod q1 (q1 prime): q0^(q1-2) mod q1
+  unsigned __int128 r = 1, b = q0 % q1;
+  uint64_t e = q1 - 2;
+  while (e) {
+    if (e & 1) r = r * b % q1;
+    b = b * b % q1;
+    e >>= 1;
+  }
+  return (uint64_t)r;
+}
+
+void poly_json(Out& o, const inspire_params& P, const uint64_t* c) {
+  const size_t n = 2 * (size_t)P.ring_dim;
+  o.lit("{\"coeffs\":[");
+  for (size_t i = 0; i < n; i++) {
+    if (i) o.ch(',');
+    o.num(c[i]);
+  }
+  o.lit("],\"moduli\":[");
+  o.num(P.crt_moduli[0]);
+  o.ch(',');
+  o.num(P.crt_moduli[1]);
+  o.lit("],\"q\":");
+  o.num(P.crt_moduli[0] * P.crt_moduli[1]);
+  o.lit(",\"dim\":");
+  o.num(P.ring_dim);
+  o.lit(",\"crt_q0_inv_mod_q1\":");
+  o.num(q0_inv_q1(P.crt_moduli[0], P.crt_moduli[1]));
+  o.lit(",\"is_ntt\":false}");
+}
+
+void rlwe_json(Out& o, const inspire_params& P, const uint64_t* ct) {
+  o.lit("{\"a\":");
+  poly_json(o, P, ct);
+  o.lit(",\"b\":");
+  poly_json(o, P, ct + 2 * (size_t)P.ring_dim);
+  o.ch('}');
+}
+
+template <class T>
+void le(std::string& s, T v) {
+  for (size_t i = 0; i < sizeof(T); i++) s.push_back((char)(uint8_t)(v >> (8 * i)));
+}
+
+bool host_is_le() {
+  const uint32_t one = 1;
+  uint8_t b;
+  memcpy(&b, &one, 1);
+  return b == 1;
+}
+
+void poly_bincode(std::string& s, const inspire_params& P, const uint64_t* c) {
+  const uint64_t n = 2 * (uint64_t)P.ring_dim;
+  le<uint64_t>(s, n);
+  if (host_is_le()) {
+    const size_t at = s.size();
+    s.resize(at + 8 * n);
+    memcpy(&s[at], c, 8 * n);
+  } else {
+    for (uint64_t i = 0; i < n; i++) le<uint64_t>(s, c[i]);
+  }
+  le<uint64_t>(s, 2);
+  le<uint64_t>(s, P.crt_moduli[0]);
+  le<uint64_t>(s, P.crt_moduli[1]);
+  le<uint64_t>(s, P.crt_moduli[0] * P.crt_moduli[1]);
+  le<uint64_t>(s, P.ring_dim);
+  le<uint64_t>(s, q0_inv_q1(P.crt_moduli[0], P.crt_moduli[1]));
+  s.push_back(0);  // is_ntt
+}
+
+int copy_out(const std::string& s, char* buf, size_t cap, size_t* len) {
+  *len = s.size();
+  if (!buf) return INSPIRE_OK;  // size query
+  if (cap < s.size()) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "output buffer too small");
+  memcpy(buf, s.data(), s.size());
+  return INSPIRE_OK;
+}
+
+bool params_ok(const inspire_params* P) {
+  return P && P->ring_dim > 0 && P->crt_count == 2 && P->gadget_len > 0 && P->crt_moduli[0] > 1 &&
+         P->crt_moduli[1] > 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int inspire_seeded_query_from_json(const inspire_params* P, const char* json, size_t len, uint32_t* shard_id,
+                                   uint8_t* seeds, uint64_t* b_rows, int32_t* packing_mode, int32_t* has_keys,
+                                   uint64_t* y_body) {
+  if (!params_ok(P) || !json || !shard_id || !seeds || !b_rows || !packing_mode || !has_keys)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument or unsupported parameters");
+  const size_t plen = 2 * (size_t)P->ring_dim;
+  const uint32_t rows_want = 2 * P->gadget_len;
+  Json j{json, json + len, "", json};
+  uint64_t sid = 0;
+  bool have_sid = false, have_rgsw = false;
+  int mode = 0;
+  int keys = 0;
+  const bool ok = j.object([&](const std::string& k) -> bool {
+    if (k == "shard_id") {
+      have_sid = true;
+      return j.u64(sid) && (sid <= 0xffffffffULL || j.fail("shard_id out of range"));
+    }
+    if (k == "rgsw_ciphertext") {
+      have_rgsw = true;
+      uint32_t nrows = 0;
+      return j.object([&](const std::string& rk) -> bool {
+        if (rk == "rows")
+          return j.array([&](size_t i) -> bool {
+            if (i >= rows_want) return j.fail("too many RGSW rows");
+            nrows = (uint32_t)i + 1;
+            bool have_seed = false, have_b = false;
+            const bool rok = j.object([&](const std::string& fk) -> bool {
+              if (fk == "seed") {
+                have_seed = true;
+                size_t nb = 0;
+                return j.array([&](size_t bi) -> bool {
+                  uint64_t v;
+                  if (bi >= 32 || !j.u64(v) || v > 255) return j.fail("seed must be 32 bytes");
+                  seeds[i * 32 + bi] = (uint8_t)v;
+                  nb = bi + 1;
+                  return true;
+                }) && (nb == 32 || j.fail("seed must be 32 bytes"));
+              }
+              if (fk == "b") {
+                have_b = true;
+                return parse_poly(j, *P, b_rows + i * plen, "rgsw row b");
+              }
+              return j.skip();
+            });
+            return rok && ((have_seed && have_b) || j.fail("RGSW row needs seed and b"));
+          }) && (nrows == rows_want || j.fail("expected 2*gadget_len RGSW rows"));
+        if (rk == "gadget") {
+          uint64_t base = 0, glen = 0;
+          return j.object([&](const std::string& gk) -> bool {
+            if (gk == "base") return j.u64(base);
+            if (gk == "len") return j.u64(glen);
+            return j.skip();
+          }) && ((base == P->gadget_base && glen == P->gadget_len) || j.fail("gadget differs from the context"));
+        }
+        return j.skip();
+      });
+    }
+    if (k == "packing_mode") {
+      std::string m;
+      if (!j.str(m)) return false;
+      if (m == "inspiring") mode = 0;
+      else if (m == "tree") mode = 1;
+      else return j.fail("unknown packing_mode");
+      return true;
+    }
+    if (k == "inspiring_packing_keys") {
+      if (j.null()) return true;  // Option::None
+      keys = 1;
+      size_t ny = 0;
+      return j.object([&](const std::string& kk) -> bool {
+        if (kk == "y_body")
+          return j.array([&](size_t i) -> bool {
+            if (i >= P->gadget_len) return j.fail("too many y_body polynomials");
+            ny = i + 1;
+            if (!y_body) return j.skip();
+            return parse_poly(j, *P, y_body + i * plen, "y_body");
+          }) && (ny == P->gadget_len || j.fail("y_body must hold gadget_len polynomials"));
+        return j.skip();  // z_body, full_key, num_to_pack
+      });
+    }
+    return j.skip();
+  });
+  if (!ok) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "SeededClientQuery JSON: " + j.err);
+  j.ws();
+  if (j.p != j.end) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "SeededClientQuery JSON: trailing data");
+  if (!have_sid || !have_rgsw)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "SeededClientQuery JSON: missing shard_id or rgsw_ciphertext");
+  *shard_id = (uint32_t)sid;
+  *packing_mode = mode;
+  *has_keys = keys;
+  return INSPIRE_OK;
+}
+
+int inspire_query_response_to_json(const inspire_params* P, const uint64_t* ct, uint32_t n_columns,
+                                   const uint64_t* columns, uint64_t processing_time_ms, char* buf, size_t cap,
+                                   size_t* len) {
+  if (!params_ok(P) || !ct || !len || (n_columns && !columns)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  Out o;
+  o.s.resize((size_t)(2 + 2 * n_columns) * 2 * P->ring_dim * 11 + 512);
+  o.lit("{\"response\":{\"ciphertext\":");
+  rlwe_json(o, *P, ct);
+  o.lit(",\"column_ciphertexts\":[");
+  for (uint32_t c = 0; c < n_columns; c++) {
+    if (c) o.ch(',');
+    rlwe_json(o, *P, columns + (size_t)c * 4 * P->ring_dim);
+  }
+  o.lit("]},\"processing_time_ms\":");
+  o.num(processing_time_ms);
+  o.ch('}');
+  return copy_out(o.done(), buf, cap, len);
+}
+
+int inspire_server_response_to_bincode(const inspire_params* P, const uint64_t* ct, uint32_t n_columns,
+                                       const uint64_t* columns, uint8_t* buf, size_t cap, size_t* len) {
+  if (!params_ok(P) || !ct || !len || (n_columns && !columns)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::string s;
+  const size_t plen = 2 * (size_t)P->ring_dim;
+  s.reserve((2 + 2 * (size_t)n_columns) * (8 * plen + 64) + 8);
+  poly_bincode(s, *P, ct);
+  poly_bincode(s, *P, ct + plen);
+  le<uint64_t>(s, n_columns);
+  for (uint32_t c = 0; c < n_columns; c++) {
+    poly_bincode(s, *P, columns + (size_t)c * 2 * plen);
+    poly_bincode(s, *P, columns + (size_t)c * 2 * plen + plen);
+  }
+  return copy_out(s, reinterpret_cast<char*>(buf), cap, len);
+}
+
+}  // extern "C"

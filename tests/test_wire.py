@@ -1,0 +1,136 @@
+"""Native wire codecs (host code, no GPU): SeededClientQuery JSON in, the
+server's JSON reply and ServerResponse's bincode out.  The expected bytes are
+built here from the crate's serde derives (field names and order of Poly,
+SeededRlweCiphertext, SeededRgswCiphertext, GadgetVector, ClientPackingKeys,
+SeededClientQuery, RlweCiphertext, ServerResponse, QueryResponse) with
+serde_json's compact formatting and bincode 1.3's fixed-width little-endian
+encoding."""
+import json
+import struct
+
+import numpy as np
+import pytest
+
+N = 2048
+Q = (268369921, 249561089)
+QC = Q[0] * Q[1]
+QINV = pow(Q[0], Q[1] - 2, Q[1])  # Poly::crt_q0_inv_mod_q1
+
+
+@pytest.fixture(scope="module")
+def wire():
+    import build_lib
+
+    build_lib.build()
+    import inspire
+    from inspire import wire as w
+
+    return inspire, w
+
+
+def poly_obj(coeffs):
+    return {"coeffs": [int(x) for x in coeffs], "moduli": list(Q), "q": QC, "dim": N, "crt_q0_inv_mod_q1": QINV,
+            "is_ntt": False}
+
+
+def query_obj(shard_id, seeds, b_rows, y_body=None, mode=None, keys_null=False):
+    q = {"shard_id": shard_id,
+         "rgsw_ciphertext": {"rows": [{"seed": [int(b) for b in seeds[i]], "b": poly_obj(b_rows[i])}
+                                      for i in range(6)],
+                             "gadget": {"base": 1 << 20, "len": 3, "q": QC}}}
+    if mode is not None:
+        q["packing_mode"] = mode
+    if y_body is not None:
+        q["inspiring_packing_keys"] = {"y_body": [poly_obj(p) for p in y_body], "full_key": False, "num_to_pack": 16}
+    elif keys_null:
+        q["inspiring_packing_keys"] = None
+    return q
+
+
+def compact(obj):
+    return json.dumps(obj, separators=(",", ":")).encode()
+
+
+def rand_polys(rng, n):
+    a = np.zeros((n, 2 * N), np.uint64)
+    a[:, :N] = rng.integers(0, Q[0], size=(n, N))
+    a[:, N:] = rng.integers(0, Q[1], size=(n, N))
+    return a
+
+
+def test_seeded_query_json_round_trip(wire):
+    inspire, w = wire
+    rng = np.random.default_rng(1)
+    params = inspire.InspireParams(p=1 << 16)
+    seeds = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+    b_rows, y_body = rand_polys(rng, 6), rand_polys(rng, 3)
+    q = w.seeded_query_from_json(params, compact(query_obj(17, seeds, b_rows, y_body, mode="inspiring")))
+    assert q.shard_id == 17 and q.packing_mode == "inspiring"
+    assert np.array_equal(q.seeds, seeds) and np.array_equal(q.b_rows, b_rows)
+    assert np.array_equal(q.inspiring_packing_keys.y_body, y_body)
+    # pretty-printed, packing_mode defaulted, keys omitted / null, tree mode
+    q2 = w.seeded_query_from_json(params, json.dumps(query_obj(3, seeds, b_rows), indent=2))
+    assert q2.packing_mode == "inspiring" and q2.inspiring_packing_keys is None
+    q3 = w.seeded_query_from_json(params, compact(query_obj(3, seeds, b_rows, mode="tree", keys_null=True)))
+    assert q3.packing_mode == "tree" and q3.inspiring_packing_keys is None
+    assert np.array_equal(q3.b_rows, b_rows)
+
+
+def test_seeded_query_json_rejects(wire):
+    inspire, w = wire
+    rng = np.random.default_rng(2)
+    params = inspire.InspireParams(p=1 << 16)
+    seeds = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+    b_rows = rand_polys(rng, 6)
+    good = query_obj(1, seeds, b_rows)
+    cases = []
+    o = json.loads(compact(good))
+    o["rgsw_ciphertext"]["rows"] = o["rgsw_ciphertext"]["rows"][:5]
+    cases.append((o, "2\\*gadget_len"))
+    o = json.loads(compact(good))
+    o["rgsw_ciphertext"]["rows"][2]["b"]["moduli"] = [12289, 40961]
+    cases.append((o, "moduli"))
+    o = json.loads(compact(good))
+    o["rgsw_ciphertext"]["rows"][0]["b"]["is_ntt"] = True
+    cases.append((o, "coefficient form"))
+    o = json.loads(compact(good))
+    o["rgsw_ciphertext"]["rows"][0]["seed"] = o["rgsw_ciphertext"]["rows"][0]["seed"][:31]
+    cases.append((o, "32 bytes"))
+    o = json.loads(compact(good))
+    o["rgsw_ciphertext"]["rows"][1]["b"]["coeffs"][0] = Q[0]
+    cases.append((o, "not reduced"))
+    o = json.loads(compact(good))
+    o["packing_mode"] = "fancy"
+    cases.append((o, "packing_mode"))
+    o = json.loads(compact(good))
+    o["rgsw_ciphertext"]["gadget"]["base"] = 1 << 16
+    cases.append((o, "gadget"))
+    for obj, msg in cases:
+        with pytest.raises(inspire.PirError, match=msg):
+            w.seeded_query_from_json(params, compact(obj))
+    with pytest.raises(inspire.PirError, match="trailing"):
+        w.seeded_query_from_json(params, compact(good) + b" x")
+    with pytest.raises(inspire.PirError, match="expected"):
+        w.seeded_query_from_json(params, compact(good)[:-10])
+
+
+def test_response_json_and_bincode(wire):
+    inspire, w = wire
+    rng = np.random.default_rng(3)
+    params = inspire.InspireParams(p=1 << 16)
+    ct = rand_polys(rng, 2)
+    cols = rand_polys(rng, 4)
+    for columns in ([], [inspire.RlweCiphertext(cols[0], cols[1]), inspire.RlweCiphertext(cols[2], cols[3])]):
+        resp = inspire.ServerResponse(inspire.RlweCiphertext(ct[0], ct[1]), columns)
+        want = compact({"response": {"ciphertext": {"a": poly_obj(ct[0]), "b": poly_obj(ct[1])},
+                                     "column_ciphertexts": [{"a": poly_obj(c.a), "b": poly_obj(c.b)} for c in columns]},
+                        "processing_time_ms": 12})
+        assert w.query_response_to_json(params, resp, 12) == want
+
+        def poly_bin(c):
+            return (struct.pack("<Q", 2 * N) + np.asarray(c, "<u8").tobytes() + struct.pack("<QQQ", 2, *Q) +
+                    struct.pack("<QQQ", QC, N, QINV) + b"\x00")
+
+        want_bin = poly_bin(ct[0]) + poly_bin(ct[1]) + struct.pack("<Q", len(columns)) + b"".join(
+            poly_bin(c.a) + poly_bin(c.b) for c in columns)
+        assert w.server_response_to_bincode(params, resp) == want_bin
