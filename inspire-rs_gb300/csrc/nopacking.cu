@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
       const uint64_t xv = P.delta * (uint64_t)__ldg(H + (size_t)c * N + x + 128 * j);
       v[j] = (uint32_t)(xv >> (ZBITS * t)) & ((1u << ZBITS) - 1);
     }
-    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);  // [0, 4q)
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);  // [0, 14q)
     {
       const int f = (x >> 1) & 3;
       uint32_t* da = PB + ((r * 3 + t) * 2 + 0) * N + 16 * x;

@@ -8,11 +8,15 @@
 // residues (no Montgomery factor); callers fold constant factors (R = 2^64 of
 // the reference form, n^-1) into loads or scalings.
 //
-// Butterflies keep values lazily reduced (Harvey's bounds, q < 2^30): the
-// forward transform takes inputs in [0, 4q) and returns values in [0, 4q); the
-// inverse takes [0, 2q) and returns [0, 2q).  canon4 / canon2 bring them to
-// [0, q).  Twiddles are read as {w, floor(w * 2^32 / q)} pairs (one 64-bit
-// load).
+// Values stay lazily reduced.  The moduli are below 2^28, so 16q < 2^32, and
+// Shoup's multiply accepts any 32-bit input and returns [0, 2q).  The forward
+// butterflies therefore skip Harvey's per-butterfly reduction: each stage
+// grows the bound by 2q, and one conditional subtraction of 8q per value at
+// each of the two exchanges keeps it below 16q.  Input [0, 4q) -> 12q after
+// stages 0-3 -> 8q -> 16q after stages 4-7 -> 8q -> output [0, 14q).  The
+// inverse (Harvey's Gentleman-Sande butterflies) takes [0, 2q) and returns
+// [0, 2q).  canon16 / canon4 / canon2 bring values to [0, q).  Twiddles are
+// read as {w, floor(w * 2^32 / q)} pairs (one 64-bit load).
 //
 // Data layout per thread x (0..127) of the group:
 //   "coefficient layout" (forward input, inverse output): v[r] = a[x + 128 r]
@@ -51,12 +55,20 @@ __device__ __forceinline__ uint32_t mul_shoup_lazy(uint32_t a, uint2 w, uint32_t
   return a * w.x - h * q;
 }
 
-// Cooley-Tukey butterfly, inputs and outputs in [0, 4q).
+// Cooley-Tukey butterfly without reducing its inputs: both outputs are below
+// the inputs' bound plus 2q.
 __device__ __forceinline__ void ct_bfly(uint32_t& a, uint32_t& b, uint2 w, uint32_t q, uint32_t q2) {
-  const uint32_t x = min(a, a - q2);
+  const uint32_t x = a;
   const uint32_t t = mul_shoup_lazy(b, w, q);
   a = x + t;
   b = x - t + q2;
+}
+
+// Every value below 16q -> below 8q.
+__device__ __forceinline__ void reduce_8q(uint32_t v[16], uint32_t q) {
+  const uint32_t q8 = 8 * q;
+#pragma unroll
+  for (int r = 0; r < 16; r++) v[r] = min(v[r], v[r] - q8);
 }
 
 // Gentleman-Sande butterfly, inputs and outputs in [0, 2q).
@@ -70,6 +82,13 @@ __device__ __forceinline__ void gs_bfly(uint32_t& a, uint32_t& b, uint2 w, uint3
 __device__ __forceinline__ uint32_t canon4(uint32_t x, uint32_t q) {
   x = min(x, x - 2 * q);
   return min(x, x - q);
+}
+
+// [0, 16q) -> [0, q) (forward transform outputs).
+__device__ __forceinline__ uint32_t canon16(uint32_t x, uint32_t q) {
+  x = min(x, x - 8 * q);
+  x = min(x, x - 4 * q);
+  return canon4(x, q);
 }
 
 __device__ __forceinline__ uint32_t canon2(uint32_t x, uint32_t q) { return min(x, x - q); }
@@ -116,7 +135,7 @@ __device__ __forceinline__ void stage(uint32_t v[16], TwiddleRef tw, int first, 
 }
 
 // Forward transform (Cooley-Tukey, decimation in time), coefficient layout in
-// ([0, 4q)), slot layout out ([0, 4q)).  `sc` is this group's scratch; `bar`
+// ([0, 4q)), slot layout out ([0, 14q)).  `sc` is this group's scratch; `bar`
 // its barrier id.
 __device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef tw, uint32_t q, int x, int bar) {
   const uint32_t q2 = 2 * q;
@@ -125,6 +144,7 @@ __device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef
   stage<1, 3, true>(v, tw, 0, q, q2);
   stage<2, 2, true>(v, tw, 0, q, q2);
   stage<3, 1, true>(v, tw, 0, q, q2);
+  reduce_8q(v, q);  // < 12q -> < 8q
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) sc[pad_a(x + 128 * r)] = v[r];
@@ -137,6 +157,7 @@ __device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef
   stage<5, 3, true>(v, tw, b << 1, q, q2);
   stage<6, 2, true>(v, tw, b << 2, q, q2);
   stage<7, 1, true>(v, tw, b << 3, q, q2);
+  reduce_8q(v, q);  // < 16q -> < 8q
   group_sync(bar);
 #pragma unroll
   for (int r = 0; r < 16; r++) sc[pad_b(128 * b + y + 8 * r)] = v[r];

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(BLOCK) ntt_ref_kernel(const DevParams P, uint3
     for (int r = 0; r < 16; r++) v[r] = mul_shoup(a[x + 128 * r], C.r64, C.r64_p, q);
     ntt_fwd(v, SC[g], fwd_tw(C), q, x, 1 + g);
 #pragma unroll
-    for (int r = 0; r < 16; r++) v[r] = canon4(v[r], q);
+    for (int r = 0; r < 16; r++) v[r] = canon16(v[r], q);
     uint4* d = reinterpret_cast<uint4*>(a + 16 * x);
 #pragma unroll
     for (int r = 0; r < 4; r++) d[r] = make_uint4(v[4 * r], v[4 * r + 1], v[4 * r + 2], v[4 * r + 3]);
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(BLOCK) external_product_kernel(const DevParams
     for (int r = 0; r < 16; r++) dh[r] = dig[d * N + x + 128 * r];
     ntt_fwd(dh, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
 #pragma unroll
-    for (int r = 0; r < 16; r++) dh[r] = canon4(dh[r], q);  // keeps dh * v < 4 q^2 < q 2^32
+    for (int r = 0; r < 16; r++) dh[r] = canon16(dh[r], q);  // keeps dh * v < 14 q^2 < q 2^32
     // row d: (a, b) of residue g
     for (int part = 0; part < 2; part++) {
       const uint32_t* rp = rows + ((size_t)(d * 2 + part) * 2 + g) * N;

@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
     for (int j = 0; j < 16; j++) v[j] = src[x + 128 * j];
     ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
 #pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = canon4(v[j], q);
+    for (int j = 0; j < 16; j++) v[j] = canon16(v[j], q);
     store16(Ahat + (kd * NR + r) * N, x, v);
   }
   __syncthreads();

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(BLOCK) encode_E_kernel(const DevParams P, cons
     }
     ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
 #pragma unroll
-    for (int rr = 0; rr < 16; rr++) v[rr] = canon4(v[rr], q);
+    for (int rr = 0; rr < 16; rr++) v[rr] = canon16(v[rr], q);
     uint4* dst = reinterpret_cast<uint4*>(Dh + j * N + 16 * x);
 #pragma unroll
     for (int rr = 0; rr < 4; rr++) dst[rr] = make_uint4(v[4 * rr], v[4 * rr + 1], v[4 * rr + 2], v[4 * rr + 3]);
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(BLOCK) crs_what_kernel(const DevParams P, cons
     for (int rr = 0; rr < 16; rr++) v[rr] = wmask[((size_t)k * 2 + g) * N + x + 128 * rr];
     ntt_fwd(v, SC[g], fwd_tw(C), C.q, x, 1 + g);
 #pragma unroll
-    for (int rr = 0; rr < 16; rr++) W[g][16 * x + rr] = canon4(v[rr], C.q);
+    for (int rr = 0; rr < 16; rr++) W[g][16 * x + rr] = canon16(v[rr], C.q);
   }
   __syncthreads();
   for (int i = 0; i + 1 < gamma; i++) {
