@@ -54,7 +54,7 @@ typedef enum {
 typedef enum { INSPIRE_MODE_COMPAT = 0, INSPIRE_MODE_CRT_FIXED = 1 } inspire_mode;
 
 /* InspireParams (src/params.rs:135-185).  The GPU path requires
- * ring_dim = 2048, two CRT primes < 2^30 with q_i = 1 mod 4096 and q0 < 2 q1,
+ * ring_dim = 2048, two CRT primes in (2^20, 2^28) with q_i = 1 mod 4096 and q0 < 2 q1,
  * gadget_base = 2^20 and gadget_len = 3 (secure_128_d2048, params.rs:213-230;
  * p may be 65537 or 2^16). */
 typedef struct {

@@ -343,8 +343,9 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
   const uint64_t q0 = prm->crt_moduli[0], q1 = prm->crt_moduli[1];
   for (uint64_t qm : {q0, q1}) {
     if (qm % (2 * N) != 1) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "CRT moduli must be = 1 (mod 2d) for NTT");
-    if (qm >= (1ULL << 30) || qm <= (1ULL << ZBITS) || !is_prime(qm))
-      return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path needs prime CRT moduli in (2^20, 2^30)");
+    // below 2^28: the lazily reduced transforms keep values below 16 q_i < 2^32
+    if (qm >= (1ULL << 28) || qm <= (1ULL << ZBITS) || !is_prime(qm))
+      return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path needs prime CRT moduli in (2^20, 2^28)");
   }
   if (q0 == q1) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "CRT moduli must be coprime");
   if (q0 >= 2 * q1) return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path needs q0 < 2 q1");
