@@ -320,6 +320,15 @@ int inspire_ntt_inverse_device(inspire_ctx *ctx, uint32_t *d_polys, uint32_t npo
 int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, const uint32_t *d_rgsw,
                                     uint32_t *d_out, uint32_t npairs, void *stream);
 
+/* Client side, for verification at scale: RlweCiphertext::decrypt
+ * (src/rlwe/enc.rs:90-108) + extract_inspiring (src/pir/extract.rs:155-182,
+ * reconstruct_entry src/pir/encode_db.rs:186-201) of n packed responses on
+ * the device.  d_sk: the client's RLWE secret key [poly] (u64, residue-major);
+ * d_ct: [n][2][poly] (u64, as the Respond calls return them); d_entries
+ * receives [n][entry_size] bytes (entry_size <= 32). */
+int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, const uint64_t *d_ct, uint32_t n,
+                                     uint32_t entry_size, uint8_t *d_entries, void *stream);
+
 /* Rate probe with no crate counterpart: blocks x 256 threads x 8
  * independent chains x iters exact 28-bit modular multiplies (Shoup's
  * method, the operation the transforms and products are built from) on

@@ -709,6 +709,15 @@ int inspire_ntt_inverse_device(inspire_ctx* c, uint32_t* d_polys, uint32_t npoly
   return INSPIRE_OK;
 }
 
+int inspire_extract_inspiring_device(inspire_ctx* c, const uint64_t* d_sk, const uint64_t* d_ct, uint32_t n,
+                                     uint32_t entry_size, uint8_t* d_entries, void* stream) {
+  if (!c || (n && (!d_sk || !d_ct || !d_entries))) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (entry_size == 0 || entry_size > 32) return fail(INSPIRE_ERR_UNSUPPORTED, "entry_size must be 1..32 on the GPU path");
+  if (int rc = set_device(c)) return rc;
+  CUDA_TRY(launch_extract(c->P, c->params.p, d_sk, d_ct, (int)n, (int)entry_size, d_entries, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
 int inspire_mulmod_rate_device(inspire_ctx* c, uint32_t blocks, uint32_t iters, uint32_t* d_sink, void* stream) {
   if (!c || (blocks && !d_sink)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   if (int rc = set_device(c)) return rc;

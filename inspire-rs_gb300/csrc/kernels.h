@@ -89,6 +89,10 @@ cudaError_t launch_client_from_yall(const DevParams& P, const uint64_t* yall, ui
                                     cudaStream_t st);
 
 // kernel-level operations
+// decrypt + extract_inspiring of n responses ct[n][2][2][N] (u64) with the
+// secret key sk[2][N] (u64); entries[n][entry_size] (entry_size <= 32).
+cudaError_t launch_extract(const DevParams& P, uint64_t p, const uint64_t* sk, const uint64_t* ct, int n,
+                           int entry_size, uint8_t* entries, cudaStream_t st);
 // blocks x 256 threads x 8 chains x iters lazy Shoup multiplies; sink[blocks * 256].
 cudaError_t launch_mulmod_rate(const DevParams& P, int blocks, int iters, uint32_t* sink, cudaStream_t st);
 cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool inverse,

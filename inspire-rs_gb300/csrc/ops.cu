@@ -122,7 +122,78 @@ __global__ void __launch_bounds__(MM_BLOCK) mulmod_rate_kernel(uint32_t q, uint3
   sink[t] = acc;
 }
 
+// Client-side decrypt + extract_inspiring for one response per CTA
+// (src/pir/extract.rs:155-182 with RlweCiphertext::decrypt,
+// src/rlwe/enc.rs:90-108, and reconstruct_entry, src/pir/encode_db.rs:186-201).
+// Only the first ncols coefficients of a*s + b are needed, so each is a
+// direct negacyclic dot product: coeff c = sum_{j<=c} a_j s_{c-j}
+// - sum_{j>c} a_j s_{N+c-j}.  Threads: 8 per (column, residue) pair; a pair's
+// residues sit 8 lanes apart in one warp.
+struct ExtractConsts {
+  uint64_t barrett[2];  // floor(2^64 / q_r)
+  uint64_t delta, p;
+  int ncols, entry_size;
+};
+
+__device__ __forceinline__ uint64_t barrett_reduce(uint64_t x, uint64_t m, uint32_t q) {
+  uint64_t r = x - __umul64hi(x, m) * q;  // < 2q
+  return r >= q ? r - q : r;
+}
+
+__global__ void __launch_bounds__(256) extract_kernel(const DevParams P, const ExtractConsts K,
+                                                      const uint64_t* __restrict__ sk, const uint64_t* __restrict__ ct,
+                                                      uint8_t* __restrict__ entries) {
+  const int i = blockIdx.x, t = threadIdx.x;
+  const int pr = t >> 3, sub = t & 7, c = pr >> 1, r = pr & 1;
+  const uint32_t q = P.r[r].q;
+  const uint64_t* a = ct + (size_t)i * 4 * N + (size_t)r * N;
+  const uint64_t* b = a + 2 * N;
+  const uint64_t* s = sk + (size_t)r * N;
+  uint64_t pos = 0, neg = 0;
+  if (c < K.ncols) {
+    int k = 0;
+    for (int j = sub; j < N; j += 8) {
+      const uint64_t prod = __ldg(a + j) * (j <= c ? __ldg(s + (c - j)) : __ldg(s + (N + c - j)));
+      if (j <= c) pos += prod;
+      else neg += prod;
+      if (++k == 32) {  // 32 products < 2^56 each fit 64 bits
+        pos = barrett_reduce(pos, K.barrett[r], q);
+        neg = barrett_reduce(neg, K.barrett[r], q);
+        k = 0;
+      }
+    }
+    pos = barrett_reduce(pos, K.barrett[r], q);
+    neg = barrett_reduce(neg, K.barrett[r], q);
+  }
+  uint64_t m = pos >= neg ? pos - neg : pos + q - neg;  // [0, q)
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);  // < 8q
+  m = barrett_reduce(m, K.barrett[r], q);
+  if (c < K.ncols) m = barrett_reduce(m + __ldg(b + c), K.barrett[r], q);
+  const uint64_t m1 = __shfl_down_sync(0xffffffffu, m, 8);  // residue 1 of this column
+  if (sub == 0 && r == 0 && c < K.ncols) {
+    const uint64_t v = crt_compose(P, (uint32_t)m, (uint32_t)m1);  // composite coefficient in [0, q)
+    const uint64_t val = ((v + K.delta / 2) / K.delta) % K.p;
+    uint8_t* e = entries + (size_t)i * K.entry_size;
+    if (2 * c < K.entry_size) e[2 * c] = (uint8_t)(val & 0xFF);
+    if (2 * c + 1 < K.entry_size) e[2 * c + 1] = (uint8_t)((val >> 8) & 0xFF);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_extract(const DevParams& P, uint64_t p, const uint64_t* sk, const uint64_t* ct, int n,
+                           int entry_size, uint8_t* entries, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  ExtractConsts K{};
+  for (int r = 0; r < 2; r++) K.barrett[r] = (uint64_t)((((unsigned __int128)1) << 64) / P.r[r].q);
+  K.delta = P.delta;
+  K.p = p;
+  K.ncols = (entry_size * 8 + 15) / 16;
+  K.entry_size = entry_size;
+  extract_kernel<<<n, 256, 0, st>>>(P, K, sk, ct, entries);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_mulmod_rate(const DevParams& P, int blocks, int iters, uint32_t* sink, cudaStream_t st) {
   if (blocks <= 0 || iters <= 0) return cudaSuccess;

@@ -168,18 +168,6 @@ struct Json {
     }
     return false;
   }
-  // array of u64 into out (cleared)
-  bool u64_array(std::vector<uint64_t>& out) {
-    out.clear();
-    if (!expect('[')) return false;
-    if (eat(']')) return true;
-    do {
-      uint64_t v;
-      if (!u64(v)) return false;
-      out.push_back(v);
-    } while (eat(','));
-    return expect(']');
-  }
   // object: calls field(key) for each key; field consumes the value
   template <class F>
   bool object(F&& field) {

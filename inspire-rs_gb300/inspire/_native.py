@@ -131,6 +131,7 @@ def load(path: str = LIB_PATH):
         "inspire_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStatsC)]),
         "inspire_now_ns": (C.c_int64, []),
         "inspire_mulmod_rate_device": (C.c_int, [vp, u32, u32, vp, vp]),
+        "inspire_extract_inspiring_device": (C.c_int, [vp, vp, vp, u32, u32, vp, vp]),
         "inspire_seeded_query_from_json": (C.c_int, [C.POINTER(InspireParamsC), C.c_char_p, C.c_size_t, vp, vp, vp,
                                                      vp, vp, vp]),
         "inspire_query_response_to_json": (C.c_int, [C.POINTER(InspireParamsC), vp, u32, vp, u64, vp, C.c_size_t,

@@ -379,6 +379,14 @@ def ntt_inverse_device(crs: ServerCrs, d_polys: int, npolys: int, stream: int) -
     _check(crs.L.inspire_ntt_inverse_device(crs.h, C.c_void_p(d_polys), npolys, C.c_void_p(stream)))
 
 
+def extract_inspiring_device(crs: ServerCrs, d_sk: int, d_ct: int, n: int, entry_size: int, d_entries: int,
+                             stream: int) -> None:
+    """decrypt + extract_inspiring (extract.rs:155-182) of n responses on the
+    device (raw device pointers as ints); asynchronous."""
+    v = C.c_void_p
+    _check(crs.L.inspire_extract_inspiring_device(crs.h, v(d_sk), v(d_ct), n, entry_size, v(d_entries), v(stream)))
+
+
 def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, stream: int) -> int:
     """Launch the modular-multiply rate probe; returns the multiplies issued."""
     _check(crs.L.inspire_mulmod_rate_device(crs.h, blocks, iters, C.c_void_p(d_sink), C.c_void_p(stream)))

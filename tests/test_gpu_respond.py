@@ -204,3 +204,34 @@ def test_full_size_database_extracts(oracle_mod):
     want = ctx.respond_inspiring(ctx.encode_shard(db, ENTRY, ix // N), ctx.expand_rgsw(seeds[0], brows[0]), W_SEED,
                                  mode=O.MODE_CRT_FIXED, pack=pack, y_body=y_body)
     assert np.array_equal(out[0], want)
+
+
+def test_extract_inspiring_device(world):
+    """decrypt + extract_inspiring on the device (extract.rs:155-182) equals
+    the oracle's extraction and recovers the queried entries."""
+    W = world
+    torch = pytest.importorskip("torch")
+    inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
+    crs, edb, pack, omode = W["w"]["crt_fixed"]
+    y_body, _ = client.packing_keys(pack)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    idxs = [0, 5, 2047, 2048, 4096 + 899, 3000]
+    seeds = np.zeros((len(idxs), 6, 32), np.uint8)
+    brows = np.zeros((len(idxs), 6, 2 * N), np.uint64)
+    for k, ix in enumerate(idxs):
+        seeds[k], brows[k] = client.query_seeded(ix % N)
+    out = inspire.respond_seeded_batch(crs, edb, [ix // N for ix in idxs], seeds, brows, [cid] * len(idxs))
+    dev = torch.device("cuda", 0)
+    d_ct = torch.from_numpy(out.view(np.int64)).to(dev)
+    d_sk = torch.from_numpy(np.ascontiguousarray(client.sk).view(np.int64)).to(dev)
+    for entry in (ENTRY, 31, 7):
+        d_e = torch.zeros((len(idxs), entry), dtype=torch.uint8, device=dev)
+        inspire.pir.extract_inspiring_device(crs, d_sk.data_ptr(), d_ct.data_ptr(), len(idxs), entry, d_e.data_ptr(),
+                                             torch.cuda.current_stream(dev).cuda_stream)
+        got = d_e.cpu().numpy()
+        for k, ix in enumerate(idxs):
+            want = client.extract_inspiring(out[k], entry)
+            assert np.array_equal(got[k], want)
+            if entry == ENTRY:
+                assert np.array_equal(got[k], W["db"][ix * ENTRY:(ix + 1) * ENTRY])
+    crs.release_client(cid)
