@@ -386,6 +386,35 @@ def main():
         kern_s = float(t.item())
     value = ws * B * L * args.steps / kern_s
 
+    # the same step captured once as a CUDA graph (2-stream fork/join inside)
+    # and replayed: launch costs leave the host path
+    value_graph = None
+    if ws == 1:
+        cap = torch.cuda.Stream(dev)
+        graph = torch.cuda.CUDAGraph()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=cap):
+            e_fork = torch.cuda.Event()
+            e_fork.record(cap)
+            for st in side:
+                st.wait_event(e_fork)
+            for j in range(L):
+                launch(j, B, side[j % len(side)])
+            for st in side:
+                e_join = torch.cuda.Event()
+                e_join.record(st)
+                cap.wait_event(e_join)
+        gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        graph.replay()
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            gev[k][0].record(stream)
+            graph.replay()
+            gev[k][1].record(stream)
+        torch.cuda.synchronize()
+        value_graph = B * L * args.steps / (sum(a.elapsed_time(b) for a, b in gev) / 1e3)
+
     # correctness of what was timed: statuses, then every response of the nb
     # pool batches decrypted and extracted on the device (checked against the
     # oracle's extraction on samples) must equal its database entry
@@ -523,6 +552,7 @@ def main():
             "clocks": clk.summary(),
             "gpu_launches": args.steps * L,
             "verified_responses": verified,
+            "value_cuda_graph": value_graph,
             "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
             "plain_single_query_qps": sweep.get("1"),

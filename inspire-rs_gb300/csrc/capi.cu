@@ -442,6 +442,14 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     P.r[r].inv = reinterpret_cast<const uint2*>(base + 2 * N);
     P.r[r].psi_pow = base + 4 * N;
   }
+  e = prepare_respond_kernels();
+  if (e == cudaSuccess) e = prepare_nopacking_kernels();
+  if (e == cudaSuccess) e = prepare_ops_kernels();
+  if (e == cudaSuccess) e = prepare_setup_kernels();
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(INSPIRE_ERR_CUDA, std::string("kernel setup: ") + cudaGetErrorString(e));
+  }
   *out = c;
   return INSPIRE_OK;
 }
@@ -568,7 +576,10 @@ int inspire_client_register(inspire_ctx* c, const uint64_t* y_body, const uint64
   std::lock_guard<std::mutex> lk(c->mu);
   if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
   if (int rc = set_device(c)) return rc;
-  return register_keys(c, y_body, y_all, id);
+  if (int rc = register_keys(c, y_body, y_all, id)) return rc;
+  // the device client table is brought up to date here, so that later
+  // launches make no copy (they can be captured in a CUDA graph)
+  return sync_client_table(c);
 }
 
 int inspire_client_release(inspire_ctx* c, int32_t id) {
@@ -578,7 +589,7 @@ int inspire_client_release(inspire_ctx* c, int32_t id) {
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "unknown client id");
   if (int rc = set_device(c)) return rc;
   release_keys(c, id);
-  return INSPIRE_OK;
+  return sync_client_table(c);
 }
 
 int inspire_respond_seeded_inspiring(inspire_ctx* c, const inspire_db* db, const inspire_seeded_query* qy,

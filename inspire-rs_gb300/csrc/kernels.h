@@ -70,6 +70,13 @@ struct NoPackingArgs {
   int* status;
 };
 
+// Set the kernels' dynamic shared-memory limits on the current device (once
+// per device, before any launch; launches then make no configuration call).
+cudaError_t prepare_respond_kernels();
+cudaError_t prepare_nopacking_kernels();
+cudaError_t prepare_ops_kernels();
+cudaError_t prepare_setup_kernels();
+
 size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);
 

@@ -167,11 +167,16 @@ size_t nopacking_smem_bytes() { return sizeof(uint32_t) * ((size_t)RG * NTT_SCRA
 
 template <bool SEEDED>
 static cudaError_t launch_np(const NoPackingArgs& a, cudaStream_t st) {
-  const size_t smem = nopacking_smem_bytes();
-  cudaError_t e = cudaFuncSetAttribute(nopacking_kernel<0, SEEDED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  nopacking_kernel<0, SEEDED><<<a.nq, RBLOCK, smem, st>>>(a);
+  nopacking_kernel<0, SEEDED><<<a.nq, RBLOCK, nopacking_smem_bytes(), st>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t prepare_nopacking_kernels() {
+  const int smem = (int)nopacking_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(nopacking_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nopacking_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
 }
 
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st) {

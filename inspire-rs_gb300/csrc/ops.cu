@@ -211,14 +211,17 @@ cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool
   return cudaGetLastError();
 }
 
+constexpr size_t EXT_SMEM = sizeof(uint32_t) * ((size_t)2 * ELL * N + 2 * NTT_SCRATCH);
+
 cudaError_t launch_external_product(const DevParams& P, const uint32_t* ct, const uint32_t* rgsw, uint32_t* out,
                                     int npairs, cudaStream_t st) {
   if (npairs <= 0) return cudaSuccess;
-  const size_t smem = sizeof(uint32_t) * ((size_t)2 * ELL * N + 2 * NTT_SCRATCH);
-  cudaError_t e = cudaFuncSetAttribute(external_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  external_product_kernel<<<npairs, BLOCK, smem, st>>>(P, ct, rgsw, out);
+  external_product_kernel<<<npairs, BLOCK, EXT_SMEM, st>>>(P, ct, rgsw, out);
   return cudaGetLastError();
+}
+
+cudaError_t prepare_ops_kernels() {
+  return cudaFuncSetAttribute(external_product_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EXT_SMEM);
 }
 
 }  // namespace ig

@@ -403,13 +403,29 @@ size_t respond_smem_bytes(int mode) {
 }
 
 template <int MODE, bool SEEDED, bool QDB>
+static cudaError_t set_smem_attr() {
+  return cudaFuncSetAttribute(respond_kernel<MODE, SEEDED, QDB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)respond_smem_bytes(MODE));
+}
+
+// Launches issue no configuration call (so they can be captured in a CUDA
+// graph): the shared-memory attribute of every variant is set once per
+// device by prepare_respond_kernels.
+template <int MODE, bool SEEDED, bool QDB>
 static cudaError_t launch_one(const RespondArgs& a, cudaStream_t st) {
-  const size_t smem = respond_smem_bytes(MODE);
-  cudaError_t e =
-      cudaFuncSetAttribute(respond_kernel<MODE, SEEDED, QDB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, smem, st>>>(a);
+  respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t prepare_respond_kernels() {
+  const cudaError_t es[] = {
+      set_smem_attr<MODE_COMPAT, false, false>(),    set_smem_attr<MODE_COMPAT, true, false>(),
+      set_smem_attr<MODE_COMPAT, false, true>(),     set_smem_attr<MODE_COMPAT, true, true>(),
+      set_smem_attr<MODE_CRT_FIXED, false, false>(), set_smem_attr<MODE_CRT_FIXED, true, false>(),
+      set_smem_attr<MODE_CRT_FIXED, false, true>(),  set_smem_attr<MODE_CRT_FIXED, true, true>()};
+  for (cudaError_t e : es)
+    if (e != cudaSuccess) return e;
+  return cudaSuccess;
 }
 
 template <int MODE>

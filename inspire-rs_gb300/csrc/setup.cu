@@ -174,11 +174,14 @@ cudaError_t launch_columns_from_raw(const uint8_t* raw, uint64_t n_entries, int 
   return cudaGetLastError();
 }
 
+cudaError_t prepare_setup_kernels() {
+  const size_t smem = sizeof(uint32_t) * ((size_t)MAX_GAMMA * N + 2 * NTT_SCRATCH + MAX_GAMMA);
+  return cudaFuncSetAttribute(encode_E_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 cudaError_t launch_encode_E(const DevParams& P, const uint16_t* H, int nshards, uint32_t* E, cudaStream_t st) {
   if (nshards <= 0) return cudaSuccess;
   const size_t smem = sizeof(uint32_t) * ((size_t)P.gamma * N + 2 * NTT_SCRATCH + MAX_GAMMA);
-  cudaError_t e = cudaFuncSetAttribute(encode_E_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
   // grid.x is limited to 2^31-1 shards; y = residue, z = digit
   encode_E_kernel<<<dim3(nshards, 2, ELL), BLOCK, smem, st>>>(P, H, E);
   return cudaGetLastError();

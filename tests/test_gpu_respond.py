@@ -235,3 +235,47 @@ def test_extract_inspiring_device(world):
             if entry == ENTRY:
                 assert np.array_equal(got[k], W["db"][ix * ENTRY:(ix + 1) * ENTRY])
     crs.release_client(cid)
+
+
+def test_batch_device_call_in_cuda_graph(world):
+    """The device-buffer batch call makes no configuration call or copy, so
+    it can be captured in a CUDA graph; replays return the same responses."""
+    W = world
+    torch = pytest.importorskip("torch")
+    inspire, client = W["inspire"], W["client"]
+    crs, edb, pack, omode = W["w"]["crt_fixed"]
+    y_body, _ = client.packing_keys(pack)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    idxs = [1, 2049, 4100, 77]
+    n = len(idxs)
+    seeds = np.zeros((n, 6, 32), np.uint8)
+    brows = np.zeros((n, 6, 2 * N), np.uint64)
+    for k, ix in enumerate(idxs):
+        seeds[k], brows[k] = client.query_seeded(ix % N)
+    want = inspire.respond_seeded_batch(crs, edb, [ix // N for ix in idxs], seeds, brows, [cid] * n)
+    dev = torch.device("cuda", 0)
+    d_sid = torch.tensor([ix // N for ix in idxs], dtype=torch.int32, device=dev)
+    d_seeds = torch.from_numpy(np.ascontiguousarray(seeds[:, 3:6])).to(dev)
+    d_brows = torch.from_numpy(np.ascontiguousarray(brows[:, 3:6]).view(np.int64)).to(dev)
+    d_cid = torch.full((n,), cid, dtype=torch.int32, device=dev)
+    d_out = torch.zeros((n, 2, 2 * N), dtype=torch.int64, device=dev)
+    d_st = torch.zeros(n, dtype=torch.int32, device=dev)
+    s = torch.cuda.Stream(dev)
+
+    def call(stream):
+        inspire.respond_seeded_batch_device(crs, edb, n, d_sid.data_ptr(), d_seeds.data_ptr(), d_brows.data_ptr(),
+                                            d_cid.data_ptr(), d_out.data_ptr(), d_st.data_ptr(), stream.cuda_stream)
+
+    with torch.cuda.stream(s):
+        call(s)  # warm-up outside the capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        call(s)
+    d_out.zero_()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert not d_st.cpu().numpy().any()
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
+    crs.release_client(cid)
