@@ -1212,3 +1212,243 @@ void io_extract_inspiring(const io_ctx *c, const uint64_t *sk,
   }
   free(m);
 }
+
+/* ===================================================================== */
+/* tree packing: respond_one_packing (pir/respond.rs:213-268) with        */
+/* pack_lwes (inspiring/automorph_pack.rs:171-485) and the Galois keys of */
+/* setup (pir/setup.rs:164-173; ks/setup.rs:118-245)                       */
+/* ===================================================================== */
+
+static int log2i(int n) {
+  int l = 0;
+  while ((1 << l) < n) l++;
+  return l;
+}
+
+void io_automorphism_ks_matrix(const io_ctx *c, io_sampler *s, io_rng *g,
+                               const uint64_t *sk, int t, uint64_t *ks) {
+  /* generate_automorphism_ks_matrix (ks/setup.rs:218-245): tau_t(s), then
+   * generate_ks_matrix (:118-162) row i = (a_i, -a_i*s + e_i + tau_t(s)*z^i) */
+  size_t L = PLEN(c);
+  uint64_t *as = (uint64_t *)malloc(8 * L), *e = (uint64_t *)malloc(8 * L);
+  uint64_t *tmp = (uint64_t *)malloc(8 * L);
+  io_automorphism(c, sk, t, as);
+  u128 pw = 1; /* GadgetVector::powers (rgsw/types.rs:79-90) */
+  for (int i = 0; i < c->ell; i++) {
+    uint64_t *a = ks + (size_t)(2 * i) * L, *b = a + L;
+    random_poly(c, g, a);
+    gaussian_poly(c, s, e);
+    io_poly_mul(c, a, sk, tmp);
+    p_neg(c, tmp, tmp);
+    p_add(c, tmp, e, tmp);
+    p_scalar(c, as, (uint64_t)pw, e);
+    p_add(c, tmp, e, b);
+    pw = (pw * c->zbase) % c->q;
+  }
+  free(as);
+  free(e);
+  free(tmp);
+}
+
+void io_galois_keys(const io_ctx *c, io_sampler *s, io_rng *g,
+                    const uint64_t *sk, uint64_t *keys) {
+  /* setup.rs:164-173: keys[i] for t = d / 2^i + 1, i < log2(d) */
+  size_t L = PLEN(c);
+  int ld = log2i(c->n);
+  for (int i = 0; i < ld; i++)
+    io_automorphism_ks_matrix(c, s, g, sk, (c->n >> i) + 1,
+                              keys + (size_t)i * 2 * c->ell * L);
+}
+
+static void homomorphic_automorph(const io_ctx *c, const uint64_t *ct, int t,
+                                  const uint64_t *ks, uint64_t *out) {
+  /* automorph_pack.rs:33-79 */
+  size_t L = PLEN(c);
+  uint64_t *aa = (uint64_t *)malloc(8 * L), *ab = (uint64_t *)malloc(8 * L);
+  uint64_t *dg = (uint64_t *)malloc(8 * L * (size_t)c->ell);
+  uint64_t *tmp = (uint64_t *)malloc(8 * L);
+  io_automorphism(c, ct, t, aa);
+  io_automorphism(c, ct + L, t, ab);
+  io_gadget_decompose(c, aa, dg);
+  memset(out, 0, 8 * L);
+  memcpy(out + L, ab, 8 * L);
+  for (int i = 0; i < c->ell; i++) {
+    const uint64_t *row = ks + (size_t)(2 * i) * L;
+    io_poly_mul(c, dg + (size_t)i * L, row, tmp);
+    p_add(c, out, tmp, out);
+    io_poly_mul(c, dg + (size_t)i * L, row + L, tmp);
+    p_add(c, out + L, tmp, out + L);
+  }
+  free(aa);
+  free(ab);
+  free(dg);
+  free(tmp);
+}
+
+static void monomial(const io_ctx *c, int k, int negative, uint64_t *out) {
+  /* YConstants::generate (automorph_pack.rs:103-132): X^k, or (q-1) X^k */
+  uint64_t *co = (uint64_t *)calloc((size_t)c->n, 8);
+  co[k] = negative ? c->q - 1 : 1;
+  io_poly_from_composite(c, co, out);
+  free(co);
+}
+
+/* pack_lwes_inner (automorph_pack.rs:171-255).  Subtrees whose leaves are
+ * all zero padding return NULL: every step maps an all-zero ciphertext to
+ * an all-zero ciphertext (0 + 0, y * 0, tau(0), gadget digits of 0), so
+ * skipping them gives the same bits. */
+static uint64_t *pack_inner(const io_ctx *c, int ell, int start,
+                            const uint64_t *leaves, int nreal,
+                            const uint64_t *keys, int log_n) {
+  size_t L = PLEN(c);
+  if (start >= nreal) return NULL;
+  if (ell == 0) {
+    uint64_t *r = (uint64_t *)malloc(16 * L);
+    memcpy(r, leaves + (size_t)start * 2 * L, 16 * L);
+    return r;
+  }
+  int step = 1 << (log_n - ell);
+  uint64_t *even = pack_inner(c, ell - 1, start, leaves, nreal, keys, log_n);
+  uint64_t *odd = pack_inner(c, ell - 1, start + step, leaves, nreal, keys, log_n);
+  uint64_t *s0 = (uint64_t *)malloc(16 * L), *s1 = (uint64_t *)malloc(16 * L);
+  memcpy(s0, even, 16 * L);
+  memcpy(s1, even, 16 * L);
+  if (odd) {
+    uint64_t *y = (uint64_t *)malloc(8 * L), *ny = (uint64_t *)malloc(8 * L);
+    uint64_t *tmp = (uint64_t *)malloc(8 * L);
+    monomial(c, c->n >> ell, 0, y);
+    monomial(c, c->n >> ell, 1, ny);
+    for (int h = 0; h < 2; h++) { /* RlweCiphertext::poly_mul (rlwe/enc.rs:147-152) */
+      io_poly_mul(c, odd + (size_t)h * L, y, tmp);
+      p_add(c, s0 + (size_t)h * L, tmp, s0 + (size_t)h * L);
+      io_poly_mul(c, odd + (size_t)h * L, ny, tmp);
+      p_add(c, s1 + (size_t)h * L, tmp, s1 + (size_t)h * L);
+    }
+    free(y);
+    free(ny);
+    free(tmp);
+  }
+  int ld = log2i(c->n);
+  uint64_t *au = (uint64_t *)malloc(16 * L);
+  homomorphic_automorph(c, s1, (1 << ell) + 1,
+                        keys + (size_t)(ld - ell) * 2 * c->ell * L, au);
+  p_add(c, s0, au, s0);
+  p_add(c, s0 + L, au + L, s0 + L);
+  free(au);
+  free(s1);
+  free(even);
+  free(odd);
+  return s0;
+}
+
+int io_pack_lwes(const io_ctx *c, const uint64_t *leaf_a, const uint64_t *bval_in,
+                 int nlwe, const uint64_t *keys, int mode, uint64_t *out_a,
+                 uint64_t *out_b) {
+  /* pack_lwes (automorph_pack.rs:418-485) on LWEs given as their prepped
+   * form: leaf_a[i] = invert_sample_extract(lwe_i.a) as a polynomial (for a
+   * sample_extract_coeff0 output that is the RLWE a itself,
+   * automorph_pack.rs:349-405), bval_in[i] = lwe_i.b (composite).  out_b
+   * holds 2 PLEN words in MODE_COMPAT with two moduli: the crate adds
+   * b_val * d to the first d words of the residue-major vector and rebuilds
+   * the polynomial from all 2d words with Poly::from_coeffs_moduli
+   * (poly.rs:127-159), giving ring dimension 2d.  MODE_CRT_FIXED adds
+   * b_val * d to composite coefficient z.  Returns the words written to out_b
+   * (PLEN or 2 PLEN), or -1 for no LWE (the zero ciphertext). */
+  size_t L = PLEN(c);
+  int n = c->n;
+  if (nlwe <= 0) {
+    memset(out_a, 0, 8 * L);
+    memset(out_b, 0, 8 * L);
+    return -1;
+  }
+  if (nlwe == 1) { /* automorph_pack.rs:439-446: (a, b_val at coefficient 0) */
+    memcpy(out_a, leaf_a, 8 * L);
+    uint64_t *bco = (uint64_t *)calloc((size_t)n, 8);
+    bco[0] = bval_in[0];
+    io_poly_from_composite(c, bco, out_b);
+    free(bco);
+    return (int)L;
+  }
+  uint64_t *leaves = (uint64_t *)calloc(2 * L * (size_t)nlwe, 8);
+  uint64_t *bval = (uint64_t *)calloc((size_t)n, 8);
+  for (int i = 0; i < nlwe; i++) {
+    memcpy(leaves + (size_t)i * 2 * L, leaf_a + (size_t)i * L, 8 * L);
+    if (i < n) bval[i] = bval_in[i];
+  }
+  int ld = log2i(n);
+  uint64_t *packed = pack_inner(c, ld, 0, leaves, nlwe, keys, ld);
+  memcpy(out_a, packed, 8 * L);
+  const uint64_t q = c->q;
+  int words = (int)L;
+  if (mode == IO_MODE_COMPAT && c->crt == 2) {
+    /* automorph_pack.rs:474-484 on the residue-major vector of 2d words */
+    uint64_t *bc = (uint64_t *)malloc(8 * L);
+    memcpy(bc, packed + L, 8 * L);
+    for (int z = 0; z < n; z++) {
+      uint64_t sc = (uint64_t)(((u128)bval[z] * (uint64_t)n) % q);
+      bc[z] = (uint64_t)(((u128)bc[z] + sc) % q);
+    }
+    for (size_t w = 0; w < L; w++) {
+      out_b[w] = bc[w] % c->mod[0];
+      out_b[L + w] = bc[w] % c->mod[1];
+    }
+    free(bc);
+    words = (int)(2 * L);
+  } else {
+    for (int z = 0; z < n; z++) {
+      uint64_t v = io_poly_coeff(c, packed + L, z);
+      uint64_t sc = (uint64_t)(((u128)bval[z] * (uint64_t)n) % q);
+      set_coeff(c, out_b, z, (uint64_t)(((u128)v + sc) % q));
+    }
+  }
+  free(packed);
+  free(bval);
+  free(leaves);
+  return words;
+}
+
+int io_respond_one_packing(const io_ctx *c, const uint64_t *shard, int ncols,
+                           const uint64_t *rgsw, const uint64_t *keys,
+                           int mode, uint64_t *out_a, uint64_t *out_b,
+                           int nthreads) {
+  /* respond.rs:213-268: column products, sample_extract_coeff0 of each
+   * (rlwe/enc.rs:195-208), pack_lwes */
+  size_t L = PLEN(c);
+  if (ncols <= 0) { /* the zero response (respond.rs:230-236) */
+    memset(out_a, 0, 8 * L);
+    memset(out_b, 0, 8 * L);
+    return -1;
+  }
+  uint64_t *cols = (uint64_t *)malloc(8 * 2 * L * (size_t)ncols);
+  column_products(c, shard, ncols, rgsw, cols, nthreads);
+  uint64_t *la = (uint64_t *)malloc(8 * L * (size_t)ncols);
+  uint64_t *bv = (uint64_t *)malloc(8 * (size_t)ncols);
+  for (int i = 0; i < ncols; i++) {
+    memcpy(la + (size_t)i * L, cols + (size_t)i * 2 * L, 8 * L);
+    bv[i] = io_poly_coeff(c, cols + (size_t)i * 2 * L + L, 0);
+  }
+  int words = io_pack_lwes(c, la, bv, ncols, keys, mode, out_a, out_b);
+  free(bv);
+  free(la);
+  free(cols);
+  return words;
+}
+
+void io_extract_packed(const io_ctx *c, const uint64_t *sk, const uint64_t *ct,
+                       int entry_size, uint8_t *out) {
+  /* extract_packed (pir/extract.rs:113-148): decrypt, then column values
+   * times d^-1 mod p (1 when d has no inverse), reconstruct_entry */
+  uint64_t *m = (uint64_t *)malloc(8 * (size_t)c->n);
+  io_decrypt(c, sk, ct, m);
+  uint64_t p = c->p, dinv = 1;
+  if (p % 2 == 1) dinv = powmod((uint64_t)c->n % p, p - 2, p); /* p prime here (65537) */
+  int ncols = io_num_columns(entry_size);
+  memset(out, 0, (size_t)entry_size);
+  for (int col = 0; col < ncols; col++) {
+    uint64_t v = (uint64_t)(((u128)m[col] * dinv) % p);
+    int bo = col * 2;
+    if (bo < entry_size) out[bo] = (uint8_t)(v & 0xFF);
+    if (bo + 1 < entry_size) out[bo + 1] = (uint8_t)((v >> 8) & 0xFF);
+  }
+  free(m);
+}

@@ -170,6 +170,20 @@ void io_query_seeded(const io_ctx *ctx, io_sampler *s, io_rng *rng,
 void io_client_packing_keys(const io_pack *pk, io_sampler *s,
                             const uint64_t *sk, uint64_t *y_body,
                             uint64_t *y_all);
+/* tree packing (respond_one_packing, pir/respond.rs:213-268) */
+void io_automorphism_ks_matrix(const io_ctx *ctx, io_sampler *s, io_rng *g,
+                               const uint64_t *sk, int t, uint64_t *ks);
+void io_galois_keys(const io_ctx *ctx, io_sampler *s, io_rng *g,
+                    const uint64_t *sk, uint64_t *keys);
+int io_pack_lwes(const io_ctx *ctx, const uint64_t *leaf_a, const uint64_t *bval,
+                 int nlwe, const uint64_t *keys, int mode, uint64_t *out_a,
+                 uint64_t *out_b);
+int io_respond_one_packing(const io_ctx *ctx, const uint64_t *shard, int ncols,
+                           const uint64_t *rgsw, const uint64_t *keys,
+                           int mode, uint64_t *out_a, uint64_t *out_b,
+                           int nthreads);
+void io_extract_packed(const io_ctx *ctx, const uint64_t *sk, const uint64_t *ct,
+                       int entry_size, uint8_t *out);
 void io_decrypt(const io_ctx *ctx, const uint64_t *sk, const uint64_t *ct,
                 uint64_t *out);
 void io_extract_inspiring(const io_ctx *ctx, const uint64_t *sk,

@@ -94,6 +94,11 @@ def lib():
         "io_client_packing_keys": (None, [vp, vp, U64P, U64P, U64P]),
         "io_decrypt": (None, [vp, U64P, U64P, U64P]),
         "io_extract_inspiring": (None, [vp, U64P, U64P, C.c_int, U8P]),
+        "io_automorphism_ks_matrix": (None, [vp, vp, vp, U64P, C.c_int, U64P]),
+        "io_galois_keys": (None, [vp, vp, vp, U64P, U64P]),
+        "io_pack_lwes": (C.c_int, [vp, U64P, U64P, C.c_int, U64P, C.c_int, U64P, U64P]),
+        "io_respond_one_packing": (C.c_int, [vp, U64P, C.c_int, U64P, U64P, C.c_int, U64P, U64P, C.c_int]),
+        "io_extract_packed": (None, [vp, U64P, U64P, C.c_int, U8P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -251,6 +256,34 @@ class Ctx:
                                     np.ascontiguousarray(rgsw, np.uint64), out, _ptr(cols), nthreads)
         return (out, cols.reshape(ncols, 2, self.plen)) if with_columns else out
 
+    def pack_lwes(self, leaf_a, bvals, keys, mode=MODE_CRT_FIXED):
+        """pack_lwes on prepped LWEs (leaf a polys, composite b values);
+        returns (a, b) with b of 2*plen words in compat mode with two moduli."""
+        la = np.ascontiguousarray(leaf_a, np.uint64).reshape(-1, self.plen)
+        bv = np.ascontiguousarray(bvals, np.uint64)
+        out_a = self.zeros()
+        out_b = self.zeros(2)
+        w = self.L.io_pack_lwes(self.h, la, bv, la.shape[0], np.ascontiguousarray(keys, np.uint64), mode, out_a,
+                                out_b.reshape(-1))
+        return out_a, out_b.reshape(-1)[:max(w, self.plen)]
+
+    def respond_one_packing(self, shard, rgsw, keys, mode=MODE_CRT_FIXED, nthreads=0):
+        """respond_one_packing (respond.rs:213-268): (a, b) of the packed
+        ciphertext, b of 2*plen words in compat mode with two moduli."""
+        ncols = shard.shape[0]
+        out_a = self.zeros()
+        out_b = self.zeros(2)
+        w = self.L.io_respond_one_packing(self.h, np.ascontiguousarray(shard, np.uint64), ncols,
+                                          np.ascontiguousarray(rgsw, np.uint64), np.ascontiguousarray(keys, np.uint64),
+                                          mode, out_a, out_b.reshape(-1), nthreads)
+        return out_a, out_b.reshape(-1)[:max(w, self.plen)]
+
+    def extract_packed(self, sk, ct, entry_size):
+        out = np.zeros(entry_size, dtype=np.uint8)
+        self.L.io_extract_packed(self.h, np.ascontiguousarray(sk, np.uint64), np.ascontiguousarray(ct, np.uint64),
+                                 entry_size, out)
+        return out
+
     # ---- client ----
     def decrypt(self, sk, ct):
         out = np.zeros(self.n, dtype=np.uint64)
@@ -395,6 +428,17 @@ class Client:
 
     def extract_inspiring(self, ct, entry_size):
         return self.ctx.extract_inspiring(self.sk, ct, entry_size)
+
+    def galois_keys(self):
+        """The tree-packing key-switching matrices of setup (setup.rs:164-173):
+        log2(d) matrices of gadget_len rows (a, b), shape (log2 d, 2*ell, plen)."""
+        ld = int(self.ctx.n).bit_length() - 1
+        out = self.ctx.zeros(ld * 2 * self.ctx.ell)
+        self.L.io_galois_keys(self.ctx.h, self.sampler.h, self.rng.h, self.sk, out)
+        return out.reshape(ld, 2 * self.ctx.ell, self.ctx.plen)
+
+    def extract_packed(self, ct, entry_size):
+        return self.ctx.extract_packed(self.sk, ct, entry_size)
 
 
 def chacha20_block(key_words, ctr_nonce):

@@ -324,3 +324,83 @@ def test_respond_nopacking_extracts(oracle_mod):
     vals = [int(cl.decrypt(col.reshape(-1))[0]) for col in cols]
     ent = db[99 * 4:100 * 4]
     assert vals == [int(ent[0]) | (int(ent[1]) << 8), int(ent[2]) | (int(ent[3]) << 8)]
+
+
+# ---------------------------------------------------------------- tree packing
+def _lwe_leaves(O, c, cl, msgs, trivial=False):
+    """RLWE encryptions of m at coefficient 0, as pack_lwes sees their
+    sample_extract_coeff0 LWEs: leaf a = the RLWE a, b = b.coeff(0)
+    (automorph_pack.rs:349-405); trivial LWEs have a = 0, b = delta * m."""
+    la, bv = [], []
+    for m in msgs:
+        if trivial:
+            la.append(c.zeros())
+            bv.append((int(c.delta) * m) % int(c.q))
+            continue
+        msg = c.zeros()
+        msg[0] = m
+        if c.crt == 2:
+            msg[c.n] = m
+        ct = cl.rlwe_encrypt(msg)
+        la.append(ct[0])
+        bv.append(c.L.io_poly_coeff(c.h, np.ascontiguousarray(ct[1]), 0))
+    return np.stack(la), np.array(bv, dtype=np.uint64)
+
+
+@pytest.mark.parametrize("case", ["single", "two", "trivial", "multiple"])
+def test_pack_lwes_kats(oracle_mod, case):
+    """automorph_pack.rs tests test_pack_lwes_single / _two / _trivial /
+    _multiple (d = 256, q = 2^60 - 2^14 + 1, p = 2^16): coefficient i of
+    the packed decryption is m_i * d mod p (m itself for a single LWE)."""
+    O = oracle_mod
+    c = single(O, 256)
+    cl = O.Client(c, seed=0, rng_seed=21)
+    keys = cl.galois_keys()
+    msgs = {"single": [12345], "two": [100, 200], "trivial": [100, 200, 300, 400],
+            "multiple": [100, 200, 300, 400]}[case]
+    la, bv = _lwe_leaves(O, c, cl, msgs, trivial=case == "trivial")
+    a, b = c.pack_lwes(la, bv, keys, mode=O.MODE_COMPAT)
+    dec = cl.decrypt(np.stack([a, b]))
+    if case == "single":
+        assert int(dec[0]) == 12345
+    else:
+        for i, m in enumerate(msgs):
+            assert int(dec[i]) == (m * 256) % 65536
+
+
+def test_tree_packing_crt_default_params_finding(oracle_mod):
+    """respond_one_packing at d = 2048 with the two CRT moduli and the crate's
+    default p = 65537 (params.rs:213-230) does not give decryptable responses:
+    (1) the crate's last step (automorph_pack.rs:474-484) returns a b
+    polynomial of dimension 2d; (2) even with the b values added per
+    composite coefficient, the 11 levels of key switching leave noise above
+    delta / 2, so extract_packed (extract.rs:113-148) loses columns."""
+    O = oracle_mod
+    c = O.Ctx(p=65537)
+    rng = np.random.default_rng(12)
+    db = rng.integers(0, 256, size=2048 * 32, dtype=np.uint8)
+    cl = O.Client(c, seed=3, rng_seed=13)
+    keys = cl.galois_keys()
+    shard = c.encode_shard(db, 32, 0)
+    seeds, brows = cl.query_seeded(5)
+    rg = c.expand_rgsw(seeds, brows)
+    a_f, b_f = c.respond_one_packing(shard, rg, keys, mode=O.MODE_CRT_FIXED)
+    a_c, b_c = c.respond_one_packing(shard, rg, keys, mode=O.MODE_COMPAT)
+    assert b_f.size == c.plen and b_c.size == 2 * c.plen and np.array_equal(a_c, a_f)
+    assert np.array_equal(b_c[16:c.n], b_f[16:c.n])  # residue-0 words without an added b value
+    got = cl.extract_packed(np.stack([a_f, b_f]), 32)
+    ent = db[5 * 32:6 * 32]
+    # a column is lost exactly when its coefficient's noise exceeds delta / 2
+    t = np.zeros(c.plen, np.uint64)
+    c.L.io_poly_mul(c.h, np.ascontiguousarray(a_f), np.ascontiguousarray(cl.sk), t)
+    q, D = int(c.q), int(c.delta)
+    lost, over = [], []
+    for k in range(16):
+        v = (int(c.L.io_poly_coeff(c.h, t, k)) + int(c.L.io_poly_coeff(c.h, np.ascontiguousarray(b_f), k))) % q
+        m = int(ent[2 * k]) | (int(ent[2 * k + 1]) << 8)
+        err = (v - D * ((m * 2048) % 65537)) % q
+        if min(err, q - err) > D // 2:
+            over.append(k)
+        if (got[2 * k], got[2 * k + 1]) != (ent[2 * k], ent[2 * k + 1]):
+            lost.append(k)
+    assert over and lost == over
