@@ -46,6 +46,7 @@ LOG2_ENTRIES = 24
 BATCH = 128
 LAUNCHES_PER_STEP = 16  # one step answers LAUNCHES_PER_STEP * BATCH queries
 POOL_BATCHES = 32       # distinct staged batches, cycled
+QUERY_POOL = 256        # distinct real seeded queries (oracle client)
 STREAMS = 2             # CUDA streams the timed launches alternate over
 REFERENCE_BUDGET_S = 150.0
 SERVE_RATE_FRACS = (0.25, 0.5, 0.75, 0.9)  # open-loop offered rates, fractions of the saturated e2e rate
@@ -319,7 +320,7 @@ def main():
     ctx = O.Ctx()
     omode = O.MODE_CRT_FIXED if args.mode == "crt_fixed" else O.MODE_COMPAT
     pack = O.Pack(ctx, GAMMA, W_SEED, mode=omode)
-    pool = make_query_pool(ctx, pack, 32, 3 + rank)
+    pool = make_query_pool(ctx, pack, QUERY_POOL, 3 + rank)
     client, locals_, seeds, brows, y_body = pool
     cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
 
@@ -550,6 +551,8 @@ def main():
                                    f"({nshards} shards), B={B} seeded queries per launch, uniform shard ids",
                        "step": f"{L} launches x {B} queries over {len(side)} streams",
                        "streams": len(side),
+                       "queries": f"{QUERY_POOL} distinct real seeded queries (oracle client), each launch slot "
+                                  "drawn from them with its own uniform shard id",
                        "mode": args.mode, "global_batch": B * ws, "ring_dim": N,
                        "crt_moduli": [268369921, 249561089], "p": 65536,
                        "l2": "flushed between timed steps (256 MiB write); resident DB 6.5 GiB > L2",
@@ -619,11 +622,9 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
     and the mixed served workload over 8 databases of 2^18..2^26 entries."""
     from inspire import serving as sv
 
-    # the 32 real queries tiled to 256 pinned rows, so that one submit call
-    # can carry up to 256 queries (each still names its own shard)
-    reps = 256 // len(locals_)
-    pool = sv.QueryPool(np.tile(seeds, (reps, 1, 1)), np.tile(brows, (reps, 1, 1)), np.tile(locals_, reps),
-                        pinned=True)
+    # the distinct real queries in pinned rows; one submit call carries up to
+    # 256 of them (each names its own shard)
+    pool = sv.QueryPool(seeds, brows, locals_, pinned=True)
     main = [sv.Target(edb, nshards, 1.0)]
     tuned = sv.autotune(lambda **kw: inspire.Server(crs, capacity=8192, **kw), main, pool, cid)
     cfg = tuned["best"]
