@@ -626,7 +626,11 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
     # 256 of them (each names its own shard)
     pool = sv.QueryPool(seeds, brows, locals_, pinned=True)
     main = [sv.Target(edb, nshards, 1.0)]
-    tuned = sv.autotune(lambda **kw: inspire.Server(crs, capacity=8192, **kw), main, pool, cid)
+    ws, _, _ = dist_env()
+    if ws == 1:
+        tuned = sv.autotune(lambda **kw: inspire.Server(crs, capacity=8192, **kw), main, pool, cid)
+    else:  # ranks share the node's host cores: one default configuration, no search
+        tuned = {"best": {"max_batch": 256, "max_inflight": 4, "batch_wait_us": 100}, "table": []}
     cfg = tuned["best"]
     srv = inspire.Server(crs, capacity=8192, **cfg)
 
@@ -690,7 +694,7 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
                         "achieved_qps": head["achieved_qps"], "load_frac": head["load_frac"]}}
     srv.close()
 
-    if not args.no_mixed:
+    if not args.no_mixed and ws == 1:
         rng = np.random.default_rng(21)
         dbs, raws, targets = [], [], []
         t0 = time.perf_counter()
