@@ -46,7 +46,8 @@ LOG2_ENTRIES = 24
 BATCH = 128
 LAUNCHES_PER_STEP = 16  # one step answers LAUNCHES_PER_STEP * BATCH queries
 POOL_BATCHES = 32       # distinct staged batches, cycled
-QUERY_POOL = 256        # distinct real seeded queries (oracle client)
+QUERY_POOL = 256        # distinct real seeded queries (oracle clients)
+N_CLIENTS = 32          # registered clients (own keys), QUERY_POOL / N_CLIENTS queries each
 STREAMS = 2             # CUDA streams the timed launches alternate over
 REFERENCE_BUDGET_S = 150.0
 SERVE_RATE_FRACS = (0.25, 0.5, 0.75, 0.9)  # open-loop offered rates, fractions of the saturated e2e rate
@@ -141,6 +142,19 @@ def make_query_pool(ctx, pack, n_queries, seed):
         seeds[k], brows[k] = client.query_seeded(int(li))
     y_body, _ = client.packing_keys(pack)
     return client, locals_, seeds, brows, y_body
+
+
+def make_client_pools(ctx, pack, n_clients, per_client, seed):
+    """n_clients oracle clients (own secret key, own packing keys), each with
+    per_client real seeded queries; query k belongs to client k // per_client."""
+    pools = [make_query_pool(ctx, pack, per_client, seed + 17 * c) for c in range(n_clients)]
+    clients = [p[0] for p in pools]
+    locals_ = np.concatenate([p[1] for p in pools])
+    seeds = np.concatenate([p[2] for p in pools])
+    brows = np.concatenate([p[3] for p in pools])
+    y_bodies = [p[4] for p in pools]
+    client_of = np.repeat(np.arange(n_clients), per_client)
+    return clients, client_of, locals_, seeds, brows, y_bodies
 
 
 def cpu_baseline(ctx, pack, db_raw, pool, budget_s=12.0, max_queries=200):
@@ -320,9 +334,14 @@ def main():
     ctx = O.Ctx()
     omode = O.MODE_CRT_FIXED if args.mode == "crt_fixed" else O.MODE_COMPAT
     pack = O.Pack(ctx, GAMMA, W_SEED, mode=omode)
-    pool = make_query_pool(ctx, pack, QUERY_POOL, 3 + rank)
-    client, locals_, seeds, brows, y_body = pool
-    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    clients, client_of, locals_, seeds, brows, y_bodies = make_client_pools(
+        ctx, pack, N_CLIENTS, QUERY_POOL // N_CLIENTS, 3 + 101 * rank)
+    client, y_body = clients[0], y_bodies[0]
+    cids = np.array([crs.register_client(inspire.ClientPackingKeys(y_body=yb)) for yb in y_bodies], np.int32)
+    qcid = cids[client_of]  # registered client id of each pool query
+    cid = int(cids[0])
+    c0 = client_of == 0  # client 0's queries (paths that take one client)
+    pool = (client, locals_[c0], seeds[c0], brows[c0], y_body)
 
     L = args.launches_per_step
     nb = POOL_BATCHES
@@ -334,7 +353,7 @@ def main():
     d_seeds = torch.from_numpy(np.ascontiguousarray(seeds[pool_idx][:, :, 3:6, :])).to(dev)
     d_brows = torch.from_numpy(np.ascontiguousarray(brows[pool_idx][:, :, 3:6, :]).view(np.int64)).to(dev)
     d_shard = torch.from_numpy(shard_ids.view(np.int32)).to(dev)
-    d_client = torch.full((nb, B), cid, dtype=torch.int32, device=dev)
+    d_client = torch.from_numpy(np.ascontiguousarray(qcid[pool_idx])).to(dev)
     d_out = torch.zeros((nb, B, 2, 2 * N), dtype=torch.int64, device=dev)
     d_status = torch.zeros((nb, B), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
@@ -421,11 +440,22 @@ def main():
     # oracle's extraction on samples) must equal its database entry
     status = d_status.cpu().numpy()
     assert not status.any(), "respond kernel reported a nonzero status"
-    d_sk = torch.from_numpy(np.ascontiguousarray(client.sk).view(np.int64)).to(dev)
-    d_ent = torch.zeros((nb * B, ENTRY), dtype=torch.uint8, device=dev)
-    inspire.pir.extract_inspiring_device(crs, d_sk.data_ptr(), d_out.data_ptr(), nb * B, ENTRY, d_ent.data_ptr(), sp)
-    torch.cuda.synchronize()
-    got_all = d_ent.cpu().numpy().reshape(nb, B, ENTRY)
+    # each client's responses decrypted with that client's key
+    owner = client_of[pool_idx].reshape(-1)
+    flat_out = d_out.view(nb * B, 2, 2 * N)
+    got_flat = np.zeros((nb * B, ENTRY), np.uint8)
+    for ci, cl in enumerate(clients):
+        sel = np.nonzero(owner == ci)[0]
+        if sel.size == 0:
+            continue
+        d_sel = flat_out[torch.from_numpy(sel).to(dev)].contiguous()
+        d_sk = torch.from_numpy(np.ascontiguousarray(cl.sk).view(np.int64)).to(dev)
+        d_ent = torch.zeros((sel.size, ENTRY), dtype=torch.uint8, device=dev)
+        inspire.pir.extract_inspiring_device(crs, d_sk.data_ptr(), d_sel.data_ptr(), sel.size, ENTRY,
+                                             d_ent.data_ptr(), sp)
+        torch.cuda.synchronize()
+        got_flat[sel] = d_ent.cpu().numpy()
+    got_all = got_flat.reshape(nb, B, ENTRY)
     gi_all = shard_ids.astype(np.int64) * N + locals_[pool_idx].astype(np.int64)
     verified = 0
     if args.mode == "crt_fixed":
@@ -435,7 +465,8 @@ def main():
     s = (args.steps * L - 1) % nb
     outs = d_out[s].cpu().numpy().view(np.uint64)
     for j in range(0, B, max(1, B // 8)):
-        assert np.array_equal(got_all[s, j], client.extract_inspiring(outs[j], ENTRY)), "device extraction differs"
+        owner_cl = clients[client_of[pool_idx[s, j]]]
+        assert np.array_equal(got_all[s, j], owner_cl.extract_inspiring(outs[j], ENTRY)), "device extraction differs"
 
     # batch-size sweep (single query = the plain GPU path)
     sweep = {}
@@ -482,7 +513,7 @@ def main():
         hs[:] = seeds[pool_idx[s]]
         hb[:] = brows[pool_idx[s]]
         t0 = time.perf_counter()
-        _respond_into(crs, edb, shard_ids[s], hs, hb, np.full(B, cid, np.int32), ho)
+        _respond_into(crs, edb, shard_ids[s], hs, hb, qcid[pool_idx[s]], ho)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             e2e_times.append(dt)
@@ -503,21 +534,21 @@ def main():
         hs1[:] = seeds[pool_idx[s, :1]]
         hb1[:] = brows[pool_idx[s, :1]]
         t0 = time.perf_counter()
-        _respond_into(crs, edb, shard_ids[s, :1], hs1, hb1, np.full(1, cid, np.int32), ho1)
+        _respond_into(crs, edb, shard_ids[s, :1], hs1, hb1, qcid[pool_idx[s, :1]], ho1)
         single_lat.append(time.perf_counter() - t0)
     single_lat = np.array(single_lat[10:]) * 1e3
     plain = {"qps": float(1e3 / single_lat.mean()), "p50_ms": float(np.percentile(single_lat, 50)),
              "p99_ms": float(np.percentile(single_lat, 99)),
              "path": "inspire_respond_seeded_batch with n=1 from host buffers, one call at a time"}
 
-    c3 = c3_bench(inspire, crs, client, pack, seeds, brows, y_body) if rank == 0 else None
+    c3 = c3_bench(inspire, crs, client, pack, seeds[c0], brows[c0], y_body) if rank == 0 else None
 
     serving = None
     e2e_value = sync_call_qps
     e2e_kind = "synchronous host-buffer batch call (inspire_respond_seeded_batch), B queries per call"
     if not args.no_serve:
-        serving = serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, db_raw, B, args,
-                              torch, dev)
+        serving = serve_bench(inspire, crs, edb, nshards, clients, client_of, qcid, locals_, seeds, brows, db_raw, B,
+                              args, torch, dev)
         closed = serving["closed_loop"]["achieved_qps"]
         if ws > 1:
             t = torch.tensor([closed], device=dev)
@@ -551,8 +582,9 @@ def main():
                                    f"({nshards} shards), B={B} seeded queries per launch, uniform shard ids",
                        "step": f"{L} launches x {B} queries over {len(side)} streams",
                        "streams": len(side),
-                       "queries": f"{QUERY_POOL} distinct real seeded queries (oracle client), each launch slot "
-                                  "drawn from them with its own uniform shard id",
+                       "queries": f"{QUERY_POOL} distinct real seeded queries from {N_CLIENTS} oracle clients "
+                                  "(each client's packing keys registered and resident); each launch slot draws one "
+                                  "with its own uniform shard id",
                        "mode": args.mode, "global_batch": B * ws, "ring_dim": N,
                        "crt_moduli": [268369921, 249561089], "p": 65536,
                        "l2": "flushed between timed steps (256 MiB write); resident DB 6.5 GiB > L2",
@@ -616,7 +648,8 @@ def c3_bench(inspire, crs, client, pack, seeds, brows, y_body, n=60):
             "p99_ms": float(np.percentile(lat, 99))}
 
 
-def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, db_raw, B, args, torch, dev):
+def serve_bench(inspire, crs, edb, nshards, clients, client_of, qcid, locals_, seeds, brows, db_raw, B, args, torch,
+                dev):
     """Serving-loop measurements: saturated closed loop (the e2e number),
     open-loop Poisson sweeps with p50/p99 latency on the 2^24-entry database,
     and the mixed served workload over 8 databases of 2^18..2^26 entries."""
@@ -624,7 +657,8 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
 
     # the distinct real queries in pinned rows; one submit call carries up to
     # 256 of them (each names its own shard)
-    pool = sv.QueryPool(seeds, brows, locals_, pinned=True)
+    pool = sv.QueryPool(seeds, brows, locals_, pinned=True, client_ids=qcid)
+    cid = int(qcid[0])  # unused when the pool names each query's client
     main = [sv.Target(edb, nshards, 1.0)]
     ws, _, _ = dist_env()
     if ws == 1:
@@ -637,7 +671,7 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
     def check(samples, raws, targets_nshards):
         for d, shard, pidx, out in samples[:16]:
             gi = shard * N + int(locals_[pidx])
-            got = client.extract_inspiring(out, ENTRY)
+            got = clients[client_of[pidx]].extract_inspiring(out, ENTRY)
             if args.mode == "crt_fixed":
                 assert np.array_equal(got, raws[d][gi * ENTRY:(gi + 1) * ENTRY]), "served response failed to decrypt"
 
@@ -660,13 +694,12 @@ def serve_bench(inspire, crs, edb, nshards, client, locals_, seeds, brows, cid, 
 
         rng = np.random.default_rng(3)
         sh = rng.integers(0, nshards, size=n).astype(np.uint32)
-        cids = np.full(pool.q, cid, np.int32)
         tickets = []
         t0 = now_ns()
         k = 0
         while k < n:
             m = min(pool.q, n - k)
-            t, rc = server.submit(edb, sh[k:k + m], pool.seeds[:m], pool.b_rows[:m], cids[:m], borrow=True)
+            t, rc = server.submit(edb, sh[k:k + m], pool.seeds[:m], pool.b_rows[:m], pool.client_ids[:m], borrow=True)
             tickets.append(t)
             k += len(t)
         done = server.poll_batch(np.concatenate(tickets))

@@ -41,8 +41,12 @@ class QueryPool:
     rows in page-locked memory and submissions borrow them (the GPU reads
     them in place; nothing is copied on the host)."""
 
-    def __init__(self, seeds: np.ndarray, b_rows: np.ndarray, locals_: Sequence[int], pinned: bool = False):
+    def __init__(self, seeds: np.ndarray, b_rows: np.ndarray, locals_: Sequence[int], pinned: bool = False,
+                 client_ids: Optional[Sequence[int]] = None):
         self.locals_ = np.asarray(locals_)
+        # registered client id of each query (its packing keys); None: the
+        # client_id given to run()
+        self.client_ids = None if client_ids is None else np.ascontiguousarray(client_ids, dtype=np.int32)
         self.borrow = pinned
         self._bufs = []
         if pinned:
@@ -140,8 +144,9 @@ class _Lane:
                 a, b = k + off, k + m
                 plo = lo + off
                 t_sub = now_ns()
+                cids = self.cids[:b - a] if self.pool.client_ids is None else self.pool.client_ids[plo:hi]
                 t, rc = self.server.submit(self.hdl[a:b], self.shards[a:b], self.pool.seeds[plo:hi],
-                                           self.pool.b_rows[plo:hi], self.cids[:b - a],
+                                           self.pool.b_rows[plo:hi], cids,
                                            self.arrivals[a:b] if self.arrivals is not None else None,
                                            borrow=self.pool.borrow)
                 if len(t):
