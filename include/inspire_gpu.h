@@ -189,6 +189,14 @@ int inspire_respond_seeded_batch(inspire_ctx *ctx, const inspire_db *db, uint32_
                                  const uint8_t *seeds, const uint64_t *b_rows, const int32_t *client_ids,
                                  uint64_t *out_ct);
 
+/* Batched respond_inspiring (full, unseeded queries, src/pir/respond.rs:284-386)
+ * over n queries with registered client keys, host buffers: shard_ids[n],
+ * rgsw[n][2*gadget_len][2][poly] (rows of (a, b)), client_ids[n],
+ * out_ct[n][2][poly].  Each result is the one respond_inspiring returns for
+ * that query alone. */
+int inspire_respond_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n, const uint32_t *shard_ids,
+                          const uint64_t *rgsw, const int32_t *client_ids, uint64_t *out_ct);
+
 /* Same on device buffers, asynchronous on `stream`.  seeds holds only rows
  * gadget_len..2*gadget_len-1 ([n][gadget_len][32]) and b_rows only those rows
  * ([n][gadget_len][poly]); d_status[n] receives 0 or a nonzero kernel status
@@ -328,6 +336,22 @@ int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, cons
  * receives [n][entry_size] bytes (entry_size <= 32). */
 int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, const uint64_t *d_ct, uint32_t n,
                                      uint32_t entry_size, uint8_t *d_entries, void *stream);
+
+/* Client side, for load generation at served rates: n seeded queries
+ * (query_seeded, src/pir/query.rs:43-85; SeededRgswCiphertext::encrypt,
+ * src/rgsw/types.rs:233-300) of the inverse monomials X^-k, k =
+ * d_local_idx[i] mod ring_dim, under the secret key d_sk [poly] (u64,
+ * residue-major).  Row seeds come from a ChaCha20 stream keyed by `key` (32
+ * bytes), indexed by query number first_query + i, and the errors are the
+ * crate's discrete Gaussian (sigma, tail cut ceil(6 sigma)) drawn by inverse
+ * table from the same stream; the crate's own randomness (thread_rng and a
+ * rejection sampler) is not reproduced.  Outputs in the crate's row order:
+ * d_seeds [n][2*gadget_len][32], d_b_rows [n][2*gadget_len][poly],
+ * d_status [n] (0, or 1 if a seed's expansion hit its bound).  Requires
+ * first_query + n <= 2^36. */
+int inspire_query_seeded_device(inspire_ctx *ctx, const uint64_t *d_sk, const uint8_t *key, uint64_t first_query,
+                                uint32_t n, const uint32_t *d_local_idx, uint8_t *d_seeds, uint64_t *d_b_rows,
+                                int32_t *d_status, void *stream);
 
 /* Rate probe with no crate counterpart: blocks x 256 threads x 8
  * independent chains x iters exact 28-bit modular multiplies (Shoup's

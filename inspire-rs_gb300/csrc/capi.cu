@@ -7,6 +7,7 @@
 // kernels in respond.cu.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -446,6 +447,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
   if (e == cudaSuccess) e = prepare_nopacking_kernels();
   if (e == cudaSuccess) e = prepare_ops_kernels();
   if (e == cudaSuccess) e = prepare_setup_kernels();
+  if (e == cudaSuccess) e = prepare_client_kernels();
   if (e != cudaSuccess) {
     delete c;
     return fail(INSPIRE_ERR_CUDA, std::string("kernel setup: ") + cudaGetErrorString(e));
@@ -677,6 +679,32 @@ int inspire_respond_seeded_batch(inspire_ctx* c, const inspire_db* db, uint32_t 
                    2 * ELL, client_ids, out_ct);
 }
 
+int inspire_respond_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,
+                          const uint64_t* rgsw, const int32_t* client_ids, uint64_t* out_ct) {
+  if (!c || !db || (n && (!shard_ids || !rgsw || !client_ids || !out_ct)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (int rc = set_device(c)) return rc;
+  for (uint32_t i = 0; i < n; i++) {
+    if (shard_ids[i] >= (uint32_t)db->nshards)
+      return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(shard_ids[i]) + " not found");
+    const int32_t id = client_ids[i];
+    if (id < 0 || (size_t)id >= c->clients.size() || !c->clients[id])
+      return fail(INSPIRE_ERR_KEYS_MISSING, "InspiRING client packing keys missing from query");
+  }
+  // rows ELL..2ELL-1 of each query, split into their a and b polys
+  const size_t pw = poly_words();
+  std::vector<uint64_t> ar((size_t)n * ELL * pw), br((size_t)n * ELL * pw);
+  for (uint32_t i = 0; i < n; i++)
+    for (int t = 0; t < ELL; t++) {
+      const uint64_t* row = rgsw + ((size_t)i * 2 * ELL + ELL + t) * 2 * pw;
+      memcpy(ar.data() + ((size_t)i * ELL + t) * pw, row, pw * sizeof(uint64_t));
+      memcpy(br.data() + ((size_t)i * ELL + t) * pw, row + pw, pw * sizeof(uint64_t));
+    }
+  return run_batch(c, db, n, shard_ids, nullptr, 0, ar.data(), br.data(), ELL, client_ids, out_ct);
+}
+
 int inspire_respond_seeded_batch_device(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* d_shard_ids,
                                         const uint8_t* d_seeds, const uint64_t* d_b_rows, const int32_t* d_client_ids,
                                         uint64_t* d_out_ct, int32_t* d_status, void* stream) {
@@ -726,6 +754,52 @@ int inspire_extract_inspiring_device(inspire_ctx* c, const uint64_t* d_sk, const
   if (entry_size == 0 || entry_size > 32) return fail(INSPIRE_ERR_UNSUPPORTED, "entry_size must be 1..32 on the GPU path");
   if (int rc = set_device(c)) return rc;
   CUDA_TRY(launch_extract(c->P, c->params.p, d_sk, d_ct, (int)n, (int)entry_size, d_entries, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_query_seeded_device(inspire_ctx* c, const uint64_t* d_sk, const uint8_t* key, uint64_t first_query,
+                                uint32_t n, const uint32_t* d_local_idx, uint8_t* d_seeds, uint64_t* d_b_rows,
+                                int32_t* d_status, void* stream) {
+  if (!c || !key || (n && (!d_sk || !d_local_idx || !d_seeds || !d_b_rows || !d_status)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!(c->params.sigma > 0.0)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "sigma must be positive");
+  // discrete Gaussian on [-T, T], T = ceil(6 sigma) (math/gaussian.rs:31-38, 88-104)
+  const int T = (int)std::ceil(c->params.sigma * 6.0);
+  if (T + 1 > MAX_CDT) return fail(INSPIRE_ERR_UNSUPPORTED, "sigma too large for the device error table");
+  // seed blocks Q * 16 + row stay below the error blocks' base 2^40
+  if (first_query > (1ull << 36) || first_query + n > (1ull << 36))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "first_query + n must be <= 2^36");
+  if (int rc = set_device(c)) return rc;
+  QueryGenArgs a{};
+  a.P = c->P;
+  a.first_query = first_query;
+  a.local_idx = d_local_idx;
+  a.sk = d_sk;
+  for (int i = 0; i < 8; i++)
+    a.key[i] = (uint32_t)key[4 * i] | ((uint32_t)key[4 * i + 1] << 8) | ((uint32_t)key[4 * i + 2] << 16) |
+               ((uint32_t)key[4 * i + 3] << 24);
+  for (int r = 0; r < 2; r++) {
+    const uint64_t q = c->params.crt_moduli[r];
+    uint64_t zp = 1;
+    for (int i = 0; i < ELL; i++) {
+      a.zpow[r][i] = (uint32_t)zp;
+      a.zpow_p[r][i] = shoup(zp, q);
+      zp = (uint64_t)((u128)zp * (c->params.gadget_base % q) % q);
+    }
+  }
+  const double s2 = 2.0 * c->params.sigma * c->params.sigma;
+  double total = 0.0;
+  for (int x = -T; x <= T; x++) total += std::exp(-(double)x * x / s2);
+  double cum = 0.0;
+  for (int j = 0; j < T; j++) {
+    cum += (j ? 2.0 : 1.0) * std::exp(-(double)j * j / s2) / total;
+    a.cdt[j] = (uint64_t)std::ldexp(std::fmin(cum, 1.0), 63);
+  }
+  a.cdt_len = T + 1;
+  a.seeds = d_seeds;
+  a.b_rows = d_b_rows;
+  a.status = d_status;
+  CUDA_TRY(launch_query_gen(a, (int)n, (cudaStream_t)stream));
   return INSPIRE_OK;
 }
 

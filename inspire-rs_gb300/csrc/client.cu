@@ -1,0 +1,141 @@
+// client.cu -- client-side seeded query generation on the device, for load
+// generation at served rates.
+//
+// query_seeded (src/pir/query.rs:43-85) builds SeededRgswCiphertext::encrypt
+// (src/rgsw/types.rs:233-300) of m = inverse_monomial(k) (X^-k,
+// src/pir/encode_db.rs:80-91) under the secret key s: for row i < ELL,
+// b = -a s + e + (m z^i) s; for row ELL + i, b = -a s + e + m z^i, where a is
+// Poly::from_seed_moduli of the row's 32-byte seed (the same expansion the
+// server runs) and z = 2^20.
+//
+// Randomness: the crate draws seeds from thread_rng and errors from a
+// rejection sampler over ChaCha20.  Here both come from ChaCha20 keyed by a
+// caller key: the seed of row r of query Q is block Q * 16 + r (first 8
+// words), and each error coefficient is a discrete Gaussian of the
+// parameters' sigma drawn by inverse cumulative table from one 64-bit word of
+// block 2^40 + (Q * 2 ELL + r) * 256 + j / 8.  The queries are valid (their
+// responses decrypt to the queried entries) but are not the crate's streams.
+#include "expand.cuh"
+#include "kernels.h"
+
+namespace ig {
+namespace {
+
+constexpr int CT = 256;  // threads per query: one expansion sub-block, two NTT groups
+
+__global__ void __launch_bounds__(CT) query_gen_kernel(const __grid_constant__ QueryGenArgs A) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint64_t* cand = reinterpret_cast<uint64_t*>(smem);        // [N] expansion candidates
+  uint32_t* a0 = smem + 2 * N;                               // [2][N] expanded a (residue 0, 1)
+  uint32_t* shat = a0 + 2 * N;                               // [2][N] NTT(s) * n^-1 2^32, slot layout
+  uint32_t* sco = shat + 2 * N;                              // [2][N] s, coefficients
+  int32_t* err = reinterpret_cast<int32_t*>(sco + 2 * N);    // [N] signed error
+  uint32_t* SC = reinterpret_cast<uint32_t*>(err + N);       // [2][NTT_SCRATCH]
+  uint64_t* cdt = reinterpret_cast<uint64_t*>(SC + 2 * NTT_SCRATCH);  // [MAX_CDT]
+  int* ws = reinterpret_cast<int*>(cdt + MAX_CDT);           // [20]
+  uint32_t* seed_w = reinterpret_cast<uint32_t*>(ws + 20);   // [8]
+  const DevParams& P = A.P;
+  const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const int qi = blockIdx.x;
+  const uint64_t Q = A.first_query + (uint64_t)qi;
+  const uint32_t k = A.local_idx[qi] & (N - 1);
+  const uint32_t q = P.r[g].q, qinv = P.r[g].qinv;
+  const int cdt_len = A.cdt_len;
+  if (tid < MAX_CDT) cdt[tid] = A.cdt[tid];
+  if (tid == 0) A.status[qi] = 0;
+
+  // s (both residues) and its transform, once per query
+  {
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const uint32_t sv = (uint32_t)A.sk[(size_t)g * N + x + 128 * j];
+      sco[g * N + x + 128 * j] = sv;
+      v[j] = sv;
+    }
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      shat[g * N + 16 * x + j] = mul_shoup(v[j], P.r[g].ninv_mont, P.r[g].ninv_mont_p, q);
+  }
+  uint32_t key[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) key[i] = A.key[i];
+
+  for (int row = 0; row < 2 * ELL; row++) {
+    __syncthreads();  // previous row's buffers are free
+    if (tid == 0) {
+      uint32_t w[16];
+      chacha20_block(key, Q * 16 + (uint64_t)row, P.one, w);
+#pragma unroll
+      for (int i = 0; i < 8; i++) seed_w[i] = w[i];
+    }
+    // error: thread tid draws coefficients 8 tid .. 8 tid + 7
+    {
+      uint32_t w[16];
+      chacha20_block(key, (1ull << 40) + (Q * 2 * ELL + (uint64_t)row) * (N / 8) + (uint64_t)tid, P.one, w);
+#pragma unroll
+      for (int e = 0; e < 8; e++) {
+        const uint64_t u = (uint64_t)w[2 * e] | ((uint64_t)w[2 * e + 1] << 32);
+        const uint64_t mag = u & 0x7fffffffffffffffull;
+        int j = 0;
+        while (j < cdt_len - 1 && mag >= cdt[j]) j++;
+        err[8 * tid + e] = (j != 0 && (u >> 63)) ? -j : j;
+      }
+    }
+    __syncthreads();
+    uint8_t* seed_out = A.seeds + ((size_t)qi * 2 * ELL + row) * 32;
+    if (tid < 32) seed_out[tid] = (uint8_t)(seed_w[tid >> 2] >> (8 * (tid & 3)));
+    // a = Poly::from_seed_moduli(seed) (poly.rs:251-281)
+    const bool ok = expand_seeded_row<2>(P, reinterpret_cast<const uint8_t*>(seed_w), cand, a0, a0 + N, ws, 3, tid);
+    if (!ok && tid == 0) A.status[qi] = ERR_EXPAND;
+    __syncthreads();
+    // a s by the NTT (n^-1 folded into s_hat), one residue per group
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = a0[g * N + x + 128 * j];
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = redc_lazy((uint64_t)v[j] * shat[g * N + 16 * x + j], q, qinv);  // [0, 2q)
+    ntt_inv_noscale(v, SC + g * NTT_SCRATCH, inv_tw(P.r[g]), q, x, 1 + g);
+    const int i = row < ELL ? row : row - ELL;
+    const uint32_t zp = A.zpow[g][i], zp_p = A.zpow_p[g][i];  // z^i mod q_g, Shoup companion
+    uint64_t* brow = A.b_rows + ((size_t)qi * 2 * ELL + row) * 2 * N + (size_t)g * N;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int c = x + 128 * j;
+      uint32_t b = canon2(v[j], q);  // a s
+      b = b ? q - b : 0;             // -a s
+      const int32_t e = err[c];
+      b = add_mod(b, e >= 0 ? (uint32_t)e : q - (uint32_t)(-e), q);
+      uint32_t msg;  // row < ELL: (m s)[c] = (X^-k s)[c]; else m[c]
+      if (row < ELL) {
+        const int src = c + (int)k;
+        msg = src < N ? sco[g * N + src] : (sco[g * N + src - N] ? q - sco[g * N + src - N] : 0);
+      } else {
+        msg = (k == 0) ? (c == 0 ? 1u : 0u) : (c == N - (int)k ? q - 1 : 0u);
+      }
+      b = add_mod(b, mul_shoup(msg, zp, zp_p, q), q);
+      brow[c] = b;
+    }
+  }
+}
+
+}  // namespace
+
+size_t query_gen_smem_bytes() {
+  return sizeof(uint32_t) * ((size_t)2 * N + 2 * N + 2 * N + 2 * N + N + 2 * NTT_SCRATCH + 2 * MAX_CDT + 20 + 8);
+}
+
+cudaError_t prepare_client_kernels() {
+  return cudaFuncSetAttribute(query_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)query_gen_smem_bytes());
+}
+
+cudaError_t launch_query_gen(const QueryGenArgs& a, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  query_gen_kernel<<<n, CT, query_gen_smem_bytes(), st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace ig

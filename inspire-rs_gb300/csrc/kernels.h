@@ -70,12 +70,33 @@ struct NoPackingArgs {
   int* status;
 };
 
+// Seeded query generation (client side): query first_query + i asks for
+// local index local_idx[i] under the secret key sk[2][N].
+constexpr int MAX_CDT = 64;  // |error| table entries (tail cut ceil(6 sigma) + 1)
+struct QueryGenArgs {
+  DevParams P;
+  uint64_t first_query;
+  const uint32_t* local_idx;  // [n]
+  const uint64_t* sk;         // [2][N] residues
+  uint32_t key[8];            // ChaCha20 key of the query stream
+  uint32_t zpow[2][ELL], zpow_p[2][ELL];  // z^i mod q_r and Shoup companions
+  uint64_t cdt[MAX_CDT];      // cdt[j] = 2^63 P(|e| <= j), j < cdt_len - 1
+  int cdt_len;
+  uint8_t* seeds;             // [n][2 ELL][32]
+  uint64_t* b_rows;           // [n][2 ELL][2][N]
+  int* status;                // [n]
+};
+
 // Set the kernels' dynamic shared-memory limits on the current device (once
 // per device, before any launch; launches then make no configuration call).
 cudaError_t prepare_respond_kernels();
 cudaError_t prepare_nopacking_kernels();
 cudaError_t prepare_ops_kernels();
 cudaError_t prepare_setup_kernels();
+cudaError_t prepare_client_kernels();
+
+size_t query_gen_smem_bytes();
+cudaError_t launch_query_gen(const QueryGenArgs& a, int n, cudaStream_t st);
 
 size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);

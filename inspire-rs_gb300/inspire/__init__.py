@@ -19,7 +19,9 @@ from .pir import (  # noqa: F401
     now_ns,
     ntt_forward_device,
     ntt_inverse_device,
+    query_seeded_device,
     respond,
+    respond_batch,
     respond_inspiring,
     respond_seeded,
     respond_seeded_batch,

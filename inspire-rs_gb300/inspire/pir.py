@@ -361,6 +361,20 @@ def respond_seeded_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids:
     return out
 
 
+def respond_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int], rgsw: np.ndarray,
+                  client_ids: Sequence[int]) -> np.ndarray:
+    """Batched respond_inspiring (full queries, respond.rs:284-386) with
+    registered client keys: rgsw (n, 2*ell, 2, plen); returns (n, 2, plen)."""
+    n = len(shard_ids)
+    plen = crs.params.plen
+    sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+    cid = np.ascontiguousarray(client_ids, dtype=np.int32)
+    rg = _u64(rgsw)
+    out = np.zeros((n, 2, plen), dtype=np.uint64)
+    _check(crs.L.inspire_respond_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(rg), _ptr(cid), _ptr(out)))
+    return out
+
+
 def respond_seeded_batch_device(crs: ServerCrs, encoded_db: EncodedDatabase, n: int, d_shard_ids: int, d_seeds: int,
                                 d_b_rows: int, d_client_ids: int, d_out: int, d_status: int, stream: int) -> None:
     """Device-buffer batch (raw device pointers as ints); asynchronous."""
@@ -385,6 +399,20 @@ def extract_inspiring_device(crs: ServerCrs, d_sk: int, d_ct: int, n: int, entry
     device (raw device pointers as ints); asynchronous."""
     v = C.c_void_p
     _check(crs.L.inspire_extract_inspiring_device(crs.h, v(d_sk), v(d_ct), n, entry_size, v(d_entries), v(stream)))
+
+
+def query_seeded_device(crs: ServerCrs, d_sk: int, key: bytes, first_query: int, n: int, d_local_idx: int,
+                        d_seeds: int, d_b_rows: int, d_status: int, stream: int) -> None:
+    """n seeded queries (query_seeded, query.rs:43-85) of the local indices
+    at d_local_idx under the secret key d_sk, generated on the device from a
+    ChaCha20 stream keyed by `key` (raw device pointers as ints); outputs
+    seeds [n][6][32], b_rows [n][6][2*ring_dim] (u64) and status [n] (i32);
+    asynchronous."""
+    if len(key) != 32:
+        raise ValueError("key must be 32 bytes")
+    v = C.c_void_p
+    _check(crs.L.inspire_query_seeded_device(crs.h, v(d_sk), bytes(key), first_query, n, v(d_local_idx), v(d_seeds),
+                                             v(d_b_rows), v(d_status), v(stream)))
 
 
 def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, stream: int) -> int:

@@ -1,0 +1,175 @@
+"""GPU seeded query generation (query_seeded, src/pir/query.rs:43-85, as
+SeededRgswCiphertext::encrypt, src/rgsw/types.rs:233-300) through the C ABI:
+bit-exact against a CPU restatement of the generator's stream built from the
+oracle's ChaCha20, Poly::from_seed_moduli and negacyclic product; errors
+within the crate's tail cut with the crate's sigma; and generated queries
+answered by the Respond path decrypt to the queried entries."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 2048
+ELL = 3
+ENTRY = 32
+SIGMA = 6.4
+W_SEED = bytes(range(3, 35))
+KEY = bytes(range(100, 132))
+Q = (268369921, 249561089)
+
+
+@pytest.fixture(scope="module")
+def gen(oracle_mod):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import inspire
+
+    O = oracle_mod
+    ctx = O.Ctx()
+    client = O.Client(ctx, seed=3, rng_seed=9)
+    crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
+    return dict(O=O, ctx=ctx, client=client, crs=crs, inspire=inspire, torch=torch)
+
+
+def device_queries(G, first_query, local_idx):
+    torch, inspire = G["torch"], G["inspire"]
+    n = len(local_idx)
+    dev = torch.device("cuda:0")
+    sk = torch.from_numpy(G["client"].sk.view(np.int64).copy()).to(dev)
+    idx = torch.tensor(np.asarray(local_idx, np.uint32).view(np.int32), device=dev)
+    seeds = torch.zeros((n, 2 * ELL, 32), dtype=torch.uint8, device=dev)
+    b_rows = torch.zeros((n, 2 * ELL, 2 * N), dtype=torch.int64, device=dev)
+    status = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    inspire.query_seeded_device(G["crs"], sk.data_ptr(), KEY, first_query, n, idx.data_ptr(), seeds.data_ptr(),
+                                b_rows.data_ptr(), status.data_ptr(), stream)
+    torch.cuda.synchronize()
+    return seeds.cpu().numpy(), b_rows.cpu().numpy().view(np.uint64), status.cpu().numpy()
+
+
+def cdt_table(sigma):
+    """Cumulative |e| table of the discrete Gaussian on [-T, T], T = ceil(6 sigma)
+    (math/gaussian.rs:31-38, 88-104): cdt[j] = floor(2^63 P(|e| <= j)), j < T."""
+    T = math.ceil(sigma * 6.0)
+    s2 = 2.0 * sigma * sigma
+    total = sum(math.exp(-x * x / s2) for x in range(-T, T + 1))
+    cum, out = 0.0, []
+    for j in range(T):
+        cum += (2.0 if j else 1.0) * math.exp(-j * j / s2) / total
+        out.append(int(math.ldexp(min(cum, 1.0), 63)))
+    return np.array(out, dtype=np.uint64), T
+
+
+def expected_query(G, first_query, qi, k):
+    """The device generator's output for query number first_query + qi."""
+    O, ctx, sk = G["O"], G["ctx"], G["client"].sk
+    key = np.frombuffer(KEY, dtype="<u4")
+    cdt, T = cdt_table(SIGMA)
+    Qn = first_query + qi
+    m = ctx.inverse_monomial(k)
+    ms = ctx.poly_mul(m, sk)
+    seeds = np.zeros((2 * ELL, 32), np.uint8)
+    b_rows = np.zeros((2 * ELL, 2 * N), np.uint64)
+    errs = np.zeros((2 * ELL, N), np.int64)
+    for row in range(2 * ELL):
+        c = Qn * 16 + row
+        w = O.chacha20_block(key, [c & 0xFFFFFFFF, c >> 32, 0, 0])
+        seeds[row] = np.frombuffer(w[:8].astype("<u4").tobytes(), np.uint8)
+        words = []
+        for t in range(N // 8):
+            c = (1 << 40) + (Qn * 2 * ELL + row) * (N // 8) + t
+            words.append(O.chacha20_block(key, [c & 0xFFFFFFFF, c >> 32, 0, 0]))
+        w64 = np.concatenate(words).astype(np.uint64)
+        u = w64[0::2] | (w64[1::2] << np.uint64(32))
+        mag = u & np.uint64((1 << 63) - 1)
+        j = np.minimum(np.searchsorted(cdt, mag, side="right"), T).astype(np.int64)
+        neg = (u >> np.uint64(63)).astype(bool) & (j != 0)
+        e = np.where(neg, -j, j)
+        errs[row] = e
+        a = ctx.poly_from_seed(seeds[row].tobytes())
+        a_s = ctx.poly_mul(a, sk)
+        i = row % ELL
+        msg = ms if row < ELL else m
+        for r in range(2):
+            q = Q[r]
+            z = pow(1 << 20, i, q)
+            sl = slice(r * N, (r + 1) * N)
+            v = (q - a_s[sl].astype(np.int64)) % q
+            v = (v + e % q) % q
+            v = (v + (msg[sl].astype(np.int64) * z) % q) % q
+            b_rows[row, sl] = v.astype(np.uint64)
+    return seeds, b_rows, errs
+
+
+@pytest.mark.parametrize("first_query", [0, 12345])
+def test_query_gen_bit_exact(gen, first_query):
+    idxs = [0, 1, 2047, 777]
+    seeds, b_rows, status = device_queries(gen, first_query, idxs)
+    assert (status == 0).all()
+    for qi, k in enumerate(idxs):
+        want_s, want_b, _ = expected_query(gen, first_query, qi, k)
+        assert np.array_equal(seeds[qi], want_s), (qi, k)
+        assert np.array_equal(b_rows[qi], want_b), (qi, k)
+
+
+def test_query_gen_errors_follow_crate_distribution(gen):
+    """Each row decrypts to its message plus an error (b + a s - m_row), and
+    the errors lie within the tail cut with the crate's sigma."""
+    ctx, sk = gen["ctx"], gen["client"].sk
+    idxs = list(range(0, 2048, 256))
+    seeds, b_rows, status = device_queries(gen, 99, idxs)
+    assert (status == 0).all()
+    cdt, T = cdt_table(SIGMA)
+    errs = []
+    for qi, k in enumerate(idxs):
+        m = ctx.inverse_monomial(k)
+        ms = ctx.poly_mul(m, sk)
+        for row in range(2 * ELL):
+            a = ctx.poly_from_seed(seeds[qi, row].tobytes())
+            dec = (b_rows[qi, row] + ctx.poly_mul(a, sk)).astype(np.uint64)
+            msg = ms if row < ELL else m
+            for r in range(2):
+                q = np.uint64(Q[r])
+                z = np.uint64(pow(1 << 20, row % ELL, Q[r]))
+                sl = slice(r * N, (r + 1) * N)
+                e = (dec[sl] % q + q - (msg[sl] * z) % q) % q
+                e = np.where(e > q // np.uint64(2), e.astype(np.int64) - int(q), e.astype(np.int64))
+                errs.append(e)
+            assert np.array_equal(errs[-1], errs[-2])  # one error, both residues
+    e = np.concatenate(errs[0::2])
+    assert np.abs(e).max() <= T
+    var = float(np.mean(e.astype(np.float64) ** 2))
+    assert abs(var / (SIGMA * SIGMA) - 1.0) < 0.05, var
+    assert abs(float(e.mean())) < 0.2
+
+
+def test_generated_queries_retrieve_entries(gen):
+    """Queries generated on the device, answered by the batched seeded Respond,
+    decrypt to the queried entries (tests/e2e_pir.rs:464-535)."""
+    inspire, O, ctx, client = gen["inspire"], gen["O"], gen["ctx"], gen["client"]
+    rng = np.random.default_rng(77)
+    n_entries = 2 * N
+    db = rng.integers(0, 256, size=n_entries * ENTRY, dtype=np.uint8)
+    crs = gen["crs"]
+    edb = inspire.EncodedDatabase(crs, db, ENTRY)
+    pack = O.Pack(ctx, 16, W_SEED, mode=O.MODE_CRT_FIXED)
+    y_body, _ = client.packing_keys(pack)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    targets = [5, 2047, 2048, 4000, 1234, 3071]
+    seeds, b_rows, status = device_queries(gen, 1 << 20, [t % N for t in targets])
+    assert (status == 0).all()
+    out = inspire.respond_seeded_batch(crs, edb, [t // N for t in targets], seeds, b_rows, [cid] * len(targets))
+    for k, t in enumerate(targets):
+        got = client.extract_inspiring(out[k], ENTRY)
+        assert np.array_equal(got, db[t * ENTRY:(t + 1) * ENTRY]), t
+
+
+def test_query_gen_rejects(gen):
+    inspire = gen["inspire"]
+    with pytest.raises(inspire.PirError, match="2\\^36"):
+        inspire.query_seeded_device(gen["crs"], 1, KEY, (1 << 36) - 1, 2, 1, 1, 1, 1, 0)
+    with pytest.raises(ValueError):
+        inspire.query_seeded_device(gen["crs"], 1, KEY[:16], 0, 1, 1, 1, 1, 1, 0)

@@ -279,3 +279,20 @@ def test_batch_device_call_in_cuda_graph(world):
     assert not d_st.cpu().numpy().any()
     assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
     crs.release_client(cid)
+
+
+def test_unseeded_batch_equals_single(world):
+    """Batched full-query respond_inspiring: each result equals the
+    single-query call and the oracle."""
+    W = world
+    inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
+    crs, edb, pack, omode = W["w"]["crt_fixed"]
+    y_body, _ = client.packing_keys(pack)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    idxs = [3, 2050, 4101]
+    rg = np.stack([ctx.expand_rgsw(*client.query_seeded(ix % N)).reshape(6, 2, 2 * N) for ix in idxs])
+    out = inspire.respond_batch(crs, edb, [ix // N for ix in idxs], rg, [cid] * len(idxs))
+    for k, ix in enumerate(idxs):
+        want = oracle_response(W, "crt_fixed", ix // N, rg[k].reshape(12, 2 * N), y_body=y_body)
+        assert np.array_equal(out[k], want)
+    crs.release_client(cid)
