@@ -337,6 +337,20 @@ int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, cons
 int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, const uint64_t *d_ct, uint32_t n,
                                      uint32_t entry_size, uint8_t *d_entries, void *stream);
 
+/* Client side, for load generation at served rates: keys of n clients,
+ * numbered first_client + i.  d_sk receives each RlweSecretKey::generate
+ * (src/rlwe/enc.rs:14-17) [n][poly] and d_y_body each ClientPackingKeys
+ * body (generate_ksk_body, src/inspiring/inspiring2.rs:846-902: tau_g(s) z^k
+ * - s w_mask[k] + e_k, g = gen_pows[1], w_mask of the loaded CRS's w_seed)
+ * [n][gadget_len][poly] (u64, residue-major); register the bodies with
+ * inspire_client_register.  Secret-key and error coefficients are the crate's
+ * discrete Gaussian drawn by inverse table from a ChaCha20 stream keyed by
+ * `key` (32 bytes), disjoint from the query streams of the same key; the
+ * crate's own randomness is not reproduced.  Requires a loaded CRS and
+ * first_client + n <= 2^30. */
+int inspire_client_keygen_device(inspire_ctx *ctx, const uint8_t *key, uint64_t first_client, uint32_t n,
+                                 uint64_t *d_sk, uint64_t *d_y_body, void *stream);
+
 /* Client side, for load generation at served rates: n seeded queries
  * (query_seeded, src/pir/query.rs:43-85; SeededRgswCiphertext::encrypt,
  * src/rgsw/types.rs:233-300) of the inverse monomials X^-k, k =

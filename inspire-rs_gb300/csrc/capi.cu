@@ -488,11 +488,10 @@ int inspire_crs_load(inspire_ctx* c, const uint8_t w_seed[32], uint32_t num_colu
       wm[((size_t)k * 2 + 0) * N + i] = (uint32_t)(v % c->params.crt_moduli[0]);
       wm[((size_t)k * 2 + 1) * N + i] = (uint32_t)(v % c->params.crt_moduli[1]);
     }
-  DevMem dwm;
-  CUDA_TRY(dwm.ensure(wm.size() * sizeof(uint32_t)));
-  CUDA_TRY(cudaMemcpy(dwm.p, wm.data(), wm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(c->wmask.ensure(wm.size() * sizeof(uint32_t)));
+  CUDA_TRY(cudaMemcpy(c->wmask.p, wm.data(), wm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
   CUDA_TRY(c->what.ensure(sizeof(uint32_t) * (size_t)std::max(1, (gamma - 1) * ELL) * 2 * N));
-  CUDA_TRY(launch_crs_what(c->P, dwm.as<uint32_t>(), c->what.as<uint32_t>(), c->stream));
+  CUDA_TRY(launch_crs_what(c->P, c->wmask.as<uint32_t>(), c->what.as<uint32_t>(), c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   // key tables of registered clients were built for the previous gamma
   for (size_t i = 0; i < c->clients.size(); i++) release_keys(c, (int32_t)i);
@@ -757,24 +756,20 @@ int inspire_extract_inspiring_device(inspire_ctx* c, const uint64_t* d_sk, const
   return INSPIRE_OK;
 }
 
-int inspire_query_seeded_device(inspire_ctx* c, const uint64_t* d_sk, const uint8_t* key, uint64_t first_query,
-                                uint32_t n, const uint32_t* d_local_idx, uint8_t* d_seeds, uint64_t* d_b_rows,
-                                int32_t* d_status, void* stream) {
-  if (!c || !key || (n && (!d_sk || !d_local_idx || !d_seeds || !d_b_rows || !d_status)))
-    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+}  // extern "C"
+
+namespace {
+
+// Client-side randomness tables: the discrete Gaussian on [-T, T],
+// T = ceil(6 sigma) (math/gaussian.rs:31-38, 88-104), as cdt[j] =
+// floor(2^63 P(|e| <= j)) for j < T, and the gadget powers z^i mod q_r
+// (rgsw/types.rs:67-90, Poly::scalar_mul poly.rs:466-486).
+template <class Args>
+int client_tables(const inspire_ctx* c, const uint8_t* key, Args& a) {
   if (!(c->params.sigma > 0.0)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "sigma must be positive");
-  // discrete Gaussian on [-T, T], T = ceil(6 sigma) (math/gaussian.rs:31-38, 88-104)
   const int T = (int)std::ceil(c->params.sigma * 6.0);
   if (T + 1 > MAX_CDT) return fail(INSPIRE_ERR_UNSUPPORTED, "sigma too large for the device error table");
-  // seed blocks Q * 16 + row stay below the error blocks' base 2^40
-  if (first_query > (1ull << 36) || first_query + n > (1ull << 36))
-    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "first_query + n must be <= 2^36");
-  if (int rc = set_device(c)) return rc;
-  QueryGenArgs a{};
   a.P = c->P;
-  a.first_query = first_query;
-  a.local_idx = d_local_idx;
-  a.sk = d_sk;
   for (int i = 0; i < 8; i++)
     a.key[i] = (uint32_t)key[4 * i] | ((uint32_t)key[4 * i + 1] << 8) | ((uint32_t)key[4 * i + 2] << 16) |
                ((uint32_t)key[4 * i + 3] << 24);
@@ -796,10 +791,49 @@ int inspire_query_seeded_device(inspire_ctx* c, const uint64_t* d_sk, const uint
     a.cdt[j] = (uint64_t)std::ldexp(std::fmin(cum, 1.0), 63);
   }
   a.cdt_len = T + 1;
+  return INSPIRE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int inspire_query_seeded_device(inspire_ctx* c, const uint64_t* d_sk, const uint8_t* key, uint64_t first_query,
+                                uint32_t n, const uint32_t* d_local_idx, uint8_t* d_seeds, uint64_t* d_b_rows,
+                                int32_t* d_status, void* stream) {
+  if (!c || !key || (n && (!d_sk || !d_local_idx || !d_seeds || !d_b_rows || !d_status)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  // seed blocks Q * 16 + row stay below the error blocks' base 2^40
+  if (first_query > (1ull << 36) || first_query + n > (1ull << 36))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "first_query + n must be <= 2^36");
+  QueryGenArgs a{};
+  if (int rc = client_tables(c, key, a)) return rc;
+  if (int rc = set_device(c)) return rc;
+  a.first_query = first_query;
+  a.local_idx = d_local_idx;
+  a.sk = d_sk;
   a.seeds = d_seeds;
   a.b_rows = d_b_rows;
   a.status = d_status;
   CUDA_TRY(launch_query_gen(a, (int)n, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_client_keygen_device(inspire_ctx* c, const uint8_t* key, uint64_t first_client, uint32_t n,
+                                 uint64_t* d_sk, uint64_t* d_y_body, void* stream) {
+  if (!c || !key || (n && (!d_sk || !d_y_body))) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (first_client > (1ull << 30) || first_client + n > (1ull << 30))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "first_client + n must be <= 2^30");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  KeyGenArgs a{};
+  if (int rc = client_tables(c, key, a)) return rc;
+  if (int rc = set_device(c)) return rc;
+  a.first_client = first_client;
+  a.wmask = c->wmask.as<uint32_t>();
+  a.sk = d_sk;
+  a.y_body = d_y_body;
+  CUDA_TRY(launch_client_keys(a, (int)n, (cudaStream_t)stream));
   return INSPIRE_OK;
 }
 

@@ -8,13 +8,22 @@
 // Poly::from_seed_moduli of the row's 32-byte seed (the same expansion the
 // server runs) and z = 2^20.
 //
+// client_keys_kernel: RlweSecretKey::generate (src/rlwe/enc.rs:14-17) and
+// ClientPackingKeys::generate's y_body (src/inspiring/inspiring2.rs:640-660,
+// generate_ksk_body :846-902): y_body[k] = tau_g(s) z^k - s w_mask[k] + e_k
+// with g = gen_pows[1] and w_mask the CRS mask of w_seed.
+//
 // Randomness: the crate draws seeds from thread_rng and errors from a
 // rejection sampler over ChaCha20.  Here both come from ChaCha20 keyed by a
-// caller key: the seed of row r of query Q is block Q * 16 + r (first 8
-// words), and each error coefficient is a discrete Gaussian of the
-// parameters' sigma drawn by inverse cumulative table from one 64-bit word of
-// block 2^40 + (Q * 2 ELL + r) * 256 + j / 8.  The queries are valid (their
-// responses decrypt to the queried entries) but are not the crate's streams.
+// caller key, each error coefficient a discrete Gaussian of the parameters'
+// sigma drawn by inverse cumulative table from one 64-bit word (8 per block).
+// Block layout of one key's stream:
+//   query Q, row r: seed = first 8 words of block Q * 16 + r; errors from
+//     blocks 2^40 + (Q * 2 ELL + r) * 256 + j / 8          (Q < 2^36)
+//   client C: secret key from blocks 2^48 + C * 1024 + j / 8; y_body[k]
+//     errors from blocks 2^48 + C * 1024 + 256 (k + 1) + j / 8  (C < 2^30)
+// The outputs are valid keys and queries (responses decrypt to the queried
+// entries) but are not the crate's random draws.
 #include "expand.cuh"
 #include "kernels.h"
 
@@ -22,6 +31,26 @@ namespace ig {
 namespace {
 
 constexpr int CT = 256;  // threads per query: one expansion sub-block, two NTT groups
+
+// Thread t (of 256) fills err[8t .. 8t+7] with discrete Gaussian samples from
+// keystream block `blk + t`.
+__device__ __forceinline__ void gaussian8(const uint32_t key[8], uint64_t blk, uint32_t one, const uint64_t* cdt,
+                                          int cdt_len, int t, int32_t* err) {
+  uint32_t w[16];
+  chacha20_block(key, blk + (uint64_t)t, one, w);
+#pragma unroll
+  for (int e = 0; e < 8; e++) {
+    const uint64_t u = (uint64_t)w[2 * e] | ((uint64_t)w[2 * e + 1] << 32);
+    const uint64_t mag = u & 0x7fffffffffffffffull;
+    int j = 0;
+    while (j < cdt_len - 1 && mag >= cdt[j]) j++;
+    err[8 * t + e] = (j != 0 && (u >> 63)) ? -j : j;
+  }
+}
+
+__device__ __forceinline__ uint32_t signed_mod(int32_t e, uint32_t q) {
+  return e >= 0 ? (uint32_t)e : q - (uint32_t)(-e);
+}
 
 __global__ void __launch_bounds__(CT) query_gen_kernel(const __grid_constant__ QueryGenArgs A) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -70,19 +99,7 @@ __global__ void __launch_bounds__(CT) query_gen_kernel(const __grid_constant__ Q
 #pragma unroll
       for (int i = 0; i < 8; i++) seed_w[i] = w[i];
     }
-    // error: thread tid draws coefficients 8 tid .. 8 tid + 7
-    {
-      uint32_t w[16];
-      chacha20_block(key, (1ull << 40) + (Q * 2 * ELL + (uint64_t)row) * (N / 8) + (uint64_t)tid, P.one, w);
-#pragma unroll
-      for (int e = 0; e < 8; e++) {
-        const uint64_t u = (uint64_t)w[2 * e] | ((uint64_t)w[2 * e + 1] << 32);
-        const uint64_t mag = u & 0x7fffffffffffffffull;
-        int j = 0;
-        while (j < cdt_len - 1 && mag >= cdt[j]) j++;
-        err[8 * tid + e] = (j != 0 && (u >> 63)) ? -j : j;
-      }
-    }
+    gaussian8(key, (1ull << 40) + (Q * 2 * ELL + (uint64_t)row) * (N / 8), P.one, cdt, cdt_len, tid, err);
     __syncthreads();
     uint8_t* seed_out = A.seeds + ((size_t)qi * 2 * ELL + row) * 32;
     if (tid < 32) seed_out[tid] = (uint8_t)(seed_w[tid >> 2] >> (8 * (tid & 3)));
@@ -106,8 +123,7 @@ __global__ void __launch_bounds__(CT) query_gen_kernel(const __grid_constant__ Q
       const int c = x + 128 * j;
       uint32_t b = canon2(v[j], q);  // a s
       b = b ? q - b : 0;             // -a s
-      const int32_t e = err[c];
-      b = add_mod(b, e >= 0 ? (uint32_t)e : q - (uint32_t)(-e), q);
+      b = add_mod(b, signed_mod(err[c], q), q);
       uint32_t msg;  // row < ELL: (m s)[c] = (X^-k s)[c]; else m[c]
       if (row < ELL) {
         const int src = c + (int)k;
@@ -121,15 +137,97 @@ __global__ void __launch_bounds__(CT) query_gen_kernel(const __grid_constant__ Q
   }
 }
 
+__global__ void __launch_bounds__(CT) client_keys_kernel(const __grid_constant__ KeyGenArgs A) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  int32_t* sk = reinterpret_cast<int32_t*>(smem);            // [N] signed secret key
+  int32_t* tau = sk + N;                                     // [N] tau_g(s), signed
+  uint32_t* shat = reinterpret_cast<uint32_t*>(tau + N);     // [2][N] NTT(s) * n^-1 2^32, slot layout
+  int32_t* err = reinterpret_cast<int32_t*>(shat + 2 * N);   // [N]
+  uint32_t* SC = reinterpret_cast<uint32_t*>(err + N);       // [2][NTT_SCRATCH]
+  uint64_t* cdt = reinterpret_cast<uint64_t*>(SC + 2 * NTT_SCRATCH);  // [MAX_CDT]
+  const DevParams& P = A.P;
+  const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const uint64_t C = A.first_client + blockIdx.x;
+  const uint32_t q = P.r[g].q, qinv = P.r[g].qinv;
+  const int cdt_len = A.cdt_len;
+  if (tid < MAX_CDT) cdt[tid] = A.cdt[tid];
+  uint32_t key[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) key[i] = A.key[i];
+  const uint64_t base = (1ull << 48) + C * 4 * (N / 8);
+  __syncthreads();
+  // s = Poly::sample_gaussian_moduli (math/poly.rs:208-232)
+  gaussian8(key, base, P.one, cdt, cdt_len, tid, sk);
+  __syncthreads();
+  uint64_t* sk_out = A.sk + (size_t)blockIdx.x * 2 * N + (size_t)g * N;
+  const uint32_t gen = gen_pow(P.gamma, 1);  // gen_pows[1] (inspiring2.rs:652-654)
+  for (int i = tid; i < N; i += CT) {
+    // apply_automorphism (rlwe/galois.rs:22-55): X^i -> X^(i g mod 2n), negated past n
+    const uint32_t j = ((uint32_t)i * gen) & (2 * N - 1);
+    if (j < (uint32_t)N) tau[j] = sk[i];
+    else tau[j - N] = -sk[i];
+  }
+  {
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      v[j] = signed_mod(sk[x + 128 * j], q);
+      sk_out[x + 128 * j] = v[j];
+    }
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      shat[g * N + 16 * x + j] = mul_shoup(v[j], P.r[g].ninv_mont, P.r[g].ninv_mont_p, q);
+  }
+  for (int k = 0; k < ELL; k++) {
+    __syncthreads();  // tau complete; previous k's errors consumed
+    gaussian8(key, base + (uint64_t)(k + 1) * (N / 8), P.one, cdt, cdt_len, tid, err);
+    // s w_mask[k] by the NTT (generate_ksk_body, inspiring2.rs:874-884)
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = A.wmask[((size_t)k * 2 + g) * N + x + 128 * j];
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = redc_lazy((uint64_t)v[j] * shat[g * N + 16 * x + j], q, qinv);
+    ntt_inv_noscale(v, SC + g * NTT_SCRATCH, inv_tw(P.r[g]), q, x, 1 + g);
+    __syncthreads();  // errors visible
+    const uint32_t zp = A.zpow[g][k], zp_p = A.zpow_p[g][k];
+    uint64_t* y = A.y_body + ((size_t)blockIdx.x * ELL + k) * 2 * N + (size_t)g * N;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int c = x + 128 * j;
+      const uint32_t sw = canon2(v[j], q);
+      uint32_t b = mul_shoup(signed_mod(tau[c], q), zp, zp_p, q);  // tau_g(s) z^k
+      b = sub_mod(b, sw, q);
+      b = add_mod(b, signed_mod(err[c], q), q);
+      y[c] = b;
+    }
+  }
+}
+
 }  // namespace
+
+size_t client_keys_smem_bytes() {
+  return sizeof(uint32_t) * ((size_t)N + N + 2 * N + N + 2 * NTT_SCRATCH + 2 * MAX_CDT);
+}
+
+cudaError_t launch_client_keys(const KeyGenArgs& a, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  client_keys_kernel<<<n, CT, client_keys_smem_bytes(), st>>>(a);
+  return cudaGetLastError();
+}
 
 size_t query_gen_smem_bytes() {
   return sizeof(uint32_t) * ((size_t)2 * N + 2 * N + 2 * N + 2 * N + N + 2 * NTT_SCRATCH + 2 * MAX_CDT + 20 + 8);
 }
 
 cudaError_t prepare_client_kernels() {
-  return cudaFuncSetAttribute(query_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)query_gen_smem_bytes());
+  cudaError_t e = cudaFuncSetAttribute(query_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)query_gen_smem_bytes());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(client_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)client_keys_smem_bytes());
+  return e;
 }
 
 cudaError_t launch_query_gen(const QueryGenArgs& a, int n, cudaStream_t st) {

@@ -70,6 +70,7 @@ struct inspire_ctx {
   int gamma = 0;
   uint8_t w_seed[32] = {};
   ighost::DevMem what;
+  ighost::DevMem wmask;  // [ELL][2][N] w_mask residues (client key generation)
   // clients
   std::vector<ighost::DevMem*> clients;
   std::vector<const uint32_t*> client_ptrs;

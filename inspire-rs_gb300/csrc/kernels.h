@@ -87,6 +87,20 @@ struct QueryGenArgs {
   int* status;                // [n]
 };
 
+// Client key generation: client first_client + i gets secret key sk[i][2][N]
+// and packing key body y_body[i][ELL][2][N] against the CRS mask wmask.
+struct KeyGenArgs {
+  DevParams P;
+  uint64_t first_client;
+  uint32_t key[8];
+  uint32_t zpow[2][ELL], zpow_p[2][ELL];
+  uint64_t cdt[MAX_CDT];
+  int cdt_len;
+  const uint32_t* wmask;      // [ELL][2][N] w_mask residues
+  uint64_t* sk;               // [n][2][N]
+  uint64_t* y_body;           // [n][ELL][2][N]
+};
+
 // Set the kernels' dynamic shared-memory limits on the current device (once
 // per device, before any launch; launches then make no configuration call).
 cudaError_t prepare_respond_kernels();
@@ -97,6 +111,8 @@ cudaError_t prepare_client_kernels();
 
 size_t query_gen_smem_bytes();
 cudaError_t launch_query_gen(const QueryGenArgs& a, int n, cudaStream_t st);
+size_t client_keys_smem_bytes();
+cudaError_t launch_client_keys(const KeyGenArgs& a, int n, cudaStream_t st);
 
 size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);

@@ -15,6 +15,7 @@ from .pir import (  # noqa: F401
     Server,
     ServerCrs,
     ServerResponse,
+    client_keygen_device,
     external_product_device,
     now_ns,
     ntt_forward_device,

@@ -415,6 +415,19 @@ def query_seeded_device(crs: ServerCrs, d_sk: int, key: bytes, first_query: int,
                                              v(d_b_rows), v(d_status), v(stream)))
 
 
+def client_keygen_device(crs: ServerCrs, key: bytes, first_client: int, n: int, d_sk: int, d_y_body: int,
+                         stream: int) -> None:
+    """Secret keys (RlweSecretKey::generate, enc.rs:14-17) and packing key
+    bodies (ClientPackingKeys::generate, inspiring2.rs:640-660) of n clients,
+    generated on the device from a ChaCha20 stream keyed by `key` (raw device
+    pointers as ints); d_sk [n][2*ring_dim], d_y_body [n][3][2*ring_dim]
+    (u64); asynchronous."""
+    if len(key) != 32:
+        raise ValueError("key must be 32 bytes")
+    v = C.c_void_p
+    _check(crs.L.inspire_client_keygen_device(crs.h, bytes(key), first_client, n, v(d_sk), v(d_y_body), v(stream)))
+
+
 def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, stream: int) -> int:
     """Launch the modular-multiply rate probe; returns the multiplies issued."""
     _check(crs.L.inspire_mulmod_rate_device(crs.h, blocks, iters, C.c_void_p(d_sink), C.c_void_p(stream)))

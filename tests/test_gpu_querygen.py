@@ -1,9 +1,13 @@
-"""GPU seeded query generation (query_seeded, src/pir/query.rs:43-85, as
-SeededRgswCiphertext::encrypt, src/rgsw/types.rs:233-300) through the C ABI:
-bit-exact against a CPU restatement of the generator's stream built from the
-oracle's ChaCha20, Poly::from_seed_moduli and negacyclic product; errors
-within the crate's tail cut with the crate's sigma; and generated queries
-answered by the Respond path decrypt to the queried entries."""
+"""GPU client side through the C ABI: seeded query generation (query_seeded,
+src/pir/query.rs:43-85, as SeededRgswCiphertext::encrypt,
+src/rgsw/types.rs:233-300) and client key generation (RlweSecretKey::generate,
+src/rlwe/enc.rs:14-17; ClientPackingKeys::generate's y_body,
+src/inspiring/inspiring2.rs:640-660, 846-902).  Bit-exact against a CPU
+restatement of the generators' streams built from the oracle's ChaCha20,
+Poly::from_seed_moduli, generate_mask_from_seed, apply_automorphism and
+negacyclic product; errors within the crate's tail cut with the crate's sigma;
+and queries and keys generated on the device, answered by the Respond path and
+extracted on the device, give back the queried entries."""
 import math
 
 import numpy as np
@@ -63,11 +67,32 @@ def cdt_table(sigma):
     return np.array(out, dtype=np.uint64), T
 
 
+def gaussian_blocks(key, blk0, n=N):
+    """n discrete Gaussian samples, 8 per keystream block blk0, blk0 + 1, ..."""
+    from oracle import oracle as O
+
+    cdt, T = cdt_table(SIGMA)
+    words = []
+    for t in range(n // 8):
+        c = blk0 + t
+        words.append(O.chacha20_block(key, [c & 0xFFFFFFFF, c >> 32, 0, 0]))
+    w64 = np.concatenate(words).astype(np.uint64)
+    u = w64[0::2] | (w64[1::2] << np.uint64(32))
+    mag = u & np.uint64((1 << 63) - 1)
+    j = np.minimum(np.searchsorted(cdt, mag, side="right"), T).astype(np.int64)
+    neg = (u >> np.uint64(63)).astype(bool) & (j != 0)
+    return np.where(neg, -j, j)
+
+
+def residues(e):
+    """Signed coefficients -> residue-major u64 poly."""
+    return np.concatenate([(e % Q[0]), (e % Q[1])]).astype(np.uint64)
+
+
 def expected_query(G, first_query, qi, k):
     """The device generator's output for query number first_query + qi."""
     O, ctx, sk = G["O"], G["ctx"], G["client"].sk
     key = np.frombuffer(KEY, dtype="<u4")
-    cdt, T = cdt_table(SIGMA)
     Qn = first_query + qi
     m = ctx.inverse_monomial(k)
     ms = ctx.poly_mul(m, sk)
@@ -78,16 +103,7 @@ def expected_query(G, first_query, qi, k):
         c = Qn * 16 + row
         w = O.chacha20_block(key, [c & 0xFFFFFFFF, c >> 32, 0, 0])
         seeds[row] = np.frombuffer(w[:8].astype("<u4").tobytes(), np.uint8)
-        words = []
-        for t in range(N // 8):
-            c = (1 << 40) + (Qn * 2 * ELL + row) * (N // 8) + t
-            words.append(O.chacha20_block(key, [c & 0xFFFFFFFF, c >> 32, 0, 0]))
-        w64 = np.concatenate(words).astype(np.uint64)
-        u = w64[0::2] | (w64[1::2] << np.uint64(32))
-        mag = u & np.uint64((1 << 63) - 1)
-        j = np.minimum(np.searchsorted(cdt, mag, side="right"), T).astype(np.int64)
-        neg = (u >> np.uint64(63)).astype(bool) & (j != 0)
-        e = np.where(neg, -j, j)
+        e = gaussian_blocks(key, (1 << 40) + (Qn * 2 * ELL + row) * (N // 8))
         errs[row] = e
         a = ctx.poly_from_seed(seeds[row].tobytes())
         a_s = ctx.poly_mul(a, sk)
@@ -173,3 +189,87 @@ def test_query_gen_rejects(gen):
         inspire.query_seeded_device(gen["crs"], 1, KEY, (1 << 36) - 1, 2, 1, 1, 1, 1, 0)
     with pytest.raises(ValueError):
         inspire.query_seeded_device(gen["crs"], 1, KEY[:16], 0, 1, 1, 1, 1, 1, 0)
+
+
+def device_keys(G, first_client, n):
+    torch, inspire = G["torch"], G["inspire"]
+    dev = torch.device("cuda:0")
+    sk = torch.zeros((n, 2 * N), dtype=torch.int64, device=dev)
+    yb = torch.zeros((n, ELL, 2 * N), dtype=torch.int64, device=dev)
+    inspire.client_keygen_device(G["crs"], KEY, first_client, n, sk.data_ptr(), yb.data_ptr(),
+                                 torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return sk, yb
+
+
+def test_client_keygen_bit_exact(gen):
+    """sk = Gaussian coefficients; y_body[k] = tau_g(s) z^k - s w_mask[k] + e_k
+    with g = gen_pows[1] = 2n/gamma + 1 (inspiring2.rs:115-127, 652-654)."""
+    ctx = gen["ctx"]
+    key = np.frombuffer(KEY, dtype="<u4")
+    sk_d, yb_d = device_keys(gen, 7, 3)
+    sk_d = sk_d.cpu().numpy().view(np.uint64)
+    yb_d = yb_d.cpu().numpy().view(np.uint64)
+    w_mask = ctx.mask_from_seed(W_SEED, ELL)
+    gen_elt = 2 * N // 16 + 1
+    for i in range(3):
+        base = (1 << 48) + (7 + i) * 4 * (N // 8)
+        s_signed = gaussian_blocks(key, base)
+        s = residues(s_signed)
+        assert np.array_equal(sk_d[i], s), i
+        tau = ctx.automorphism(s, gen_elt)
+        for k in range(ELL):
+            e = gaussian_blocks(key, base + (k + 1) * (N // 8))
+            sw = ctx.poly_mul(s, w_mask[k])
+            want = np.zeros(2 * N, np.uint64)
+            for r in range(2):
+                q = Q[r]
+                sl = slice(r * N, (r + 1) * N)
+                z = pow(1 << 20, k, q)
+                v = (tau[sl].astype(np.int64) * z) % q
+                v = (v - sw[sl].astype(np.int64)) % q
+                v = (v + e % q) % q
+                want[sl] = v.astype(np.uint64)
+            assert np.array_equal(yb_d[i, k], want), (i, k)
+
+
+def test_device_client_end_to_end(gen):
+    """Every client-side step on the device: keys of three clients, their
+    registered packing keys, queries under each secret key, batched Respond,
+    and decrypt + extract with each client's key (no oracle involved)."""
+    inspire, torch = gen["inspire"], gen["torch"]
+    rng = np.random.default_rng(5)
+    n_entries = 3 * N
+    db = rng.integers(0, 256, size=n_entries * ENTRY, dtype=np.uint8)
+    crs = gen["crs"]
+    edb = inspire.EncodedDatabase(crs, db, ENTRY)
+    sk, yb = device_keys(gen, 100, 3)
+    ybh = yb.cpu().numpy().view(np.uint64)
+    cids = [crs.register_client(inspire.ClientPackingKeys(y_body=ybh[c])) for c in range(3)]
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream().cuda_stream
+    targets = rng.integers(0, n_entries, size=(3, 5))
+    for c in range(3):
+        idx = torch.tensor((targets[c] % N).astype(np.int32), device=dev)
+        seeds = torch.zeros((5, 2 * ELL, 32), dtype=torch.uint8, device=dev)
+        b_rows = torch.zeros((5, 2 * ELL, 2 * N), dtype=torch.int64, device=dev)
+        status = torch.full((5,), -1, dtype=torch.int32, device=dev)
+        inspire.query_seeded_device(crs, sk[c].data_ptr(), KEY, 1000 * c, 5, idx.data_ptr(), seeds.data_ptr(),
+                                    b_rows.data_ptr(), status.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert not status.cpu().numpy().any()
+        out = inspire.respond_seeded_batch(crs, edb, [int(t) // N for t in targets[c]], seeds.cpu().numpy(),
+                                           b_rows.cpu().numpy().view(np.uint64), [cids[c]] * 5)
+        d_ct = torch.from_numpy(out.view(np.int64)).to(dev)
+        ent = torch.zeros((5, ENTRY), dtype=torch.uint8, device=dev)
+        inspire.pir.extract_inspiring_device(crs, sk[c].data_ptr(), d_ct.data_ptr(), 5, ENTRY, ent.data_ptr(), stream)
+        torch.cuda.synchronize()
+        got = ent.cpu().numpy()
+        for j, t in enumerate(targets[c]):
+            assert np.array_equal(got[j], db[t * ENTRY:(t + 1) * ENTRY]), (c, t)
+
+
+def test_client_keygen_rejects(gen):
+    inspire = gen["inspire"]
+    with pytest.raises(inspire.PirError, match="2\\^30"):
+        inspire.client_keygen_device(gen["crs"], KEY, (1 << 30) - 1, 2, 1, 1, 0)
