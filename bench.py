@@ -4,8 +4,10 @@ Workload (the metric's configuration): a 2^24-entry x 32-byte database of
 uniform random bytes (seed 1) encoded resident in HBM (8192 shards of 2048
 entries), d = 2048, CRT q = [268369921, 249561089], p = 2^16; each step is one
 launch answering B = 128 seeded queries (real client queries made by the
-oracle client, each routed to a uniformly drawn shard), with per-client
-packing keys resident.  Metric: Respond queries/s.
+library's device-side client -- inspire_client_keygen_device and
+inspire_query_seeded_device -- each routed to a uniformly drawn shard), with
+per-client packing keys resident.  Metric: Respond queries/s.  Every timed
+response is decrypted and extracted on the device with its client's key.
 
   value : device-resident inputs, CUDA-event time of the Respond launches
           (each step: LAUNCHES_PER_STEP launches of B queries spread over
@@ -46,7 +48,7 @@ LOG2_ENTRIES = 24
 BATCH = 128
 LAUNCHES_PER_STEP = 16  # one step answers LAUNCHES_PER_STEP * BATCH queries
 POOL_BATCHES = 32       # distinct staged batches, cycled
-QUERY_POOL = 256        # distinct real seeded queries (oracle clients)
+QUERY_POOL = 256        # distinct real seeded queries (device-side clients)
 N_CLIENTS = 32          # registered clients (own keys), QUERY_POOL / N_CLIENTS queries each
 STREAMS = 2             # CUDA streams the timed launches alternate over
 REFERENCE_BUDGET_S = 150.0
@@ -129,8 +131,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_query_pool(ctx, pack, n_queries, seed):
-    """Real seeded queries and the client's y_body from the oracle client."""
+def reference_query_pool(ctx, pack, n_queries, seed):
+    """Seeded queries and y_body from the oracle's restatement of the crate's
+    client (query.rs:43-85, inspiring2.rs:640-707), for the reference arm."""
     from oracle import oracle as O
 
     client = O.Client(ctx, seed=seed, rng_seed=seed + 1000)
@@ -144,25 +147,66 @@ def make_query_pool(ctx, pack, n_queries, seed):
     return client, locals_, seeds, brows, y_body
 
 
-def make_client_pools(ctx, pack, n_clients, per_client, seed):
-    """n_clients oracle clients (own secret key, own packing keys), each with
-    per_client real seeded queries; query k belongs to client k // per_client."""
-    pools = [make_query_pool(ctx, pack, per_client, seed + 17 * c) for c in range(n_clients)]
-    clients = [p[0] for p in pools]
-    locals_ = np.concatenate([p[1] for p in pools])
-    seeds = np.concatenate([p[2] for p in pools])
-    brows = np.concatenate([p[3] for p in pools])
-    y_bodies = [p[4] for p in pools]
-    client_of = np.repeat(np.arange(n_clients), per_client)
-    return clients, client_of, locals_, seeds, brows, y_bodies
+class DeviceClients:
+    """n_clients clients made on the device: secret keys and packing key
+    bodies (inspire_client_keygen_device), per_client seeded queries each
+    (inspire_query_seeded_device) of uniform local indices; query k belongs to
+    client k // per_client.  Responses are checked with extract()."""
+
+    def __init__(self, inspire, crs, torch, dev, n_clients, per_client, seed):
+        self.inspire, self.crs, self.torch, self.dev = inspire, crs, torch, dev
+        key = np.random.default_rng(seed).integers(0, 256, size=32, dtype=np.uint8).tobytes()
+        sp = torch.cuda.current_stream(dev).cuda_stream
+        self.d_sk = torch.zeros((n_clients, 2 * N), dtype=torch.int64, device=dev)
+        d_yb = torch.zeros((n_clients, 3, 2 * N), dtype=torch.int64, device=dev)
+        inspire.client_keygen_device(crs, key, 0, n_clients, self.d_sk.data_ptr(), d_yb.data_ptr(), sp)
+        nq = n_clients * per_client
+        self.locals_ = np.random.default_rng(seed + 1).integers(0, N, size=nq)
+        self.client_of = np.repeat(np.arange(n_clients), per_client)
+        d_idx = torch.from_numpy(self.locals_.astype(np.int32)).to(dev)
+        d_seeds = torch.zeros((nq, 6, 32), dtype=torch.uint8, device=dev)
+        d_brows = torch.zeros((nq, 6, 2 * N), dtype=torch.int64, device=dev)
+        d_status = torch.full((nq,), -1, dtype=torch.int32, device=dev)
+        for c in range(n_clients):
+            sl = slice(c * per_client, (c + 1) * per_client)
+            inspire.query_seeded_device(crs, self.d_sk[c].data_ptr(), key, c * per_client, per_client,
+                                        d_idx[sl].data_ptr(), d_seeds[sl].data_ptr(), d_brows[sl].data_ptr(),
+                                        d_status[sl].data_ptr(), sp)
+        torch.cuda.synchronize()
+        assert not d_status.cpu().numpy().any(), "query generation reported a nonzero status"
+        self.seeds = d_seeds.cpu().numpy()
+        self.brows = d_brows.cpu().numpy().view(np.uint64)
+        self.y_bodies = d_yb.cpu().numpy().view(np.uint64)
+        self.n_clients = n_clients
+
+    def extract(self, client, d_ct):
+        """decrypt + extract_inspiring of the device responses d_ct [n][2][2N]
+        (int64 tensor) with `client`'s key, on the device; entries as numpy."""
+        torch = self.torch
+        d_ct = d_ct.contiguous()
+        n = d_ct.shape[0]
+        d_ent = torch.zeros((n, ENTRY), dtype=torch.uint8, device=self.dev)
+        self.inspire.pir.extract_inspiring_device(self.crs, self.d_sk[client].data_ptr(), d_ct.data_ptr(), n, ENTRY,
+                                                  d_ent.data_ptr(), torch.cuda.current_stream(self.dev).cuda_stream)
+        torch.cuda.synchronize()
+        return d_ent.cpu().numpy()
+
+    def extract_host(self, client, cts):
+        """The same for host responses cts [n][2][2N] (u64)."""
+        cts = np.ascontiguousarray(cts, dtype=np.uint64).reshape(-1, 2, 2 * N)
+        return self.extract(client, self.torch.from_numpy(cts.view(np.int64)).to(self.dev))
 
 
-def cpu_baseline(ctx, pack, db_raw, pool, budget_s=12.0, max_queries=200):
+def cpu_baseline(db_raw, pool, mode, budget_s=12.0, max_queries=200):
     """Oracle (C restatement of the crate) respond_seeded_inspiring with
-    PackParams / OfflinePackingKeys built once, OpenMP over the 16 columns."""
+    PackParams / OfflinePackingKeys built once, OpenMP over the 16 columns,
+    on the same queries and packing keys as the GPU run."""
     from oracle import oracle as O
 
-    client, locals_, seeds, brows, y_body = pool
+    ctx = O.Ctx()
+    omode = O.MODE_CRT_FIXED if mode == "crt_fixed" else O.MODE_COMPAT
+    pack = O.Pack(ctx, GAMMA, W_SEED, mode=omode)
+    locals_, seeds, brows, y_body = pool
     rng = np.random.default_rng(99)
     nshards = (len(db_raw) // ENTRY) // N
     t0 = time.perf_counter()
@@ -171,7 +215,7 @@ def cpu_baseline(ctx, pack, db_raw, pool, budget_s=12.0, max_queries=200):
         k = done % len(locals_)
         shard = ctx.encode_shard(db_raw, ENTRY, int(rng.integers(0, nshards)))
         rgsw = ctx.expand_rgsw(seeds[k], brows[k])
-        ctx.respond_inspiring(shard, rgsw, W_SEED, mode=O.MODE_CRT_FIXED, pack=pack, y_body=y_body)
+        ctx.respond_inspiring(shard, rgsw, W_SEED, mode=omode, pack=pack, y_body=y_body)
         done += 1
     dt = time.perf_counter() - t0
     return done / dt, done, dt
@@ -238,7 +282,7 @@ def reference_arm(args):
         return
     ctx = O.Ctx()
     pack_tmp = O.Pack(ctx, GAMMA, W_SEED, mode=O.MODE_COMPAT)
-    pool = make_query_pool(ctx, pack_tmp, 8, 7)
+    pool = reference_query_pool(ctx, pack_tmp, 8, 7)
     client, locals_, seeds, brows, y_body = pool
     rng = np.random.default_rng(1)
     shard_db = rng.integers(0, 256, size=N * ENTRY, dtype=np.uint8)
@@ -317,7 +361,6 @@ def main():
         torch.distributed.barrier()
 
     import inspire
-    from oracle import oracle as O
 
     B = args.batch
     n_entries = 1 << args.log2_entries
@@ -331,17 +374,13 @@ def main():
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
 
-    ctx = O.Ctx()
-    omode = O.MODE_CRT_FIXED if args.mode == "crt_fixed" else O.MODE_COMPAT
-    pack = O.Pack(ctx, GAMMA, W_SEED, mode=omode)
-    clients, client_of, locals_, seeds, brows, y_bodies = make_client_pools(
-        ctx, pack, N_CLIENTS, QUERY_POOL // N_CLIENTS, 3 + 101 * rank)
-    client, y_body = clients[0], y_bodies[0]
-    cids = np.array([crs.register_client(inspire.ClientPackingKeys(y_body=yb)) for yb in y_bodies], np.int32)
+    clients = DeviceClients(inspire, crs, torch, dev, N_CLIENTS, QUERY_POOL // N_CLIENTS, 3 + 101 * rank)
+    client_of, locals_, seeds, brows = clients.client_of, clients.locals_, clients.seeds, clients.brows
+    y_body = clients.y_bodies[0]
+    cids = np.array([crs.register_client(inspire.ClientPackingKeys(y_body=yb)) for yb in clients.y_bodies], np.int32)
     qcid = cids[client_of]  # registered client id of each pool query
-    cid = int(cids[0])
     c0 = client_of == 0  # client 0's queries (paths that take one client)
-    pool = (client, locals_[c0], seeds[c0], brows[c0], y_body)
+    pool = (locals_[c0], seeds[c0], brows[c0], y_body)
 
     L = args.launches_per_step
     nb = POOL_BATCHES
@@ -436,25 +475,17 @@ def main():
         value_graph = B * L * args.steps / (sum(a.elapsed_time(b) for a, b in gev) / 1e3)
 
     # correctness of what was timed: statuses, then every response of the nb
-    # pool batches decrypted and extracted on the device (checked against the
-    # oracle's extraction on samples) must equal its database entry
+    # pool batches decrypted and extracted on the device with its client's key
+    # must equal its database entry
     status = d_status.cpu().numpy()
     assert not status.any(), "respond kernel reported a nonzero status"
-    # each client's responses decrypted with that client's key
     owner = client_of[pool_idx].reshape(-1)
     flat_out = d_out.view(nb * B, 2, 2 * N)
     got_flat = np.zeros((nb * B, ENTRY), np.uint8)
-    for ci, cl in enumerate(clients):
+    for ci in range(clients.n_clients):
         sel = np.nonzero(owner == ci)[0]
-        if sel.size == 0:
-            continue
-        d_sel = flat_out[torch.from_numpy(sel).to(dev)].contiguous()
-        d_sk = torch.from_numpy(np.ascontiguousarray(cl.sk).view(np.int64)).to(dev)
-        d_ent = torch.zeros((sel.size, ENTRY), dtype=torch.uint8, device=dev)
-        inspire.pir.extract_inspiring_device(crs, d_sk.data_ptr(), d_sel.data_ptr(), sel.size, ENTRY,
-                                             d_ent.data_ptr(), sp)
-        torch.cuda.synchronize()
-        got_flat[sel] = d_ent.cpu().numpy()
+        if sel.size:
+            got_flat[sel] = clients.extract(ci, flat_out[torch.from_numpy(sel).to(dev)])
     got_all = got_flat.reshape(nb, B, ENTRY)
     gi_all = shard_ids.astype(np.int64) * N + locals_[pool_idx].astype(np.int64)
     verified = 0
@@ -462,11 +493,6 @@ def main():
         want_all = db_raw.reshape(-1, ENTRY)[gi_all]
         verified = int(np.all(got_all == want_all, axis=2).sum())
         assert verified == nb * B, f"{nb * B - verified} timed responses failed to decrypt"
-    s = (args.steps * L - 1) % nb
-    outs = d_out[s].cpu().numpy().view(np.uint64)
-    for j in range(0, B, max(1, B // 8)):
-        owner_cl = clients[client_of[pool_idx[s, j]]]
-        assert np.array_equal(got_all[s, j], owner_cl.extract_inspiring(outs[j], ENTRY)), "device extraction differs"
 
     # batch-size sweep (single query = the plain GPU path)
     sweep = {}
@@ -541,7 +567,7 @@ def main():
              "p99_ms": float(np.percentile(single_lat, 99)),
              "path": "inspire_respond_seeded_batch with n=1 from host buffers, one call at a time"}
 
-    c3 = c3_bench(inspire, crs, client, pack, seeds[c0], brows[c0], y_body) if rank == 0 else None
+    c3 = c3_bench(inspire, crs, seeds[c0], brows[c0], y_body) if rank == 0 else None
 
     serving = None
     e2e_value = sync_call_qps
@@ -570,7 +596,7 @@ def main():
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline and ws == 1:
-            qps, nq, dt = cpu_baseline(ctx, pack, db_raw, pool)
+            qps, nq, dt = cpu_baseline(db_raw, pool, args.mode)
             cpu = {"value": qps, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"{nq} queries in {dt:.1f} s (oracle C restatement, PackParams/OfflinePackingKeys "
                              f"hoisted, OpenMP over 16 columns)"}
@@ -582,9 +608,9 @@ def main():
                                    f"({nshards} shards), B={B} seeded queries per launch, uniform shard ids",
                        "step": f"{L} launches x {B} queries over {len(side)} streams",
                        "streams": len(side),
-                       "queries": f"{QUERY_POOL} distinct real seeded queries from {N_CLIENTS} oracle clients "
-                                  "(each client's packing keys registered and resident); each launch slot draws one "
-                                  "with its own uniform shard id",
+                       "queries": f"{QUERY_POOL} distinct real seeded queries from {N_CLIENTS} clients generated "
+                                  "on the device (keys, packing keys and queries; packing keys registered and "
+                                  "resident); each launch slot draws one with its own uniform shard id",
                        "mode": args.mode, "global_batch": B * ws, "ring_dim": N,
                        "crt_moduli": [268369921, 249561089], "p": 65536,
                        "l2": "flushed between timed steps (256 MiB write); resident DB 6.5 GiB > L2",
@@ -624,7 +650,7 @@ def main():
         torch.distributed.destroy_process_group()
 
 
-def c3_bench(inspire, crs, client, pack, seeds, brows, y_body, n=60):
+def c3_bench(inspire, crs, seeds, brows, y_body, n=60):
     """C3: plain single-query InsPIRe^2 on 2^20 entries x 32 B resident, one
     query at a time through respond_seeded_inspiring with the packing keys in
     the query (the crate's per-request path: the server rotates y_body for
@@ -671,7 +697,7 @@ def serve_bench(inspire, crs, edb, nshards, clients, client_of, qcid, locals_, s
     def check(samples, raws, targets_nshards):
         for d, shard, pidx, out in samples[:16]:
             gi = shard * N + int(locals_[pidx])
-            got = clients[client_of[pidx]].extract_inspiring(out, ENTRY)
+            got = clients.extract_host(int(client_of[pidx]), out)[0]
             if args.mode == "crt_fixed":
                 assert np.array_equal(got, raws[d][gi * ENTRY:(gi + 1) * ENTRY]), "served response failed to decrypt"
 
