@@ -37,12 +37,14 @@ namespace {
 // b0_c for every column c and residue (see file comment).  bp (6N words) is
 // scratch; bpoly[r * 16 + c] receives the result.  Warp c handles column c:
 // lane l takes the coefficient pairs i = 2 (l + 32 m) + {0, 1}, reading the
-// raw column as u32 pairs (four loads in flight) and the staged rows as
-// 64-bit words, so every shared-memory read of a warp covers 256 contiguous
-// bytes (no bank conflicts).
+// raw column as u32 pairs and the staged rows as 64-bit words, so every
+// shared-memory read of a warp covers 256 contiguous bytes (no bank
+// conflicts).  Each lane issues its column loads 16 at a time, so the column
+// costs two memory latencies.
 __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* __restrict__ brows,
                           uint32_t* bp, uint32_t* bpoly) {
   const int tid = threadIdx.x, gamma = P.gamma;
+  const int lane = tid & 31, c = tid >> 5;
 #pragma unroll 8
   for (int idx = tid; idx < ELL * 2 * N; idx += RBLOCK) {
     const int i = idx & (N - 1), tr = idx >> LOGN, r = tr & 1;
@@ -52,18 +54,17 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
     bp[idx] = v;
   }
   __syncthreads();
-  const int lane = tid & 31, c = tid >> 5;
   if (c < gamma) {
     const uint32_t* h2 = reinterpret_cast<const uint32_t*>(H + (size_t)c * N);
     const uint2* b2 = reinterpret_cast<const uint2*>(bp);
     uint64_t acc0 = 0, acc1 = 0;
 #pragma unroll 1
-    for (int m0 = 0; m0 < N / 64; m0 += 4) {
-      uint32_t hw[4];
+    for (int m0 = 0; m0 < N / 64; m0 += 16) {
+      uint32_t hw[16];
 #pragma unroll
-      for (int m = 0; m < 4; m++) hw[m] = __ldg(h2 + lane + 32 * (m0 + m));
+      for (int m = 0; m < 16; m++) hw[m] = __ldg(h2 + lane + 32 * (m0 + m));
 #pragma unroll
-      for (int m = 0; m < 4; m++) {
+      for (int m = 0; m < 16; m++) {
         const int j = lane + 32 * (m0 + m);  // pair index: coefficients 2j, 2j + 1
         const uint2 b00 = b2[0 * (N / 2) + j], b01 = b2[1 * (N / 2) + j];  // digit 0: residue 0, 1
         const uint2 b10 = b2[2 * (N / 2) + j], b11 = b2[3 * (N / 2) + j];  // digit 1
