@@ -63,9 +63,9 @@ ALG_BYTES_PER_QUERY = 192 * 1024
 MULMODS_PER_QUERY = 3.4e6
 # resident database bytes one query reads: contracted form 768 KiB + raw columns 64 KiB
 DB_BYTES_PER_QUERY = (768 + 64) * 1024
-# dram__bytes_read.sum + dram__bytes_write.sum of one B=128 respond launch, from the
-# ncu capture summarised in profiles/respond_kernel_b128.md
-NCU_TRAFFIC_PER_LAUNCH_B128 = 114.9e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one B=128 respond launch (queries of
+# 32 clients), from the ncu capture summarised in profiles/respond_kernel_b128.md
+NCU_TRAFFIC_PER_LAUNCH_B128 = 151.8e6
 
 
 def dist_env():
