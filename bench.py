@@ -59,12 +59,13 @@ W_SEED = bytes(range(100, 132))
 METRIC = "Respond queries/s (batched InsPIRe^2, seeded queries, InspiRING packing)"
 # algorithmic bytes per query (raw shard 64 KiB + query b-rows 48 KiB + y_body 48 KiB + response 32 KiB)
 ALG_BYTES_PER_QUERY = 192 * 1024
-# exact modular multiplies per query (transform butterflies + pointwise products), see the design doc
+# exact modular multiplies per query: 68 transforms per residue x 1024 x 11 butterflies
+# (~0.77 M) + ~0.93 M pointwise products per residue, two residues
 MULMODS_PER_QUERY = 3.4e6
 # resident database bytes one query reads: contracted form 768 KiB + raw columns 64 KiB
 DB_BYTES_PER_QUERY = (768 + 64) * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one B=128 respond launch (queries of
-# 32 clients), from the ncu capture summarised in profiles/respond_kernel_b128.md
+# 32 clients), from one ncu capture of the first timed launch on the 2^20-entry database
 NCU_TRAFFIC_PER_LAUNCH_B128 = 151.8e6
 
 
@@ -620,7 +621,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved_gbs / hbm_peak,
                          "traffic": NCU_TRAFFIC_PER_LAUNCH_B128 if B == 128 else None,
-                         "note": "algorithmic bytes 192 KiB/query; the kernel is integer-issue bound, see DESIGN.md"},
+                         "note": "algorithmic bytes 192 KiB/query; the kernel is bound by integer issue, see int_roofline"},
             "int_roofline": {"bound": "integer pipes", "achieved": value * MULMODS_PER_QUERY / 1e12,
                              "peak": micro["mulmod_rate_tps"], "unit": "10^12 modular multiplies/s",
                              "frac": value * MULMODS_PER_QUERY / 1e12 / micro["mulmod_rate_tps"],
