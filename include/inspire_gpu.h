@@ -168,6 +168,27 @@ int inspire_respond_inspiring(inspire_ctx *ctx, const inspire_db *db, const insp
 int inspire_respond(inspire_ctx *ctx, const inspire_db *db, const inspire_query *query, uint64_t *out_ct,
                     uint64_t *out_columns);
 
+/* ServerCrs.galois_keys (src/pir/setup.rs:164-173) for tree packing: nkeys =
+ * log2(ring_dim) key-switching matrices, matrix i for the automorphism
+ * X -> X^(ring_dim / 2^i + 1), each 2*gadget_len polys [row 0 a, row 0 b,
+ * row 1 a, ...] (u64, residue-major, reduced).  Kept in HBM in NTT form. */
+int inspire_crs_load_galois_keys(inspire_ctx *ctx, const uint64_t *keys, uint32_t nkeys);
+
+/* respond_one_packing (src/pir/respond.rs:213-268), the tree-packing
+ * variant: the column products, the LWEs at their coefficient 0, and
+ * pack_lwes (src/inspiring/automorph_pack.rs:418-485) with the Galois keys.
+ * out_a receives the packed a (one poly); out_b (room for two polys) receives
+ * *b_words words: one poly, or -- in compat mode with more than one column --
+ * the crate's b polynomial of dimension 2*ring_dim (2 polys' words).
+ * Packing keys in the query are ignored, as in the crate. */
+int inspire_respond_one_packing(inspire_ctx *ctx, const inspire_db *db, const inspire_query *query,
+                                uint64_t *out_a, uint64_t *out_b, uint32_t *b_words);
+
+/* respond_seeded_packed (src/pir/respond.rs:428-435): expand, then
+ * respond_one_packing. */
+int inspire_respond_seeded_packed(inspire_ctx *ctx, const inspire_db *db, const inspire_seeded_query *query,
+                                  uint64_t *out_a, uint64_t *out_b, uint32_t *b_words);
+
 /* respond_seeded (src/pir/respond.rs:408-415): SeededClientQuery::expand then
  * respond. */
 int inspire_respond_seeded(inspire_ctx *ctx, const inspire_db *db, const inspire_seeded_query *query,

@@ -225,16 +225,18 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
 
 // Stage n NoPacking queries (same row layout as run_batch) and run the
 // NoPacking kernel; out_columns may be null.
-int run_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
-                  size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
-                  uint64_t* out_ct, uint64_t* out_columns) {
-  if (n == 0) return INSPIRE_OK;
+// Stage n queries' rows and enqueue the NoPacking kernel on the context's
+// stream: combined ciphertexts into d_out, and (columns) every column
+// ciphertext into d_cols.
+int enqueue_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,
+                      const uint8_t* seeds, size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows,
+                      size_t stride_polys, bool columns) {
   const size_t pw = poly_words();
   const size_t col_words = (size_t)db->gamma * 2 * pw;
   CUDA_TRY(c->d_shard.ensure(sizeof(uint32_t) * n));
   CUDA_TRY(c->d_brows.ensure(sizeof(uint64_t) * n * ELL * pw));
   CUDA_TRY(c->d_out.ensure(sizeof(uint64_t) * n * 2 * pw));
-  if (out_columns) CUDA_TRY(c->d_cols.ensure(sizeof(uint64_t) * n * col_words));
+  if (columns) CUDA_TRY(c->d_cols.ensure(sizeof(uint64_t) * n * col_words));
   CUDA_TRY(c->d_status.ensure(sizeof(int32_t) * n));
   CUDA_TRY(cudaMemcpyAsync(c->d_shard.p, shard_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpy2DAsync(c->d_brows.p, sizeof(uint64_t) * ELL * pw, b_rows, sizeof(uint64_t) * stride_polys * pw,
@@ -259,13 +261,15 @@ int run_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32
   a.nshards = db->nshards;
   a.H = db->H.as<uint16_t>();
   a.out = c->d_out.as<uint64_t>();
-  a.out_columns = out_columns ? c->d_cols.as<uint64_t>() : nullptr;
+  a.out_columns = columns ? c->d_cols.as<uint64_t>() : nullptr;
   a.status = c->d_status.as<int>();
   CUDA_TRY(launch_nopacking(a, seeded, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(out_ct, c->d_out.p, sizeof(uint64_t) * n * 2 * pw, cudaMemcpyDeviceToHost, c->stream));
-  if (out_columns)
-    CUDA_TRY(cudaMemcpyAsync(out_columns, c->d_cols.p, sizeof(uint64_t) * n * col_words, cudaMemcpyDeviceToHost,
-                             c->stream));
+  return INSPIRE_OK;
+}
+
+// Copy the n query statuses back, wait for the stream, and turn a nonzero
+// status into an error.
+int finish_status(inspire_ctx* c, uint32_t n, const char* what) {
   c->h_status.resize(n);
   CUDA_TRY(cudaMemcpyAsync(c->h_status.data(), c->d_status.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
                            c->stream));
@@ -273,7 +277,57 @@ int run_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32
   for (uint32_t i = 0; i < n; i++)
     if (c->h_status[i] != 0)
       return fail(INSPIRE_ERR_DEVICE_STATUS,
-                  "nopacking kernel status " + std::to_string(c->h_status[i]) + " for query " + std::to_string(i));
+                  std::string(what) + " kernel status " + std::to_string(c->h_status[i]) + " for query " +
+                      std::to_string(i));
+  return INSPIRE_OK;
+}
+
+int run_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
+                  size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
+                  uint64_t* out_ct, uint64_t* out_columns) {
+  if (n == 0) return INSPIRE_OK;
+  const size_t pw = poly_words();
+  const size_t col_words = (size_t)db->gamma * 2 * pw;
+  if (int rc = enqueue_nopacking(c, db, n, shard_ids, seeds, seed_stride, a_rows, b_rows, stride_polys,
+                                 out_columns != nullptr))
+    return rc;
+  CUDA_TRY(cudaMemcpyAsync(out_ct, c->d_out.p, sizeof(uint64_t) * n * 2 * pw, cudaMemcpyDeviceToHost, c->stream));
+  if (out_columns)
+    CUDA_TRY(cudaMemcpyAsync(out_columns, c->d_cols.p, sizeof(uint64_t) * n * col_words, cudaMemcpyDeviceToHost,
+                             c->stream));
+  return finish_status(c, n, "nopacking");
+}
+
+// respond_one_packing (src/pir/respond.rs:213-268) of one query: column
+// products on the GPU (the NoPacking kernel, columns kept on the device),
+// then pack_lwes with the CRS's Galois keys (tree.cu).  out_b receives
+// *b_words words: one polynomial, or two in compat mode (the crate's
+// dimension-2d b polynomial).
+int run_tree(inspire_ctx* c, const inspire_db* db, uint32_t shard_id, const uint8_t* seeds, size_t seed_stride,
+             const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys, uint64_t* out_a, uint64_t* out_b,
+             uint32_t* b_words) {
+  const size_t pw = poly_words();
+  if (!c->has_galois) return fail(INSPIRE_ERR_NO_CRS, "no Galois keys loaded (inspire_crs_load_galois_keys)");
+  if (int rc = enqueue_nopacking(c, db, 1, &shard_id, seeds, seed_stride, a_rows, b_rows, stride_polys, true))
+    return rc;
+  CUDA_TRY(c->tree_work.ensure(sizeof(uint32_t) * tree_work_words_per_query()));
+  CUDA_TRY(c->d_tree_out.ensure(sizeof(uint64_t) * 3 * pw));
+  TreeArgs t{};
+  t.P = c->P;
+  t.nq = 1;
+  t.ncols = db->gamma;
+  t.mode = c->mode;
+  t.cols = c->d_cols.as<uint64_t>();
+  t.ks = c->galois.as<uint32_t>();
+  t.work = c->tree_work.as<uint32_t>();
+  t.out_a = c->d_tree_out.as<uint64_t>();
+  t.out_b = t.out_a + pw;
+  CUDA_TRY(launch_pack_tree(t, c->stream));
+  const uint32_t words = (c->mode == MODE_COMPAT && db->gamma > 1) ? (uint32_t)(2 * pw) : (uint32_t)pw;
+  CUDA_TRY(cudaMemcpyAsync(out_a, t.out_a, sizeof(uint64_t) * pw, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(out_b, t.out_b, sizeof(uint64_t) * words, cudaMemcpyDeviceToHost, c->stream));
+  if (int rc = finish_status(c, 1, "nopacking")) return rc;
+  *b_words = words;
   return INSPIRE_OK;
 }
 
@@ -448,6 +502,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
   if (e == cudaSuccess) e = prepare_ops_kernels();
   if (e == cudaSuccess) e = prepare_setup_kernels();
   if (e == cudaSuccess) e = prepare_client_kernels();
+  if (e == cudaSuccess) e = prepare_tree_kernels();
   if (e != cudaSuccess) {
     delete c;
     return fail(INSPIRE_ERR_CUDA, std::string("kernel setup: ") + cudaGetErrorString(e));
@@ -642,6 +697,60 @@ int inspire_respond(inspire_ctx* c, const inspire_db* db, const inspire_query* q
     memcpy(br.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t) + 1) * pw, pw * sizeof(uint64_t));
   }
   return run_nopacking(c, db, 1, &qy->shard_id, nullptr, 0, ar.data(), br.data(), ELL, out_ct, out_columns);
+}
+
+int inspire_crs_load_galois_keys(inspire_ctx* c, const uint64_t* keys, uint32_t nkeys) {
+  if (!c || !keys) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (nkeys != (uint32_t)LOGN)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "expected log2(ring_dim) = " + std::to_string(LOGN) + " Galois keys");
+  const size_t pw = poly_words();
+  const size_t npolys = (size_t)nkeys * 2 * ELL;
+  for (size_t p = 0; p < npolys; p++)
+    for (int r = 0; r < 2; r++)
+      for (int i = 0; i < N; i++)
+        if (keys[p * pw + (size_t)r * N + i] >= c->params.crt_moduli[r])
+          return fail(INSPIRE_ERR_INVALID_ARGUMENT, "Galois key coefficients must be reduced mod each CRT modulus");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (int rc = set_device(c)) return rc;
+  DevMem staged;
+  CUDA_TRY(staged.ensure(sizeof(uint64_t) * npolys * pw));
+  CUDA_TRY(cudaMemcpyAsync(staged.p, keys, sizeof(uint64_t) * npolys * pw, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c->galois.ensure(sizeof(uint32_t) * npolys * pw));
+  CUDA_TRY(launch_galois_prep(c->P, staged.as<uint64_t>(), (int)npolys, c->galois.as<uint32_t>(), c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->has_galois = true;
+  return INSPIRE_OK;
+}
+
+int inspire_respond_one_packing(inspire_ctx* c, const inspire_db* db, const inspire_query* qy, uint64_t* out_a,
+                                uint64_t* out_b, uint32_t* b_words) {
+  if (!c || !db || !qy || !out_a || !out_b || !b_words) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!qy->rgsw) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null query rows");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (qy->shard_id >= (uint32_t)db->nshards)
+    return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(qy->shard_id) + " not found");
+  if (int rc = set_device(c)) return rc;
+  const size_t pw = poly_words();
+  std::vector<uint64_t> ar((size_t)ELL * pw), br((size_t)ELL * pw);
+  for (int t = 0; t < ELL; t++) {
+    memcpy(ar.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t)) * pw, pw * sizeof(uint64_t));
+    memcpy(br.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t) + 1) * pw, pw * sizeof(uint64_t));
+  }
+  return run_tree(c, db, qy->shard_id, nullptr, 0, ar.data(), br.data(), ELL, out_a, out_b, b_words);
+}
+
+int inspire_respond_seeded_packed(inspire_ctx* c, const inspire_db* db, const inspire_seeded_query* qy,
+                                  uint64_t* out_a, uint64_t* out_b, uint32_t* b_words) {
+  if (!c || !db || !qy || !out_a || !out_b || !b_words) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!qy->seeds || !qy->b_rows) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null query rows");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (qy->shard_id >= (uint32_t)db->nshards)
+    return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(qy->shard_id) + " not found");
+  if (int rc = set_device(c)) return rc;
+  return run_tree(c, db, qy->shard_id, qy->seeds + 32 * ELL, (size_t)64 * ELL, nullptr,
+                  qy->b_rows + (size_t)ELL * poly_words(), 2 * ELL, out_a, out_b, b_words);
 }
 
 int inspire_respond_seeded_nopacking_batch(inspire_ctx* c, const inspire_db* db, uint32_t n,

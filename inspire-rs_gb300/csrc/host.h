@@ -71,6 +71,9 @@ struct inspire_ctx {
   uint8_t w_seed[32] = {};
   ighost::DevMem what;
   ighost::DevMem wmask;  // [ELL][2][N] w_mask residues (client key generation)
+  // tree packing: the CRS's Galois key table, the tree's work area and output
+  bool has_galois = false;
+  ighost::DevMem galois, tree_work, d_tree_out;
   // clients
   std::vector<ighost::DevMem*> clients;
   std::vector<const uint32_t*> client_ptrs;

@@ -101,6 +101,18 @@ struct KeyGenArgs {
   uint64_t* y_body;           // [n][ELL][2][N]
 };
 
+// Tree packing (respond_one_packing) of nq queries' column ciphertexts.
+struct TreeArgs {
+  DevParams P;
+  int nq, ncols;
+  int mode;
+  const uint64_t* cols;  // [nq][ncols][2 (a, b)][2][N] column ciphertexts
+  const uint32_t* ks;    // [log2 N][ELL][2 (a, b)][2][N] Galois keys, NTT domain x n^-1 2^32
+  uint32_t* work;        // [nq][tree_work_words_per_query()] ciphertexts of the tree
+  uint64_t* out_a;       // [nq][2][N]
+  uint64_t* out_b;       // [nq][4][N]: 2 residues x N, or 4 N words in compat mode
+};
+
 // Set the kernels' dynamic shared-memory limits on the current device (once
 // per device, before any launch; launches then make no configuration call).
 cudaError_t prepare_respond_kernels();
@@ -111,6 +123,11 @@ cudaError_t prepare_client_kernels();
 
 size_t query_gen_smem_bytes();
 cudaError_t launch_query_gen(const QueryGenArgs& a, int n, cudaStream_t st);
+size_t tree_smem_bytes();
+size_t tree_work_words_per_query();
+cudaError_t prepare_tree_kernels();
+cudaError_t launch_pack_tree(const TreeArgs& a, cudaStream_t st);
+cudaError_t launch_galois_prep(const DevParams& P, const uint64_t* keys, int npolys, uint32_t* ks, cudaStream_t st);
 size_t client_keys_smem_bytes();
 cudaError_t launch_client_keys(const KeyGenArgs& a, int n, cudaStream_t st);
 

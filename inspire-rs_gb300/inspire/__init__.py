@@ -24,11 +24,13 @@ from .pir import (  # noqa: F401
     respond,
     respond_batch,
     respond_inspiring,
+    respond_one_packing,
     respond_seeded,
     respond_seeded_batch,
     respond_seeded_batch_device,
     respond_seeded_inspiring,
     respond_seeded_nopacking_batch,
+    respond_seeded_packed,
     respond_seeded_with_variant,
     respond_with_variant,
 )

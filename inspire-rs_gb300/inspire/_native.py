@@ -134,6 +134,9 @@ def load(path: str = LIB_PATH):
         "inspire_mulmod_rate_device": (C.c_int, [vp, u32, u32, vp, vp]),
         "inspire_extract_inspiring_device": (C.c_int, [vp, vp, vp, u32, u32, vp, vp]),
         "inspire_query_seeded_device": (C.c_int, [vp, vp, C.c_char_p, u64, u32, vp, vp, vp, vp, vp]),
+        "inspire_crs_load_galois_keys": (C.c_int, [vp, vp, u32]),
+        "inspire_respond_one_packing": (C.c_int, [vp, vp, C.POINTER(QueryC), vp, vp, C.POINTER(u32)]),
+        "inspire_respond_seeded_packed": (C.c_int, [vp, vp, C.POINTER(SeededQueryC), vp, vp, C.POINTER(u32)]),
         "inspire_client_keygen_device": (C.c_int, [vp, C.c_char_p, u64, u32, vp, vp, vp]),
         "inspire_seeded_query_from_json": (C.c_int, [C.POINTER(InspireParamsC), C.c_char_p, C.c_size_t, vp, vp, vp,
                                                      vp, vp, vp]),

@@ -170,6 +170,13 @@ class ServerCrs:
     def release_client(self, client_id: int) -> None:
         _check(self.L.inspire_client_release(self.h, client_id))
 
+    def load_galois_keys(self, galois_keys: np.ndarray) -> None:
+        """ServerCrs.galois_keys (setup.rs:164-173) for tree packing: log2(d)
+        key-switching matrices of 2*gadget_len rows [a, b] each, shape
+        (log2 d, 2*ell, plen), uint64 residues."""
+        keys = _u64(galois_keys)
+        _check(self.L.inspire_crs_load_galois_keys(self.h, _ptr(keys), keys.shape[0]))
+
 
 class EncodedDatabase:
     """EncodedDatabase (setup.rs:104-120) resident in HBM: shards of ring_dim
@@ -301,6 +308,44 @@ def respond_seeded(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededCli
     return _nopacking_response(out, cols, plen)
 
 
+def _packed_response(out_a, out_b, words) -> ServerResponse:
+    return ServerResponse(RlweCiphertext(out_a, out_b[:words]), [])
+
+
+def respond_one_packing(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery) -> ServerResponse:
+    """respond_one_packing (respond.rs:213-268): column products, then
+    pack_lwes with the CRS's Galois keys (load_galois_keys).  In compat mode
+    with more than one column the b polynomial has 2*plen words, as the
+    crate's pack_lwes returns it (automorph_pack.rs:474-484)."""
+    plen = crs.params.plen
+    ell = crs.params.gadget_len
+    rgsw = _u64(query.rgsw).reshape(2 * ell, 2, plen)
+    q = nat.QueryC(query.shard_id, rgsw.ctypes.data_as(C.c_void_p), 0, None, None)
+    out_a = np.zeros(plen, dtype=np.uint64)
+    out_b = np.zeros(2 * plen, dtype=np.uint64)
+    words = C.c_uint32(0)
+    _check(crs.L.inspire_respond_one_packing(crs.h, encoded_db.h, C.byref(q), _ptr(out_a), _ptr(out_b),
+                                             C.byref(words)))
+    return _packed_response(out_a, out_b, words.value)
+
+
+def respond_seeded_packed(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery) -> ServerResponse:
+    """respond_seeded_packed (respond.rs:428-435): expand, then
+    respond_one_packing."""
+    plen = crs.params.plen
+    ell = crs.params.gadget_len
+    seeds = np.ascontiguousarray(query.seeds, dtype=np.uint8).reshape(2 * ell, 32)
+    b_rows = _u64(query.b_rows).reshape(2 * ell, plen)
+    q = nat.SeededQueryC(query.shard_id, seeds.ctypes.data_as(C.c_void_p), b_rows.ctypes.data_as(C.c_void_p),
+                         0, None, None)
+    out_a = np.zeros(plen, dtype=np.uint64)
+    out_b = np.zeros(2 * plen, dtype=np.uint64)
+    words = C.c_uint32(0)
+    _check(crs.L.inspire_respond_seeded_packed(crs.h, encoded_db.h, C.byref(q), _ptr(out_a), _ptr(out_b),
+                                               C.byref(words)))
+    return _packed_response(out_a, out_b, words.value)
+
+
 def respond_seeded_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int],
                                    seeds: np.ndarray, b_rows: np.ndarray) -> np.ndarray:
     """Batched respond_seeded: (n, 2, plen) combined ciphertexts."""
@@ -317,12 +362,11 @@ def respond_seeded_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, 
 
 def respond_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery,
                          variant: InspireVariant) -> ServerResponse:
-    """respond_with_variant (respond.rs:129-151).  Tree packing
-    (respond_one_packing) is not part of the GPU path."""
+    """respond_with_variant (respond.rs:129-151)."""
     if variant == InspireVariant.NoPacking:
         return respond(crs, encoded_db, query)
     if query.packing_mode == "tree":
-        raise PirError("tree packing is not implemented on the GPU path", nat.ERR_UNSUPPORTED)
+        return respond_one_packing(crs, encoded_db, query)
     if query.inspiring_packing_keys is None:
         raise PirError("InspiRING packing keys missing (set packing_mode=tree to use tree packing)",
                        nat.ERR_KEYS_MISSING)
@@ -331,12 +375,11 @@ def respond_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, query: Cli
 
 def respond_seeded_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery,
                                 variant: InspireVariant) -> ServerResponse:
-    """respond_seeded_with_variant (respond.rs:161-183).  Tree packing
-    (respond_seeded_packed) is not part of the GPU path."""
+    """respond_seeded_with_variant (respond.rs:161-183)."""
     if variant == InspireVariant.NoPacking:
         return respond_seeded(crs, encoded_db, query)
     if query.packing_mode == "tree":
-        raise PirError("tree packing is not implemented on the GPU path", nat.ERR_UNSUPPORTED)
+        return respond_seeded_packed(crs, encoded_db, query)
     if query.inspiring_packing_keys is None:
         raise PirError("InspiRING packing keys missing (set packing_mode=tree to use tree packing)",
                        nat.ERR_KEYS_MISSING)

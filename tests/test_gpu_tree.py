@@ -1,0 +1,98 @@
+"""GPU tree packing (respond_one_packing / respond_seeded_packed,
+src/pir/respond.rs:213-268, 428-435) through the C ABI, bit-exact against the
+oracle's restatement of pack_lwes (src/inspiring/automorph_pack.rs:171-485)
+with the CRS's Galois keys (src/pir/setup.rs:164-173): both automorphism
+modes (compat returns the crate's b polynomial of dimension 2d), full and
+seeded queries, first and partial last shard, 1, 2 and 16 columns (one LWE
+is returned unpacked, automorph_pack.rs:439-446), the variant dispatch, and
+the errors."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 2048
+W_SEED = bytes(range(40, 72))
+
+
+@pytest.fixture(scope="module")
+def tree(oracle_mod):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import inspire
+
+    O = oracle_mod
+    ctx = O.Ctx()
+    client = O.Client(ctx, seed=4, rng_seed=44)
+    keys = client.galois_keys()
+    return dict(O=O, inspire=inspire, ctx=ctx, client=client, keys=keys, dbs={})
+
+
+def world(T, mode, gamma):
+    """CRS + database (2 shards, the last partial) for `gamma` columns."""
+    key = (mode, gamma)
+    if key not in T["dbs"]:
+        inspire = T["inspire"]
+        entry = 2 * gamma
+        rng = np.random.default_rng(gamma)
+        n_entries = N + 700
+        db = rng.integers(0, 256, size=n_entries * entry, dtype=np.uint8)
+        crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, gamma, mode=mode)
+        crs.load_galois_keys(T["keys"])
+        edb = inspire.EncodedDatabase(crs, db, entry)
+        shards = [T["ctx"].encode_shard(db, entry, s) for s in range(2)]
+        T["dbs"][key] = (crs, edb, db, shards)
+    return T["dbs"][key]
+
+
+@pytest.mark.parametrize("mode", ["crt_fixed", "compat"])
+@pytest.mark.parametrize("gamma,index", [(16, 5), (16, N + 699), (2, 77), (1, 1500)])
+def test_seeded_packed_bit_exact(tree, mode, gamma, index):
+    T = tree
+    O, inspire, ctx, client = T["O"], T["inspire"], T["ctx"], T["client"]
+    crs, edb, db, shards = world(T, mode, gamma)
+    sid, local = divmod(index, N)
+    seeds, b_rows = client.query_seeded(local)
+    omode = O.MODE_CRT_FIXED if mode == "crt_fixed" else O.MODE_COMPAT
+    want_a, want_b = ctx.respond_one_packing(shards[sid], ctx.expand_rgsw(seeds, b_rows), T["keys"], mode=omode)
+    resp = inspire.respond_seeded_packed(crs, edb, inspire.SeededClientQuery(sid, seeds, b_rows))
+    assert resp.column_ciphertexts == []
+    assert np.array_equal(resp.ciphertext.a, want_a)
+    assert resp.ciphertext.b.size == want_b.size
+    assert np.array_equal(resp.ciphertext.b, want_b)
+
+
+def test_full_query_and_variant_dispatch(tree):
+    T = tree
+    O, inspire, ctx, client = T["O"], T["inspire"], T["ctx"], T["client"]
+    crs, edb, db, shards = world(T, "crt_fixed", 16)
+    seeds, b_rows = client.query_seeded(1234)
+    rgsw = ctx.expand_rgsw(seeds, b_rows)
+    want_a, want_b = ctx.respond_one_packing(shards[0], rgsw, T["keys"], mode=O.MODE_CRT_FIXED)
+    full = inspire.respond_one_packing(crs, edb, inspire.ClientQuery(0, rgsw.reshape(6, 2, 2 * N)))
+    assert np.array_equal(full.ciphertext.a, want_a) and np.array_equal(full.ciphertext.b, want_b)
+    q = inspire.SeededClientQuery(0, seeds, b_rows, packing_mode="tree")
+    via = inspire.respond_seeded_with_variant(crs, edb, q, inspire.InspireVariant.OnePacking)
+    assert np.array_equal(via.ciphertext.a, want_a) and np.array_equal(via.ciphertext.b, want_b)
+
+
+def test_tree_errors(tree):
+    T = tree
+    inspire, client = T["inspire"], T["client"]
+    crs, edb, db, shards = world(T, "crt_fixed", 16)
+    seeds, b_rows = client.query_seeded(3)
+    with pytest.raises(inspire.PirError, match="Shard 9 not found"):
+        inspire.respond_seeded_packed(crs, edb, inspire.SeededClientQuery(9, seeds, b_rows))
+    bare = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
+    edb2 = inspire.EncodedDatabase(bare, db, 32)
+    with pytest.raises(inspire.PirError, match="Galois keys"):
+        inspire.respond_seeded_packed(bare, edb2, inspire.SeededClientQuery(0, seeds, b_rows))
+    with pytest.raises(inspire.PirError, match="log2"):
+        bare.load_galois_keys(T["keys"][:10])
+    bad = T["keys"].copy()
+    bad[0, 0, 0] = 268369921
+    with pytest.raises(inspire.PirError, match="reduced"):
+        bare.load_galois_keys(bad)
+    edb2.close()
+    bare.close()
