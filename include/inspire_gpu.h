@@ -189,6 +189,13 @@ int inspire_respond_one_packing(inspire_ctx *ctx, const inspire_db *db, const in
 int inspire_respond_seeded_packed(inspire_ctx *ctx, const inspire_db *db, const inspire_seeded_query *query,
                                   uint64_t *out_a, uint64_t *out_b, uint32_t *b_words);
 
+/* A batch of respond_seeded_packed calls: query i (shard_ids[i], seeds
+ * [n][2*gadget_len][32], b_rows [n][2*gadget_len][poly]) is answered into
+ * out_a[i] (one poly) and out_b[i] (two polys' room; *b_words words used). */
+int inspire_respond_seeded_packed_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n, const uint32_t *shard_ids,
+                                        const uint8_t *seeds, const uint64_t *b_rows, uint64_t *out_a,
+                                        uint64_t *out_b, uint32_t *b_words);
+
 /* respond_seeded (src/pir/respond.rs:408-415): SeededClientQuery::expand then
  * respond. */
 int inspire_respond_seeded(inspire_ctx *ctx, const inspire_db *db, const inspire_seeded_query *query,
@@ -357,6 +364,19 @@ int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, cons
  * receives [n][entry_size] bytes (entry_size <= 32). */
 int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, const uint64_t *d_ct, uint32_t n,
                                      uint32_t entry_size, uint8_t *d_entries, void *stream);
+
+/* Setup side: the log2(ring_dim) Galois key-switching matrices of the
+ * secret key d_sk [poly] (ServerCrs.galois_keys, src/pir/setup.rs:164-173;
+ * generate_automorphism_ks_matrix, src/ks/setup.rs:218-245): matrix i for
+ * t = ring_dim / 2^i + 1, row k = (a, -a s + e + tau_t(s) z^k), written to
+ * d_keys [log2(ring_dim)][2*gadget_len][poly] in the layout
+ * inspire_crs_load_galois_keys reads; d_status [log2(ring_dim)].  a is
+ * uniform (Poly::from_seed_moduli of a seed) and e the crate's discrete
+ * Gaussian, both from a ChaCha20 stream keyed by `key`, disjoint from the
+ * query and client-key streams of the same key; the crate's thread_rng draws
+ * are not reproduced. */
+int inspire_galois_keygen_device(inspire_ctx *ctx, const uint8_t *key, const uint64_t *d_sk, uint64_t *d_keys,
+                                 int32_t *d_status, void *stream);
 
 /* Client side, for load generation at served rates: keys of n clients,
  * numbered first_client + i.  d_sk receives each RlweSecretKey::generate

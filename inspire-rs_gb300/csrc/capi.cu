@@ -298,37 +298,38 @@ int run_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32
   return finish_status(c, n, "nopacking");
 }
 
-// respond_one_packing (src/pir/respond.rs:213-268) of one query: column
+// respond_one_packing (src/pir/respond.rs:213-268) of n queries: column
 // products on the GPU (the NoPacking kernel, columns kept on the device),
-// then pack_lwes with the CRS's Galois keys (tree.cu).  out_b receives
-// *b_words words: one polynomial, or two in compat mode (the crate's
+// then pack_lwes with the CRS's Galois keys (tree.cu).  Query i's packed a
+// goes to out_a[i] (one poly) and its b to out_b[i] (room for two polys):
+// *b_words words, one poly, or two in compat mode (the crate's
 // dimension-2d b polynomial).
-int run_tree(inspire_ctx* c, const inspire_db* db, uint32_t shard_id, const uint8_t* seeds, size_t seed_stride,
-             const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys, uint64_t* out_a, uint64_t* out_b,
-             uint32_t* b_words) {
+int run_tree(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
+             size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys, uint64_t* out_a,
+             uint64_t* out_b, uint32_t* b_words) {
   const size_t pw = poly_words();
   if (!c->has_galois) return fail(INSPIRE_ERR_NO_CRS, "no Galois keys loaded (inspire_crs_load_galois_keys)");
-  if (int rc = enqueue_nopacking(c, db, 1, &shard_id, seeds, seed_stride, a_rows, b_rows, stride_polys, true))
+  const uint32_t words = (c->mode == MODE_COMPAT && db->gamma > 1) ? (uint32_t)(2 * pw) : (uint32_t)pw;
+  *b_words = words;
+  if (n == 0) return INSPIRE_OK;
+  if (int rc = enqueue_nopacking(c, db, n, shard_ids, seeds, seed_stride, a_rows, b_rows, stride_polys, true))
     return rc;
-  CUDA_TRY(c->tree_work.ensure(sizeof(uint32_t) * tree_work_words_per_query()));
-  CUDA_TRY(c->d_tree_out.ensure(sizeof(uint64_t) * 3 * pw));
+  CUDA_TRY(c->tree_work.ensure(sizeof(uint32_t) * tree_work_words_per_query() * n));
+  CUDA_TRY(c->d_tree_out.ensure(sizeof(uint64_t) * 3 * pw * n));
   TreeArgs t{};
   t.P = c->P;
-  t.nq = 1;
+  t.nq = (int)n;
   t.ncols = db->gamma;
   t.mode = c->mode;
   t.cols = c->d_cols.as<uint64_t>();
   t.ks = c->galois.as<uint32_t>();
   t.work = c->tree_work.as<uint32_t>();
   t.out_a = c->d_tree_out.as<uint64_t>();
-  t.out_b = t.out_a + pw;
+  t.out_b = t.out_a + pw * n;
   CUDA_TRY(launch_pack_tree(t, c->stream));
-  const uint32_t words = (c->mode == MODE_COMPAT && db->gamma > 1) ? (uint32_t)(2 * pw) : (uint32_t)pw;
-  CUDA_TRY(cudaMemcpyAsync(out_a, t.out_a, sizeof(uint64_t) * pw, cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(out_b, t.out_b, sizeof(uint64_t) * words, cudaMemcpyDeviceToHost, c->stream));
-  if (int rc = finish_status(c, 1, "nopacking")) return rc;
-  *b_words = words;
-  return INSPIRE_OK;
+  CUDA_TRY(cudaMemcpyAsync(out_a, t.out_a, sizeof(uint64_t) * pw * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(out_b, t.out_b, sizeof(uint64_t) * 2 * pw * n, cudaMemcpyDeviceToHost, c->stream));
+  return finish_status(c, n, "nopacking");
 }
 
 // Validation order of respond_inspiring (src/pir/respond.rs:295-305, 365-370).
@@ -737,7 +738,11 @@ int inspire_respond_one_packing(inspire_ctx* c, const inspire_db* db, const insp
     memcpy(ar.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t)) * pw, pw * sizeof(uint64_t));
     memcpy(br.data() + t * pw, qy->rgsw + (size_t)(2 * (ELL + t) + 1) * pw, pw * sizeof(uint64_t));
   }
-  return run_tree(c, db, qy->shard_id, nullptr, 0, ar.data(), br.data(), ELL, out_a, out_b, b_words);
+  std::vector<uint64_t> ob(2 * pw);
+  if (int rc = run_tree(c, db, 1, &qy->shard_id, nullptr, 0, ar.data(), br.data(), ELL, out_a, ob.data(), b_words))
+    return rc;
+  memcpy(out_b, ob.data(), sizeof(uint64_t) * *b_words);
+  return INSPIRE_OK;
 }
 
 int inspire_respond_seeded_packed(inspire_ctx* c, const inspire_db* db, const inspire_seeded_query* qy,
@@ -749,9 +754,29 @@ int inspire_respond_seeded_packed(inspire_ctx* c, const inspire_db* db, const in
   if (qy->shard_id >= (uint32_t)db->nshards)
     return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(qy->shard_id) + " not found");
   if (int rc = set_device(c)) return rc;
-  return run_tree(c, db, qy->shard_id, qy->seeds + 32 * ELL, (size_t)64 * ELL, nullptr,
-                  qy->b_rows + (size_t)ELL * poly_words(), 2 * ELL, out_a, out_b, b_words);
+  std::vector<uint64_t> ob(2 * poly_words());
+  if (int rc = run_tree(c, db, 1, &qy->shard_id, qy->seeds + 32 * ELL, (size_t)64 * ELL, nullptr,
+                        qy->b_rows + (size_t)ELL * poly_words(), 2 * ELL, out_a, ob.data(), b_words))
+    return rc;
+  memcpy(out_b, ob.data(), sizeof(uint64_t) * *b_words);
+  return INSPIRE_OK;
 }
+
+int inspire_respond_seeded_packed_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids,
+                                        const uint8_t* seeds, const uint64_t* b_rows, uint64_t* out_a,
+                                        uint64_t* out_b, uint32_t* b_words) {
+  if (!c || !db || !b_words || (n && (!shard_ids || !seeds || !b_rows || !out_a || !out_b)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  for (uint32_t i = 0; i < n; i++)
+    if (shard_ids[i] >= (uint32_t)db->nshards)
+      return fail(INSPIRE_ERR_SHARD_NOT_FOUND, "Shard " + std::to_string(shard_ids[i]) + " not found");
+  if (int rc = set_device(c)) return rc;
+  return run_tree(c, db, n, shard_ids, seeds + 32 * ELL, (size_t)64 * ELL, nullptr, b_rows + (size_t)ELL * poly_words(),
+                  2 * ELL, out_a, out_b, b_words);
+}
+
 
 int inspire_respond_seeded_nopacking_batch(inspire_ctx* c, const inspire_db* db, uint32_t n,
                                            const uint32_t* shard_ids, const uint8_t* seeds, const uint64_t* b_rows,
@@ -943,6 +968,19 @@ int inspire_client_keygen_device(inspire_ctx* c, const uint8_t* key, uint64_t fi
   a.sk = d_sk;
   a.y_body = d_y_body;
   CUDA_TRY(launch_client_keys(a, (int)n, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_galois_keygen_device(inspire_ctx* c, const uint8_t* key, const uint64_t* d_sk, uint64_t* d_keys,
+                                 int32_t* d_status, void* stream) {
+  if (!c || !key || !d_sk || !d_keys || !d_status) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  GaloisGenArgs a{};
+  if (int rc = client_tables(c, key, a)) return rc;
+  if (int rc = set_device(c)) return rc;
+  a.sk = d_sk;
+  a.keys = d_keys;
+  a.status = d_status;
+  CUDA_TRY(launch_galois_keys(a, LOGN, (cudaStream_t)stream));
   return INSPIRE_OK;
 }
 

@@ -13,6 +13,11 @@
 // generate_ksk_body :846-902): y_body[k] = tau_g(s) z^k - s w_mask[k] + e_k
 // with g = gen_pows[1] and w_mask the CRS mask of w_seed.
 //
+// galois_keys_kernel: the CRS's Galois key-switching matrices of setup
+// (src/pir/setup.rs:164-173; generate_automorphism_ks_matrix and
+// generate_ks_matrix, src/ks/setup.rs:118-162, 218-245): matrix i for
+// t = N / 2^i + 1, row k = (a, -a s + e + tau_t(s) z^k) with a uniform.
+//
 // Randomness: the crate draws seeds from thread_rng and errors from a
 // rejection sampler over ChaCha20.  Here both come from ChaCha20 keyed by a
 // caller key, each error coefficient a discrete Gaussian of the parameters'
@@ -22,6 +27,9 @@
 //     blocks 2^40 + (Q * 2 ELL + r) * 256 + j / 8          (Q < 2^36)
 //   client C: secret key from blocks 2^48 + C * 1024 + j / 8; y_body[k]
 //     errors from blocks 2^48 + C * 1024 + 256 (k + 1) + j / 8  (C < 2^30)
+//   Galois matrix i, row k (m = 3 i + k): a from the seed = first 8 words
+//     of block 2^52 + m (Poly::from_seed_moduli of it), errors from blocks
+//     2^52 + 2^20 + m * 256 + j / 8
 // The outputs are valid keys and queries (responses decrypt to the queried
 // entries) but are not the crate's random draws.
 #include "expand.cuh"
@@ -205,7 +213,96 @@ __global__ void __launch_bounds__(CT) client_keys_kernel(const __grid_constant__
   }
 }
 
+__global__ void __launch_bounds__(CT) galois_keys_kernel(const __grid_constant__ GaloisGenArgs A) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint64_t* cand = reinterpret_cast<uint64_t*>(smem);        // [N] expansion candidates
+  uint32_t* a0 = smem + 2 * N;                               // [2][N] a (residue 0, 1)
+  uint32_t* shat = a0 + 2 * N;                               // [2][N] NTT(s) * n^-1 2^32, slot layout
+  uint32_t* tau = shat + 2 * N;                              // [2][N] tau_t(s), residues
+  int32_t* err = reinterpret_cast<int32_t*>(tau + 2 * N);    // [N]
+  uint32_t* SC = reinterpret_cast<uint32_t*>(err + N);       // [2][NTT_SCRATCH]
+  uint64_t* cdt = reinterpret_cast<uint64_t*>(SC + 2 * NTT_SCRATCH);  // [MAX_CDT]
+  int* ws = reinterpret_cast<int*>(cdt + MAX_CDT);           // [20]
+  uint32_t* seed_w = reinterpret_cast<uint32_t*>(ws + 20);   // [8]
+  const DevParams& P = A.P;
+  const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
+  const int mi = blockIdx.x;                                 // matrix i: t = N / 2^i + 1
+  const uint32_t t = (uint32_t)(N >> mi) + 1u;
+  const uint32_t q = P.r[g].q, qinv = P.r[g].qinv;
+  const int cdt_len = A.cdt_len;
+  if (tid < MAX_CDT) cdt[tid] = A.cdt[tid];
+  if (tid == 0) A.status[mi] = 0;
+  uint32_t key[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) key[i] = A.key[i];
+  // tau_t(s) per residue (rlwe/galois.rs:22-55)
+  for (int c = tid; c < N; c += CT) {
+    const uint32_t j = ((uint32_t)c * t) & (2 * N - 1);
+#pragma unroll
+    for (int rr = 0; rr < 2; rr++) {
+      const uint32_t sv = (uint32_t)A.sk[(size_t)rr * N + c];
+      if (j < (uint32_t)N) tau[rr * N + j] = sv;
+      else tau[rr * N + j - N] = sv ? P.r[rr].q - sv : 0;
+    }
+  }
+  {
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = (uint32_t)A.sk[(size_t)g * N + x + 128 * j];
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      shat[g * N + 16 * x + j] = mul_shoup(v[j], P.r[g].ninv_mont, P.r[g].ninv_mont_p, q);
+  }
+  for (int k = 0; k < ELL; k++) {
+    const uint64_t m = (uint64_t)mi * ELL + (uint64_t)k;
+    __syncthreads();  // tau and shat complete; the previous row's buffers consumed
+    if (tid == 0) {
+      uint32_t w[16];
+      chacha20_block(key, (1ull << 52) + m, P.one, w);
+#pragma unroll
+      for (int i = 0; i < 8; i++) seed_w[i] = w[i];
+    }
+    gaussian8(key, (1ull << 52) + (1ull << 20) + m * (N / 8), P.one, cdt, cdt_len, tid, err);
+    __syncthreads();
+    const bool ok = expand_seeded_row<2>(P, reinterpret_cast<const uint8_t*>(seed_w), cand, a0, a0 + N, ws, 3, tid);
+    if (!ok && tid == 0) A.status[mi] = ERR_EXPAND;
+    __syncthreads();
+    uint64_t* row_a = A.keys + ((size_t)m * 2 + 0) * 2 * N + (size_t)g * N;
+    uint64_t* row_b = A.keys + ((size_t)m * 2 + 1) * 2 * N + (size_t)g * N;
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      v[j] = a0[g * N + x + 128 * j];
+      row_a[x + 128 * j] = v[j];
+    }
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[g]), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = redc_lazy((uint64_t)v[j] * shat[g * N + 16 * x + j], q, qinv);
+    ntt_inv_noscale(v, SC + g * NTT_SCRATCH, inv_tw(P.r[g]), q, x, 1 + g);
+    const uint32_t zp = A.zpow[g][k], zp_p = A.zpow_p[g][k];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int c = x + 128 * j;
+      uint32_t b = mul_shoup(tau[g * N + c], zp, zp_p, q);  // tau_t(s) z^k
+      b = sub_mod(b, canon2(v[j], q), q);                   // - a s
+      b = add_mod(b, signed_mod(err[c], q), q);
+      row_b[c] = b;
+    }
+  }
+}
+
 }  // namespace
+
+size_t galois_keys_smem_bytes() {
+  return sizeof(uint32_t) * ((size_t)2 * N + 2 * N + 2 * N + 2 * N + N + 2 * NTT_SCRATCH + 2 * MAX_CDT + 20 + 8);
+}
+
+cudaError_t launch_galois_keys(const GaloisGenArgs& a, int nmat, cudaStream_t st) {
+  if (nmat <= 0) return cudaSuccess;
+  galois_keys_kernel<<<nmat, CT, galois_keys_smem_bytes(), st>>>(a);
+  return cudaGetLastError();
+}
 
 size_t client_keys_smem_bytes() {
   return sizeof(uint32_t) * ((size_t)N + N + 2 * N + N + 2 * NTT_SCRATCH + 2 * MAX_CDT);
@@ -227,6 +324,9 @@ cudaError_t prepare_client_kernels() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(client_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)client_keys_smem_bytes());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(galois_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)galois_keys_smem_bytes());
   return e;
 }
 

@@ -101,6 +101,19 @@ struct KeyGenArgs {
   uint64_t* y_body;           // [n][ELL][2][N]
 };
 
+// Galois key-switching matrices of the secret key sk[2][N]: keys[i][k][a, b][2][N]
+// for i < nmat (t = N / 2^i + 1), k < ELL.
+struct GaloisGenArgs {
+  DevParams P;
+  uint32_t key[8];
+  uint32_t zpow[2][ELL], zpow_p[2][ELL];
+  uint64_t cdt[MAX_CDT];
+  int cdt_len;
+  const uint64_t* sk;
+  uint64_t* keys;
+  int* status;  // [nmat]
+};
+
 // Tree packing (respond_one_packing) of nq queries' column ciphertexts.
 struct TreeArgs {
   DevParams P;
@@ -128,6 +141,8 @@ size_t tree_work_words_per_query();
 cudaError_t prepare_tree_kernels();
 cudaError_t launch_pack_tree(const TreeArgs& a, cudaStream_t st);
 cudaError_t launch_galois_prep(const DevParams& P, const uint64_t* keys, int npolys, uint32_t* ks, cudaStream_t st);
+size_t galois_keys_smem_bytes();
+cudaError_t launch_galois_keys(const GaloisGenArgs& a, int nmat, cudaStream_t st);
 size_t client_keys_smem_bytes();
 cudaError_t launch_client_keys(const KeyGenArgs& a, int n, cudaStream_t st);
 

@@ -16,6 +16,7 @@ from .pir import (  # noqa: F401
     ServerCrs,
     ServerResponse,
     client_keygen_device,
+    galois_keygen_device,
     external_product_device,
     now_ns,
     ntt_forward_device,
@@ -31,6 +32,7 @@ from .pir import (  # noqa: F401
     respond_seeded_inspiring,
     respond_seeded_nopacking_batch,
     respond_seeded_packed,
+    respond_seeded_packed_batch,
     respond_seeded_with_variant,
     respond_with_variant,
 )

@@ -346,6 +346,23 @@ def respond_seeded_packed(crs: ServerCrs, encoded_db: EncodedDatabase, query: Se
     return _packed_response(out_a, out_b, words.value)
 
 
+def respond_seeded_packed_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int],
+                                seeds: np.ndarray, b_rows: np.ndarray):
+    """Batched respond_seeded_packed: (a (n, plen), b (n, words)) with words
+    plen, or 2*plen in compat mode with more than one column."""
+    n = len(shard_ids)
+    plen = crs.params.plen
+    sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+    sd = np.ascontiguousarray(seeds, dtype=np.uint8)
+    br = _u64(b_rows)
+    out_a = np.zeros((n, plen), dtype=np.uint64)
+    out_b = np.zeros((n, 2 * plen), dtype=np.uint64)
+    words = C.c_uint32(0)
+    _check(crs.L.inspire_respond_seeded_packed_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br),
+                                                     _ptr(out_a), _ptr(out_b), C.byref(words)))
+    return out_a, out_b[:, :words.value]
+
+
 def respond_seeded_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int],
                                    seeds: np.ndarray, b_rows: np.ndarray) -> np.ndarray:
     """Batched respond_seeded: (n, 2, plen) combined ciphertexts."""
@@ -469,6 +486,17 @@ def client_keygen_device(crs: ServerCrs, key: bytes, first_client: int, n: int, 
         raise ValueError("key must be 32 bytes")
     v = C.c_void_p
     _check(crs.L.inspire_client_keygen_device(crs.h, bytes(key), first_client, n, v(d_sk), v(d_y_body), v(stream)))
+
+
+def galois_keygen_device(crs: ServerCrs, key: bytes, d_sk: int, d_keys: int, d_status: int, stream: int) -> None:
+    """The log2(d) Galois key-switching matrices of the secret key at d_sk
+    (setup.rs:164-173), generated on the device from a ChaCha20 stream keyed
+    by `key`; d_keys [log2 d][6][2*ring_dim] (u64), d_status [log2 d] (i32);
+    asynchronous."""
+    if len(key) != 32:
+        raise ValueError("key must be 32 bytes")
+    v = C.c_void_p
+    _check(crs.L.inspire_galois_keygen_device(crs.h, bytes(key), v(d_sk), v(d_keys), v(d_status), v(stream)))
 
 
 def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, stream: int) -> int:

@@ -96,3 +96,68 @@ def test_tree_errors(tree):
         bare.load_galois_keys(bad)
     edb2.close()
     bare.close()
+
+
+def test_batch_equals_single(tree):
+    T = tree
+    inspire, client = T["inspire"], T["client"]
+    for mode in ("crt_fixed", "compat"):
+        crs, edb, db, shards = world(T, mode, 16)
+        idx = [(0, 17), (1, 600), (0, 2047)]
+        qs = [client.query_seeded(li) for _, li in idx]
+        a, b = inspire.respond_seeded_packed_batch(crs, edb, [s for s, _ in idx], np.stack([q[0] for q in qs]),
+                                                   np.stack([q[1] for q in qs]))
+        for k, (sid, li) in enumerate(idx):
+            one = inspire.respond_seeded_packed(crs, edb, inspire.SeededClientQuery(sid, *qs[k]))
+            assert np.array_equal(a[k], one.ciphertext.a) and np.array_equal(b[k], one.ciphertext.b)
+
+
+def test_galois_keygen_device(tree):
+    """Galois matrices made on the device: bit-exact against a CPU restatement
+    of the stream (matrix i for t = d / 2^i + 1, row k = (a, -a s + e +
+    tau_t(s) z^k), setup.rs:164-173, ks/setup.rs:118-162, 218-245), and tree
+    packing with them equals the oracle's with the same keys."""
+    from client_stream import gaussian_blocks
+
+    T = tree
+    torch, O, inspire, ctx = pytest.importorskip("torch"), T["O"], T["inspire"], T["ctx"]
+    key = bytes(range(7, 39))
+    dev = torch.device("cuda:0")
+    crs, edb, db, shards = world(T, "crt_fixed", 16)
+    sk = T["client"].sk
+    d_sk = torch.from_numpy(sk.view(np.int64).copy()).to(dev)
+    d_keys = torch.zeros((11, 6, 2 * N), dtype=torch.int64, device=dev)
+    d_st = torch.full((11,), -1, dtype=torch.int32, device=dev)
+    inspire.galois_keygen_device(crs, key, d_sk.data_ptr(), d_keys.data_ptr(), d_st.data_ptr(),
+                                 torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert not d_st.cpu().numpy().any()
+    keys = d_keys.cpu().numpy().view(np.uint64)
+    kw = np.frombuffer(key, dtype="<u4")
+    Q = (268369921, 249561089)
+    for i in (0, 5, 10):
+        tau = ctx.automorphism(sk, (N >> i) + 1)
+        for k in range(3):
+            m = 3 * i + k
+            w = O.chacha20_block(kw, [(2 ** 52 + m) & 0xFFFFFFFF, (2 ** 52 + m) >> 32, 0, 0])
+            a = ctx.poly_from_seed(w[:8].astype("<u4").tobytes())
+            assert np.array_equal(keys[i, 2 * k], a), (i, k)
+            e = gaussian_blocks(kw, 2 ** 52 + 2 ** 20 + m * (N // 8))
+            a_s = ctx.poly_mul(a, sk)
+            want = np.zeros(2 * N, np.uint64)
+            for r in range(2):
+                q = Q[r]
+                sl = slice(r * N, (r + 1) * N)
+                v = (tau[sl].astype(np.int64) * pow(1 << 20, k, q)) % q
+                v = (v - a_s[sl].astype(np.int64)) % q
+                want[sl] = ((v + e % q) % q).astype(np.uint64)
+            assert np.array_equal(keys[i, 2 * k + 1], want), (i, k)
+    crs2 = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
+    crs2.load_galois_keys(keys)
+    edb2 = inspire.EncodedDatabase(crs2, db, 32)
+    seeds, b_rows = T["client"].query_seeded(99)
+    want_a, want_b = ctx.respond_one_packing(shards[0], ctx.expand_rgsw(seeds, b_rows), keys, mode=O.MODE_CRT_FIXED)
+    got = inspire.respond_seeded_packed(crs2, edb2, inspire.SeededClientQuery(0, seeds, b_rows))
+    assert np.array_equal(got.ciphertext.a, want_a) and np.array_equal(got.ciphertext.b, want_b)
+    edb2.close()
+    crs2.close()
