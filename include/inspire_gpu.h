@@ -365,6 +365,25 @@ int inspire_external_product_device(inspire_ctx *ctx, const uint32_t *d_ct, cons
 int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, const uint64_t *d_ct, uint32_t n,
                                      uint32_t entry_size, uint8_t *d_entries, void *stream);
 
+/* Allocation-free tree packing on device buffers; no reference counterpart.
+ * Answers n <= 2 seeded queries like inspire_respond_seeded_packed_batch, but
+ * takes device pointers (d_shard_ids [n], d_seeds [n][gadget_len][32] and
+ * d_b_rows [n][gadget_len][poly] of RGSW rows gadget_len..2*gadget_len-1,
+ * as inspire_respond_seeded_batch_device takes them; d_out_a [n][poly],
+ * d_out_b [n][2 polys], d_status [n]) and enqueues its work on `stream`
+ * without allocating: its scratch (column ciphertexts, combined ciphertext,
+ * the tree's work area; 1.3 MiB per query) is one static device array per
+ * device, located once with cudaGetSymbolAddress.  n > 2 is rejected.
+ * Calls that overlap on the device (from several host threads, or on
+ * streams that run concurrently) race on that array: issue them on one
+ * stream, or wait for one to finish before the next starts.  A query whose
+ * status is nonzero has undefined outputs.  *b_words is set as for the
+ * other tree-packing calls. */
+int inspire_respond_seeded_packed_noalloc_device(inspire_ctx *ctx, const inspire_db *db, uint32_t n,
+                                                 const uint32_t *d_shard_ids, const uint8_t *d_seeds,
+                                                 const uint64_t *d_b_rows, uint64_t *d_out_a, uint64_t *d_out_b,
+                                                 int32_t *d_status, uint32_t *b_words, void *stream);
+
 /* Setup side: the log2(ring_dim) Galois key-switching matrices of the
  * secret key d_sk [poly] (ServerCrs.galois_keys, src/pir/setup.rs:164-173;
  * generate_automorphism_ks_matrix, src/ks/setup.rs:218-245): matrix i for

@@ -971,6 +971,55 @@ int inspire_client_keygen_device(inspire_ctx* c, const uint8_t* key, uint64_t fi
   return INSPIRE_OK;
 }
 
+int inspire_respond_seeded_packed_noalloc_device(inspire_ctx* c, const inspire_db* db, uint32_t n,
+                                                 const uint32_t* d_shard_ids, const uint8_t* d_seeds,
+                                                 const uint64_t* d_b_rows, uint64_t* d_out_a, uint64_t* d_out_b,
+                                                 int32_t* d_status, uint32_t* b_words, void* stream) {
+  if (!c || !db || !b_words || (n && (!d_shard_ids || !d_seeds || !d_b_rows || !d_out_a || !d_out_b || !d_status)))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (n > (uint32_t)TREE_NOALLOC_MAX_QUERIES)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT,
+                "at most " + std::to_string(TREE_NOALLOC_MAX_QUERIES) + " queries per allocation-free call");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  if (!c->has_galois) return fail(INSPIRE_ERR_NO_CRS, "no Galois keys loaded (inspire_crs_load_galois_keys)");
+  const size_t pw = poly_words();
+  *b_words = (c->mode == MODE_COMPAT && db->gamma > 1) ? (uint32_t)(2 * pw) : (uint32_t)pw;
+  if (n == 0) return INSPIRE_OK;
+  if (int rc = set_device(c)) return rc;
+  void* scratch = nullptr;
+  CUDA_TRY(tree_noalloc_scratch(c->device, &scratch));
+  // carve: columns [n][gamma][2][poly] u64, combined [n][2][poly] u64, tree work (u32)
+  uint64_t* cols = static_cast<uint64_t*>(scratch);
+  uint64_t* comb = cols + (size_t)n * db->gamma * 2 * pw;
+  uint32_t* work = reinterpret_cast<uint32_t*>(comb + (size_t)n * 2 * pw);
+  NoPackingArgs a{};
+  a.P = c->P;
+  a.nq = (int)n;
+  a.shard = d_shard_ids;
+  a.seeds = d_seeds;
+  a.arows = nullptr;
+  a.brows = d_b_rows;
+  a.nshards = db->nshards;
+  a.H = db->H.as<uint16_t>();
+  a.out = comb;
+  a.out_columns = cols;
+  a.status = d_status;
+  CUDA_TRY(launch_nopacking(a, true, (cudaStream_t)stream));
+  TreeArgs t{};
+  t.P = c->P;
+  t.nq = (int)n;
+  t.ncols = db->gamma;
+  t.mode = c->mode;
+  t.cols = cols;
+  t.ks = c->galois.as<uint32_t>();
+  t.work = work;
+  t.out_a = d_out_a;
+  t.out_b = d_out_b;
+  CUDA_TRY(launch_pack_tree(t, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
 int inspire_galois_keygen_device(inspire_ctx* c, const uint8_t* key, const uint64_t* d_sk, uint64_t* d_keys,
                                  int32_t* d_status, void* stream) {
   if (!c || !key || !d_sk || !d_keys || !d_status) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");

@@ -136,6 +136,11 @@ cudaError_t prepare_client_kernels();
 
 size_t query_gen_smem_bytes();
 cudaError_t launch_query_gen(const QueryGenArgs& a, int n, cudaStream_t st);
+// Allocation-free tree packing: a static device array holds the scratch of
+// up to TREE_NOALLOC_MAX_QUERIES queries.
+constexpr int TREE_NOALLOC_MAX_QUERIES = 2;
+size_t tree_noalloc_query_bytes();
+cudaError_t tree_noalloc_scratch(int device, void** ptr);
 size_t tree_smem_bytes();
 size_t tree_work_words_per_query();
 cudaError_t prepare_tree_kernels();

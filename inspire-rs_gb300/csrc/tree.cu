@@ -24,6 +24,8 @@
 // and inverse-transform the a / b products and write node = s0 + out.
 // Ciphertexts of the tree live in a per-query global work area (8 buffers of
 // 2 polys x 2 residues, L2-resident); the key switch works in shared memory.
+#include <mutex>
+
 #include "kernels.h"
 
 namespace ig {
@@ -259,7 +261,31 @@ __global__ void __launch_bounds__(BLOCK) galois_prep_kernel(const DevParams P, c
   for (int j = 0; j < 16; j++) ks[((size_t)p * 2 + g) * N + 16 * x + j] = mul_shoup(v[j], C.ninv_mont, C.ninv_mont_p, C.q);
 }
 
+// Static scratch of the allocation-free tree-packing entry: per query the
+// column ciphertexts (MAX_GAMMA columns, u64), the combined NoPacking
+// ciphertext (u64) and the tree's work area (u32).
+constexpr size_t NOALLOC_QUERY_BYTES =
+    sizeof(uint64_t) * ((size_t)MAX_GAMMA * 2 * 2 * N + 2 * 2 * N) + sizeof(uint32_t) * (size_t)8 * CT_WORDS;
+__device__ __align__(256) unsigned char g_tree_noalloc_scratch[TREE_NOALLOC_MAX_QUERIES * NOALLOC_QUERY_BYTES];
+
 }  // namespace
+
+size_t tree_noalloc_query_bytes() { return NOALLOC_QUERY_BYTES; }
+
+// Device address of the static scratch on the current device, looked up once
+// per device (the symbol has one instance per device context).
+cudaError_t tree_noalloc_scratch(int device, void** ptr) {
+  static std::mutex mu;
+  static void* addr[64] = {};
+  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[device]) {
+    cudaError_t e = cudaGetSymbolAddress(&addr[device], g_tree_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+  }
+  *ptr = addr[device];
+  return cudaSuccess;
+}
 
 size_t tree_smem_bytes() { return sizeof(uint32_t) * (size_t)S_TOTAL; }
 size_t tree_work_words_per_query() { return (size_t)8 * CT_WORDS; }

@@ -488,6 +488,21 @@ def client_keygen_device(crs: ServerCrs, key: bytes, first_client: int, n: int, 
     _check(crs.L.inspire_client_keygen_device(crs.h, bytes(key), first_client, n, v(d_sk), v(d_y_body), v(stream)))
 
 
+def respond_seeded_packed_noalloc_device(crs: ServerCrs, encoded_db: EncodedDatabase, n: int, d_shard_ids: int,
+                                         d_seeds: int, d_b_rows: int, d_out_a: int, d_out_b: int, d_status: int,
+                                         stream: int) -> int:
+    """Tree packing of n <= 2 seeded queries on device buffers without
+    allocating (static device scratch; overlapping calls race on it, see
+    include/inspire_gpu.h); asynchronous on `stream`.  Returns the b words
+    per query."""
+    v = C.c_void_p
+    words = C.c_uint32(0)
+    _check(crs.L.inspire_respond_seeded_packed_noalloc_device(crs.h, encoded_db.h, n, v(d_shard_ids), v(d_seeds),
+                                                              v(d_b_rows), v(d_out_a), v(d_out_b), v(d_status),
+                                                              C.byref(words), v(stream)))
+    return words.value
+
+
 def galois_keygen_device(crs: ServerCrs, key: bytes, d_sk: int, d_keys: int, d_status: int, stream: int) -> None:
     """The log2(d) Galois key-switching matrices of the secret key at d_sk
     (setup.rs:164-173), generated on the device from a ChaCha20 stream keyed
