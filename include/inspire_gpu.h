@@ -110,6 +110,13 @@ void inspire_db_destroy(inspire_db *db);
  * equals inspire_db_create on the raw entries the files encode. */
 int inspire_db_load_shards(inspire_ctx *ctx, const char *dir, inspire_db **out);
 
+/* The server's encoded_db.json (src/bin/server.rs:292-301): serde_json of
+ * EncodedDatabase {shards: [ShardData {id, polynomials: [Poly]}], config:
+ * ShardConfig} (src/pir/setup.rs:104-120, src/params.rs:432-450) made
+ * resident like inspire_db_create.  Shard ids must be 0, 1, ... in order,
+ * each with the CRS's num_columns polynomials of encoded 16-bit columns. */
+int inspire_db_load_json(inspire_ctx *ctx, const char *json, size_t len, inspire_db **out);
+
 /* Write a resident database as the crate's binary shard files into `dir`
  * (which must exist), in save_shards_binary's format, with the moduli of
  * `params`. */

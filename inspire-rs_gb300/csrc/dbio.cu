@@ -95,6 +95,41 @@ std::string read_shard(const std::string& path, uint32_t want_id, const inspire_
 
 }  // namespace
 
+namespace ighost {
+
+// A resident database from host raw columns Hh[nshards][gamma][N] (gamma = the
+// context's CRS columns): upload, then the contracted form on the GPU.
+int db_from_host_columns(inspire_ctx* c, const uint16_t* Hh, int nshards, uint64_t n_entries, uint32_t entry_size,
+                         inspire_db** out) {
+  const int gamma = c->gamma;
+  inspire_db* db = new inspire_db();
+  db->ctx = c;
+  db->device = c->device;
+  db->gamma = gamma;
+  db->nshards = nshards;
+  db->n_entries = n_entries;
+  db->entry_size = entry_size;
+  if (nshards > 0) {
+    cudaError_t e = db->H.ensure(sizeof(uint16_t) * (size_t)nshards * gamma * N);
+    if (e == cudaSuccess) e = db->E.ensure(sizeof(uint32_t) * (size_t)nshards * 2 * ELL * gamma * N);
+    if (e != cudaSuccess) {
+      delete db;
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, "database allocation failed");
+    }
+    e = cudaMemcpy(db->H.p, Hh, sizeof(uint16_t) * (size_t)nshards * gamma * N, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_encode_E(c->P, db->H.as<uint16_t>(), nshards, db->E.as<uint32_t>(), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      delete db;
+      return fail(INSPIRE_ERR_CUDA, std::string("database upload / encode: ") + cudaGetErrorString(e));
+    }
+  }
+  *out = db;
+  return INSPIRE_OK;
+}
+
+}  // namespace ighost
+
 extern "C" {
 
 int inspire_db_load_shards(inspire_ctx* c, const char* dir, inspire_db** out) {

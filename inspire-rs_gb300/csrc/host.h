@@ -104,6 +104,10 @@ namespace ighost {
 
 inline size_t poly_words() { return (size_t)2 * N; }
 
+// dbio.cu: a resident database from host raw columns [nshards][gamma][N].
+int db_from_host_columns(inspire_ctx* c, const uint16_t* Hh, int nshards, uint64_t n_entries, uint32_t entry_size,
+                         inspire_db** out);
+
 inline int sync_client_table(inspire_ctx* c) {
   if (!c->client_table_dirty) return INSPIRE_OK;
   // grown in steps of 256 entries: a reallocation (which waits for the

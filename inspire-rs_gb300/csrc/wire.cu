@@ -472,4 +472,76 @@ int inspire_server_response_to_bincode(const inspire_params* P, const uint64_t* 
   return copy_out(s, reinterpret_cast<char*>(buf), cap, len);
 }
 
+int inspire_db_load_json(inspire_ctx* c, const char* json, size_t len, inspire_db** out) {
+  if (!c || !json || !out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  *out = nullptr;
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  const int gamma = c->gamma;
+  const inspire_params& P = c->params;
+  Json j{json, json + len, "", json};
+  std::vector<uint16_t> H;
+  std::vector<uint64_t> poly(2 * (size_t)N);
+  uint64_t entry_size = 0, total_entries = 0;
+  bool have_shards = false, have_config = false;
+  int nshards = 0;
+  const bool ok = j.object([&](const std::string& k) {
+    if (k == "shards") {
+      have_shards = true;
+      return j.array([&](size_t) {
+        uint64_t id = ~0ull;
+        int npolys = 0;
+        const bool sok = j.object([&](const std::string& f) {
+          if (f == "id") return j.u64(id);
+          if (f == "polynomials") {
+            return j.array([&](size_t) {
+              const std::string what = "shard " + std::to_string(nshards) + " polynomial " + std::to_string(npolys);
+              if (npolys >= gamma) return j.fail(what + ": the CRS packs " + std::to_string(gamma) + " columns");
+              if (!parse_poly(j, P, poly.data(), what)) return false;
+              H.resize((size_t)(nshards + 1) * gamma * N);
+              uint16_t* dst = H.data() + ((size_t)nshards * gamma + npolys) * N;
+              for (int i = 0; i < N; i++) {
+                if (poly[i] >= 65536 || poly[N + i] != poly[i])
+                  return j.fail(what + ": not an encoded 16-bit column (coefficient " + std::to_string(i) + ")");
+                dst[i] = (uint16_t)poly[i];
+              }
+              npolys++;
+              return true;
+            });
+          }
+          return j.skip();
+        });
+        if (!sok) return false;
+        if (id != (uint64_t)nshards) return j.fail("shard ids must be 0, 1, ... in order");
+        if (npolys != gamma)
+          return j.fail("shard " + std::to_string(nshards) + ": " + std::to_string(npolys) +
+                        " polynomials, the CRS packs " + std::to_string(gamma));
+        if (nshards == 0x7fffffff) return j.fail("too many shards");
+        nshards++;
+        return true;
+      });
+    }
+    if (k == "config") {
+      have_config = true;
+      return j.object([&](const std::string& f) {
+        if (f == "entry_size_bytes") return j.u64(entry_size);
+        if (f == "total_entries") return j.u64(total_entries);
+        return j.skip();  // shard_size_bytes
+      });
+    }
+    return j.skip();
+  });
+  if (ok) j.ws();
+  if (!ok || j.p != j.end)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT,
+                "EncodedDatabase JSON: " + (j.err.empty() ? std::string("trailing characters") : j.err));
+  if (!have_shards || !have_config) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "EncodedDatabase JSON: missing shards or config");
+  if ((entry_size * 8 + 15) / 16 != (uint64_t)gamma)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ceil(entry_size/2) must equal the CRS num_columns");
+  if (total_entries > (uint64_t)nshards * N)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "total_entries exceeds the shards' capacity");
+  if (int rc = set_device(c)) return rc;
+  return db_from_host_columns(c, H.data(), nshards, total_entries, (uint32_t)entry_size, out);
+}
+
 }  // extern "C"

@@ -209,6 +209,19 @@ class EncodedDatabase:
         _check(crs.L.inspire_db_load_shards(crs.h, str(directory).encode(), C.byref(h)))
         return cls(crs, b"", 2 * crs.inspiring_num_columns, _handle=h)
 
+    @classmethod
+    def load_json(cls, crs: ServerCrs, encoded_db_json) -> "EncodedDatabase":
+        """Load the server's encoded_db.json (serde_json of EncodedDatabase,
+        server.rs:292-301) -- a path or the JSON bytes -- into HBM."""
+        data = encoded_db_json
+        if isinstance(data, str):
+            with open(data, "rb") as f:
+                data = f.read()
+        data = bytes(data)
+        h = C.c_void_p()
+        _check(crs.L.inspire_db_load_json(crs.h, data, len(data), C.byref(h)))
+        return cls(crs, b"", 2 * crs.inspiring_num_columns, _handle=h)
+
     def save_shards(self, directory: str) -> None:
         """Write this database as the crate's binary shard files."""
         pc = self.crs.params.to_c()

@@ -142,3 +142,59 @@ def test_loader_errors(world, tmp_path):
         inspire.respond_seeded_batch(W["crs"], db, sids, seeds, brows, [W["cid"]])
     with pytest.raises(inspire.PirError, match="cannot open"):
         inspire.EncodedDatabase.load_shards(W["crs"], tmp_path / "nope")
+
+
+def encoded_db_json(shards, entry_size, total_entries, ids=None, indent=None):
+    """serde_json of EncodedDatabase (pir/setup.rs:104-120, params.rs:432-450)
+    with Poly's derive (math/poly.rs:64-77): the server's encoded_db.json."""
+    import json
+
+    qc = Q[0] * Q[1]
+
+    def poly(p):
+        return {"coeffs": [int(x) for x in p], "moduli": list(Q), "q": qc, "dim": N,
+                "crt_q0_inv_mod_q1": pow(Q[0], Q[1] - 2, Q[1]), "is_ntt": False}
+
+    obj = {"shards": [{"id": (ids[s] if ids else s), "polynomials": [poly(p) for p in sh]}
+                      for s, sh in enumerate(shards)],
+           "config": {"shard_size_bytes": N * entry_size, "entry_size_bytes": entry_size,
+                      "total_entries": total_entries}}
+    return json.dumps(obj, indent=indent, separators=None if indent else (",", ":")).encode()
+
+
+def test_encoded_db_json_answers_like_raw(world):
+    """encoded_db.json (server.rs:292-301) loaded into HBM answers bit for
+    bit like the database built from the raw entries."""
+    W = world
+    inspire, crs, raw = W["inspire"], W["crs"], W["raw"]
+    n_entries = raw.size // ENTRY
+    loaded = inspire.EncodedDatabase.load_json(crs, encoded_db_json(W["shards"], ENTRY, n_entries, indent=1))
+    built = inspire.EncodedDatabase(crs, raw, ENTRY)
+    assert loaded.num_shards == 4
+    sids, seeds, brows = queries(W, [0, N + 5, 3 * N + 122, 2 * N + 2047])
+    got = inspire.respond_seeded_batch(crs, loaded, sids, seeds, brows, [W["cid"]] * 4)
+    want = inspire.respond_seeded_batch(crs, built, sids, seeds, brows, [W["cid"]] * 4)
+    assert np.array_equal(got, want)
+    loaded.close()
+    built.close()
+
+
+def test_encoded_db_json_rejects(world):
+    W = world
+    inspire, crs, raw = W["inspire"], W["crs"], W["raw"]
+    n_entries = raw.size // ENTRY
+    sh = W["shards"][:2]
+    with pytest.raises(inspire.PirError, match="in order"):
+        inspire.EncodedDatabase.load_json(crs, encoded_db_json(sh, ENTRY, 2 * N, ids=[1, 0]))
+    bad = [sh[0].copy(), sh[1]]
+    bad[0][3, N + 7] = (int(bad[0][3, 7]) + 1) % Q[1]  # residues of one coefficient disagree
+    with pytest.raises(inspire.PirError, match="encoded 16-bit column"):
+        inspire.EncodedDatabase.load_json(crs, encoded_db_json(bad, ENTRY, 2 * N))
+    with pytest.raises(inspire.PirError, match="polynomials"):
+        inspire.EncodedDatabase.load_json(crs, encoded_db_json([sh[0][:15]], ENTRY, N))
+    with pytest.raises(inspire.PirError, match="num_columns"):
+        inspire.EncodedDatabase.load_json(crs, encoded_db_json(sh, 8, 2 * N))
+    with pytest.raises(inspire.PirError, match="capacity"):
+        inspire.EncodedDatabase.load_json(crs, encoded_db_json(sh, ENTRY, 2 * N + 1))
+    with pytest.raises(inspire.PirError, match="EncodedDatabase JSON"):
+        inspire.EncodedDatabase.load_json(crs, encoded_db_json(sh, ENTRY, 2 * N)[:-3])
