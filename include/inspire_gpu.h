@@ -110,6 +110,19 @@ void inspire_db_destroy(inspire_db *db);
  * equals inspire_db_create on the raw entries the files encode. */
 int inspire_db_load_shards(inspire_ctx *ctx, const char *dir, inspire_db **out);
 
+/* The loaded CRS's inspiring_w_seed (32 bytes), inspiring_num_columns, and
+ * whether Galois keys are loaded. */
+int inspire_crs_info(inspire_ctx *ctx, uint8_t *w_seed, uint32_t *num_columns, int32_t *has_galois_keys);
+
+/* The server's crs.json (src/bin/server.rs:255-264): serde_json of ServerCrs
+ * (src/pir/setup.rs:52-87).  params must equal the context's; the InspiRING
+ * part (inspiring_w_seed, inspiring_num_columns) is loaded as
+ * inspire_crs_load does and galois_keys, if present, as
+ * inspire_crs_load_galois_keys; the other fields (k_g, k_h, crs_a_vectors,
+ * packing_k_*, inspiring_precomp, ...) are not read by the Respond paths and
+ * are skipped. */
+int inspire_crs_load_json(inspire_ctx *ctx, const char *json, size_t len);
+
 /* The server's encoded_db.json (src/bin/server.rs:292-301): serde_json of
  * EncodedDatabase {shards: [ShardData {id, polynomials: [Poly]}], config:
  * ShardConfig} (src/pir/setup.rs:104-120, src/params.rs:432-450) made

@@ -700,6 +700,16 @@ int inspire_respond(inspire_ctx* c, const inspire_db* db, const inspire_query* q
   return run_nopacking(c, db, 1, &qy->shard_id, nullptr, 0, ar.data(), br.data(), ELL, out_ct, out_columns);
 }
 
+int inspire_crs_info(inspire_ctx* c, uint8_t* w_seed, uint32_t* num_columns, int32_t* has_galois_keys) {
+  if (!c || !w_seed || !num_columns || !has_galois_keys) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
+  memcpy(w_seed, c->w_seed, 32);
+  *num_columns = (uint32_t)c->gamma;
+  *has_galois_keys = c->has_galois ? 1 : 0;
+  return INSPIRE_OK;
+}
+
 int inspire_crs_load_galois_keys(inspire_ctx* c, const uint64_t* keys, uint32_t nkeys) {
   if (!c || !keys) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   if (nkeys != (uint32_t)LOGN)

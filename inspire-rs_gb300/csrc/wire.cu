@@ -472,6 +472,94 @@ int inspire_server_response_to_bincode(const inspire_params* P, const uint64_t* 
   return copy_out(s, reinterpret_cast<char*>(buf), cap, len);
 }
 
+int inspire_crs_load_json(inspire_ctx* c, const char* json, size_t len) {
+  if (!c || !json) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  const inspire_params P = c->params;
+  Json j{json, json + len, "", json};
+  uint8_t w_seed[32] = {};
+  size_t nseed = 0;
+  uint64_t num_columns = 0;
+  bool have_seed = false, have_cols = false, have_params = false;
+  std::vector<uint64_t> keys;  // [matrix][row][a, b][poly]
+  size_t nmat = 0;
+  const size_t pw = 2 * (size_t)P.ring_dim;
+  const bool ok = j.object([&](const std::string& k) {
+    if (k == "params") {
+      have_params = true;
+      uint64_t ring_dim = 0, q = 0, p = 0, gbase = 0, glen = 0;
+      uint64_t mod[3] = {0, 0, 0};
+      size_t nmod = 0;
+      const bool pok = j.object([&](const std::string& f) {
+        if (f == "ring_dim") return j.u64(ring_dim);
+        if (f == "q") return j.u64(q);
+        if (f == "crt_moduli") return j.u64_array_into(mod, 3, &nmod);
+        if (f == "p") return j.u64(p);
+        if (f == "gadget_base") return j.u64(gbase);
+        if (f == "gadget_len") return j.u64(glen);
+        return j.skip();  // sigma, security_level
+      });
+      if (!pok) return false;
+      if (ring_dim != P.ring_dim || nmod != 2 || mod[0] != P.crt_moduli[0] || mod[1] != P.crt_moduli[1] ||
+          p != P.p || gbase != P.gadget_base || glen != P.gadget_len)
+        return j.fail("params differ from the context's");
+      return true;
+    }
+    if (k == "galois_keys") {
+      return j.array([&](size_t) {  // KeySwitchingMatrix {rows, gadget}
+        size_t nrows = 0;
+        keys.resize((nmat + 1) * 2 * ELL * pw);
+        const bool mok = j.object([&](const std::string& f) {
+          if (f == "rows") {
+            return j.array([&](size_t) {  // RlweCiphertext {a, b}
+              if (nrows >= (size_t)ELL) return j.fail("a Galois key has more than gadget_len rows");
+              const bool rok = j.object([&](const std::string& g) {
+                if (g == "a" || g == "b") {
+                  uint64_t* dst = keys.data() + ((nmat * ELL + nrows) * 2 + (g == "b")) * pw;
+                  return parse_poly(j, P, dst, "Galois key " + std::to_string(nmat) + " row " + std::to_string(nrows));
+                }
+                return j.skip();
+              });
+              nrows++;
+              return rok;
+            });
+          }
+          return j.skip();  // gadget
+        });
+        if (!mok) return false;
+        if (nrows != (size_t)ELL) return j.fail("a Galois key has fewer than gadget_len rows");
+        nmat++;
+        return true;
+      });
+    }
+    if (k == "inspiring_w_seed") {
+      have_seed = true;
+      uint64_t v[32];
+      if (!j.u64_array_into(v, 32, &nseed)) return false;
+      for (size_t i = 0; i < nseed; i++) {
+        if (v[i] > 255) return j.fail("inspiring_w_seed bytes must be < 256");
+        w_seed[i] = (uint8_t)v[i];
+      }
+      return nseed == 32 || j.fail("inspiring_w_seed must hold 32 bytes");
+    }
+    if (k == "inspiring_num_columns") {
+      have_cols = true;
+      return j.u64(num_columns);
+    }
+    return j.skip();  // k_g, k_h, rgsw_gadget, crs_a_vectors, packing_k_*, inspiring_precomp, inspiring_v_seed
+  });
+  if (ok) j.ws();
+  if (!ok || j.p != j.end)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ServerCrs JSON: " + (j.err.empty() ? std::string("trailing characters") : j.err));
+  if (!have_params || !have_seed || !have_cols)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ServerCrs JSON: missing params, inspiring_w_seed or inspiring_num_columns");
+  if (num_columns > 0xffffffffull) return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path supports num_columns in {1, 2, 4, 8, 16}");
+  if (int rc = inspire_crs_load(c, w_seed, (uint32_t)num_columns)) return rc;
+  // galois_keys is empty in CRSs made without tree packing; a tree-packing
+  // call then reports the missing keys
+  if (nmat > 0) return inspire_crs_load_galois_keys(c, keys.data(), (uint32_t)nmat);
+  return INSPIRE_OK;
+}
+
 int inspire_db_load_json(inspire_ctx* c, const char* json, size_t len, inspire_db** out) {
   if (!c || !json || !out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   std::lock_guard<std::mutex> lk(c->mu);

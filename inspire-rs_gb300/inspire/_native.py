@@ -109,6 +109,8 @@ def load(path: str = LIB_PATH):
         "inspire_db_destroy": (None, [vp]),
         "inspire_db_load_shards": (C.c_int, [vp, C.c_char_p, C.POINTER(vp)]),
         "inspire_db_load_json": (C.c_int, [vp, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
+        "inspire_crs_load_json": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
+        "inspire_crs_info": (C.c_int, [vp, vp, C.POINTER(u32), C.POINTER(i32)]),
         "inspire_db_save_shards": (C.c_int, [vp, C.POINTER(InspireParamsC), C.c_char_p]),
         "inspire_db_num_shards": (u32, [vp]),
         "inspire_db_device_bytes": (u64, [vp]),

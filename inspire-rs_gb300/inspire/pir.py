@@ -122,11 +122,9 @@ class ServerCrs:
     residues (the responses decrypt)."""
 
     def __init__(self, params: InspireParams, inspiring_w_seed: bytes, inspiring_num_columns: int,
-                 mode: str = "crt_fixed", device: int = 0):
+                 mode: str = "crt_fixed", device: int = 0, _crs_json: Optional[bytes] = None):
         self.L = nat.load()
         self.params = params
-        self.inspiring_w_seed = bytes(inspiring_w_seed)
-        self.inspiring_num_columns = int(inspiring_num_columns)
         self.mode = mode
         if mode not in ("compat", "crt_fixed"):
             raise ValueError("mode must be 'compat' or 'crt_fixed'")
@@ -136,8 +134,28 @@ class ServerCrs:
                                          C.byref(h)))
         self.h = h
         _LIVE_CRS.add(self)
-        seed = (C.c_uint8 * 32).from_buffer_copy(self.inspiring_w_seed)
-        _check(self.L.inspire_crs_load(self.h, C.cast(seed, C.c_void_p), self.inspiring_num_columns))
+        if _crs_json is not None:
+            _check(self.L.inspire_crs_load_json(self.h, _crs_json, len(_crs_json)))
+            seed = (C.c_uint8 * 32)()
+            cols, galois = C.c_uint32(0), C.c_int32(0)
+            _check(self.L.inspire_crs_info(self.h, C.cast(seed, C.c_void_p), C.byref(cols), C.byref(galois)))
+            inspiring_w_seed, inspiring_num_columns = bytes(seed), cols.value
+        self.inspiring_w_seed = bytes(inspiring_w_seed)
+        self.inspiring_num_columns = int(inspiring_num_columns)
+        if _crs_json is None:
+            seed = (C.c_uint8 * 32).from_buffer_copy(self.inspiring_w_seed)
+            _check(self.L.inspire_crs_load(self.h, C.cast(seed, C.c_void_p), self.inspiring_num_columns))
+
+    @classmethod
+    def load_json(cls, params: InspireParams, crs_json, mode: str = "crt_fixed", device: int = 0) -> "ServerCrs":
+        """The server's crs.json (serde_json of ServerCrs, setup.rs:52-87) --
+        a path or the JSON bytes: the InspiRING seed and column count, and
+        the Galois keys if present; params must match."""
+        data = crs_json
+        if isinstance(data, str):
+            with open(data, "rb") as f:
+                data = f.read()
+        return cls(params, b"", 0, mode=mode, device=device, _crs_json=bytes(data))
 
     def close(self):
         if getattr(self, "h", None):

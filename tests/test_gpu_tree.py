@@ -161,3 +161,59 @@ def test_galois_keygen_device(tree):
     assert np.array_equal(got.ciphertext.a, want_a) and np.array_equal(got.ciphertext.b, want_b)
     edb2.close()
     crs2.close()
+
+
+def crs_json(keys, w_seed, num_columns, p=1 << 16):
+    """serde_json of ServerCrs (pir/setup.rs:52-87) as the server's crs.json:
+    the fields the Respond paths read, plus small stand-ins for the others."""
+    import json
+
+    Q = (268369921, 249561089)
+    qc = Q[0] * Q[1]
+    gadget = {"base": 1 << 20, "len": 3, "q": qc}
+
+    def poly(c):
+        return {"coeffs": [int(x) for x in c], "moduli": list(Q), "q": qc, "dim": N,
+                "crt_q0_inv_mod_q1": pow(Q[0], Q[1] - 2, Q[1]), "is_ntt": False}
+
+    def ksm(mat):
+        return {"rows": [{"a": poly(mat[2 * k]), "b": poly(mat[2 * k + 1])} for k in range(3)], "gadget": gadget}
+
+    obj = {"params": {"ring_dim": N, "q": qc, "crt_moduli": list(Q), "p": p, "sigma": 6.4, "gadget_base": 1 << 20,
+                      "gadget_len": 3, "security_level": "Bits128"},
+           "k_g": ksm(keys[0]), "k_h": ksm(keys[1]),
+           "galois_keys": [ksm(m) for m in keys],
+           "rgsw_gadget": gadget, "crs_a_vectors": [[1, 2, 3], [4, 5, 6]],
+           "packing_k_g": None, "packing_k_h": None, "inspiring_precomp": None,
+           "inspiring_w_seed": list(w_seed), "inspiring_v_seed": list(range(32)),
+           "inspiring_num_columns": num_columns}
+    return json.dumps(obj, separators=(",", ":")).encode()
+
+
+def test_crs_json_load(tree):
+    """crs.json (server.rs:255-264) loaded into a context answers like a
+    context loaded field by field: InspiRING with registered keys and tree
+    packing with the Galois keys."""
+    T = tree
+    O, inspire, ctx, client = T["O"], T["inspire"], T["ctx"], T["client"]
+    crs, edb, db, shards = world(T, "crt_fixed", 16)
+    params = inspire.InspireParams(p=1 << 16)
+    loaded = inspire.ServerCrs.load_json(params, crs_json(T["keys"], W_SEED, 16), mode="crt_fixed")
+    assert loaded.inspiring_w_seed == W_SEED and loaded.inspiring_num_columns == 16
+    edb2 = inspire.EncodedDatabase(loaded, db, 32)
+    pack = O.Pack(ctx, 16, W_SEED, mode=O.MODE_CRT_FIXED)
+    y_body, _ = client.packing_keys(pack)
+    seeds, b_rows = client.query_seeded(321)
+    q = inspire.SeededClientQuery(1, seeds, b_rows, inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body))
+    a = inspire.respond_seeded_inspiring(loaded, edb2, q)
+    b = inspire.respond_seeded_inspiring(crs, edb, q)
+    assert np.array_equal(a.ciphertext.a, b.ciphertext.a) and np.array_equal(a.ciphertext.b, b.ciphertext.b)
+    ta = inspire.respond_seeded_packed(loaded, edb2, inspire.SeededClientQuery(1, seeds, b_rows))
+    tb = inspire.respond_seeded_packed(crs, edb, inspire.SeededClientQuery(1, seeds, b_rows))
+    assert np.array_equal(ta.ciphertext.a, tb.ciphertext.a) and np.array_equal(ta.ciphertext.b, tb.ciphertext.b)
+    with pytest.raises(inspire.PirError, match="params differ"):
+        inspire.ServerCrs.load_json(params, crs_json(T["keys"], W_SEED, 16, p=65537))
+    with pytest.raises(inspire.PirError, match="ServerCrs JSON"):
+        inspire.ServerCrs.load_json(params, crs_json(T["keys"], W_SEED, 16)[:-2])
+    edb2.close()
+    loaded.close()
