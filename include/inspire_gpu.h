@@ -247,8 +247,9 @@ int inspire_respond_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n, co
 
 /* Same on device buffers, asynchronous on `stream`.  seeds holds only rows
  * gadget_len..2*gadget_len-1 ([n][gadget_len][32]) and b_rows only those rows
- * ([n][gadget_len][poly]); d_status[n] receives 0 or a nonzero kernel status
- * (unknown shard or client id, exhausted expansion bound). */
+ * ([n][gadget_len][poly], 16-byte aligned); d_status[n] receives 0 or a
+ * nonzero kernel status (unknown shard or client id, exhausted expansion
+ * bound). */
 int inspire_respond_seeded_batch_device(inspire_ctx *ctx, const inspire_db *db, uint32_t n,
                                         const uint32_t *d_shard_ids, const uint8_t *d_seeds,
                                         const uint64_t *d_b_rows, const int32_t *d_client_ids, uint64_t *d_out_ct,

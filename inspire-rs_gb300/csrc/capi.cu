@@ -853,6 +853,8 @@ int inspire_respond_seeded_batch_device(inspire_ctx* c, const inspire_db* db, ui
                                         uint64_t* d_out_ct, int32_t* d_status, void* stream) {
   if (!c || !db || (n && (!d_shard_ids || !d_seeds || !d_b_rows || !d_client_ids || !d_out_ct || !d_status)))
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (reinterpret_cast<uintptr_t>(d_b_rows) % 16)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "d_b_rows must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(c->mu);
   if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
   if (int rc = set_device(c)) return rc;

@@ -34,22 +34,23 @@ namespace ig {
 
 namespace {
 
-// b0_c for every column c and residue (see file comment).  bp (6N words) is
-// scratch; bpoly[r * 16 + c] receives the result.  Warp c handles column c:
+// b0_c for every column c and residue (see file comment).  rows holds the
+// query's rows ELL..2ELL-1 (b polys, u64; device memory or staged in shared
+// memory); bp (6N words) is scratch; bpoly[r * 16 + c] receives the result.
+// Warp c handles column c:
 // lane l takes the coefficient pairs i = 2 (l + 32 m) + {0, 1}, reading the
 // raw column as u32 pairs and the staged rows as 64-bit words, so every
 // shared-memory read of a warp covers 256 contiguous bytes (no bank
 // conflicts).  Each lane issues its column loads 16 at a time, so the column
 // costs two memory latencies.
-__device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* __restrict__ brows,
-                          uint32_t* bp, uint32_t* bpoly) {
+__device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* rows, uint32_t* bp,
+                          uint32_t* bpoly) {
   const int tid = threadIdx.x, gamma = P.gamma;
   const int lane = tid & 31, c = tid >> 5;
 #pragma unroll 8
   for (int idx = tid; idx < ELL * 2 * N; idx += RBLOCK) {
     const int i = idx & (N - 1), tr = idx >> LOGN, r = tr & 1;
-    const uint64_t* row = brows + (size_t)tr * N;
-    uint32_t v = (uint32_t)__ldcg(row + (i == 0 ? 0 : N - i));  // rows may be in host memory
+    uint32_t v = (uint32_t)rows[(size_t)tr * N + (i == 0 ? 0 : N - i)];
     if (i != 0 && v != 0) v = P.r[r].q - v;
     bp[idx] = v;
   }
@@ -113,6 +114,14 @@ __device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
   }
 }
 
+// 16-byte asynchronous copy global -> shared (the source may be mapped host
+// memory); completed by cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // R_i (NTT domain, scaled by n^-1) of packing_offline step 1 for one residue,
 // scattered to dst[slot]: source slot u contributes to slot s with
 // 2brv(s)+1 = h_i (2brv(u)+1) mod 2n, where h_i = g^-i
@@ -145,6 +154,7 @@ struct Smem {
   static constexpr int SCAT = T + 3 * N;                   // [2][N] R_i (slot layout, swizzled)
   static constexpr int PB = SCAT + 2 * N;                  // [2][2][N] partial products of digits 1, 2
   static constexpr int ACC = PB + 4 * N;                   // [RG][N] per-group b accumulators
+  // SCAT..ACC (12N words) also hold the query's raw b rows (u64) until the b side
   static constexpr int MISC = ACC + RG * N;                // bpoly[32], ws[3][20], staged seeds (96 B)
   static constexpr int TOTAL = MISC + 128;
 };
@@ -191,32 +201,43 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
   const uint64_t* brows = QDB ? D->brows : A.brows + (size_t)qi * ELL * 2 * N;
 
-  // stream what the b side reads (raw columns, query b rows) into L2 first;
-  // the contracted shard and the client key table follow once the b side is
-  // done, during the compute-bound row expansion, so that the burst of a
-  // whole launch's prefetches does not delay the b side's loads.  (Rows in
-  // host memory are not prefetched.)
+  // Serving loop (rows in host memory): the query's b rows (96 KiB) are
+  // copied asynchronously into shared memory (SCAT..ACC) while the rows are
+  // expanded, so the host link's latency stays off the critical path, and the
+  // b side follows the row NTTs.  Rows in device memory: the b side comes
+  // first, reading them directly, with the raw columns and rows streamed into
+  // L2 ahead of it and the contracted shard and client keys after it.
+  uint64_t* raw = reinterpret_cast<uint64_t*>(SCAT);  // 16-byte aligned
+  if (QDB) {
+    const uint4* src = reinterpret_cast<const uint4*>(brows);
+#pragma unroll
+    for (int k = 0; k < ELL * 2 * N / 2 / RBLOCK; k++) {
+      const int chunk = tid + RBLOCK * k;
+      cp_async16(raw + 2 * chunk, src + chunk);
+    }
+  }
   if (tid == 0) {
     prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
     if (!QDB) prefetch_l2(brows, sizeof(uint64_t) * (size_t)ELL * 2 * N);
   }
   // seeds in host memory: staged into shared memory (ordered before the
-  // expansion by the b side's barriers)
+  // expansion by the barrier below)
   uint8_t* seed_sm = reinterpret_cast<uint8_t*>(smem + L::MISC + 96);
   if (QDB && tid < ELL * 32) seed_sm[tid] = __ldcv(D->seeds + tid);
-
-  // ---- b part of the column products (bp aliases SCAT+PB) ----
-  column_b0(P, H, brows, SCAT, bpoly);
-
-  // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
+  if (!QDB) column_b0(P, H, brows, SCAT, bpoly);  // bp aliases SCAT+PB
   if (tid == 0) {
     prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
     if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
   }
+  if (QDB) __syncthreads();
+
+  // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
   {
     const int t = tid >> 8, lt = tid & 255;
     uint64_t* cand = reinterpret_cast<uint64_t*>(SC) + t * N;  // 3 x 16 KiB within SC
-    uint32_t* a0 = T + t * 2 * N;                               // 3 x 16 KiB within T..PB
+    // serving loop: in place of the row's transforms (SCAT..ACC hold the
+    // staged rows); otherwise within T..PB
+    uint32_t* a0 = QDB ? Ahat + t * NR * N : T + t * 2 * N;
     uint32_t* a1 = a0 + N;
     if (SEEDED) {
       const uint8_t* seed = QDB ? seed_sm + 32 * t : A.seeds + ((size_t)qi * ELL + t) * 32;
@@ -227,12 +248,13 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
       for (int j = lt; j < NR * N; j += SUB) a0[j] = (uint32_t)ar[j];  // a1 follows a0
     }
   }
+  if (QDB) cp_async_wait_all();
   __syncthreads();
   // the query's status is written once, by one thread
   if (tid == 0) *status_ptr() = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
   if (r < NR) {  // group (r, t=kd) transforms row kd, residue r
     uint32_t v[16];
-    const uint32_t* src = T + kd * 2 * N + r * N;
+    const uint32_t* src = QDB ? Ahat + (kd * NR + r) * N : T + kd * 2 * N + r * N;
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = src[x + 128 * j];
     ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
@@ -241,6 +263,9 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
     store16(Ahat + (kd * NR + r) * N, x, v);
   }
   __syncthreads();
+
+  // ---- serving loop: b part of the column products (bp in SC, rows staged) ----
+  if (QDB) column_b0(P, H, raw, SC, bpoly);
 
   // scatter roles: fixed mode -> groups (r,1),(r,2) do residue r;
   // compat -> groups with digit 1, 2 of both residues do residue 0
