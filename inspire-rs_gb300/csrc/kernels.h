@@ -10,6 +10,7 @@ namespace ig {
 
 constexpr int ERR_EXPAND = 1;  // seeded expansion exceeded its iteration bound
 constexpr int ERR_INDEX = 2;   // shard or client id out of range
+constexpr int ERR_STAGE = 3;   // the query's rows did not arrive in shared memory within the wait bound
 
 // One resident database as the Respond kernel sees it.
 struct DbView {

@@ -114,13 +114,43 @@ __device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
   }
 }
 
-// 16-byte asynchronous copy global -> shared (the source may be mapped host
-// memory); completed by cp_async_wait_all.
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
-  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// mbarrier with one arrival, visible to the bulk-copy (async) proxy.
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// The single arrival, announcing `bytes` of bulk copies to complete.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+// from global memory -- device or mapped host memory -- into this CTA's shared
+// memory, completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Wait, with an iteration bound, for phase `parity` of `bar` to complete;
+// false when the bound ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 20); it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 
 // R_i (NTT domain, scaled by n^-1) of packing_offline step 1 for one residue,
 // scattered to dst[slot]: source slot u contributes to slot s with
@@ -202,19 +232,16 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   const uint64_t* brows = QDB ? D->brows : A.brows + (size_t)qi * ELL * 2 * N;
 
   // Serving loop (rows in host memory): the query's b rows (96 KiB) are
-  // copied asynchronously into shared memory (SCAT..ACC) while the rows are
+  // bulk-copied (TMA) into shared memory (SCAT..ACC) while the rows are
   // expanded, so the host link's latency stays off the critical path, and the
   // b side follows the row NTTs.  Rows in device memory: the b side comes
   // first, reading them directly, with the raw columns and rows streamed into
   // L2 ahead of it and the contracted shard and client keys after it.
-  uint64_t* raw = reinterpret_cast<uint64_t*>(SCAT);  // 16-byte aligned
-  if (QDB) {
-    const uint4* src = reinterpret_cast<const uint4*>(brows);
-#pragma unroll
-    for (int k = 0; k < ELL * 2 * N / 2 / RBLOCK; k++) {
-      const int chunk = tid + RBLOCK * k;
-      cp_async16(raw + 2 * chunk, src + chunk);
-    }
+  uint64_t* raw = reinterpret_cast<uint64_t*>(SCAT);           // 16-byte aligned
+  uint64_t* rbar = reinterpret_cast<uint64_t*>(smem + L::MISC + 120);  // the rows' mbarrier
+  if (QDB && tid == 0) {
+    mbar_init(rbar);
+    wsb[18] = 0;  // set when the rows do not arrive
   }
   if (tid == 0) {
     prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
@@ -229,7 +256,14 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
     prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
     if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
   }
-  if (QDB) __syncthreads();
+  if (QDB) {
+    __syncthreads();  // the mbarrier is initialised, the seeds staged
+    if (tid == 0) {
+      mbar_expect_tx(rbar, (uint32_t)(sizeof(uint64_t) * ELL * 2 * N));
+#pragma unroll
+      for (int p = 0; p < 2 * ELL; p++) bulk_g2s(raw + (size_t)p * N, brows + (size_t)p * N, sizeof(uint64_t) * N, rbar);
+    }
+  }
 
   // ---- rows ELL..2ELL-1: expand (one sub-block per row), forward NTT ----
   {
@@ -248,8 +282,18 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
       for (int j = lt; j < NR * N; j += SUB) a0[j] = (uint32_t)ar[j];  // a1 follows a0
     }
   }
-  if (QDB) cp_async_wait_all();
+  if (QDB) {
+    // rows that never arrive (the bound ran out) end the query with a status,
+    // after a second bounded wait for the copies still in flight
+    const bool arrived = mbar_wait(rbar, 0);
+    if (!arrived) wsb[18] = 1;
+  }
   __syncthreads();
+  if (QDB && wsb[18]) {
+    mbar_wait(rbar, 0);
+    if (tid == 0) *status_ptr() = ERR_STAGE;
+    return;  // uniform over the CTA
+  }
   // the query's status is written once, by one thread
   if (tid == 0) *status_ptr() = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
   if (r < NR) {  // group (r, t=kd) transforms row kd, residue r
