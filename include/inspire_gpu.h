@@ -289,10 +289,11 @@ int inspire_server_create(inspire_ctx *ctx, const inspire_server_config *cfg, in
 /* Waits for batches in flight, then frees the loop.  Unpolled tickets die. */
 void inspire_server_destroy(inspire_server *srv);
 
-/* Submission flag: read the query rows in place instead of copying them.
- * seeds and b_rows must then lie in page-locked host memory (for instance
- * from inspire_pinned_alloc) with b_rows 16-byte aligned, and must stay
- * unchanged until every ticket of the call has been collected. */
+/* Submission flag: read the query b rows in place instead of copying them.
+ * b_rows must then lie in page-locked host memory (for instance from
+ * inspire_pinned_alloc), 16-byte aligned; seeds and b_rows must stay
+ * unchanged until every ticket of the call has been collected (the seeds are
+ * read when the query's batch is launched). */
 #define INSPIRE_SUBMIT_BORROW 1u
 
 /* Submit n seeded InspiRING queries; query i asks database dbs[i] (any

@@ -20,11 +20,12 @@ struct DbView {
   int pad;
 };
 
-// One admitted query of the serving loop.  The descriptor itself is copied to
-// device memory per batch; the rows and the response live in pinned host
-// memory that the Respond kernel reads and writes directly.
+// One admitted query of the serving loop.  The descriptor itself -- with the
+// query's seeds inline -- is copied to device memory per batch; the rows and
+// the response live in pinned host memory that the Respond kernel reads and
+// writes directly.
 struct QueryDesc {
-  const uint8_t* seeds;   // [ELL][32] seeds of rows ELL..2ELL-1
+  uint8_t seeds[ELL * 32];  // seeds of rows ELL..2ELL-1
   const uint64_t* brows;  // [ELL][2][N] b-polys of rows ELL..2ELL-1 (16-byte aligned)
   uint64_t* out;          // [2][2][N] response destination (16-byte aligned)
   int32_t* status;        // kernel status destination

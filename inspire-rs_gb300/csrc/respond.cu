@@ -247,10 +247,10 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
     prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
     if (!QDB) prefetch_l2(brows, sizeof(uint64_t) * (size_t)ELL * 2 * N);
   }
-  // seeds in host memory: staged into shared memory (ordered before the
-  // expansion by the barrier below)
+  // the seeds, inline in the query's descriptor: staged into shared memory
+  // (ordered before the expansion by the barrier below)
   uint8_t* seed_sm = reinterpret_cast<uint8_t*>(smem + L::MISC + 96);
-  if (QDB && tid < ELL * 32) seed_sm[tid] = __ldcv(D->seeds + tid);
+  if (QDB && tid < ELL * 32) seed_sm[tid] = D->seeds[tid];
   if (!QDB) column_b0(P, H, brows, SCAT, bpoly);  // bp aliases SCAT+PB
   if (tid == 0) {
     prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);

@@ -48,7 +48,7 @@ enum RecState { FREE = 0, PENDING = 1, INFLIGHT = 2, DONE = 3, COLLECTING = 4 };
 struct Rec {
   uint64_t gen = 1;
   RecState state = FREE;
-  const uint8_t* seeds = nullptr;   // device-accessible rows: the pool record's or borrowed
+  const uint8_t* seeds = nullptr;   // host rows: the pool record's or borrowed
   const uint64_t* brows = nullptr;
   const inspire_db* db = nullptr;
   uint32_t shard = 0;
@@ -99,7 +99,7 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
     const Rec& r = recs[batch[k]];
     uint8_t* p = dev_rec_ptr(batch[k]);
     QueryDesc& d = s.desc[k];
-    d.seeds = r.seeds;
+    memcpy(d.seeds, r.seeds, sizeof(d.seeds));
     d.brows = r.brows;
     d.out = reinterpret_cast<uint64_t*>(p + REC_OUT);
     d.status = reinterpret_cast<int32_t*>(p + REC_STATUS);
@@ -324,16 +324,16 @@ int inspire_server_submit(inspire_server* s, uint32_t n, const inspire_db* const
   if (flags & ~INSPIRE_SUBMIT_BORROW) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "unknown submit flags");
   const bool borrow = flags & INSPIRE_SUBMIT_BORROW;
   const size_t pw = poly_words();
-  const uint8_t* d_seeds = nullptr;
+  // borrowed b rows are read in place by the GPU; the seeds (96 bytes per
+  // query) are copied into the batch's descriptors by the dispatcher
   const uint8_t* d_brows = nullptr;
   if (borrow && n) {
     // pointer attributes are looked up in this thread's current context
     if (int rc = set_device(s->ctx)) return rc;
     if (reinterpret_cast<uintptr_t>(b_rows) % 16)
       return fail(INSPIRE_ERR_INVALID_ARGUMENT, "borrowed b_rows must be 16-byte aligned");
-    d_seeds = mapped_range(seeds, (size_t)n * 64 * ELL);
     d_brows = mapped_range(b_rows, sizeof(uint64_t) * (size_t)n * 2 * ELL * pw);
-    if (!d_seeds || !d_brows)
+    if (!d_brows)
       return fail(INSPIRE_ERR_INVALID_ARGUMENT, "borrowed query rows must lie in page-locked host memory");
   }
   const int64_t t_submit = now_ns();
@@ -383,13 +383,13 @@ int inspire_server_submit(inspire_server* s, uint32_t n, const inspire_db* const
     const size_t so = (size_t)k * 64 * ELL + 32 * ELL;                        // bytes into seeds
     const size_t bo = sizeof(uint64_t) * ((size_t)k * 2 * ELL + ELL) * pw;    // bytes into b_rows
     if (borrow) {
-      r.seeds = d_seeds + so;
+      r.seeds = seeds + so;
       r.brows = reinterpret_cast<const uint64_t*>(d_brows + bo);
     } else {
       uint8_t* p = s->rec_ptr(got[k]);
       memcpy(p + REC_SEEDS, seeds + so, 32 * ELL);
       memcpy(p + REC_BROWS, reinterpret_cast<const uint8_t*>(b_rows) + bo, sizeof(uint64_t) * ELL * pw);
-      r.seeds = s->dev_rec_ptr(got[k]) + REC_SEEDS;
+      r.seeds = p + REC_SEEDS;
       r.brows = reinterpret_cast<const uint64_t*>(s->dev_rec_ptr(got[k]) + REC_BROWS);
     }
     r.db = dbs[k];

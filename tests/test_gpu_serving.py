@@ -179,9 +179,10 @@ def test_serving_errors_and_tickets(world):
 def test_device_budget_limits_streams(world):
     W = world
     inspire = W["inspire"]
-    # in-flight device memory per batch: one 64-byte descriptor per query (the
-    # rows and responses stay in pinned host memory)
-    one_batch = 8 * 64
+    # in-flight device memory per batch: one 152-byte descriptor per query
+    # (96 bytes of seeds inline; the rows and responses stay in pinned host
+    # memory)
+    one_batch = 8 * 152
     srv = inspire.Server(W["crs"], max_batch=8, max_inflight=4, capacity=32, device_budget=2 * one_batch + 10)
     assert srv.stats()["streams"] == 2
     srv.close()
