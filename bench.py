@@ -475,6 +475,33 @@ def main():
         torch.cuda.synchronize()
         value_graph = B * L * args.steps / (sum(a.elapsed_time(b) for a, b in gev) / 1e3)
 
+    # capped grid: one launch per step answers all L * B queries with one CTA
+    # per SM, each CTA taking queries in turn (no idle SMs until the last round)
+    value_grid = None
+    if ws == 1 and nb % L == 0:
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        flat = lambda t: t.view(-1, *t.shape[2:])
+        f_shard, f_seeds, f_brows = flat(d_shard), flat(d_seeds), flat(d_brows)
+        f_client, f_out, f_status = flat(d_client), flat(d_out), flat(d_status)
+
+        def grid_step(k):
+            b0 = (k * L) % nb * B
+            inspire.respond_seeded_batch_device(crs, edb, L * B, f_shard[b0].data_ptr(), f_seeds[b0].data_ptr(),
+                                                f_brows[b0].data_ptr(), f_client[b0].data_ptr(), f_out[b0].data_ptr(),
+                                                f_status[b0].data_ptr(), sp, max_ctas=n_sm)
+
+        for k in range(args.warmup):
+            grid_step(k)
+        torch.cuda.synchronize()
+        gev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            gev2[k][0].record(stream)
+            grid_step(k)
+            gev2[k][1].record(stream)
+        torch.cuda.synchronize()
+        value_grid = L * B * args.steps / (sum(a.elapsed_time(b) for a, b in gev2) / 1e3)
+
     # correctness of what was timed: statuses, then every response of the nb
     # pool batches decrypted and extracted on the device with its client's key
     # must equal its database entry
@@ -633,6 +660,7 @@ def main():
             "gpu_launches": args.steps * L,
             "verified_responses": verified,
             "value_cuda_graph": value_graph,
+            "value_capped_grid": value_grid,
             "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
             "plain_single_query_qps": sweep.get("1"),

@@ -255,6 +255,14 @@ int inspire_respond_seeded_batch_device(inspire_ctx *ctx, const inspire_db *db, 
                                         const uint64_t *d_b_rows, const int32_t *d_client_ids, uint64_t *d_out_ct,
                                         int32_t *d_status, void *stream);
 
+/* The same with the grid capped at max_ctas CTAs (0: one CTA per query):
+ * CTA b answers queries b, b + max_ctas, ... in turn, so one call can answer
+ * a large batch with one CTA per SM and no SM idles until the last round. */
+int inspire_respond_seeded_batch_device_grid(inspire_ctx *ctx, const inspire_db *db, uint32_t n,
+                                             const uint32_t *d_shard_ids, const uint8_t *d_seeds,
+                                             const uint64_t *d_b_rows, const int32_t *d_client_ids,
+                                             uint64_t *d_out_ct, int32_t *d_status, uint32_t max_ctas, void *stream);
+
 /* ---- Serving loop ----
  * The crate serves each HTTP request with one synchronous respond call on a
  * tokio worker (src/bin/server.rs:179-236).  The serving loop replaces that

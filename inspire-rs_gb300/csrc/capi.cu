@@ -851,10 +851,19 @@ int inspire_respond_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, cons
 int inspire_respond_seeded_batch_device(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* d_shard_ids,
                                         const uint8_t* d_seeds, const uint64_t* d_b_rows, const int32_t* d_client_ids,
                                         uint64_t* d_out_ct, int32_t* d_status, void* stream) {
+  return inspire_respond_seeded_batch_device_grid(c, db, n, d_shard_ids, d_seeds, d_b_rows, d_client_ids, d_out_ct,
+                                                  d_status, 0, stream);
+}
+
+int inspire_respond_seeded_batch_device_grid(inspire_ctx* c, const inspire_db* db, uint32_t n,
+                                             const uint32_t* d_shard_ids, const uint8_t* d_seeds,
+                                             const uint64_t* d_b_rows, const int32_t* d_client_ids, uint64_t* d_out_ct,
+                                             int32_t* d_status, uint32_t max_ctas, void* stream) {
   if (!c || !db || (n && (!d_shard_ids || !d_seeds || !d_b_rows || !d_client_ids || !d_out_ct || !d_status)))
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   if (reinterpret_cast<uintptr_t>(d_b_rows) % 16)
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "d_b_rows must be 16-byte aligned");
+  if (max_ctas > 0x7fffffffu) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "max_ctas out of range");
   std::lock_guard<std::mutex> lk(c->mu);
   if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
   if (int rc = set_device(c)) return rc;
@@ -875,7 +884,7 @@ int inspire_respond_seeded_batch_device(inspire_ctx* c, const inspire_db* db, ui
   a.what = c->what.as<uint32_t>();
   a.out = d_out_ct;
   a.status = d_status;
-  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream));
+  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream, (int)max_ctas));
   return INSPIRE_OK;
 }
 

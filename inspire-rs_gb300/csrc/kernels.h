@@ -157,7 +157,8 @@ size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);
 
 size_t respond_smem_bytes(int mode);
-cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st);
+// max_ctas > 0 caps the grid: each CTA then answers several queries in turn.
+cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st, int max_ctas = 0);
 
 // setup-time kernels
 cudaError_t launch_columns_from_raw(const uint8_t* raw, uint64_t n_entries, int entry_size,

@@ -189,8 +189,9 @@ struct Smem {
   static constexpr int TOTAL = MISC + 128;
 };
 
+// One query (index qi) by the whole CTA; every return is uniform over the CTA.
 template <int MODE, bool SEEDED, bool QDB>
-__global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constant__ RespondArgs A) {
+__device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
   using L = Smem<NR>;
   extern __shared__ __align__(16) uint32_t smem[];
@@ -203,7 +204,6 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   int* wsb = (int*)(smem + L::MISC + 32);
 
   const DevParams& P = A.P;
-  const int qi = blockIdx.x;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
   const int r = g / 3, kd = g - 3 * r;  // residue, gadget digit of this group
   uint32_t* ACC = smem + L::ACC + g * N;  // this group's b accumulator
@@ -466,6 +466,23 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constan
   }
 }
 
+// One query per CTA.
+template <int MODE, bool SEEDED, bool QDB>
+__global__ void __launch_bounds__(RBLOCK, 1) respond_kernel(const __grid_constant__ RespondArgs A) {
+  respond_one<MODE, SEEDED, QDB>(A, blockIdx.x);
+}
+
+// Capped grid (device-resident rows): CTA b answers queries b, b + gridDim.x,
+// ... in turn, so a grid of one CTA per SM keeps every SM busy to the end of
+// a large batch.
+template <int MODE, bool SEEDED>
+__global__ void __launch_bounds__(RBLOCK, 1) respond_kernel_loop(const __grid_constant__ RespondArgs A) {
+  for (int qi = blockIdx.x; qi < A.nq; qi += gridDim.x) {
+    if (qi != (int)blockIdx.x) __syncthreads();  // the previous query's shared memory is no longer read
+    respond_one<MODE, SEEDED, false>(A, qi);
+  }
+}
+
 }  // namespace
 
 size_t respond_smem_bytes(int mode) {
@@ -474,16 +491,23 @@ size_t respond_smem_bytes(int mode) {
 
 template <int MODE, bool SEEDED, bool QDB>
 static cudaError_t set_smem_attr() {
-  return cudaFuncSetAttribute(respond_kernel<MODE, SEEDED, QDB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)respond_smem_bytes(MODE));
+  cudaError_t e = cudaFuncSetAttribute(respond_kernel<MODE, SEEDED, QDB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)respond_smem_bytes(MODE));
+  if (e == cudaSuccess && !QDB)
+    e = cudaFuncSetAttribute(respond_kernel_loop<MODE, SEEDED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)respond_smem_bytes(MODE));
+  return e;
 }
 
 // Launches issue no configuration call (so they can be captured in a CUDA
 // graph): the shared-memory attribute of every variant is set once per
 // device by prepare_respond_kernels.
 template <int MODE, bool SEEDED, bool QDB>
-static cudaError_t launch_one(const RespondArgs& a, cudaStream_t st) {
-  respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
+static cudaError_t launch_one(const RespondArgs& a, int ctas, cudaStream_t st) {
+  if (!QDB && ctas < a.nq)
+    respond_kernel_loop<MODE, SEEDED><<<ctas, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
+  else
+    respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
   return cudaGetLastError();
 }
 
@@ -499,14 +523,16 @@ cudaError_t prepare_respond_kernels() {
 }
 
 template <int MODE>
-static cudaError_t launch_mode(const RespondArgs& a, bool seeded, cudaStream_t st) {
-  if (a.qdesc) return seeded ? launch_one<MODE, true, true>(a, st) : launch_one<MODE, false, true>(a, st);
-  return seeded ? launch_one<MODE, true, false>(a, st) : launch_one<MODE, false, false>(a, st);
+static cudaError_t launch_mode(const RespondArgs& a, bool seeded, int ctas, cudaStream_t st) {
+  if (a.qdesc) return seeded ? launch_one<MODE, true, true>(a, ctas, st) : launch_one<MODE, false, true>(a, ctas, st);
+  return seeded ? launch_one<MODE, true, false>(a, ctas, st) : launch_one<MODE, false, false>(a, ctas, st);
 }
 
-cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st) {
+cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st, int max_ctas) {
   if (a.nq <= 0) return cudaSuccess;
-  return a.P.mode == MODE_COMPAT ? launch_mode<MODE_COMPAT>(a, seeded, st) : launch_mode<MODE_CRT_FIXED>(a, seeded, st);
+  const int ctas = (max_ctas > 0 && max_ctas < a.nq) ? max_ctas : a.nq;
+  return a.P.mode == MODE_COMPAT ? launch_mode<MODE_COMPAT>(a, seeded, ctas, st)
+                                 : launch_mode<MODE_CRT_FIXED>(a, seeded, ctas, st);
 }
 
 }  // namespace ig

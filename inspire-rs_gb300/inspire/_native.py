@@ -124,6 +124,7 @@ def load(path: str = LIB_PATH):
         "inspire_respond_seeded_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp]),
         "inspire_respond_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp]),
         "inspire_respond_seeded_batch_device": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp]),
+        "inspire_respond_seeded_batch_device_grid": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp, u32, vp]),
         "inspire_server_config_default": (None, [C.POINTER(ServerConfigC)]),
         "inspire_server_create": (C.c_int, [vp, C.POINTER(ServerConfigC), C.POINTER(vp)]),
         "inspire_server_destroy": (None, [vp]),

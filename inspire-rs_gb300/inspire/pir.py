@@ -467,9 +467,16 @@ def respond_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequen
 
 
 def respond_seeded_batch_device(crs: ServerCrs, encoded_db: EncodedDatabase, n: int, d_shard_ids: int, d_seeds: int,
-                                d_b_rows: int, d_client_ids: int, d_out: int, d_status: int, stream: int) -> None:
-    """Device-buffer batch (raw device pointers as ints); asynchronous."""
+                                d_b_rows: int, d_client_ids: int, d_out: int, d_status: int, stream: int,
+                                max_ctas: int = 0) -> None:
+    """Device-buffer batch (raw device pointers as ints); asynchronous.
+    max_ctas > 0 caps the grid (each CTA then answers several queries)."""
     v = C.c_void_p
+    if max_ctas:
+        _check(crs.L.inspire_respond_seeded_batch_device_grid(crs.h, encoded_db.h, n, v(d_shard_ids), v(d_seeds),
+                                                              v(d_b_rows), v(d_client_ids), v(d_out), v(d_status),
+                                                              max_ctas, v(stream)))
+        return
     _check(crs.L.inspire_respond_seeded_batch_device(crs.h, encoded_db.h, n, v(d_shard_ids), v(d_seeds), v(d_b_rows),
                                                      v(d_client_ids), v(d_out), v(d_status), v(stream)))
 

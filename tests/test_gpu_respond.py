@@ -296,3 +296,37 @@ def test_unseeded_batch_equals_single(world):
         want = oracle_response(W, "crt_fixed", ix // N, rg[k].reshape(12, 2 * N), y_body=y_body)
         assert np.array_equal(out[k], want)
     crs.release_client(cid)
+
+
+def test_batch_device_capped_grid(world):
+    """inspire_respond_seeded_batch_device_grid: with the grid capped below
+    the batch each CTA answers several queries in turn; the responses equal
+    the one-CTA-per-query call's."""
+    W = world
+    torch = pytest.importorskip("torch")
+    inspire, client = W["inspire"], W["client"]
+    crs, edb, pack, omode = W["w"]["crt_fixed"]
+    y_body, _ = client.packing_keys(pack)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+    idxs = [3, 2050, 4101, 78, 1999, 4995, 11]
+    n = len(idxs)
+    seeds = np.zeros((n, 6, 32), np.uint8)
+    brows = np.zeros((n, 6, 2 * N), np.uint64)
+    for k, ix in enumerate(idxs):
+        seeds[k], brows[k] = client.query_seeded(ix % N)
+    want = inspire.respond_seeded_batch(crs, edb, [ix // N for ix in idxs], seeds, brows, [cid] * n)
+    dev = torch.device("cuda", 0)
+    d_sid = torch.tensor([ix // N for ix in idxs], dtype=torch.int32, device=dev)
+    d_seeds = torch.from_numpy(np.ascontiguousarray(seeds[:, 3:6])).to(dev)
+    d_brows = torch.from_numpy(np.ascontiguousarray(brows[:, 3:6]).view(np.int64)).to(dev)
+    d_cid = torch.full((n,), cid, dtype=torch.int32, device=dev)
+    for ctas in (1, 3, 7, 100):
+        d_out = torch.zeros((n, 2, 2 * N), dtype=torch.int64, device=dev)
+        d_st = torch.full((n,), -1, dtype=torch.int32, device=dev)
+        inspire.respond_seeded_batch_device(crs, edb, n, d_sid.data_ptr(), d_seeds.data_ptr(), d_brows.data_ptr(),
+                                            d_cid.data_ptr(), d_out.data_ptr(), d_st.data_ptr(),
+                                            torch.cuda.current_stream().cuda_stream, max_ctas=ctas)
+        torch.cuda.synchronize()
+        assert not d_st.cpu().numpy().any(), ctas
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), ctas
+    crs.release_client(cid)
