@@ -16,14 +16,16 @@
 // gadget digits (base 2^20, 3 digits) of tau_t(a), and
 //   out = (sum_k digit_k * K[k].a, tau_t(b) + sum_k digit_k * K[k].b).
 //
-// One CTA of 768 threads (six groups: CRT residue r x digit k) per query.
-// Per combine: [K1] every thread gathers s1 for its source coefficients,
+// Two kernels, 768 threads per CTA (six groups: CRT residue r x digit k):
+// the per-LWE chains of levels 1..7 run one CTA per (query, LWE), side by
+// side; then one CTA per query combines levels 8..11.  Per combine: [K1] every thread gathers s1 for its source coefficients,
 // applies tau_t (a scattered write in shared memory) and splits the
 // composite coefficient into digits; [K3] group (r,k) transforms digit k mod
 // q_r and multiplies it into both key parts; [K4] groups (r,0) / (r,1) sum
 // and inverse-transform the a / b products and write node = s0 + out.
-// Ciphertexts of the tree live in a per-query global work area (8 buffers of
-// 2 polys x 2 residues, L2-resident); the key switch works in shared memory.
+// Ciphertexts of the tree live in a per-query global work area (22 buffers
+// of 2 polys x 2 residues, L2-resident); the key switch works in shared
+// memory.
 #include <mutex>
 
 #include "kernels.h"
@@ -159,6 +161,28 @@ __device__ void combine(const TreeArgs& A, uint32_t* sm, const uint32_t* E, cons
   __syncthreads();
 }
 
+// Work area of one query: buffers 0..15 hold the level-7 node of each LWE
+// (its key-switch chain), 16-17 level 8, 18-19 level 9, 20-21 level 10.
+constexpr int TREE_BUFS = 22;
+
+// Levels 1..7 for one LWE: node(l, s) = node(l-1, s) + homomorphic_automorph
+// (its odd child is absent), one CTA per (query, LWE), so the 16 chains of a
+// query run side by side.
+__global__ void __launch_bounds__(TT, 1) tree_chain_kernel(const __grid_constant__ TreeArgs A) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int nreal = A.ncols;
+  const int qi = blockIdx.x / nreal, leaf = blockIdx.x - qi * nreal, tid = threadIdx.x;
+  const uint64_t* ca = A.cols + ((size_t)qi * nreal + leaf) * 2 * 2 * N;  // the column's a, residues
+  uint32_t* c = A.work + ((size_t)qi * TREE_BUFS + leaf) * CT_WORDS;
+  for (int w = tid; w < 2 * N; w += TT) {  // leaf ciphertext (a of the column, b = 0)
+    c[w] = (uint32_t)ca[w];
+    c[2 * N + w] = 0;
+  }
+  __syncthreads();
+  for (int l = 1; l <= 7; l++) combine(A, sm, c, nullptr, c, l);
+}
+
+// Levels 8..11 of one query from its chains, then pack_lwes' last step.
 __global__ void __launch_bounds__(TT, 1) pack_tree_kernel(const __grid_constant__ TreeArgs A) {
   extern __shared__ __align__(16) uint32_t sm[];
   const DevParams& P = A.P;
@@ -174,9 +198,7 @@ __global__ void __launch_bounds__(TT, 1) pack_tree_kernel(const __grid_constant_
     }
     return;
   }
-  // work buffers: 0-1 level-7 chains (even, odd leaf), 2-3 level 8, 4-5
-  // level 9, 6-7 level 10
-  uint32_t* W = A.work + (size_t)qi * 8 * CT_WORDS;
+  uint32_t* W = A.work + (size_t)qi * TREE_BUFS * CT_WORDS;
   auto buf = [&](int b) { return W + (size_t)b * CT_WORDS; };
   for (int s10 = 0; s10 < 2; s10++) {
     if (s10 >= nreal) continue;
@@ -186,29 +208,16 @@ __global__ void __launch_bounds__(TT, 1) pack_tree_kernel(const __grid_constant_
       for (int h8 = 0; h8 < 2; h8++) {
         const int s8 = s9 + 4 * h8;
         if (s8 >= nreal) continue;
-        for (int h7 = 0; h7 < 2; h7++) {
-          const int leaf = s8 + 8 * h7;
-          if (leaf >= nreal) continue;
-          // leaf ciphertext (a of the column, b = 0)
-          const uint64_t* ca = cols + (size_t)leaf * 2 * 2 * N;
-          uint32_t* c = buf(h7);
-          for (int w = tid; w < 2 * N; w += TT) {
-            c[w] = (uint32_t)ca[w];
-            c[2 * N + w] = 0;
-          }
-          __syncthreads();
-          for (int l = 1; l <= 7; l++) combine(A, sm, c, nullptr, c, l);
-        }
-        combine(A, sm, buf(0), s8 + 8 < nreal ? buf(1) : nullptr, buf(2 + h8), 8);
+        combine(A, sm, buf(s8), s8 + 8 < nreal ? buf(s8 + 8) : nullptr, buf(16 + h8), 8);
       }
-      combine(A, sm, buf(2), s9 + 4 < nreal ? buf(3) : nullptr, buf(4 + h9), 9);
+      combine(A, sm, buf(16), s9 + 4 < nreal ? buf(17) : nullptr, buf(18 + h9), 9);
     }
-    combine(A, sm, buf(4), s10 + 2 < nreal ? buf(5) : nullptr, buf(6 + s10), 10);
+    combine(A, sm, buf(18), s10 + 2 < nreal ? buf(19) : nullptr, buf(20 + s10), 10);
   }
-  combine(A, sm, buf(6), 1 < nreal ? buf(7) : nullptr, buf(6), 11);
+  combine(A, sm, buf(20), 1 < nreal ? buf(21) : nullptr, buf(20), 11);
   // pack_lwes' last step (automorph_pack.rs:466-484): b_val_z * d added at
   // coefficient z < nreal
-  const uint32_t* root = buf(6);
+  const uint32_t* root = buf(20);
   const uint32_t q0 = P.r[0].q, q1 = P.r[1].q;
   for (int w = tid; w < 2 * N; w += TT) out_a[w] = root[w];
   if (A.mode == MODE_CRT_FIXED) {
@@ -265,7 +274,7 @@ __global__ void __launch_bounds__(BLOCK) galois_prep_kernel(const DevParams P, c
 // column ciphertexts (MAX_GAMMA columns, u64), the combined NoPacking
 // ciphertext (u64) and the tree's work area (u32).
 constexpr size_t NOALLOC_QUERY_BYTES =
-    sizeof(uint64_t) * ((size_t)MAX_GAMMA * 2 * 2 * N + 2 * 2 * N) + sizeof(uint32_t) * (size_t)8 * CT_WORDS;
+    sizeof(uint64_t) * ((size_t)MAX_GAMMA * 2 * 2 * N + 2 * 2 * N) + sizeof(uint32_t) * (size_t)TREE_BUFS * CT_WORDS;
 __device__ __align__(256) unsigned char g_tree_noalloc_scratch[TREE_NOALLOC_MAX_QUERIES * NOALLOC_QUERY_BYTES];
 
 }  // namespace
@@ -288,14 +297,23 @@ cudaError_t tree_noalloc_scratch(int device, void** ptr) {
 }
 
 size_t tree_smem_bytes() { return sizeof(uint32_t) * (size_t)S_TOTAL; }
-size_t tree_work_words_per_query() { return (size_t)8 * CT_WORDS; }
+size_t tree_work_words_per_query() { return (size_t)TREE_BUFS * CT_WORDS; }
 
 cudaError_t prepare_tree_kernels() {
-  return cudaFuncSetAttribute(pack_tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem_bytes());
+  cudaError_t e = cudaFuncSetAttribute(pack_tree_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tree_smem_bytes());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tree_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem_bytes());
+  return e;
 }
 
 cudaError_t launch_pack_tree(const TreeArgs& a, cudaStream_t st) {
   if (a.nq <= 0) return cudaSuccess;
+  if (a.ncols > 1) {
+    tree_chain_kernel<<<a.nq * a.ncols, TT, tree_smem_bytes(), st>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   pack_tree_kernel<<<a.nq, TT, tree_smem_bytes(), st>>>(a);
   return cudaGetLastError();
 }
