@@ -597,6 +597,7 @@ def main():
 
     c3 = c3_bench(inspire, crs, seeds[c0], brows[c0], y_body) if rank == 0 else None
     tree = tree_bench(inspire, crs, edb, nshards, clients, seeds[c0], brows[c0], torch, dev, B) if rank == 0 else None
+    nopack = nopacking_bench(inspire, crs, edb, nshards, seeds, brows, B) if rank == 0 else None
 
     serving = None
     e2e_value = sync_call_qps
@@ -668,6 +669,7 @@ def main():
             "same_shard_batch_qps": same_shard,
             "c3_single_query": c3,
             "tree_packing": tree,
+            "nopacking": nopack,
             "batched_over_plain": value / plain["qps"],
             "p50_ms": None if serving is None else serving["headline"]["p50_ms"],
             "p99_ms": None if serving is None else serving["headline"]["p99_ms"],
@@ -740,6 +742,21 @@ def tree_bench(inspire, crs, edb, nshards, clients, seeds, brows, torch, dev, B,
             "batch": B, "batch_qps": batch_qps,
             "note": "host-buffer calls; at d = 2048 with two CRT primes the crate's tree-packed responses do not "
                     "decrypt, so this path is measured for parity with the crate, not used for retrieval"}
+
+
+def nopacking_bench(inspire, crs, edb, nshards, seeds, brows, B, reps=3):
+    """The NoPacking variant (respond_seeded, combined ciphertext only) on the
+    same resident database: batches of B queries per host-buffer call."""
+    rng = np.random.default_rng(9)
+    sid = rng.integers(0, nshards, size=B).astype(np.uint32)
+    pick = rng.integers(0, len(seeds), size=B)
+    inspire.respond_seeded_nopacking_batch(crs, edb, sid, seeds[pick], brows[pick])  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        inspire.respond_seeded_nopacking_batch(crs, edb, sid, seeds[pick], brows[pick])
+    return {"workload": f"respond_seeded (NoPacking) on the resident database, 16 columns, batches of {B} "
+                        "queries per host-buffer call (rows copied in, combined ciphertexts copied out)",
+            "batch": B, "batch_qps": B * reps / (time.perf_counter() - t0)}
 
 
 def serve_bench(inspire, crs, edb, nshards, clients, client_of, qcid, locals_, seeds, brows, db_raw, B, args, torch,
