@@ -402,7 +402,7 @@ int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, con
  * as inspire_respond_seeded_batch_device takes them; d_out_a [n][poly],
  * d_out_b [n][2 polys], d_status [n]) and enqueues its work on `stream`
  * without allocating: its scratch (column ciphertexts, combined ciphertext,
- * the tree's work area; 1.8 MiB per query) is one static device array per
+ * the tree's work area; 2.0 MiB per query) is one static device array per
  * device, located once with cudaGetSymbolAddress.  n > 2 is rejected.
  * Calls that overlap on the device (from several host threads, or on
  * streams that run concurrently) race on that array: issue them on one

@@ -16,14 +16,14 @@
 // gadget digits (base 2^20, 3 digits) of tau_t(a), and
 //   out = (sum_k digit_k * K[k].a, tau_t(b) + sum_k digit_k * K[k].b).
 //
-// Two kernels, 768 threads per CTA (six groups: CRT residue r x digit k):
-// the per-LWE chains of levels 1..7 run one CTA per (query, LWE), side by
-// side; then one CTA per query combines levels 8..11.  Per combine: [K1] every thread gathers s1 for its source coefficients,
+// 768 threads per CTA (six groups: CRT residue r x digit k).  The per-LWE
+// chains of levels 1..7 run one CTA per (query, LWE), side by side; each of
+// levels 8..11 is one launch with one CTA per (query, node).  Per combine: [K1] every thread gathers s1 for its source coefficients,
 // applies tau_t (a scattered write in shared memory) and splits the
 // composite coefficient into digits; [K3] group (r,k) transforms digit k mod
 // q_r and multiplies it into both key parts; [K4] groups (r,0) / (r,1) sum
 // and inverse-transform the a / b products and write node = s0 + out.
-// Ciphertexts of the tree live in a per-query global work area (22 buffers
+// Ciphertexts of the tree live in a per-query global work area (31 buffers
 // of 2 polys x 2 residues, L2-resident); the key switch works in shared
 // memory.
 #include <mutex>
@@ -161,9 +161,11 @@ __device__ void combine(const TreeArgs& A, uint32_t* sm, const uint32_t* E, cons
   __syncthreads();
 }
 
-// Work area of one query: buffers 0..15 hold the level-7 node of each LWE
-// (its key-switch chain), 16-17 level 8, 18-19 level 9, 20-21 level 10.
-constexpr int TREE_BUFS = 22;
+// Work area of one query: the node (l, s) of levels 7..11 in buffer
+// level_base(l) + s: 0..15 level 7 (each LWE's key-switch chain), 16..23
+// level 8, 24..27 level 9, 28..29 level 10, 30 the root.
+constexpr int TREE_BUFS = 31;
+__host__ __device__ constexpr int level_base(int l) { return l == 7 ? 0 : l == 8 ? 16 : l == 9 ? 24 : l == 10 ? 28 : 30; }
 
 // Levels 1..7 for one LWE: node(l, s) = node(l-1, s) + homomorphic_automorph
 // (its odd child is absent), one CTA per (query, LWE), so the 16 chains of a
@@ -182,9 +184,21 @@ __global__ void __launch_bounds__(TT, 1) tree_chain_kernel(const __grid_constant
   for (int l = 1; l <= 7; l++) combine(A, sm, c, nullptr, c, l);
 }
 
-// Levels 8..11 of one query from its chains, then pack_lwes' last step.
-__global__ void __launch_bounds__(TT, 1) pack_tree_kernel(const __grid_constant__ TreeArgs A) {
+// Level l (8..11) of the tree: one CTA per (query, node s < 2^(11-l)); node
+// (l, s) combines (l-1, s) and (l-1, s + 2^(11-l)), absent past the last LWE.
+__global__ void __launch_bounds__(TT, 1) tree_level_kernel(const __grid_constant__ TreeArgs A, int l) {
   extern __shared__ __align__(16) uint32_t sm[];
+  const int nn = 1 << (11 - l), nreal = A.ncols;
+  const int qi = blockIdx.x / nn, s = blockIdx.x - qi * nn;
+  if (s >= nreal) return;  // absent node (uniform over the CTA)
+  uint32_t* W = A.work + (size_t)qi * TREE_BUFS * CT_WORDS;
+  auto buf = [&](int b) { return W + (size_t)b * CT_WORDS; };
+  const int cb = level_base(l - 1);
+  combine(A, sm, buf(cb + s), s + nn < nreal ? buf(cb + s + nn) : nullptr, buf(level_base(l) + s), l);
+}
+
+// pack_lwes' result: the root, or the single LWE unpacked.
+__global__ void __launch_bounds__(TT, 1) pack_tree_kernel(const __grid_constant__ TreeArgs A) {
   const DevParams& P = A.P;
   const int qi = blockIdx.x, tid = threadIdx.x;
   const int nreal = A.ncols;
@@ -200,24 +214,9 @@ __global__ void __launch_bounds__(TT, 1) pack_tree_kernel(const __grid_constant_
   }
   uint32_t* W = A.work + (size_t)qi * TREE_BUFS * CT_WORDS;
   auto buf = [&](int b) { return W + (size_t)b * CT_WORDS; };
-  for (int s10 = 0; s10 < 2; s10++) {
-    if (s10 >= nreal) continue;
-    for (int h9 = 0; h9 < 2; h9++) {
-      const int s9 = s10 + 2 * h9;
-      if (s9 >= nreal) continue;
-      for (int h8 = 0; h8 < 2; h8++) {
-        const int s8 = s9 + 4 * h8;
-        if (s8 >= nreal) continue;
-        combine(A, sm, buf(s8), s8 + 8 < nreal ? buf(s8 + 8) : nullptr, buf(16 + h8), 8);
-      }
-      combine(A, sm, buf(16), s9 + 4 < nreal ? buf(17) : nullptr, buf(18 + h9), 9);
-    }
-    combine(A, sm, buf(18), s10 + 2 < nreal ? buf(19) : nullptr, buf(20 + s10), 10);
-  }
-  combine(A, sm, buf(20), 1 < nreal ? buf(21) : nullptr, buf(20), 11);
   // pack_lwes' last step (automorph_pack.rs:466-484): b_val_z * d added at
   // coefficient z < nreal
-  const uint32_t* root = buf(20);
+  const uint32_t* root = buf(level_base(11));
   const uint32_t q0 = P.r[0].q, q1 = P.r[1].q;
   for (int w = tid; w < 2 * N; w += TT) out_a[w] = root[w];
   if (A.mode == MODE_CRT_FIXED) {
@@ -304,6 +303,8 @@ cudaError_t prepare_tree_kernels() {
                                        (int)tree_smem_bytes());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(tree_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem_bytes());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tree_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tree_smem_bytes());
   return e;
 }
 
@@ -311,10 +312,14 @@ cudaError_t launch_pack_tree(const TreeArgs& a, cudaStream_t st) {
   if (a.nq <= 0) return cudaSuccess;
   if (a.ncols > 1) {
     tree_chain_kernel<<<a.nq * a.ncols, TT, tree_smem_bytes(), st>>>(a);
-    const cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    for (int l = 8; l <= 11 && e == cudaSuccess; l++) {
+      tree_level_kernel<<<a.nq << (11 - l), TT, tree_smem_bytes(), st>>>(a, l);
+      e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return e;
   }
-  pack_tree_kernel<<<a.nq, TT, tree_smem_bytes(), st>>>(a);
+  pack_tree_kernel<<<a.nq, TT, 0, st>>>(a);
   return cudaGetLastError();
 }
 
