@@ -427,6 +427,25 @@ int inspire_respond_seeded_packed_noalloc_device(inspire_ctx *ctx, const inspire
 int inspire_galois_keygen_device(inspire_ctx *ctx, const uint8_t *key, const uint64_t *d_sk, uint64_t *d_keys,
                                  int32_t *d_status, void *stream);
 
+/* Setup side: every public key of setup (src/pir/setup.rs:151-200) for the
+ * secret key d_sk [poly].  d_ks receives log2(ring_dim) + 4 key-switching
+ * matrices [.][2*gadget_len][poly], row k = (a, -a s + e + s_i z^k):
+ *   i < log2(ring_dim): galois_keys, equal to inspire_galois_keygen_device's
+ *     output for the same key;
+ *   i = log2(ring_dim): k_g, s_i = tau_3(s); i = log2(ring_dim) + 1: k_h,
+ *     s_i = tau_{2 ring_dim - 1}(s) (generate_automorphism_ks_matrix,
+ *     src/ks/setup.rs:218-245; galois_generators, src/rlwe/galois.rs:80-91);
+ *   i = log2(ring_dim) + 2, + 3: packing_k_g, packing_k_h, s_i the LWE key
+ *     of s (generate_packing_ks_matrix, src/ks/setup.rs:183-205;
+ *     LweSecretKey::from_rlwe, src/lwe/enc.rs:53-66).
+ * d_crs_a (may be NULL) receives crs_a_vectors (setup.rs:175-180):
+ * ring_dim uniform polys [ring_dim][poly].  d_status [log2(ring_dim) + 5]:
+ * one per matrix, the last for crs_a_vectors.  Uniform polys and errors come
+ * from the ChaCha20 stream keyed by `key` (as inspire_galois_keygen_device);
+ * the crate's thread_rng draws are not reproduced. */
+int inspire_setup_keygen_device(inspire_ctx *ctx, const uint8_t *key, const uint64_t *d_sk, uint64_t *d_ks,
+                                uint64_t *d_crs_a, int32_t *d_status, void *stream);
+
 /* Client side, for load generation at served rates: keys of n clients,
  * numbered first_client + i.  d_sk receives each RlweSecretKey::generate
  * (src/rlwe/enc.rs:14-17) [n][poly] and d_y_body each ClientPackingKeys

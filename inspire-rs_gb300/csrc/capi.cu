@@ -1050,7 +1050,24 @@ int inspire_galois_keygen_device(inspire_ctx* c, const uint8_t* key, const uint6
   a.sk = d_sk;
   a.keys = d_keys;
   a.status = d_status;
-  CUDA_TRY(launch_galois_keys(a, LOGN, (cudaStream_t)stream));
+  CUDA_TRY(launch_ks_matrices(a, LOGN, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_setup_keygen_device(inspire_ctx* c, const uint8_t* key, const uint64_t* d_sk, uint64_t* d_ks,
+                                uint64_t* d_crs_a, int32_t* d_status, void* stream) {
+  if (!c || !key || !d_sk || !d_ks || !d_status) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  GaloisGenArgs a{};
+  if (int rc = client_tables(c, key, a)) return rc;
+  if (int rc = set_device(c)) return rc;
+  a.sk = d_sk;
+  a.keys = d_ks;
+  a.status = d_status;
+  const cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(launch_ks_matrices(a, LOGN + 4, st));
+  a.status = d_status + LOGN + 4;
+  CUDA_TRY(cudaMemsetAsync(a.status, 0, sizeof(int32_t), st));
+  if (d_crs_a) CUDA_TRY(launch_crs_a(a, N, d_crs_a, st));
   return INSPIRE_OK;
 }
 

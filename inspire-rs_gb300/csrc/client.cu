@@ -13,10 +13,19 @@
 // generate_ksk_body :846-902): y_body[k] = tau_g(s) z^k - s w_mask[k] + e_k
 // with g = gen_pows[1] and w_mask the CRS mask of w_seed.
 //
-// galois_keys_kernel: the CRS's Galois key-switching matrices of setup
-// (src/pir/setup.rs:164-173; generate_automorphism_ks_matrix and
-// generate_ks_matrix, src/ks/setup.rs:118-162, 218-245): matrix i for
-// t = N / 2^i + 1, row k = (a, -a s + e + tau_t(s) z^k) with a uniform.
+// ks_matrices_kernel: the key-switching matrices of setup
+// (src/pir/setup.rs:151-200; generate_ks_matrix, src/ks/setup.rs:118-162):
+// row k of matrix i = (a, -a s + e + s_i z^k) with a uniform, where the
+// source key s_i is
+//   i < LOGN:        tau_t(s), t = N / 2^i + 1 (galois_keys, setup.rs:164-173;
+//                    generate_automorphism_ks_matrix, ks/setup.rs:218-245)
+//   i = LOGN:        tau_3(s)     (k_g; galois_generators, rlwe/galois.rs:80-91)
+//   i = LOGN + 1:    tau_{2N-1}(s) (k_h)
+//   i = LOGN + 2, 3: the LWE key of s, s_lwe[0] = s[0], s_lwe[j] = -s[j]
+//                    (packing_k_g, packing_k_h; generate_packing_ks_matrix,
+//                    ks/setup.rs:183-205; LweSecretKey::from_rlwe,
+//                    lwe/enc.rs:53-66)
+// crs_a_kernel: setup's crs_a_vectors (setup.rs:175-180), N uniform polys.
 //
 // Randomness: the crate draws seeds from thread_rng and errors from a
 // rejection sampler over ChaCha20.  Here both come from ChaCha20 keyed by a
@@ -27,9 +36,11 @@
 //     blocks 2^40 + (Q * 2 ELL + r) * 256 + j / 8          (Q < 2^36)
 //   client C: secret key from blocks 2^48 + C * 1024 + j / 8; y_body[k]
 //     errors from blocks 2^48 + C * 1024 + 256 (k + 1) + j / 8  (C < 2^30)
-//   Galois matrix i, row k (m = 3 i + k): a from the seed = first 8 words
-//     of block 2^52 + m (Poly::from_seed_moduli of it), errors from blocks
-//     2^52 + 2^20 + m * 256 + j / 8
+//   key-switching matrix i, row k (m = 3 i + k): a from the seed = first 8
+//     words of block 2^52 + m (Poly::from_seed_moduli of it), errors from
+//     blocks 2^52 + 2^20 + m * 256 + j / 8
+//   crs_a vector v: Poly::from_seed_moduli of the first 8 words of block
+//     2^53 + v
 // The outputs are valid keys and queries (responses decrypt to the queried
 // entries) but are not the crate's random draws.
 #include "expand.cuh"
@@ -213,7 +224,12 @@ __global__ void __launch_bounds__(CT) client_keys_kernel(const __grid_constant__
   }
 }
 
-__global__ void __launch_bounds__(CT) galois_keys_kernel(const __grid_constant__ GaloisGenArgs A) {
+// Source key of matrix mi: t > 0 for tau_t(s), 0 for the LWE key of s.
+__device__ __forceinline__ uint32_t ks_source(int mi) {
+  return mi < LOGN ? (uint32_t)(N >> mi) + 1u : mi == LOGN ? 3u : mi == LOGN + 1 ? 2u * N - 1u : 0u;
+}
+
+__global__ void __launch_bounds__(CT) ks_matrices_kernel(const __grid_constant__ GaloisGenArgs A) {
   extern __shared__ __align__(16) uint32_t smem[];
   uint64_t* cand = reinterpret_cast<uint64_t*>(smem);        // [N] expansion candidates
   uint32_t* a0 = smem + 2 * N;                               // [2][N] a (residue 0, 1)
@@ -226,8 +242,8 @@ __global__ void __launch_bounds__(CT) galois_keys_kernel(const __grid_constant__
   uint32_t* seed_w = reinterpret_cast<uint32_t*>(ws + 20);   // [8]
   const DevParams& P = A.P;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
-  const int mi = blockIdx.x;                                 // matrix i: t = N / 2^i + 1
-  const uint32_t t = (uint32_t)(N >> mi) + 1u;
+  const int mi = blockIdx.x;
+  const uint32_t t = ks_source(mi);
   const uint32_t q = P.r[g].q, qinv = P.r[g].qinv;
   const int cdt_len = A.cdt_len;
   if (tid < MAX_CDT) cdt[tid] = A.cdt[tid];
@@ -235,9 +251,9 @@ __global__ void __launch_bounds__(CT) galois_keys_kernel(const __grid_constant__
   uint32_t key[8];
 #pragma unroll
   for (int i = 0; i < 8; i++) key[i] = A.key[i];
-  // tau_t(s) per residue (rlwe/galois.rs:22-55)
+  // the source key per residue: tau_t(s) (rlwe/galois.rs:22-55) or s_lwe
   for (int c = tid; c < N; c += CT) {
-    const uint32_t j = ((uint32_t)c * t) & (2 * N - 1);
+    const uint32_t j = t ? ((uint32_t)c * t) & (2 * N - 1) : (c ? (uint32_t)(c + N) : 0u);
 #pragma unroll
     for (int rr = 0; rr < 2; rr++) {
       const uint32_t sv = (uint32_t)A.sk[(size_t)rr * N + c];
@@ -292,15 +308,49 @@ __global__ void __launch_bounds__(CT) galois_keys_kernel(const __grid_constant__
   }
 }
 
+// One CTA per vector v: Poly::from_seed_moduli (poly.rs:251-281) of the
+// stream's block 2^53 + v, written as [2][N] u64.
+__global__ void __launch_bounds__(CT) crs_a_kernel(const __grid_constant__ GaloisGenArgs A, uint64_t* out) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  uint64_t* cand = reinterpret_cast<uint64_t*>(smem);  // [N]
+  uint32_t* a0 = smem + 2 * N;                         // [2][N]
+  int* ws = reinterpret_cast<int*>(a0 + 2 * N);        // [20]
+  uint32_t* seed_w = reinterpret_cast<uint32_t*>(ws + 20);
+  const int tid = threadIdx.x, v = blockIdx.x;
+  if (tid == 0) {
+    uint32_t key[8], w[16];
+#pragma unroll
+    for (int i = 0; i < 8; i++) key[i] = A.key[i];
+    chacha20_block(key, (1ull << 53) + (uint64_t)v, A.P.one, w);
+#pragma unroll
+    for (int i = 0; i < 8; i++) seed_w[i] = w[i];
+  }
+  __syncthreads();
+  const bool ok = expand_seeded_row<2>(A.P, reinterpret_cast<const uint8_t*>(seed_w), cand, a0, a0 + N, ws, 3, tid);
+  if (!ok && tid == 0) A.status[0] = ERR_EXPAND;
+  __syncthreads();
+  uint64_t* o = out + (size_t)v * 2 * N;
+  for (int c = tid; c < 2 * N; c += CT) o[c] = a0[c];
+}
+
 }  // namespace
 
 size_t galois_keys_smem_bytes() {
   return sizeof(uint32_t) * ((size_t)2 * N + 2 * N + 2 * N + 2 * N + N + 2 * NTT_SCRATCH + 2 * MAX_CDT + 20 + 8);
 }
 
-cudaError_t launch_galois_keys(const GaloisGenArgs& a, int nmat, cudaStream_t st) {
+cudaError_t launch_ks_matrices(const GaloisGenArgs& a, int nmat, cudaStream_t st) {
   if (nmat <= 0) return cudaSuccess;
-  galois_keys_kernel<<<nmat, CT, galois_keys_smem_bytes(), st>>>(a);
+  if (nmat > LOGN + 4) return cudaErrorInvalidValue;
+  ks_matrices_kernel<<<nmat, CT, galois_keys_smem_bytes(), st>>>(a);
+  return cudaGetLastError();
+}
+
+size_t crs_a_smem_bytes() { return sizeof(uint32_t) * ((size_t)2 * N + 2 * N + 20 + 8); }
+
+cudaError_t launch_crs_a(const GaloisGenArgs& a, int nvec, uint64_t* out, cudaStream_t st) {
+  if (nvec <= 0) return cudaSuccess;
+  crs_a_kernel<<<nvec, CT, crs_a_smem_bytes(), st>>>(a, out);
   return cudaGetLastError();
 }
 
@@ -325,8 +375,10 @@ cudaError_t prepare_client_kernels() {
     e = cudaFuncSetAttribute(client_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)client_keys_smem_bytes());
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(galois_keys_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(ks_matrices_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)galois_keys_smem_bytes());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(crs_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)crs_a_smem_bytes());
   return e;
 }
 

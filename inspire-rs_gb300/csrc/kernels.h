@@ -149,7 +149,11 @@ cudaError_t prepare_tree_kernels();
 cudaError_t launch_pack_tree(const TreeArgs& a, cudaStream_t st);
 cudaError_t launch_galois_prep(const DevParams& P, const uint64_t* keys, int npolys, uint32_t* ks, cudaStream_t st);
 size_t galois_keys_smem_bytes();
-cudaError_t launch_galois_keys(const GaloisGenArgs& a, int nmat, cudaStream_t st);
+// Key-switching matrices 0 .. nmat-1 (nmat <= LOGN + 4): the LOGN Galois
+// matrices, k_g, k_h, packing_k_g, packing_k_h.
+cudaError_t launch_ks_matrices(const GaloisGenArgs& a, int nmat, cudaStream_t st);
+// nvec uniform polys [nvec][2][N] u64 (setup's crs_a_vectors).
+cudaError_t launch_crs_a(const GaloisGenArgs& a, int nvec, uint64_t* out, cudaStream_t st);
 size_t client_keys_smem_bytes();
 cudaError_t launch_client_keys(const KeyGenArgs& a, int n, cudaStream_t st);
 

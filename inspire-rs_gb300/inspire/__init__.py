@@ -35,4 +35,5 @@ from .pir import (  # noqa: F401
     respond_seeded_packed_batch,
     respond_seeded_with_variant,
     respond_with_variant,
+    setup_keygen_device,
 )

@@ -143,6 +143,7 @@ def load(path: str = LIB_PATH):
         "inspire_respond_seeded_packed": (C.c_int, [vp, vp, C.POINTER(SeededQueryC), vp, vp, C.POINTER(u32)]),
         "inspire_respond_seeded_packed_batch": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, C.POINTER(u32)]),
         "inspire_galois_keygen_device": (C.c_int, [vp, C.c_char_p, vp, vp, vp, vp]),
+        "inspire_setup_keygen_device": (C.c_int, [vp, C.c_char_p, vp, vp, vp, vp, vp]),
         "inspire_respond_seeded_packed_noalloc_device": (C.c_int, [vp, vp, u32, vp, vp, vp, vp, vp, vp,
                                                                    C.POINTER(u32), vp]),
         "inspire_client_keygen_device": (C.c_int, [vp, C.c_char_p, u64, u32, vp, vp, vp]),

@@ -552,6 +552,19 @@ def galois_keygen_device(crs: ServerCrs, key: bytes, d_sk: int, d_keys: int, d_s
     _check(crs.L.inspire_galois_keygen_device(crs.h, bytes(key), v(d_sk), v(d_keys), v(d_status), v(stream)))
 
 
+def setup_keygen_device(crs: ServerCrs, key: bytes, d_sk: int, d_ks: int, d_crs_a: int, d_status: int,
+                        stream: int) -> None:
+    """setup's public keys (setup.rs:151-200) of the secret key at d_sk, on the
+    device: d_ks [log2 d + 4][6][2*ring_dim] (u64) = galois_keys, k_g, k_h,
+    packing_k_g, packing_k_h; d_crs_a [ring_dim][2*ring_dim] (u64, 0 to skip)
+    = crs_a_vectors; d_status [log2 d + 5] (i32); asynchronous."""
+    if len(key) != 32:
+        raise ValueError("key must be 32 bytes")
+    v = C.c_void_p
+    _check(crs.L.inspire_setup_keygen_device(crs.h, bytes(key), v(d_sk), v(d_ks), v(d_crs_a), v(d_status),
+                                             v(stream)))
+
+
 def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, stream: int) -> int:
     """Launch the modular-multiply rate probe; returns the multiplies issued."""
     _check(crs.L.inspire_mulmod_rate_device(crs.h, blocks, iters, C.c_void_p(d_sink), C.c_void_p(stream)))

@@ -112,6 +112,33 @@ def test_batch_equals_single(tree):
             assert np.array_equal(a[k], one.ciphertext.a) and np.array_equal(b[k], one.ciphertext.b)
 
 
+Q = (268369921, 249561089)
+
+
+def check_ks_matrix(O, ctx, kw, sk, rows, i, src):
+    """rows [6][2N] of key-switching matrix i against a CPU restatement of the
+    device stream: row k = (a, -a s + e + src z^k) (generate_ks_matrix,
+    ks/setup.rs:118-162), a = Poly::from_seed_moduli of the first 8 words of
+    block 2^52 + 3 i + k, e the Gaussian blocks 2^52 + 2^20 + (3 i + k) 256."""
+    from client_stream import gaussian_blocks
+
+    for k in range(3):
+        m = 3 * i + k
+        w = O.chacha20_block(kw, [(2 ** 52 + m) & 0xFFFFFFFF, (2 ** 52 + m) >> 32, 0, 0])
+        a = ctx.poly_from_seed(w[:8].astype("<u4").tobytes())
+        assert np.array_equal(rows[2 * k], a), (i, k)
+        e = gaussian_blocks(kw, 2 ** 52 + 2 ** 20 + m * (N // 8))
+        a_s = ctx.poly_mul(a, sk)
+        want = np.zeros(2 * N, np.uint64)
+        for r in range(2):
+            q = Q[r]
+            sl = slice(r * N, (r + 1) * N)
+            v = (src[sl].astype(np.int64) * pow(1 << 20, k, q)) % q
+            v = (v - a_s[sl].astype(np.int64)) % q
+            want[sl] = ((v + e % q) % q).astype(np.uint64)
+        assert np.array_equal(rows[2 * k + 1], want), (i, k)
+
+
 def test_galois_keygen_device(tree):
     """Galois matrices made on the device: bit-exact against a CPU restatement
     of the stream (matrix i for t = d / 2^i + 1, row k = (a, -a s + e +
@@ -134,24 +161,8 @@ def test_galois_keygen_device(tree):
     assert not d_st.cpu().numpy().any()
     keys = d_keys.cpu().numpy().view(np.uint64)
     kw = np.frombuffer(key, dtype="<u4")
-    Q = (268369921, 249561089)
     for i in (0, 5, 10):
-        tau = ctx.automorphism(sk, (N >> i) + 1)
-        for k in range(3):
-            m = 3 * i + k
-            w = O.chacha20_block(kw, [(2 ** 52 + m) & 0xFFFFFFFF, (2 ** 52 + m) >> 32, 0, 0])
-            a = ctx.poly_from_seed(w[:8].astype("<u4").tobytes())
-            assert np.array_equal(keys[i, 2 * k], a), (i, k)
-            e = gaussian_blocks(kw, 2 ** 52 + 2 ** 20 + m * (N // 8))
-            a_s = ctx.poly_mul(a, sk)
-            want = np.zeros(2 * N, np.uint64)
-            for r in range(2):
-                q = Q[r]
-                sl = slice(r * N, (r + 1) * N)
-                v = (tau[sl].astype(np.int64) * pow(1 << 20, k, q)) % q
-                v = (v - a_s[sl].astype(np.int64)) % q
-                want[sl] = ((v + e % q) % q).astype(np.uint64)
-            assert np.array_equal(keys[i, 2 * k + 1], want), (i, k)
+        check_ks_matrix(O, ctx, kw, sk, keys[i], i, ctx.automorphism(sk, (N >> i) + 1))
     crs2 = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
     crs2.load_galois_keys(keys)
     edb2 = inspire.EncodedDatabase(crs2, db, 32)
@@ -161,6 +172,56 @@ def test_galois_keygen_device(tree):
     assert np.array_equal(got.ciphertext.a, want_a) and np.array_equal(got.ciphertext.b, want_b)
     edb2.close()
     crs2.close()
+
+
+def test_setup_keygen_device(tree):
+    """setup's public keys made on the device (setup.rs:151-200): the Galois
+    matrices equal galois_keygen_device's; k_g (tau_3), k_h (tau_{2d-1}) and
+    packing_k_g, packing_k_h (the LWE key of s: s[0], -s[1..], lwe/enc.rs:53-66)
+    bit-exact against a CPU restatement of the stream; crs_a_vectors are
+    Poly::from_seed_moduli of the stream's blocks 2^53 + v."""
+    T = tree
+    torch, O, inspire, ctx = pytest.importorskip("torch"), T["O"], T["inspire"], T["ctx"]
+    key = bytes(range(101, 133))
+    dev = torch.device("cuda:0")
+    crs, edb, db, shards = world(T, "crt_fixed", 16)
+    sk = T["client"].sk
+    d_sk = torch.from_numpy(sk.view(np.int64).copy()).to(dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    d_ks = torch.zeros((15, 6, 2 * N), dtype=torch.int64, device=dev)
+    d_crs_a = torch.zeros((N, 2 * N), dtype=torch.int64, device=dev)
+    d_st = torch.full((16,), -1, dtype=torch.int32, device=dev)
+    inspire.setup_keygen_device(crs, key, d_sk.data_ptr(), d_ks.data_ptr(), d_crs_a.data_ptr(), d_st.data_ptr(),
+                                stream)
+    d_g = torch.zeros((11, 6, 2 * N), dtype=torch.int64, device=dev)
+    d_gst = torch.full((11,), -1, dtype=torch.int32, device=dev)
+    inspire.galois_keygen_device(crs, key, d_sk.data_ptr(), d_g.data_ptr(), d_gst.data_ptr(), stream)
+    d_ks2 = torch.zeros((15, 6, 2 * N), dtype=torch.int64, device=dev)
+    d_st2 = torch.full((16,), -1, dtype=torch.int32, device=dev)
+    inspire.setup_keygen_device(crs, key, d_sk.data_ptr(), d_ks2.data_ptr(), 0, d_st2.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert not d_st.cpu().numpy().any() and not d_gst.cpu().numpy().any()
+    assert not d_st2.cpu().numpy()[:15].any()
+    ks = d_ks.cpu().numpy().view(np.uint64)
+    assert np.array_equal(ks[:11], d_g.cpu().numpy().view(np.uint64))
+    assert np.array_equal(ks, d_ks2.cpu().numpy().view(np.uint64))
+    kw = np.frombuffer(key, dtype="<u4")
+    lwe = sk.copy()
+    for r in range(2):
+        c = sk[r * N + 1:(r + 1) * N]
+        lwe[r * N + 1:(r + 1) * N] = np.where(c == 0, 0, np.uint64(Q[r]) - c)
+    sources = {11: ctx.automorphism(sk, 3), 12: ctx.automorphism(sk, 2 * N - 1), 13: lwe, 14: lwe}
+    for i, src in sources.items():
+        check_ks_matrix(O, ctx, kw, sk, ks[i], i, src)
+    # packing_k_g and packing_k_h have the same source, different draws
+    assert not np.array_equal(ks[13, 0], ks[14, 0])
+    crs_a = d_crs_a.cpu().numpy().view(np.uint64)
+    for v in (0, 1, 777, N - 1):
+        w = O.chacha20_block(kw, [(2 ** 53 + v) & 0xFFFFFFFF, (2 ** 53 + v) >> 32, 0, 0])
+        assert np.array_equal(crs_a[v], ctx.poly_from_seed(w[:8].astype("<u4").tobytes())), v
+    assert len({crs_a[v].tobytes() for v in range(0, N, 97)}) == len(range(0, N, 97))
+    for r in range(2):
+        assert crs_a[:, r * N:(r + 1) * N].max() < Q[r]
 
 
 def crs_json(keys, w_seed, num_columns, p=1 << 16):
