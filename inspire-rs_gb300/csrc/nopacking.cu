@@ -58,6 +58,77 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
   __syncthreads();
   // the query's status is written once, by one thread
   if (tid == 0) A.status[qi] = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
+  if (!A.out_columns) {
+    // Combined ciphertext only.  The NTT is linear mod q_r, so
+    // sum_c NTT(D_{c,t}) = NTT(sum_c D_{c,t} mod q_r): one transform of the
+    // digit sum per group gives the sum of the column products exactly.
+    const ResidueConsts& C = P.r[r];
+    uint32_t v[16], w[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = 0;
+    for (int c = 0; c < gamma; c++) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const uint64_t xv = P.delta * (uint64_t)__ldg(H + (size_t)c * N + x + 128 * j);
+        const uint32_t s = v[j] + ((uint32_t)(xv >> (ZBITS * t)) & ((1u << ZBITS) - 1));
+        v[j] = min(s, s - q);  // < q
+      }
+    }
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+#pragma unroll
+    for (int j = 0; j < 16; j++) w[j] = PB[t * 2 * N + r * N + x + 128 * j];
+    __syncthreads();  // every group holds its a row: PB (row staging) is reused for products
+    const int f = (x >> 1) & 3;
+    const uint64_t* brow = A.brows + (((size_t)qi * ELL + t) * 2 + r) * N;
+#pragma unroll 1
+    for (int ab = 0; ab < 2; ab++) {
+      if (ab == 1) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) w[j] = (uint32_t)__ldg(brow + x + 128 * j);
+      }
+      ntt_fwd(w, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+      uint32_t* dst = PB + ((r * 3 + t) * 2 + ab) * N + 16 * x;
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        uint32_t pr[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int j = 4 * r4 + e;
+          const uint32_t h = mul_shoup(w[j], C.ninv_mont, C.ninv_mont_p, q);
+          pr[e] = redc_lazy((uint64_t)v[j] * h, q, qinv);
+        }
+        *reinterpret_cast<uint4*>(dst + 4 * (r4 ^ f)) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+      }
+    }
+    __syncthreads();
+    if (t < 2) {  // (r,0): a, (r,1): b
+      const uint32_t* p0 = PB + ((r * 3 + 0) * 2 + t) * N + 16 * x;
+      const uint32_t* p1 = PB + ((r * 3 + 1) * 2 + t) * N + 16 * x;
+      const uint32_t* p2 = PB + ((r * 3 + 2) * 2 + t) * N + 16 * x;
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        const int o = 4 * (r4 ^ f);
+        const uint4 a4 = *reinterpret_cast<const uint4*>(p0 + o);
+        const uint4 b4 = *reinterpret_cast<const uint4*>(p1 + o);
+        const uint4 c4 = *reinterpret_cast<const uint4*>(p2 + o);
+        const uint32_t aa[4] = {a4.x, a4.y, a4.z, a4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w},
+                       cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          uint32_t sm = aa[e] + bb[e] + cc[e];  // < 6q
+          sm = min(sm, sm - 4 * q);
+          sm = min(sm, sm - 2 * q);
+          v[4 * r4 + e] = min(sm, sm - q);
+        }
+      }
+      ntt_inv_noscale(v, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);
+      uint64_t* o = A.out + (size_t)qi * 4 * N + (size_t)t * 2 * N + (size_t)r * N;
+#pragma unroll
+      for (int j = 0; j < 16; j++) o[x + 128 * j] = canon2(v[j], q);
+    }
+    return;
+  }
+
   // group (r,t): NTT(a_t mod q_r), NTT(b_t mod q_r), kept as x * n^-1 * 2^32
   uint32_t ah[16], bh[16];
   {

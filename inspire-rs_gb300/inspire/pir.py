@@ -377,17 +377,29 @@ def respond_seeded_packed(crs: ServerCrs, encoded_db: EncodedDatabase, query: Se
     return _packed_response(out_a, out_b, words.value)
 
 
+def _out_array(out, shape):
+    """A caller's output array (e.g. a PinnedBuffer's) checked for shape and
+    layout, or a new one."""
+    if out is None:
+        return np.empty(shape, dtype=np.uint64)
+    if out.shape != shape or out.dtype != np.uint64 or not out.flags.c_contiguous:
+        raise ValueError(f"out must be a C-contiguous uint64 array of shape {shape}")
+    return out
+
+
 def respond_seeded_packed_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int],
-                                seeds: np.ndarray, b_rows: np.ndarray):
+                                seeds: np.ndarray, b_rows: np.ndarray, out_a: np.ndarray = None,
+                                out_b: np.ndarray = None):
     """Batched respond_seeded_packed: (a (n, plen), b (n, words)) with words
-    plen, or 2*plen in compat mode with more than one column."""
+    plen, or 2*plen in compat mode with more than one column.  out_a (n, plen)
+    and out_b (n, 2*plen) may be given (page-locked arrays copy faster)."""
     n = len(shard_ids)
     plen = crs.params.plen
     sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
     sd = np.ascontiguousarray(seeds, dtype=np.uint8)
     br = _u64(b_rows)
-    out_a = np.zeros((n, plen), dtype=np.uint64)
-    out_b = np.zeros((n, 2 * plen), dtype=np.uint64)
+    out_a = _out_array(out_a, (n, plen))
+    out_b = _out_array(out_b, (n, 2 * plen))
     words = C.c_uint32(0)
     _check(crs.L.inspire_respond_seeded_packed_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br),
                                                      _ptr(out_a), _ptr(out_b), C.byref(words)))
@@ -395,14 +407,15 @@ def respond_seeded_packed_batch(crs: ServerCrs, encoded_db: EncodedDatabase, sha
 
 
 def respond_seeded_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int],
-                                   seeds: np.ndarray, b_rows: np.ndarray) -> np.ndarray:
-    """Batched respond_seeded: (n, 2, plen) combined ciphertexts."""
+                                   seeds: np.ndarray, b_rows: np.ndarray, out: np.ndarray = None) -> np.ndarray:
+    """Batched respond_seeded: (n, 2, plen) combined ciphertexts, into `out`
+    when given (page-locked arrays copy faster)."""
     n = len(shard_ids)
     plen = crs.params.plen
     sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
     sd = np.ascontiguousarray(seeds, dtype=np.uint8)
     br = _u64(b_rows)
-    out = np.zeros((n, 2, plen), dtype=np.uint64)
+    out = _out_array(out, (n, 2, plen))
     _check(crs.L.inspire_respond_seeded_nopacking_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br),
                                                         _ptr(out)))
     return out

@@ -79,14 +79,25 @@ def test_unseeded_nopacking_and_variant(world):
     assert len(r3.column_ciphertexts) == 16
 
 
-def test_combined_only_matches(world):
+@pytest.mark.parametrize("index", [9, 2048 + 777, 4096 + 299])
+def test_combined_only_matches(world, index):
+    """Without column ciphertexts the kernel transforms the digit sums over
+    the columns once (one NTT per digit instead of one per column and digit);
+    the combined ciphertext must equal the oracle's sum of the column
+    products, and the with-columns path's, bit for bit (full and partial
+    shards)."""
     W = world
     inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
-    seeds, b_rows = client.query_seeded(9)
-    want = ctx.respond_nopacking(W["shards"][0], ctx.expand_rgsw(seeds, b_rows))
-    resp = inspire.respond_seeded(W["crs"], W["edb"], inspire.SeededClientQuery(0, seeds, b_rows), with_columns=False)
+    sid, local = divmod(index, N)
+    seeds, b_rows = client.query_seeded(local)
+    want = ctx.respond_nopacking(W["shards"][sid], ctx.expand_rgsw(seeds, b_rows))
+    q = inspire.SeededClientQuery(sid, seeds, b_rows)
+    resp = inspire.respond_seeded(W["crs"], W["edb"], q, with_columns=False)
     assert resp.column_ciphertexts == []
     assert np.array_equal(np.stack([resp.ciphertext.a, resp.ciphertext.b]), want)
+    full = inspire.respond_seeded(W["crs"], W["edb"], q)
+    assert np.array_equal(full.ciphertext.b, resp.ciphertext.b)
+    assert np.array_equal(full.ciphertext.a, resp.ciphertext.a)
 
 
 def test_nopacking_batch_equals_single(world):
@@ -99,6 +110,12 @@ def test_nopacking_batch_equals_single(world):
         seeds[k], brows[k] = client.query_seeded(ix % N)
     sids = [ix // N for ix in idxs]
     out = inspire.respond_seeded_nopacking_batch(W["crs"], W["edb"], sids, seeds, brows)
+    pinned = inspire.pir.PinnedBuffer(out.shape, np.uint64)
+    got = inspire.respond_seeded_nopacking_batch(W["crs"], W["edb"], sids, seeds, brows, out=pinned.array)
+    assert got is pinned.array and np.array_equal(got, out)
+    pinned.close()
+    with pytest.raises(ValueError):
+        inspire.respond_seeded_nopacking_batch(W["crs"], W["edb"], sids, seeds, brows, out=np.empty((1, 2, 2 * N)))
     for k in range(len(idxs)):
         r = inspire.respond_seeded(W["crs"], W["edb"], inspire.SeededClientQuery(sids[k], seeds[k], brows[k]),
                                    with_columns=False)
