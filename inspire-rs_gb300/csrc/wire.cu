@@ -104,13 +104,66 @@ struct Json {
     *n = 0;
     if (!expect('[')) return false;
     if (eat(']')) return true;
-    do {
+    for (;;) {
       uint64_t v;
-      if (!u64(v)) return false;
+      // compact runs ("123,45,...") eight bytes at a time; anything else
+      // (whitespace, long or malformed numbers, the last bytes) takes u64()
+      if (!digits_fast(v) && !u64(v)) return false;
       if (*n >= cap) return fail("array too long");
       out[(*n)++] = v;
-    } while (eat(','));
+      if (p < end && *p == ',') {
+        p++;
+        continue;
+      }
+      if (!eat(',')) break;
+    }
     return expect(']');
+  }
+  // One number of 1..16 digits directly followed by ',' or ']', with 17
+  // readable bytes: parsed by SWAR on little-endian 8-byte words (x86-64 and
+  // AArch64 alike).  Returns false, consuming nothing, for every other case.
+  bool digits_fast(uint64_t& v) {
+    if (end - p < 17) return false;
+    uint64_t w0, w1;
+    memcpy(&w0, p, 8);
+    memcpy(&w1, p + 8, 8);
+    const int n0 = digit_run(w0);
+    if (n0 == 0) return false;
+    uint64_t x = swar_value(w0, n0);
+    int len = n0;
+    if (n0 == 8) {
+      const int n1 = digit_run(w1);
+      if (n1 == 8) return false;  // 17+ digits: the checked path
+      if (n1) x = x * pow10(n1) + swar_value(w1, n1);
+      len += n1;
+    }
+    const char t = p[len];
+    if (t != ',' && t != ']') return false;
+    p += len;
+    v = x;
+    return true;
+  }
+  // number of leading ASCII digits in the 8 bytes of w (first byte lowest)
+  static int digit_run(uint64_t w) {
+    const uint64_t H = 0x8080808080808080ull;
+    const uint64_t ge0 = ((w | H) - 0x3030303030303030ull) & H;  // (b & 0x7f) >= '0'
+    const uint64_t ge10 = ((w | H) - 0x3a3a3a3a3a3a3a3aull) & H; // (b & 0x7f) > '9'
+    const uint64_t digit = ge0 & ~ge10 & ~(w & H);
+    const uint64_t other = ~digit & H;
+    return other ? __builtin_ctzll(other) >> 3 : 8;
+  }
+  // value of the first n (1..8) digits of w
+  static uint64_t swar_value(uint64_t w, int n) {
+    uint64_t d = w - 0x3030303030303030ull;  // the low n bytes are 0..9
+    d <<= 8 * (8 - n);                        // right-align: leading zero digits
+    d = (d * 10 + (d >> 8)) & 0x00ff00ff00ff00ffull;     // digit pairs
+    d = (d * 100 + (d >> 16)) & 0x0000ffff0000ffffull;   // groups of four
+    return (d * 10000 + (d >> 32)) & 0xffffffffull;      // eight digits
+  }
+  static uint64_t pow10(int n) {
+    uint64_t r = 1;
+    while (n--) r *= 10;
+    return r;
   }
   bool boolean(bool& b) {
     ws();

@@ -114,6 +114,41 @@ def test_seeded_query_json_rejects(wire):
         w.seeded_query_from_json(params, compact(good)[:-10])
 
 
+def test_seeded_query_json_number_forms(wire):
+    """Integer arrays in every form the parser meets: 1..9-digit values,
+    whitespace around values and commas, values at the end of an array, and
+    over-long, overflowing and non-integer numbers (the compact form is
+    parsed eight bytes at a time, everything else by the checked path)."""
+    inspire, w = wire
+    rng = np.random.default_rng(3)
+    params = inspire.InspireParams(p=1 << 16)
+    seeds = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+    b_rows = rand_polys(rng, 6)
+    # row 0's coefficients with 1..9 digits each, row 1 with random spacing
+    for i in range(2 * N):
+        nd = 1 + i % 9
+        b_rows[0, i] = int(rng.integers(10 ** (nd - 1) if nd > 1 else 0, min(10 ** nd, Q[i // N])))
+    good = compact(query_obj(1, seeds, b_rows))
+    spaced = ",".join(rng.choice(["", " ", "\n", "  \t"]) + str(int(v)) + rng.choice(["", " ", "\r\n"])
+                      for v in b_rows[1])
+    body = good.replace(b'"coeffs":[' + ",".join(str(int(v)) for v in b_rows[1]).encode() + b"]",
+                        b'"coeffs":[' + spaced.encode() + b"]")
+    assert body != good
+    for text in (good, body):
+        q = w.seeded_query_from_json(params, text)
+        assert np.array_equal(q.b_rows, b_rows)
+    first = str(int(b_rows[2, 0])).encode()
+    key = b'"coeffs":[' + first + b","
+    assert good.count(key) == 1
+    bad = [(b"1234567890123456", "not reduced"), (b"99999999999999999", "not reduced"),
+           (b"18446744073709551615", "not reduced"), (b"18446744073709551616", "overflow"),
+           (b"123456789012345678901", "overflow"), (b"12.5", "integer"), (b"1e3", "integer"),
+           (b"-4", "unsigned"), (b"12a", "expected")]
+    for num, msg in bad:
+        with pytest.raises(inspire.PirError, match=msg):
+            w.seeded_query_from_json(params, good.replace(key, b'"coeffs":[' + num + b","))
+
+
 def test_response_json_and_bincode(wire):
     inspire, w = wire
     rng = np.random.default_rng(3)
