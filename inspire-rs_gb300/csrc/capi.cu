@@ -223,6 +223,17 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
   return INSPIRE_OK;
 }
 
+// CTAs per query of the NoPacking kernel.  Few queries with column
+// ciphertexts: each query's columns are split over CTAs (each expands the
+// rows itself) so that a small batch fills the SMs; the combined
+// ciphertexts are then summed from the columns.
+int column_groups(const inspire_ctx* c, const inspire_db* db, uint32_t n, bool columns) {
+  if (!columns || db->gamma <= 1 || n == 0) return 1;
+  const int want = std::min(db->gamma, std::max(1, c->sm_count / (int)std::min<uint32_t>(n, 1u << 20)));
+  const int per = (db->gamma + want - 1) / want;
+  return (db->gamma + per - 1) / per;
+}
+
 // Stage n NoPacking queries (same row layout as run_batch) and run the
 // NoPacking kernel; out_columns may be null.
 // Stage n queries' rows and enqueue the NoPacking kernel on the context's
@@ -254,6 +265,7 @@ int enqueue_nopacking(inspire_ctx* c, const inspire_db* db, uint32_t n, const ui
   NoPackingArgs a{};
   a.P = c->P;
   a.nq = (int)n;
+  a.col_groups = column_groups(c, db, n, columns);
   a.shard = c->d_shard.as<uint32_t>();
   a.seeds = seeded ? c->d_seeds.as<uint8_t>() : nullptr;
   a.arows = seeded ? nullptr : c->d_arows.as<uint64_t>();
@@ -424,6 +436,11 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
   if (e != cudaSuccess) {
     delete c;
     return fail(INSPIRE_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      c->sm_count <= 0) {
+    delete c;
+    return fail(INSPIRE_ERR_CUDA, "cannot read the SM count");
   }
   // tables per residue: fwd pairs (2N words), inv pairs (2N words), psi_pow (2N)
   const size_t per = 6 * (size_t)N;
@@ -1026,6 +1043,7 @@ int inspire_respond_seeded_packed_noalloc_device(inspire_ctx* c, const inspire_d
   a.out = comb;
   a.out_columns = cols;
   a.status = d_status;
+  a.col_groups = column_groups(c, db, n, true);
   CUDA_TRY(launch_nopacking(a, true, (cudaStream_t)stream));
   TreeArgs t{};
   t.P = c->P;

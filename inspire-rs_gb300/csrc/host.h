@@ -61,6 +61,7 @@ struct inspire_ctx {
   std::mutex mu;
   int device = 0;
   int mode = 0;
+  int sm_count = 0;
   inspire_params params{};
   uint64_t q = 0;  // composite modulus
   ig::DevParams P{};

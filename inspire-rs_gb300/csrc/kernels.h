@@ -70,6 +70,10 @@ struct NoPackingArgs {
   uint64_t* out;
   uint64_t* out_columns;
   int* status;
+  // CTAs per query, each answering ceil(gamma / col_groups) of its columns
+  // (1: one CTA per query).  Above 1, out_columns is required and the
+  // combined ciphertexts are summed from the columns by a second launch.
+  int col_groups;
 };
 
 // Seeded query generation (client side): query first_query + i asks for

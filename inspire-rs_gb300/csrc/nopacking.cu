@@ -28,13 +28,16 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
   uint32_t* SUMB = PB + 12 * N;               // [2 r][2 (a,b)][N] running sum over columns (swizzled)
   int* wsb = reinterpret_cast<int*>(SUMB + 4 * N);  // [3][20]
   const DevParams& P = A.P;
-  const int qi = blockIdx.x;
+  const int ngroups = A.col_groups;
+  const int qi = blockIdx.x / ngroups, cg = blockIdx.x - qi * ngroups;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
   const int r = g / 3, t = g - 3 * r;
   const int gamma = P.gamma;
+  const int cper = (gamma + ngroups - 1) / ngroups;
+  const int c0 = cg * cper, c1 = min(gamma, c0 + cper);
   const uint32_t shard = A.shard[qi];
   if (shard >= (uint32_t)A.nshards) {
-    if (tid == 0) A.status[qi] = ERR_INDEX;
+    if (tid == 0 && cg == 0) A.status[qi] = ERR_INDEX;
     return;  // uniform over the CTA
   }
   const uint16_t* H = A.H + (size_t)shard * gamma * N;
@@ -57,7 +60,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
   }
   __syncthreads();
   // the query's status is written once, by one thread
-  if (tid == 0) A.status[qi] = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
+  if (tid == 0 && cg == 0) A.status[qi] = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
   if (!A.out_columns) {
     // Combined ciphertext only.  The NTT is linear mod q_r, so
     // sum_c NTT(D_{c,t}) = NTT(sum_c D_{c,t} mod q_r): one transform of the
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
   }
   uint64_t* outc = A.out_columns ? A.out_columns + (size_t)qi * gamma * 4 * N : nullptr;
 
-  for (int c = 0; c < gamma; c++) {
+  for (int c = c0; c < c1; c++) {
     // digit t of Delta * h_c, NTT mod q_r, products with this group's row
     uint32_t v[16];
 #pragma unroll
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
     __syncthreads();
   }
   // combined ciphertext = sum of the column ciphertexts (respond.rs:102-109)
-  if (t < 2) {
+  if (ngroups == 1 && t < 2) {
     uint32_t sv[16];
     load16(sumb, x, sv);
     ntt_inv_noscale(sv, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
@@ -232,14 +235,38 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
   }
 }
 
+// Combined ciphertexts of split queries: out[q] = sum_c columns[q][c] mod q_r
+// (respond.rs:102-109), in the coefficient domain (the sum commutes with the
+// inverse NTT, so this equals the one-CTA path's bits).
+__global__ void column_sum_kernel(const DevParams P, int nq, int gamma, const uint64_t* __restrict__ cols,
+                                  uint64_t* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;  // over nq * 4N words
+  if (i >= (size_t)nq * 4 * N) return;
+  const size_t qi = i / (4 * N), w = i - qi * 4 * N;  // w: part (a, b) x residue x coefficient
+  const uint32_t q = P.r[(w / N) & 1].q;
+  const uint64_t* src = cols + qi * (size_t)gamma * 4 * N + w;
+  uint32_t s = 0;
+  for (int c = 0; c < gamma; c++) {
+    const uint32_t v = s + (uint32_t)src[(size_t)c * 4 * N];
+    s = min(v, v - q);
+  }
+  out[i] = s;
+}
+
 }  // namespace
 
 size_t nopacking_smem_bytes() { return sizeof(uint32_t) * ((size_t)RG * NTT_SCRATCH + 16 * N + 64); }
 
 template <bool SEEDED>
 static cudaError_t launch_np(const NoPackingArgs& a, cudaStream_t st) {
-  nopacking_kernel<0, SEEDED><<<a.nq, RBLOCK, nopacking_smem_bytes(), st>>>(a);
-  return cudaGetLastError();
+  nopacking_kernel<0, SEEDED><<<a.nq * a.col_groups, RBLOCK, nopacking_smem_bytes(), st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && a.col_groups > 1) {
+    const size_t words = (size_t)a.nq * 4 * N;
+    column_sum_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a.P, a.nq, a.P.gamma, a.out_columns, a.out);
+    e = cudaGetLastError();
+  }
+  return e;
 }
 
 cudaError_t prepare_nopacking_kernels() {
@@ -252,6 +279,7 @@ cudaError_t prepare_nopacking_kernels() {
 
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st) {
   if (a.nq <= 0) return cudaSuccess;
+  if (a.col_groups < 1 || (a.col_groups > 1 && !a.out_columns)) return cudaErrorInvalidValue;
   return seeded ? launch_np<true>(a, st) : launch_np<false>(a, st);
 }
 

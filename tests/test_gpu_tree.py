@@ -112,6 +112,27 @@ def test_batch_equals_single(tree):
             assert np.array_equal(a[k], one.ciphertext.a) and np.array_equal(b[k], one.ciphertext.b)
 
 
+def test_batch_column_split_regimes(tree):
+    """The NoPacking front end splits a query's columns over CTAs when the
+    batch is small (1 query: 16 CTAs of one column; 12 queries: 8 CTAs of two
+    columns; 160 queries: one CTA per query).  The three regimes give the
+    same tree-packed responses."""
+    T = tree
+    inspire, client = T["inspire"], T["client"]
+    crs, edb, db, shards = world(T, "crt_fixed", 16)
+    base = [client.query_seeded(li) for li in (5, 999, 2040, 64)]
+    n = 160
+    sids = [k % 2 for k in range(n)]
+    seeds = np.stack([base[k % 4][0] for k in range(n)])
+    rows = np.stack([base[k % 4][1] for k in range(n)])
+    a_all, b_all = inspire.respond_seeded_packed_batch(crs, edb, sids, seeds, rows)
+    a12, b12 = inspire.respond_seeded_packed_batch(crs, edb, sids[:12], seeds[:12], rows[:12])
+    assert np.array_equal(a12, a_all[:12]) and np.array_equal(b12, b_all[:12])
+    for k in (0, 5, 159):
+        one = inspire.respond_seeded_packed(crs, edb, inspire.SeededClientQuery(sids[k], seeds[k], rows[k]))
+        assert np.array_equal(one.ciphertext.a, a_all[k]) and np.array_equal(one.ciphertext.b, b_all[k])
+
+
 Q = (268369921, 249561089)
 
 
