@@ -272,6 +272,59 @@ def kernel_microbench(inspire, crs, torch, dev, reps=20):
     return res
 
 
+def client_bench(inspire, crs, torch, dev, reps=3):
+    """The device-side client and setup kernels, timed with CUDA events on the
+    launching stream: seeded query generation (query_seeded) and decrypt +
+    extract_inspiring of 4096 queries / responses per launch, key generation
+    of 1024 clients per launch, and setup's public keys (15 key-switching
+    matrices + 2048 crs_a vectors) for one secret key."""
+    st = torch.cuda.current_stream(dev)
+    sp = st.cuda_stream
+    key = bytes(range(64, 96))
+    nq, ncl = 4096, 1024
+    d_sk = torch.zeros((ncl, 2 * N), dtype=torch.int64, device=dev)
+    d_yb = torch.zeros((ncl, 3, 2 * N), dtype=torch.int64, device=dev)
+    d_idx = torch.arange(nq, dtype=torch.int32, device=dev) % N
+    d_seeds = torch.zeros((nq, 6, 32), dtype=torch.uint8, device=dev)
+    d_brows = torch.zeros((nq, 6, 2 * N), dtype=torch.int64, device=dev)
+    d_qst = torch.zeros(nq, dtype=torch.int32, device=dev)
+    q = crs.params.crt_moduli
+    g = torch.Generator(device="cpu").manual_seed(12)
+    d_ct = torch.stack([torch.randint(0, q[0], (nq, 2, N), generator=g, dtype=torch.int64),
+                        torch.randint(0, q[1], (nq, 2, N), generator=g, dtype=torch.int64)], 2).reshape(nq, 2, 2 * N)
+    d_ct = d_ct.to(dev)
+    d_ent = torch.zeros((nq, ENTRY), dtype=torch.uint8, device=dev)
+    d_ks = torch.zeros((15, 6, 2 * N), dtype=torch.int64, device=dev)
+    d_crs_a = torch.zeros((N, 2 * N), dtype=torch.int64, device=dev)
+    d_kst = torch.zeros(16, dtype=torch.int32, device=dev)
+    ops = (("client_keygen", ncl, lambda: inspire.client_keygen_device(crs, key, 0, ncl, d_sk.data_ptr(),
+                                                                       d_yb.data_ptr(), sp)),
+           ("query_gen", nq, lambda: inspire.query_seeded_device(crs, d_sk[0].data_ptr(), key, 0, nq, d_idx.data_ptr(),
+                                                                  d_seeds.data_ptr(), d_brows.data_ptr(),
+                                                                  d_qst.data_ptr(), sp)),
+           ("extract", nq, lambda: inspire.pir.extract_inspiring_device(crs, d_sk[0].data_ptr(), d_ct.data_ptr(), nq,
+                                                                         ENTRY, d_ent.data_ptr(), sp)),
+           ("setup_keys", 1, lambda: inspire.setup_keygen_device(crs, key, d_sk[0].data_ptr(), d_ks.data_ptr(),
+                                                                 d_crs_a.data_ptr(), d_kst.data_ptr(), sp)))
+    res = {"workload": f"device-side client: {ncl} client keys, {nq} seeded queries and {nq} extractions per "
+                       "launch; setup's public keys for one secret key"}
+    for name, n, fn in ops:
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) / 1e3 / reps
+        res[name + "_ms"] = dt * 1e3
+        if n > 1:
+            res[name + "_per_s"] = n / dt
+    assert not d_qst.cpu().numpy().any() and not d_kst.cpu().numpy().any(), "client kernels reported a nonzero status"
+    return res
+
+
 def reference_arm(args):
     """The crate's Respond path restated on the host cores: respond_seeded_inspiring
     exactly as respond.rs:391-398 runs it, including PackParams::new (brute-force
@@ -554,6 +607,7 @@ def main():
         same_shard = B * 5 / (e0.elapsed_time(e1) / 1e3)
 
     micro = kernel_microbench(inspire, crs, torch, dev)
+    client_side = client_bench(inspire, crs, torch, dev) if rank == 0 else None
     codec = wire_bench(inspire, crs, seeds[0], brows[0], y_body, d_out[0, 0].cpu().numpy().view(np.uint64)
                        .reshape(2, 2 * N))
 
@@ -676,6 +730,7 @@ def main():
             "p99_ms": None if serving is None else serving["headline"]["p99_ms"],
             "serving": serving,
             "kernel_microbench": micro,
+            "client_side": client_side,
             "wire_codec": codec,
             "wall_s_timed_region": wall,
         }
