@@ -210,7 +210,8 @@ struct Json {
     }
     // number (possibly signed / fractional)
     const char* s = p;
-    while (p < end && (strchr("+-.eE", *p) || (*p >= '0' && *p <= '9'))) p++;
+    while (p < end && (*p == '+' || *p == '-' || *p == '.' || *p == 'e' || *p == 'E' || (*p >= '0' && *p <= '9')))
+      p++;
     return p > s || fail("unexpected character");
   }
   bool null() {
