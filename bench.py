@@ -651,6 +651,7 @@ def main():
              "path": "inspire_respond_seeded_batch with n=1 from host buffers, one call at a time"}
 
     c3 = c3_bench(inspire, crs, seeds[c0], brows[c0], y_body) if rank == 0 else None
+    shard_files = shard_file_bench(inspire, crs, seeds[c0], brows[c0], y_body) if rank == 0 else None
     tree = tree_bench(inspire, crs, edb, nshards, clients, seeds[c0], brows[c0], torch, dev, B) if rank == 0 else None
     nopack = nopacking_bench(inspire, crs, edb, nshards, seeds, brows, B) if rank == 0 else None
 
@@ -723,6 +724,7 @@ def main():
             "plain_single_query_host": plain,
             "same_shard_batch_qps": same_shard,
             "c3_single_query": c3,
+            "shard_files": shard_files,
             "tree_packing": tree,
             "nopacking": nopack,
             "batched_over_plain": value / plain["qps"],
@@ -737,6 +739,43 @@ def main():
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def shard_file_bench(inspire, crs, seeds, brows, y_body, log2_entries=20):
+    """Setup from files: a 2^20-entry database written as the crate's binary
+    shard files (save_shards_binary layout) to a temporary directory and read
+    back into HBM with inspire_db_load_shards (page cache warm), checked by
+    answering one query from both databases."""
+    import shutil
+    import tempfile
+
+    rng = np.random.default_rng(6)
+    raw = np.frombuffer(rng.bytes((1 << log2_entries) * ENTRY), dtype=np.uint8)
+    edb = inspire.EncodedDatabase(crs, raw, ENTRY)
+    d = tempfile.mkdtemp(prefix="inspire_shards_")
+    try:
+        t0 = time.perf_counter()
+        edb.save_shards(d)
+        save_s = time.perf_counter() - t0
+        files = os.listdir(d)
+        nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in files)
+        inspire.EncodedDatabase.load_shards(crs, d).close()  # warm the page cache
+        t0 = time.perf_counter()
+        edb2 = inspire.EncodedDatabase.load_shards(crs, d)
+        load_s = time.perf_counter() - t0
+        q = inspire.SeededClientQuery(7, seeds[0], brows[0],
+                                      inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body))
+        r1 = inspire.respond_seeded_inspiring(crs, edb, q)
+        r2 = inspire.respond_seeded_inspiring(crs, edb2, q)
+        same = bool(np.array_equal(r1.ciphertext.a, r2.ciphertext.a) and np.array_equal(r1.ciphertext.b, r2.ciphertext.b))
+        edb2.close()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+        edb.close()
+    assert same, "database loaded from shard files answers differently"
+    return {"workload": f"2^{log2_entries} entries x 32 B as {len(files)} shard files ({nbytes / 2**20:.0f} MiB), "
+                        "read into HBM (contracted form built on the GPU), page cache warm",
+            "load_s": load_s, "load_gbs": nbytes / load_s / 1e9, "save_s": save_s, "same_response": same}
 
 
 def c3_bench(inspire, crs, seeds, brows, y_body, n=60):

@@ -15,9 +15,11 @@
 // Respond kernel's contracted form on the GPU exactly as inspire_db_create.
 #include <dirent.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "host.h"
@@ -73,17 +75,17 @@ std::string read_shard(const std::string& path, uint32_t want_id, const inspire_
     if (!read_le(f, &m)) return path + ": truncated header";
     if (m != c->params.crt_moduli[r]) return path + ": moduli differ from the context";
   }
-  std::vector<uint64_t> poly((size_t)2 * N);
-  std::vector<uint8_t> buf(sizeof(uint64_t) * 2 * N);
+  std::vector<uint8_t> buf(sizeof(uint64_t) * 2 * N * num_polys);
+  if (fread(buf.data(), 1, buf.size(), f) != buf.size()) return path + ": truncated polynomial data";
+  auto word = [&](size_t i) {  // little-endian u64 i of the polynomial data
+    uint64_t x = 0;
+    for (int b = 0; b < 8; b++) x |= (uint64_t)buf[8 * i + b] << (8 * b);
+    return x;
+  };
   for (uint32_t p = 0; p < num_polys; p++) {
-    if (fread(buf.data(), 1, buf.size(), f) != buf.size()) return path + ": truncated polynomial data";
-    for (size_t i = 0; i < poly.size(); i++) {
-      uint64_t x = 0;
-      for (int b = 0; b < 8; b++) x |= (uint64_t)buf[8 * i + b] << (8 * b);
-      poly[i] = x;
-    }
+    const size_t base = (size_t)p * 2 * N;
     for (int k = 0; k < N; k++) {
-      const uint64_t v0 = poly[k], v1 = poly[N + k];
+      const uint64_t v0 = word(base + k), v1 = word(base + N + k);
       if (v0 >= 65536 || v1 != v0)
         return path + ": polynomial " + std::to_string(p) + " is not an encoded 16-bit column (coefficient " +
                std::to_string(k) + ")";
@@ -164,11 +166,24 @@ int inspire_db_load_shards(inspire_ctx* c, const char* dir, inspire_db** out) {
     // shards in chunks of up to 256 MiB of raw columns
     const int per_chunk = std::max(1, (int)((256u << 20) / (sizeof(uint16_t) * gamma * N)));
     std::vector<uint16_t> Hh((size_t)std::min(per_chunk, nshards) * gamma * N);
+    // the files of a chunk are read by up to 16 host threads; the error
+    // reported is the one of the lowest shard id, as a serial read would give
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    std::vector<std::string> errs((size_t)std::min(per_chunk, nshards));
     for (int s0 = 0; s0 < nshards; s0 += per_chunk) {
       const int s1 = std::min(nshards, s0 + per_chunk);
+      const int nt = std::min({16, hw, s1 - s0});
+      auto work = [&](int t) {
+        for (int s = s0 + t; s < s1; s += nt)
+          errs[(size_t)(s - s0)] = read_shard(shard_path(dir, (uint32_t)s), (uint32_t)s, c,
+                                              Hh.data() + (size_t)(s - s0) * gamma * N);
+      };
+      std::vector<std::thread> pool;
+      for (int t = 1; t < nt; t++) pool.emplace_back(work, t);
+      work(0);
+      for (std::thread& th : pool) th.join();
       for (int s = s0; s < s1; s++) {
-        const std::string err = read_shard(shard_path(dir, (uint32_t)s), (uint32_t)s, c,
-                                           Hh.data() + (size_t)(s - s0) * gamma * N);
+        const std::string& err = errs[(size_t)(s - s0)];
         if (!err.empty()) {
           delete db;
           return fail(err.rfind("Shard ", 0) == 0 ? INSPIRE_ERR_SHARD_NOT_FOUND : INSPIRE_ERR_INVALID_ARGUMENT, err);

@@ -104,6 +104,20 @@ def test_loader_errors(world, tmp_path):
     write_shard_file(gap / "shard-0002.bin", 2, polys)
     with pytest.raises(inspire.PirError, match="Shard 1 not found"):
         inspire.EncodedDatabase.load_shards(W["crs"], gap)
+    # several bad files (read in parallel): the lowest shard id's error wins
+    many = tmp_path / "many"
+    many.mkdir()
+    for sid in range(40):
+        if sid != 5:
+            write_shard_file(many / f"shard-{sid:04d}.bin", sid, polys)
+    write_shard_file(many / "shard-0040.bin", 40, polys)
+    with open(many / "shard-0031.bin", "r+b") as f:
+        f.truncate(1000)
+    with pytest.raises(inspire.PirError, match="Shard 5 not found"):
+        inspire.EncodedDatabase.load_shards(W["crs"], many)
+    write_shard_file(many / "shard-0005.bin", 5, polys)
+    with pytest.raises(inspire.PirError, match="shard-0031.bin: truncated"):
+        inspire.EncodedDatabase.load_shards(W["crs"], many)
     # other moduli
     bad = tmp_path / "moduli"
     bad.mkdir()
