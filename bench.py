@@ -556,6 +556,48 @@ def main():
         torch.cuda.synchronize()
         value_grid = L * B * args.steps / (sum(a.elapsed_time(b) for a, b in gev2) / 1e3)
 
+    # one wave per launch: the same step shape with launches of one query per
+    # SM (152 on GB300) instead of B, drawn from the same pool, responses into
+    # a scratch buffer
+    value_wave = None
+    if ws == 1:
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        tot = nb * B
+        if n_sm <= tot:
+            flat = lambda t: t.view(-1, *t.shape[2:])
+            f_shard, f_seeds, f_brows, f_client = flat(d_shard), flat(d_seeds), flat(d_brows), flat(d_client)
+            w_out = torch.empty_like(flat(d_out))
+            w_status = torch.zeros(tot, dtype=torch.int32, device=dev)
+
+            def wave_step(k, e_start, e_end):
+                e_start.record(stream)
+                for st in side:
+                    st.wait_event(e_start)
+                for j in range(L):
+                    b0 = ((k * L + j) * n_sm) % (tot - n_sm + 1)
+                    inspire.respond_seeded_batch_device(crs, edb, n_sm, f_shard[b0].data_ptr(),
+                                                        f_seeds[b0].data_ptr(), f_brows[b0].data_ptr(),
+                                                        f_client[b0].data_ptr(), w_out[b0].data_ptr(),
+                                                        w_status[b0].data_ptr(), side[j % len(side)].cuda_stream)
+                for st in side:
+                    e = torch.cuda.Event()
+                    e.record(st)
+                    stream.wait_event(e)
+                e_end.record(stream)
+
+            for k in range(args.warmup):
+                wave_step(k, torch.cuda.Event(), torch.cuda.Event())
+            torch.cuda.synchronize()
+            wev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(args.steps)]
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)
+                wave_step(k, *wev[k])
+            torch.cuda.synchronize()
+            assert not w_status.cpu().numpy().any(), "one-wave launches reported a nonzero status"
+            value_wave = L * n_sm * args.steps / (sum(a.elapsed_time(b) for a, b in wev) / 1e3)
+            del w_out
+
     # correctness of what was timed: statuses, then every response of the nb
     # pool batches decrypted and extracted on the device with its client's key
     # must equal its database entry
@@ -718,6 +760,7 @@ def main():
             "verified_responses": verified,
             "value_cuda_graph": value_graph,
             "value_capped_grid": value_grid,
+            "value_one_wave": value_wave,
             "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
             "plain_single_query_qps": sweep.get("1"),
