@@ -127,7 +127,7 @@ class _Lane:
         self.queue = deque()          # (tickets, arrival_ns, pool_idx, db_idx, shard) chunks for the collector
         self.cv = threading.Condition()
         self.submitted_all = False
-        self.done_arrival, self.done_at = [], []
+        self.done_arrival, self.done_at, self.done_submit = [], [], []
         self.samples = []             # (db_idx, shard, pool_idx, out) of kept outputs
         self.error: Optional[BaseException] = None
         self.pool_pos = 0
@@ -152,8 +152,9 @@ class _Lane:
                 if len(t):
                     arr = self.arrivals[a:a + len(t)] if self.arrivals is not None else \
                         np.full(len(t), t_sub, np.int64)
+                    sub = np.full(len(t), t_sub, np.int64)
                     with self.cv:
-                        self.queue.append((t, arr, np.arange(plo, plo + len(t)), self.dbi[a:a + len(t)],
+                        self.queue.append((t, arr, sub, np.arange(plo, plo + len(t)), self.dbi[a:a + len(t)],
                                            self.shards[a:a + len(t)]))
                         self.cv.notify()
                 off += len(t)
@@ -195,13 +196,14 @@ class _Lane:
                         self.cv.wait(0.01)
                     if not self.queue and self.submitted_all:
                         return
-                    t, arr, pidx, d, sh = self.queue.popleft()
+                    t, arr, sub, pidx, d, sh = self.queue.popleft()
                 got = 0
                 out = np.zeros((len(t), 2, self.pool.b_rows.shape[-1]), np.uint64) if self.keep else None
                 while got < len(t):
                     o = None if out is None else out[got:]
                     done = self.server.poll_batch(t[got:], o, timeout_us=2000)
                     self.done_arrival.append(arr[got:got + len(done)])
+                    self.done_submit.append(sub[got:got + len(done)])
                     self.done_at.append(done)
                     got += len(done)
                 if self.keep:
@@ -260,11 +262,17 @@ def run(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate:
             raise ln.error
     arr = np.concatenate([np.concatenate(ln.done_arrival) for ln in lanes if ln.done_arrival])
     done = np.concatenate([np.concatenate(ln.done_at) for ln in lanes if ln.done_at])
+    sub = np.concatenate([np.concatenate(ln.done_submit) for ln in lanes if ln.done_submit])
     n_all = int(arr.size)
     if rate is not None and settle_frac > 0:
         keep = arr >= t0 + int(settle_frac * duration_s * 1e9)
-        arr, done = arr[keep], done[keep]
+        arr, done, sub = arr[keep], done[keep], sub[keep]
     res = latency_summary(arr, done)
+    if rate is not None and sub.size:
+        # from the submit call instead of the scheduled arrival: the server's
+        # own latency, without the load generator's lag in submitting
+        srv = latency_summary(sub, done)
+        res["from_submit_p50_ms"], res["from_submit_p99_ms"] = srv["p50_ms"], srv["p99_ms"]
     res["n_total"] = n_all
     res["offered_qps"] = rate
     res["wall_s"] = wall

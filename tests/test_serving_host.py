@@ -109,6 +109,8 @@ def test_run_against_fake_server(serving, rate):
         assert abs(res["n_total"] - 1500) < 5 * np.sqrt(1500)
         assert abs(res["n"] - 0.9 * 1500) < 5 * np.sqrt(1500)  # the first 10% of arrivals are not counted
         assert res["p50_ms"] >= 0.2
+        # submit happens at or after the scheduled arrival
+        assert 0 < res["from_submit_p50_ms"] <= res["p50_ms"] + 1e-9
     for db, shard, word in srv.answers:
         assert shard < (3 if db == "A" else 50)
         assert 1000 <= word < 1008
