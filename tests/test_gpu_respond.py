@@ -330,3 +330,50 @@ def test_batch_device_capped_grid(world):
         assert not d_st.cpu().numpy().any(), ctas
         assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), ctas
     crs.release_client(cid)
+
+
+def test_concurrent_host_calls_on_one_context(world):
+    """Several host threads calling the synchronous entry points on one
+    context at once (the crate's callers hold Arc<AppState> on tokio workers):
+    every result equals the one the same call returns alone."""
+    import threading
+
+    W = world
+    inspire, client = W["inspire"], W["client"]
+    crs, edb, pack, omode = W["w"]["crt_fixed"]
+    y_body, _ = client.packing_keys(pack)
+    keys = inspire.ClientPackingKeys(y_body=y_body)
+    qs = []
+    for k, index in enumerate((3, 2050, 4100, 777, 1999, 4096 + 898)):
+        sid, local = divmod(index, N)
+        seeds, b_rows = client.query_seeded(local)
+        qs.append(inspire.SeededClientQuery(sid, seeds, b_rows, inspiring_packing_keys=keys))
+
+    def call(kind, q):
+        if kind == 0:
+            r = inspire.respond_seeded_inspiring(crs, edb, q)
+        else:
+            r = inspire.respond_seeded(crs, edb, q, with_columns=(kind == 2))
+        return np.concatenate([r.ciphertext.a, r.ciphertext.b])
+
+    jobs = [(kind, k) for k in range(len(qs)) for kind in range(3)]
+    alone = {j: call(j[0], qs[j[1]]) for j in jobs}
+    got, errors = {}, []
+
+    def worker(t):
+        try:
+            for rep in range(3):
+                for j in jobs[t::4]:
+                    got[(j, rep, t)] = call(j[0], qs[j[1]])
+        except BaseException as e:  # reported below
+            errors.append(e)
+
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    assert not errors, errors
+    assert len(got) == 3 * len(jobs)
+    for (j, rep, t), v in got.items():
+        assert np.array_equal(v, alone[j]), (j, rep, t)
