@@ -167,11 +167,53 @@ void release_keys(inspire_ctx* c, int32_t id) {
 // a_rows/b_rows point at the first needed poly of query 0 (ELL contiguous
 // polys per query, query pitch `stride_polys`); seeds at the first needed seed
 // (ELL contiguous seeds, query pitch `seed_stride` bytes).
+int finish_status(inspire_ctx* c, uint32_t n, const char* what);
+
 int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
               size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
               const int32_t* client_ids, uint64_t* out_ct) {
   if (n == 0) return INSPIRE_OK;
   const size_t pw = poly_words();
+  if (seeds) {
+    // Page-locked rows and responses (16-byte aligned): the serving variant
+    // of the kernel reads each query's rows in place and writes its response
+    // straight to the caller's memory, so nothing is staged or copied back.
+    const size_t row_bytes = sizeof(uint64_t) * stride_polys * pw;
+    const size_t rows_span = row_bytes * (n - 1) + sizeof(uint64_t) * ELL * pw;
+    const size_t out_span = sizeof(uint64_t) * n * 2 * pw;
+    const uint8_t* d_rows = ((uintptr_t)b_rows % 16 == 0 && row_bytes % 16 == 0 && (uintptr_t)out_ct % 16 == 0)
+                                ? mapped_range(b_rows, rows_span)
+                                : nullptr;
+    const uint8_t* d_outp = d_rows ? mapped_range(out_ct, out_span) : nullptr;
+    if (d_rows && d_outp) {
+      CUDA_TRY(c->d_status.ensure(sizeof(int32_t) * n));
+      CUDA_TRY(c->d_desc.ensure(sizeof(QueryDesc) * n));
+      c->h_desc.resize(n);
+      const DbView view{db->E.as<uint32_t>(), db->H.as<uint16_t>(), db->nshards, 0};
+      for (uint32_t i = 0; i < n; i++) {
+        QueryDesc& d = c->h_desc[i];
+        memcpy(d.seeds, seeds + i * seed_stride, sizeof(d.seeds));
+        d.brows = reinterpret_cast<const uint64_t*>(d_rows + i * row_bytes);
+        d.out = const_cast<uint64_t*>(reinterpret_cast<const uint64_t*>(d_outp)) + (size_t)i * 2 * pw;
+        d.status = c->d_status.as<int32_t>() + i;
+        d.db = view;
+        d.shard = shard_ids[i];
+        d.client = client_ids[i];
+      }
+      CUDA_TRY(cudaMemcpyAsync(c->d_desc.p, c->h_desc.data(), sizeof(QueryDesc) * n, cudaMemcpyHostToDevice,
+                               c->stream));
+      if (int rc = sync_client_table(c)) return rc;
+      RespondArgs a{};
+      a.P = c->P;
+      a.nq = (int)n;
+      a.yhat_table = c->client_table.as<const uint32_t*>();
+      a.nclients = (int)c->client_ptrs.size();
+      a.what = c->what.as<uint32_t>();
+      a.qdesc = c->d_desc.as<QueryDesc>();
+      CUDA_TRY(launch_respond(a, true, c->stream));
+      return finish_status(c, n, "respond");
+    }
+  }
   CUDA_TRY(c->d_shard.ensure(sizeof(uint32_t) * n));
   CUDA_TRY(c->d_client.ensure(sizeof(int32_t) * n));
   CUDA_TRY(c->d_brows.ensure(sizeof(uint64_t) * n * ELL * pw));

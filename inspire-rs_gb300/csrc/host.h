@@ -82,7 +82,8 @@ struct inspire_ctx {
   bool client_table_dirty = true;
   // staging for host-buffer calls
   cudaStream_t stream = nullptr;
-  ighost::DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys;
+  ighost::DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys, d_desc;
+  std::vector<ig::QueryDesc> h_desc;
   std::vector<int32_t> h_status;
 
   ~inspire_ctx() {
@@ -106,6 +107,9 @@ namespace ighost {
 inline size_t poly_words() { return (size_t)2 * N; }
 
 // dbio.cu: a resident database from host raw columns [nshards][gamma][N].
+// Device address of a page-locked host range [p, p + bytes) (cudaHostAlloc
+// or cudaHostRegister memory, one mapping), or null for any other memory.
+const uint8_t* mapped_range(const void* p, size_t bytes);
 int db_from_host_columns(inspire_ctx* c, const uint16_t* Hh, int nshards, uint64_t n_entries, uint32_t entry_size,
                          inspire_db** out);
 

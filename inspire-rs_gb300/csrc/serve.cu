@@ -212,6 +212,26 @@ void inspire_server::run() {
   }
 }
 
+namespace ighost {
+
+// Device address of a page-locked host range [p, p + bytes), or null.
+const uint8_t* mapped_range(const void* p, size_t bytes) {
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const uint8_t* last = static_cast<const uint8_t*>(p) + bytes - 1;
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess || b.type != cudaMemoryTypeHost || !b.devicePointer ||
+      static_cast<const uint8_t*>(b.devicePointer) != static_cast<const uint8_t*>(a.devicePointer) + (bytes - 1)) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return static_cast<const uint8_t*>(a.devicePointer);
+}
+
+}  // namespace ighost
+
 extern "C" {
 
 void inspire_server_config_default(inspire_server_config* cfg) {
@@ -299,21 +319,6 @@ void inspire_server_destroy(inspire_server* s) {
   delete s;
 }
 
-// Device address of a page-locked host range [p, p + bytes), or null.
-static const uint8_t* mapped_range(const void* p, size_t bytes) {
-  cudaPointerAttributes a{}, b{};
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  const uint8_t* last = static_cast<const uint8_t*>(p) + bytes - 1;
-  if (cudaPointerGetAttributes(&b, last) != cudaSuccess || b.type != cudaMemoryTypeHost || !b.devicePointer ||
-      static_cast<const uint8_t*>(b.devicePointer) != static_cast<const uint8_t*>(a.devicePointer) + (bytes - 1)) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  return static_cast<const uint8_t*>(a.devicePointer);
-}
 
 int inspire_server_submit(inspire_server* s, uint32_t n, const inspire_db* const* dbs, const uint32_t* shard_ids,
                           const uint8_t* seeds, const uint64_t* b_rows, const int32_t* client_ids,

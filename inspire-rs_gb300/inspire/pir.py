@@ -448,18 +448,20 @@ def respond_seeded_with_variant(crs: ServerCrs, encoded_db: EncodedDatabase, que
 
 
 def respond_seeded_batch(crs: ServerCrs, encoded_db: EncodedDatabase, shard_ids: Sequence[int], seeds: np.ndarray,
-                         b_rows: np.ndarray, client_ids: Sequence[int]) -> np.ndarray:
+                         b_rows: np.ndarray, client_ids: Sequence[int], out: np.ndarray = None) -> np.ndarray:
     """Batched respond_seeded_inspiring with registered client keys.
 
     seeds (n, 2*ell, 32) uint8; b_rows (n, 2*ell, plen) uint64; returns
-    (n, 2, plen) uint64 = the (a, b) of each response."""
+    (n, 2, plen) uint64 = the (a, b) of each response, in `out` when given.
+    With page-locked b_rows and out (e.g. PinnedBuffer arrays) the GPU reads
+    the rows and writes the responses in place, without staging copies."""
     n = len(shard_ids)
     plen = crs.params.plen
     sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
     cid = np.ascontiguousarray(client_ids, dtype=np.int32)
     sd = np.ascontiguousarray(seeds, dtype=np.uint8)
     br = _u64(b_rows)
-    out = np.zeros((n, 2, plen), dtype=np.uint64)
+    out = _out_array(out, (n, 2, plen))
     _check(crs.L.inspire_respond_seeded_batch(crs.h, encoded_db.h, n, _ptr(sid), _ptr(sd), _ptr(br), _ptr(cid),
                                               _ptr(out)))
     return out

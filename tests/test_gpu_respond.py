@@ -377,3 +377,38 @@ def test_concurrent_host_calls_on_one_context(world):
     assert len(got) == 3 * len(jobs)
     for (j, rep, t), v in got.items():
         assert np.array_equal(v, alone[j]), (j, rep, t)
+
+
+def test_batch_from_page_locked_buffers(world):
+    """respond_seeded_batch with page-locked rows and responses: the kernel
+    reads the rows in place and writes the responses straight to host memory;
+    the results equal the staged call's, and both modes match the oracle."""
+    W = world
+    inspire, ctx, client = W["inspire"], W["ctx"], W["client"]
+    idxs = [5, 2048 + 17, 4096 + 898, 1024, 3000]
+    for mode in ("crt_fixed", "compat"):
+        crs, edb, pack, omode = W["w"][mode]
+        y_body, _ = client.packing_keys(pack)
+        cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+        n = len(idxs)
+        seeds = inspire.pir.PinnedBuffer((n, 6, 32), np.uint8)
+        rows = inspire.pir.PinnedBuffer((n, 6, 2 * N), np.uint64)
+        out = inspire.pir.PinnedBuffer((n, 2, 2 * N), np.uint64)
+        sids = []
+        for k, index in enumerate(idxs):
+            sid, local = divmod(index, N)
+            seeds.array[k], rows.array[k] = client.query_seeded(local)
+            sids.append(sid)
+        staged = inspire.respond_seeded_batch(crs, edb, sids, seeds.array.copy(), rows.array.copy(), [cid] * n)
+        out.array[...] = 0
+        got = inspire.respond_seeded_batch(crs, edb, sids, seeds.array, rows.array, [cid] * n, out=out.array)
+        assert got is out.array and np.array_equal(got, staged)
+        k = 2
+        want = oracle_response(W, mode, sids[k], ctx.expand_rgsw(seeds.array[k], rows.array[k]), y_body=y_body)
+        assert np.array_equal(got[k, 0], want[0]) and np.array_equal(got[k, 1], want[1])
+        with pytest.raises(inspire.PirError, match="Shard 9 not found"):
+            inspire.respond_seeded_batch(crs, edb, [0, 9, 0, 0, 0], seeds.array, rows.array, [cid] * n,
+                                         out=out.array)
+        for b in (seeds, rows, out):
+            b.close()
+        crs.release_client(cid)
