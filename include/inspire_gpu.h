@@ -232,7 +232,10 @@ int inspire_respond_seeded_nopacking_batch(inspire_ctx *ctx, const inspire_db *d
  * keys, host buffers: shard_ids[n], seeds[n][2*gadget_len][32],
  * b_rows[n][2*gadget_len][poly], client_ids[n], out_ct[n][2][poly].  Queries
  * may name different shards.  Each result is the one respond_seeded_inspiring
- * returns for that query alone. */
+ * returns for that query alone.  When b_rows and out_ct are page-locked
+ * (inspire_pinned_alloc, cudaHostAlloc or cudaHostRegister memory) and
+ * 16-byte aligned, the GPU reads the rows and writes the responses in place
+ * (no staging copies); other memory is staged through device buffers. */
 int inspire_respond_seeded_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n, const uint32_t *shard_ids,
                                  const uint8_t *seeds, const uint64_t *b_rows, const int32_t *client_ids,
                                  uint64_t *out_ct);
