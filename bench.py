@@ -756,7 +756,7 @@ def main():
                                      "rate probe (independent lazy Shoup multiply chains, all SMs)"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "gpu_launches": args.steps * L,
+            "gpu_launches": args.steps * L * 2,  # each device-row batch call: b-side launch + Respond launch
             "verified_responses": verified,
             "value_cuda_graph": value_graph,
             "value_capped_grid": value_grid,

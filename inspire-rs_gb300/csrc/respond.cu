@@ -43,12 +43,13 @@ namespace {
 // shared-memory read of a warp covers 256 contiguous bytes (no bank
 // conflicts).  Each lane issues its column loads 16 at a time, so the column
 // costs two memory latencies.
+template <int NT>
 __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, const uint64_t* rows, uint32_t* bp,
                           uint32_t* bpoly) {
   const int tid = threadIdx.x, gamma = P.gamma;
   const int lane = tid & 31, c = tid >> 5;
 #pragma unroll 8
-  for (int idx = tid; idx < ELL * 2 * N; idx += RBLOCK) {
+  for (int idx = tid; idx < ELL * 2 * N; idx += NT) {
     const int i = idx & (N - 1), tr = idx >> LOGN, r = tr & 1;
     uint32_t v = (uint32_t)rows[(size_t)tr * N + (i == 0 ? 0 : N - i)];
     if (i != 0 && v != 0) v = P.r[r].q - v;
@@ -93,6 +94,27 @@ __device__ void column_b0(const DevParams& P, const uint16_t* __restrict__ H, co
     }
   }
   __syncthreads();
+}
+
+// Device-row launches compute the b side in a launch of their own
+// (bside_kernel, 512 threads and 48 KiB of shared memory per query, so many
+// queries' loads are in flight per SM) and park each query's 32 b0 values in
+// the last 128 bytes of its response, which the Respond kernel reads at its
+// start and overwrites with the response at its end.
+constexpr int BSIDE_THREADS = 512;
+__device__ __forceinline__ uint32_t* b_parking(uint64_t* out, int qi) {
+  return reinterpret_cast<uint32_t*>(out + (size_t)qi * 4 * N + 4 * N - 16);
+}
+
+__global__ void __launch_bounds__(BSIDE_THREADS) bside_kernel(const __grid_constant__ RespondArgs A) {
+  extern __shared__ __align__(16) uint32_t sm[];  // [ELL][2][N] staged rows, then bpoly[32]
+  const int qi = blockIdx.x;
+  const uint32_t shard = A.shard[qi];
+  if (shard >= (uint32_t)A.nshards) return;  // the Respond kernel reports it
+  uint32_t* bpoly = sm + ELL * 2 * N;
+  if (threadIdx.x < 32) bpoly[threadIdx.x] = 0;  // columns past gamma
+  column_b0<BSIDE_THREADS>(A.P, A.H + (size_t)shard * A.P.gamma * N, A.brows + (size_t)qi * ELL * 2 * N, sm, bpoly);
+  if (threadIdx.x < 32) b_parking(A.out, qi)[threadIdx.x] = bpoly[threadIdx.x];
 }
 
 // A 64-bit load the compiler may neither hoist nor keep in a register: used
@@ -243,15 +265,12 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     mbar_init(rbar);
     wsb[18] = 0;  // set when the rows do not arrive
   }
-  if (tid == 0) {
-    prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
-    if (!QDB) prefetch_l2(brows, sizeof(uint64_t) * (size_t)ELL * 2 * N);
-  }
+  if (QDB && tid == 0) prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
   // the seeds, inline in the query's descriptor: staged into shared memory
   // (ordered before the expansion by the barrier below)
   uint8_t* seed_sm = reinterpret_cast<uint8_t*>(smem + L::MISC + 96);
   if (QDB && tid < ELL * 32) seed_sm[tid] = D->seeds[tid];
-  if (!QDB) column_b0(P, H, brows, SCAT, bpoly);  // bp aliases SCAT+PB
+  if (!QDB && tid < 32) bpoly[tid] = b_parking(A.out, qi)[tid];  // parked by bside_kernel
   if (tid == 0) {
     prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
     if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
@@ -309,7 +328,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   __syncthreads();
 
   // ---- serving loop: b part of the column products (bp in SC, rows staged) ----
-  if (QDB) column_b0(P, H, raw, SC, bpoly);
+  if (QDB) column_b0<RBLOCK>(P, H, raw, SC, bpoly);
 
   // scatter roles: fixed mode -> groups (r,1),(r,2) do residue r;
   // compat -> groups with digit 1, 2 of both residues do residue 0
@@ -502,8 +521,15 @@ static cudaError_t set_smem_attr() {
 // Launches issue no configuration call (so they can be captured in a CUDA
 // graph): the shared-memory attribute of every variant is set once per
 // device by prepare_respond_kernels.
+size_t bside_smem_bytes() { return sizeof(uint32_t) * ((size_t)ELL * 2 * N + 32); }
+
 template <int MODE, bool SEEDED, bool QDB>
 static cudaError_t launch_one(const RespondArgs& a, int ctas, cudaStream_t st) {
+  if (!QDB) {
+    bside_kernel<<<a.nq, BSIDE_THREADS, bside_smem_bytes(), st>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   if (!QDB && ctas < a.nq)
     respond_kernel_loop<MODE, SEEDED><<<ctas, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
   else
@@ -519,7 +545,7 @@ cudaError_t prepare_respond_kernels() {
       set_smem_attr<MODE_CRT_FIXED, false, true>(),  set_smem_attr<MODE_CRT_FIXED, true, true>()};
   for (cudaError_t e : es)
     if (e != cudaSuccess) return e;
-  return cudaSuccess;
+  return cudaFuncSetAttribute(bside_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bside_smem_bytes());
 }
 
 template <int MODE>
