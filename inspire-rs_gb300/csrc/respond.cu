@@ -26,7 +26,9 @@
 // r and gadget digit k.  Per recursion step, groups (r,0) run the inverse NTT
 // while groups (r,1),(r,2) scatter the query-only term R_i; then the three
 // digit NTTs of each residue run concurrently.  All intermediate state lives
-// in shared memory and registers; the kernel uses no global scratch.
+// in shared memory and registers, and no global scratch is used: device-row
+// launches take the b side from bside_kernel, which parks it in the last
+// 128 bytes of each query's response slot.
 #include "expand.cuh"
 #include "kernels.h"
 
@@ -256,9 +258,9 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   // Serving loop (rows in host memory): the query's b rows (96 KiB) are
   // bulk-copied (TMA) into shared memory (SCAT..ACC) while the rows are
   // expanded, so the host link's latency stays off the critical path, and the
-  // b side follows the row NTTs.  Rows in device memory: the b side comes
-  // first, reading them directly, with the raw columns and rows streamed into
-  // L2 ahead of it and the contracted shard and client keys after it.
+  // b side follows the row NTTs.  Rows in device memory: bside_kernel has
+  // already computed the b side and parked it in the response slot; the
+  // contracted shard and client keys are streamed into L2 from the start.
   uint64_t* raw = reinterpret_cast<uint64_t*>(SCAT);           // 16-byte aligned
   uint64_t* rbar = reinterpret_cast<uint64_t*>(smem + L::MISC + 120);  // the rows' mbarrier
   if (QDB && tid == 0) {
