@@ -50,7 +50,7 @@ LAUNCHES_PER_STEP = 16  # one step answers LAUNCHES_PER_STEP * BATCH queries
 POOL_BATCHES = 32       # distinct staged batches, cycled
 QUERY_POOL = 256        # distinct real seeded queries (device-side clients)
 N_CLIENTS = 32          # registered clients (own keys), QUERY_POOL / N_CLIENTS queries each
-STREAMS = 2             # CUDA streams the timed launches alternate over
+STREAMS = 4             # CUDA streams the timed launches alternate over
 REFERENCE_BUDGET_S = 150.0
 SERVE_RATE_FRACS = (0.25, 0.5, 0.75, 0.9)  # open-loop offered rates, fractions of the saturated e2e rate
 SERVE_DURATION_S = 1.5
@@ -734,7 +734,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "u32 modular integer (exact)", "data": "synthetic",
             "config": {"workload": f"batched InsPIRe^2 respond: 2^{args.log2_entries} entries x 32 B resident "
                                    f"({nshards} shards), B={B} seeded queries per launch, uniform shard ids",
-                       "step": f"{L} launches x {B} queries over {len(side)} streams",
+                       "step": f"{L} batch calls x {B} queries (a b-side and a Respond launch each) over "
+                               f"{len(side)} streams",
                        "streams": len(side),
                        "queries": f"{QUERY_POOL} distinct real seeded queries from {N_CLIENTS} clients generated "
                                   "on the device (keys, packing keys and queries; packing keys registered and "
