@@ -64,9 +64,10 @@ ALG_BYTES_PER_QUERY = 192 * 1024
 MULMODS_PER_QUERY = 3.4e6
 # resident database bytes one query reads: contracted form 768 KiB + raw columns 64 KiB
 DB_BYTES_PER_QUERY = (768 + 64) * 1024
-# dram__bytes_read.sum + dram__bytes_write.sum of one B=128 respond launch (queries of
-# 32 clients), from one ncu capture of the first timed launch on the 2^20-entry database
-NCU_TRAFFIC_PER_LAUNCH_B128 = 151.8e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one B=128 batch call (queries of 32
+# clients), from one ncu capture of the first timed call on the 2^20-entry database:
+# the Respond launch (131.7 MB) plus its b-side launch (19.7 MB)
+NCU_TRAFFIC_PER_LAUNCH_B128 = 151.4e6
 
 
 def dist_env():
