@@ -131,3 +131,37 @@ def test_nopacking_shard_not_found(world):
     with pytest.raises(inspire.PirError, match="Shard 7 not found"):
         inspire.respond_seeded_nopacking_batch(W["crs"], W["edb"], [0, 7], np.zeros((2, 6, 32), np.uint8),
                                                np.zeros((2, 6, 2 * N), np.uint64))
+
+
+@pytest.mark.parametrize("entry_size,gamma", [(2, 1), (4, 2), (16, 8)])
+def test_nopacking_other_column_counts(oracle_mod, entry_size, gamma):
+    """NoPacking with fewer columns (gamma = 1, 2, 8), full and partial
+    shards: the combined-only path (digit sums) and the with-columns path (a
+    single query: its columns split over CTAs), against the oracle.  Column
+    counts that are not powers of two are refused by the GPU path."""
+    import inspire
+
+    O = oracle_mod
+    rng = np.random.default_rng(100 + entry_size)
+    n_entries = N + 500
+    db = rng.integers(0, 256, size=n_entries * entry_size, dtype=np.uint8)
+    ctx = O.Ctx()
+    client = O.Client(ctx, seed=2, rng_seed=entry_size)
+    crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, gamma, mode="crt_fixed")
+    edb = inspire.EncodedDatabase(crs, db, entry_size)
+    for index in (7, N + 499):
+        sid, local = divmod(index, N)
+        seeds, b_rows = client.query_seeded(local)
+        want, want_cols = ctx.respond_nopacking(ctx.encode_shard(db, entry_size, sid), ctx.expand_rgsw(seeds, b_rows),
+                                                with_columns=True)
+        q = inspire.SeededClientQuery(sid, seeds, b_rows)
+        full = inspire.respond_seeded(crs, edb, q)
+        assert len(full.column_ciphertexts) == gamma
+        assert np.array_equal(np.stack([full.ciphertext.a, full.ciphertext.b]), want)
+        assert np.array_equal(np.stack([np.stack([c.a, c.b]) for c in full.column_ciphertexts]), want_cols)
+        comb = inspire.respond_seeded(crs, edb, q, with_columns=False)
+        assert np.array_equal(np.stack([comb.ciphertext.a, comb.ciphertext.b]), want)
+    edb.close()
+    crs.close()
+    with pytest.raises(inspire.PirError, match="num_columns"):
+        inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 3, mode="crt_fixed")
