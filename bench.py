@@ -560,7 +560,7 @@ def main():
     # one wave per launch: the same step shape with launches of one query per
     # SM (152 on GB300) instead of B, drawn from the same pool, responses into
     # a scratch buffer
-    value_wave = None
+    value_wave = value_one_call = None
     if ws == 1:
         n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
         tot = nb * B
@@ -597,6 +597,28 @@ def main():
             torch.cuda.synchronize()
             assert not w_status.cpu().numpy().any(), "one-wave launches reported a nonzero status"
             value_wave = L * n_sm * args.steps / (sum(a.elapsed_time(b) for a, b in wev) / 1e3)
+
+            # the whole step as one batch call (L * B queries, one CTA each)
+            def one_call(k):
+                b0 = ((k * L * B) % (tot - L * B + 1)) if tot > L * B else 0
+                inspire.respond_seeded_batch_device(crs, edb, L * B, f_shard[b0].data_ptr(), f_seeds[b0].data_ptr(),
+                                                    f_brows[b0].data_ptr(), f_client[b0].data_ptr(),
+                                                    w_out[b0].data_ptr(), w_status[b0].data_ptr(), sp)
+
+            if L * B <= tot:
+                for k in range(args.warmup):
+                    one_call(k)
+                torch.cuda.synchronize()
+                oev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                       for _ in range(args.steps)]
+                for k in range(args.steps):
+                    flush.fill_(k & 0xFF)
+                    oev[k][0].record(stream)
+                    one_call(k)
+                    oev[k][1].record(stream)
+                torch.cuda.synchronize()
+                assert not w_status.cpu().numpy().any(), "the one-call step reported a nonzero status"
+                value_one_call = L * B * args.steps / (sum(a.elapsed_time(b) for a, b in oev) / 1e3)
             del w_out
 
     # correctness of what was timed: statuses, then every response of the nb
@@ -763,6 +785,7 @@ def main():
             "value_cuda_graph": value_graph,
             "value_capped_grid": value_grid,
             "value_one_wave": value_wave,
+            "value_one_call": value_one_call,
             "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
             "plain_single_query_qps": sweep.get("1"),
