@@ -252,7 +252,11 @@ int inspire_respond_batch(inspire_ctx *ctx, const inspire_db *db, uint32_t n, co
  * gadget_len..2*gadget_len-1 ([n][gadget_len][32]) and b_rows only those rows
  * ([n][gadget_len][poly], 16-byte aligned); d_status[n] receives 0 or a
  * nonzero kernel status (unknown shard or client id, exhausted expansion
- * bound). */
+ * bound).  Two launches: the b side of every query, parked in the last 128
+ * bytes of its d_out_ct slot, then the Respond kernel, which overwrites the
+ * slot with the response (a slot whose status is nonzero holds no response).
+ * No allocation and no configuration call: the call can be captured in a
+ * CUDA graph. */
 int inspire_respond_seeded_batch_device(inspire_ctx *ctx, const inspire_db *db, uint32_t n,
                                         const uint32_t *d_shard_ids, const uint8_t *d_seeds,
                                         const uint64_t *d_b_rows, const int32_t *d_client_ids, uint64_t *d_out_ct,
