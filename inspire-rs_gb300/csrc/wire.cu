@@ -104,6 +104,7 @@ struct Json {
     *n = 0;
     if (!expect('[')) return false;
     if (eat(']')) return true;
+    if (compact_run(out, cap, n)) return expect(']');
     for (;;) {
       uint64_t v;
       // compact runs ("123,45,...") eight bytes at a time; anything else
@@ -142,6 +143,87 @@ struct Json {
     p += len;
     v = x;
     return true;
+  }
+  // A compact run "d,d,...,d" of unsigned integers of 1..16 digits up to
+  // the closing ']': the commas are located first, eight bytes at a time,
+  // then every number is parsed on its own (SWAR), so that parsing one
+  // number does not wait for the end of the previous one to be found.
+  // Returns false, consuming nothing, for any other array body (whitespace,
+  // signs, empty or long elements, too many elements): the checked path
+  // then parses it and reports its errors.
+  bool compact_run(uint64_t* out, size_t cap, size_t* n) {
+    const char* s = p;
+    const char* q = s;
+    cpos.clear();
+    constexpr uint64_t H = 0x8080808080808080ull;
+    bool stop = false;
+    while (!stop && end - q >= 8) {
+      uint64_t w;
+      memcpy(&w, q, 8);
+      const uint64_t comma = byte_eq(w, ',');
+      const uint64_t other = ~(digit_bits(w) | comma) & H;
+      uint64_t cm = comma;
+      if (other) {
+        cm &= (other & (0 - other)) - 1;  // the commas before the first other byte
+        stop = true;
+      }
+      for (; cm; cm &= cm - 1) cpos.push_back((uint32_t)(q - s) + (uint32_t)(__builtin_ctzll(cm) >> 3));
+      q += other ? (__builtin_ctzll(other) >> 3) : 8;
+    }
+    if (!stop)
+      for (; q < end && ((unsigned)(*q - '0') < 10u || *q == ','); q++)
+        if (*q == ',') cpos.push_back((uint32_t)(q - s));
+    if (q >= end || *q != ']' || q == s) return false;
+    const size_t k = cpos.size() + 1;
+    if (k > cap) return false;
+    uint32_t start = 0;
+    for (size_t i = 0; i < k; i++) {
+      const uint32_t stop_at = i + 1 < k ? cpos[i] : (uint32_t)(q - s);
+      const uint32_t len = stop_at - start;
+      if (len == 0 || len > 16) return false;
+      const char* a = s + start;
+      uint64_t v;
+      if (end - a >= 16) {
+        // branch-free over the length: 8- and 9-digit values alternate at random
+        uint64_t w0, w1;
+        memcpy(&w0, a, 8);
+        memcpy(&w1, a + 8, 8);
+        const int l0 = len < 8 ? (int)len : 8, l1 = (int)len - l0;
+        v = swar_any(w0, l0) * kPow10[l1] + swar_any(w1, l1);
+      } else {
+        v = 0;
+        for (uint32_t j = 0; j < len; j++) v = v * 10 + (uint64_t)(a[j] - '0');
+      }
+      out[i] = v;
+      start = stop_at + 1;
+    }
+    *n = k;
+    p = q;
+    return true;
+  }
+  std::vector<uint32_t> cpos;  // comma offsets of the current compact run
+  static constexpr uint64_t kPow10[9] = {1, 10, 100, 1000, 10000, 100000, 1000000, 10000000, 100000000};
+  // value of the first n (0..8) digits of w; 0 for n = 0
+  static uint64_t swar_any(uint64_t w, int n) {
+    uint64_t d = w - 0x3030303030303030ull;
+    const int sh = 4 * (8 - n);  // two shifts: n = 0 clears d without a 64-bit shift
+    d = (d << sh) << sh;
+    d = (d * 10 + (d >> 8)) & 0x00ff00ff00ff00ffull;
+    d = (d * 100 + (d >> 16)) & 0x0000ffff0000ffffull;
+    return (d * 10000 + (d >> 32)) & 0xffffffffull;
+  }
+  // high bit of every byte of w equal to c
+  static uint64_t byte_eq(uint64_t w, char c) {
+    const uint64_t L7 = 0x7f7f7f7f7f7f7f7full;
+    const uint64_t x = w ^ (0x0101010101010101ull * (uint8_t)c);
+    return ~(((x & L7) + L7) | x | L7);
+  }
+  // high bit of every ASCII digit byte of w
+  static uint64_t digit_bits(uint64_t w) {
+    const uint64_t H = 0x8080808080808080ull;
+    const uint64_t ge0 = ((w | H) - 0x3030303030303030ull) & H;
+    const uint64_t ge10 = ((w | H) - 0x3a3a3a3a3a3a3a3aull) & H;
+    return ge0 & ~ge10 & ~(w & H);
   }
   // number of leading ASCII digits in the 8 bytes of w (first byte lowest)
   static int digit_run(uint64_t w) {
@@ -272,8 +354,12 @@ bool parse_poly(Json& j, const inspire_params& P, uint64_t* dst, const std::stri
     return j.fail(what + ": moduli differ from the context");
   if (dim != P.ring_dim || ncoeffs != plen) return j.fail(what + ": dimension mismatch");
   if (is_ntt) return j.fail(what + ": expected coefficient form (is_ntt false)");
-  for (size_t i = 0; i < plen; i++)
-    if (dst[i] >= moduli[i / P.ring_dim]) return j.fail(what + ": residue not reduced");
+  for (size_t r = 0; r < 2; r++) {  // residue-major: coefficient i of residue r at r * ring_dim + i
+    const uint64_t m = moduli[r], *d = dst + r * P.ring_dim;
+    uint64_t bad = 0;
+    for (size_t i = 0; i < (size_t)P.ring_dim; i++) bad |= (uint64_t)(d[i] >= m);
+    if (bad) return j.fail(what + ": residue not reduced");
+  }
   return true;
 }
 
