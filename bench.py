@@ -265,6 +265,25 @@ def kernel_microbench(inspire, crs, torch, dev, reps=20):
         dt = e0.elapsed_time(e1) / 1e3
         best = dt if best is None else min(best, dt)
     res["mulmod_rate_tps"] = nmm / best / 1e12  # 10^12 modular multiplies per second
+    # integer tensor cores: INT8 MMA rate (mma.sync m16n8k32 s8 -> s32; the
+    # tcgen05 INT8 kind does not exist for sm_103a), exactness checked
+    ga = torch.Generator(device="cpu").manual_seed(8)
+    a8 = torch.randint(-128, 128, (16, 32), generator=ga, dtype=torch.int8)
+    b8 = torch.randint(-128, 128, (32, 8), generator=ga, dtype=torch.int8)
+    da, db_ = a8.to(dev), b8.to(dev)
+    dout = torch.zeros(4 * 16 * 8, dtype=torch.int32, device=dev)
+    best = None
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        nops = inspire.pir.int8_mma_rate_device(crs, 152 * 8, 4096, da.data_ptr(), db_.data_ptr(), dout.data_ptr(), sp)
+        e1.record(st)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) / 1e3
+        best = dt if best is None else min(best, dt)
+    want = 4096 * (a8.to(torch.int64) @ b8.to(torch.int64))
+    res["int8_mma_tops"] = nops / best / 1e12
+    res["int8_mma_exact"] = bool(torch.equal(dout.cpu().view(4, 16, 8).to(torch.int64), want.expand(4, 16, 8)))
     # bytes moved per NTT launch: read + write of 4096 x 2 x 2048 u32
     byts = 2 * 4096 * 2 * N * 4
     res["ntt_forward_gbs"] = byts / (res["ntt_forward_4096x2_us"] * 1e-6) / 1e9

@@ -290,6 +290,13 @@ typedef struct {
                              Fewer streams are used if max_inflight batches do not fit. */
   uint32_t batch_wait_us; /* while at least one query per SM is in flight, a free
                              stream waits up to this long for a full batch */
+  uint32_t stage_wait_iters; /* bound of the Respond kernel's wait for a query's rows,
+                             copied from pinned host memory into shared memory, in
+                             wait iterations.  When it runs out the query fails
+                             (INSPIRE_ERR_DEVICE_STATUS) and the next batches are
+                             served as usual; 0 gives up at once (a test of that
+                             path).  If the copies are still in flight after a
+                             second, longer wait, every query of that batch fails. */
 } inspire_server_config;
 
 typedef struct {
@@ -298,7 +305,8 @@ typedef struct {
   uint32_t streams;                       /* streams in use (after the device budget) */
 } inspire_server_stats;
 
-/* max_batch 128, max_inflight 4, capacity 4096, device_budget 0, batch_wait_us 100. */
+/* max_batch 128, max_inflight 4, capacity 4096, device_budget 0, batch_wait_us 100,
+ * stage_wait_iters 2^20. */
 void inspire_server_config_default(inspire_server_config *cfg);
 int inspire_server_create(inspire_ctx *ctx, const inspire_server_config *cfg, inspire_server **out);
 /* Waits for batches in flight, then frees the loop.  Unpolled tickets die. */
@@ -410,7 +418,10 @@ int inspire_extract_inspiring_device(inspire_ctx *ctx, const uint64_t *d_sk, con
  * d_out_b [n][2 polys], d_status [n]) and enqueues its work on `stream`
  * without allocating: its scratch (column ciphertexts, combined ciphertext,
  * the tree's work area; 2.0 MiB per query) is one static device array per
- * device, located once with cudaGetSymbolAddress.  n > 2 is rejected.
+ * device, whose address is looked up with cudaGetSymbolAddress on every
+ * call.  The first call on a device may load the library's device code into
+ * that device's context (CUDA's lazy loading), so make it before any stream
+ * capture.  n > 2 is rejected.
  * Calls that overlap on the device (from several host threads, or on
  * streams that run concurrently) race on that array: issue them on one
  * stream, or wait for one to finish before the next starts.  A query whose
@@ -489,6 +500,15 @@ int inspire_query_seeded_device(inspire_ctx *ctx, const uint64_t *d_sk, const ui
  * `stream`; d_sink receives blocks * 256 u32.  Timing it gives the integer
  * roofline denominator of the integer-bound kernels. */
 int inspire_mulmod_rate_device(inspire_ctx *ctx, uint32_t blocks, uint32_t iters, uint32_t *d_sink, void *stream);
+
+/* Rate probe with no crate counterpart: the integer tensor-core rate that an
+ * 8-bit-limb contraction would run at.  blocks x 8 warps x 4 chains x iters
+ * INT8 MMAs (mma.sync m16n8k32, s8 x s8 -> s32; 8192 operations each) of
+ * d_a (16 x 32 s8, row-major) by d_b (32 x 8 s8, row-major) on `stream`.
+ * d_out [4][16][8] receives the first warp's four accumulators, each exactly
+ * iters * (A B).  iters <= 4096 (no INT32 overflow). */
+int inspire_int8_mma_rate_device(inspire_ctx *ctx, uint32_t blocks, uint32_t iters, const int8_t *d_a,
+                                 const int8_t *d_b, int32_t *d_out, void *stream);
 
 #ifdef __cplusplus
 }

@@ -120,7 +120,11 @@ int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all,
   if (!y_body && !y_all)
     return fail(INSPIRE_ERR_KEYS_INVALID, "InspiRING packing keys invalid: y_all and y_body are both empty");
   const int gamma = c->gamma;
-  const size_t tbl_words = (size_t)std::max(1, (gamma - 1) * ELL) * poly_words();
+  // From y_body at gamma = 16 the table holds NTT(y_body) only (48 KiB, the
+  // Respond kernel forms each rotation in registers); from an explicit y_all,
+  // or at smaller gamma, all (gamma-1)*ELL rotated polys.
+  const bool body_form = !y_all && gamma == MAX_GAMMA;
+  const size_t tbl_words = (size_t)std::max(1, body_form ? ELL : (gamma - 1) * ELL) * poly_words();
   DevMem* m = new DevMem();
   cudaError_t e = m->ensure(tbl_words * sizeof(uint32_t));
   if (e != cudaSuccess) {
@@ -133,7 +137,8 @@ int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all,
     CUDA_TRY(cudaMemcpyAsync(c->d_keys.p, y_all ? y_all : y_body, in_polys * poly_words() * sizeof(uint64_t),
                              cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(y_all ? launch_client_from_yall(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream)
-                   : launch_client_from_ybody(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream));
+                   : launch_client_from_ybody(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(),
+                                              body_form ? 1 : gamma - 1, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
   }
   int slot = -1;
@@ -148,7 +153,10 @@ int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all,
     c->client_ptrs.push_back(nullptr);
   }
   c->clients[slot] = m;
-  c->client_ptrs[slot] = m->as<uint32_t>();
+  // bit 0 of the device table entry marks a body table (allocations are
+  // 256-byte aligned)
+  c->client_ptrs[slot] = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(m->as<uint32_t>()) |
+                                                           (body_form ? 1u : 0u));
   c->client_table_dirty = true;
   *id = slot;
   return INSPIRE_OK;
@@ -1135,6 +1143,16 @@ int inspire_mulmod_rate_device(inspire_ctx* c, uint32_t blocks, uint32_t iters, 
   if (!c || (blocks && !d_sink)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   if (int rc = set_device(c)) return rc;
   CUDA_TRY(launch_mulmod_rate(c->P, (int)blocks, (int)iters, d_sink, (cudaStream_t)stream));
+  return INSPIRE_OK;
+}
+
+int inspire_int8_mma_rate_device(inspire_ctx* c, uint32_t blocks, uint32_t iters, const int8_t* d_a, const int8_t* d_b,
+                                 int32_t* d_out, void* stream) {
+  if (!c || !d_a || !d_b || !d_out) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (blocks == 0 || blocks > (1u << 20) || iters == 0 || iters > 4096)
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "blocks in [1, 2^20] and iters in [1, 4096]");
+  if (int rc = set_device(c)) return rc;
+  CUDA_TRY(launch_int8_mma_rate(d_a, d_b, (int)blocks, (int)iters, d_out, (cudaStream_t)stream));
   return INSPIRE_OK;
 }
 

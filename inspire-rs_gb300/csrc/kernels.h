@@ -11,6 +11,12 @@ namespace ig {
 constexpr int ERR_EXPAND = 1;  // seeded expansion exceeded its iteration bound
 constexpr int ERR_INDEX = 2;   // shard or client id out of range
 constexpr int ERR_STAGE = 3;   // the query's rows did not arrive in shared memory within the wait bound
+// ... and the copies were still in flight after the drain wait: results of
+// the whole launch are unreliable (a later CTA on the SM may have received
+// the late copies in its shared memory)
+constexpr int ERR_STAGE_LOST = 4;
+constexpr uint32_t STAGE_WAIT_ITERS_DEFAULT = 1u << 20;
+constexpr uint32_t STAGE_DRAIN_ITERS = 1u << 22;
 
 // One resident database as the Respond kernel sees it.
 struct DbView {
@@ -42,7 +48,10 @@ struct RespondArgs {
   const uint64_t* arows;         // [nq][ELL][2][N] a-polys of rows ELL..2ELL-1 (unseeded queries) or null
   const uint64_t* brows;         // [nq][ELL][2][N] b-polys of rows ELL..2ELL-1
   const int32_t* client;         // [nq] client id
-  const uint32_t* const* yhat_table;  // [nclients] -> key table [(gamma-1)][ELL][2][N]
+  // [nclients] -> client key table: [(gamma-1)][ELL][2][N] rotated keys,
+  // or, when the pointer's bit 0 is set (gamma = 16 only), the body table
+  // [ELL][2][N] whose rotations the kernel forms
+  const uint32_t* const* yhat_table;
   int nclients, nshards;
   const uint32_t* E;             // [nshards][2][ELL][gamma][N] contracted database
   const uint16_t* H;             // [nshards][gamma][N] raw 16-bit columns
@@ -53,6 +62,9 @@ struct RespondArgs {
   // client, seeds, brows, E/H/nshards, out and status; rows are read from and
   // responses written to the pinned host memory they point at), or null.
   const struct QueryDesc* qdesc;
+  // Serving loop: bound of the wait for a query's staged rows, in wait
+  // iterations (0: give up at once)
+  uint32_t stage_wait_iters;
 };
 
 // NoPacking respond (respond.rs:71-115): per query the combined ciphertext
@@ -175,7 +187,9 @@ cudaError_t launch_encode_E(const DevParams& P, const uint16_t* H, int nshards, 
                             cudaStream_t st);
 cudaError_t launch_crs_what(const DevParams& P, const uint32_t* wmask, uint32_t* what,
                             cudaStream_t st);
-cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat,
+// The first nrot rotations y_all[0..nrot) of the client key table (nrot =
+// gamma - 1: the full table; 1: the body table the Respond kernel rotates).
+cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat, int nrot,
                                      cudaStream_t st);
 cudaError_t launch_client_from_yall(const DevParams& P, const uint64_t* yall, uint32_t* yhat,
                                     cudaStream_t st);
@@ -187,6 +201,10 @@ cudaError_t launch_extract(const DevParams& P, uint64_t p, const uint64_t* sk, c
                            int entry_size, uint8_t* entries, cudaStream_t st);
 // blocks x 256 threads x 8 chains x iters lazy Shoup multiplies; sink[blocks * 256].
 cudaError_t launch_mulmod_rate(const DevParams& P, int blocks, int iters, uint32_t* sink, cudaStream_t st);
+// blocks x 8 warps x 4 chains x iters INT8 MMAs (m16n8k32); out[4][16][8]
+// receives warp 0's accumulators (= iters * A B for iters <= 4096).
+cudaError_t launch_int8_mma_rate(const int8_t* A, const int8_t* B, int blocks, int iters, int32_t* out,
+                                 cudaStream_t st);
 cudaError_t launch_ntt_ref(const DevParams& P, uint32_t* polys, int npolys, bool inverse,
                            cudaStream_t st);
 cudaError_t launch_external_product(const DevParams& P, const uint32_t* ct, const uint32_t* rgsw,

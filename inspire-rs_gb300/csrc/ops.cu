@@ -122,6 +122,56 @@ __global__ void __launch_bounds__(MM_BLOCK) mulmod_rate_kernel(uint32_t q, uint3
   sink[t] = acc;
 }
 
+// Integer tensor-core probe.  sm_103a has no tcgen05 INT8 MMA (ptxas
+// rejects tcgen05.mma .kind::i8 for this target), so the only INT8 tensor
+// instruction is the legacy warp-level mma.sync m16n8k32 s8 x s8 -> s32.
+// Every warp loads the same A (16 x 32, row-major) and B (32 x 8,
+// column-major) fragments and runs I8_CHAINS independent accumulators
+// through `iters` dependent MMAs (D = A B + D).  Warp 0 of block 0 writes its
+// accumulators, which must equal iters * A B exactly (|A B| <= 32 * 128^2,
+// so iters <= 4096 cannot overflow): the check of the fragment layout and of
+// exact INT32 accumulation.  Operations per MMA: 2 * 16 * 8 * 32.
+constexpr int I8_CHAINS = 4;
+
+__device__ __forceinline__ uint32_t pack_s8(const int8_t* p, int stride) {
+  return (uint32_t)(uint8_t)p[0] | ((uint32_t)(uint8_t)p[stride] << 8) | ((uint32_t)(uint8_t)p[2 * stride] << 16) |
+         ((uint32_t)(uint8_t)p[3 * stride] << 24);
+}
+
+__global__ void __launch_bounds__(MM_BLOCK) int8_mma_rate_kernel(const int8_t* __restrict__ A,
+                                                                 const int8_t* __restrict__ B, int iters,
+                                                                 int32_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31, grp = lane >> 2, tig = lane & 3;
+  // A fragment: rows grp / grp + 8, columns 4 tig + {0..3} and 16 + 4 tig + {0..3}
+  const uint32_t a0 = pack_s8(A + grp * 32 + 4 * tig, 1), a1 = pack_s8(A + (grp + 8) * 32 + 4 * tig, 1);
+  const uint32_t a2 = pack_s8(A + grp * 32 + 16 + 4 * tig, 1), a3 = pack_s8(A + (grp + 8) * 32 + 16 + 4 * tig, 1);
+  // B fragment (B stored row-major 32 x 8 here): rows 4 tig + {0..3} and 16 + 4 tig + {0..3}, column grp
+  const uint32_t b0 = pack_s8(B + (4 * tig) * 8 + grp, 8), b1 = pack_s8(B + (16 + 4 * tig) * 8 + grp, 8);
+  int32_t d[I8_CHAINS][4] = {};
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int c = 0; c < I8_CHAINS; c++)
+      asm volatile(
+          "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+          "{%0, %1, %2, %3};"
+          : "+r"(d[c][0]), "+r"(d[c][1]), "+r"(d[c][2]), "+r"(d[c][3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    // D fragment: d0, d1 at row grp, columns 2 tig + {0, 1}; d2, d3 at row grp + 8
+#pragma unroll
+    for (int c = 0; c < I8_CHAINS; c++) {
+      int32_t* o = out + c * 16 * 8;
+      o[grp * 8 + 2 * tig] = d[c][0];
+      o[grp * 8 + 2 * tig + 1] = d[c][1];
+      o[(grp + 8) * 8 + 2 * tig] = d[c][2];
+      o[(grp + 8) * 8 + 2 * tig + 1] = d[c][3];
+    }
+  } else if (d[0][0] == 0x7fffffff && d[1][1] == 0x7fffffff && d[2][2] == d[3][3]) {
+    out[0] = 0;  // never taken for iters <= 4096; keeps the MMAs live
+  }
+}
+
 // Client-side decrypt + extract_inspiring for one response per CTA
 // (src/pir/extract.rs:155-182 with RlweCiphertext::decrypt,
 // src/rlwe/enc.rs:90-108, and reconstruct_entry, src/pir/encode_db.rs:186-201).
@@ -192,6 +242,12 @@ cudaError_t launch_extract(const DevParams& P, uint64_t p, const uint64_t* sk, c
   K.ncols = (entry_size * 8 + 15) / 16;
   K.entry_size = entry_size;
   extract_kernel<<<n, 256, 0, st>>>(P, K, sk, ct, entries);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_int8_mma_rate(const int8_t* A, const int8_t* B, int blocks, int iters, int32_t* out,
+                                 cudaStream_t st) {
+  int8_mma_rate_kernel<<<blocks, MM_BLOCK, 0, st>>>(A, B, iters, out);
   return cudaGetLastError();
 }
 

@@ -162,9 +162,9 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }
 
 // Wait, with an iteration bound, for phase `parity` of `bar` to complete;
-// false when the bound ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 20); it++) {
+// false when the bound ran out (at once for limit 0).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; it++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -197,6 +197,44 @@ __device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint3
     const uint32_t s = brv11(((hi * e) & (2 * N - 1)) >> 1);
     dst[swz(s)] = redc(T, q, qinv);
   }
+}
+
+// y_all[i][k] from NTT(y_body[k]) in registers (gamma = 16).  In the NTT
+// domain tau_{g^i} (generate_rotations, inspiring2.rs:1309-1323) is the slot
+// permutation s -> u with 2brv(u)+1 = g^i (2brv(s)+1) mod 2n.  With
+// g = 2n/16 + 1, g^i = 1 + 256 i mod 2n, so brv(u) = brv(s) + 128 delta mod
+// 2n with delta = i (2brv(s)+1) mod 16: only the top four bits of brv(s)
+// move, i.e. only the low four bits of s, and delta depends on s only
+// through s >> 4.  Each thread's run of slots 16x..16x+15 is therefore a
+// rotation by delta of itself, indexed by brv4 of the slot's low bits:
+// out[brv4(h)] = in[brv4((h + delta) mod 16)].  Done as a four-stage barrel
+// shift of register selects.
+__device__ __forceinline__ void rotate_key_run(uint4 (&y)[4], int i, int x) {
+  uint32_t z[16];  // z[h] = in[brv4(h)]
+#pragma unroll
+  for (int h = 0; h < 16; h++) {
+    const int j = ((h & 1) << 3) | ((h & 2) << 1) | ((h & 4) >> 1) | ((h & 8) >> 3);
+    const uint4& c = y[j >> 2];
+    z[h] = (j & 3) == 0 ? c.x : (j & 3) == 1 ? c.y : (j & 3) == 2 ? c.z : c.w;
+  }
+  const uint32_t delta = ((uint32_t)i * (2u * brv11(16u * (uint32_t)x) + 1u)) & 15u;
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const bool on = (delta >> b) & 1u;
+    uint32_t t[16];
+#pragma unroll
+    for (int h = 0; h < 16; h++) t[h] = on ? z[(h + (1 << b)) & 15] : z[h];
+#pragma unroll
+    for (int h = 0; h < 16; h++) z[h] = t[h];
+  }
+  uint32_t o[16];
+#pragma unroll
+  for (int h = 0; h < 16; h++) {
+    const int j = ((h & 1) << 3) | ((h & 2) << 1) | ((h & 4) >> 1) | ((h & 8) >> 3);
+    o[j] = z[h];
+  }
+#pragma unroll
+  for (int r4 = 0; r4 < 4; r4++) y[r4] = make_uint4(o[4 * r4], o[4 * r4 + 1], o[4 * r4 + 2], o[4 * r4 + 3]);
 }
 
 // Shared-memory layout in u32 words (NR = residues of the a side).
@@ -251,7 +289,12 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   }
   const uint32_t* E = Ebase + (size_t)shard * 2 * ELL * gamma * N;
   const uint16_t* H = Hbase + (size_t)shard * gamma * N;
-  const uint32_t* Y = A.yhat_table[cid];
+  // The client's key table: a body table (tag bit 0 set: NTT(y_body[k]),
+  // ELL polys, 48 KiB) whose rotations are formed in registers, or the full
+  // table of (gamma-1)*ELL rotated polys (explicit y_all).
+  const uintptr_t ytag = reinterpret_cast<uintptr_t>(A.yhat_table[cid]);
+  const bool ybody = (ytag & 1) != 0;
+  const uint32_t* Y = reinterpret_cast<const uint32_t*>(ytag & ~(uintptr_t)1);
   const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
   const uint64_t* brows = QDB ? D->brows : A.brows + (size_t)qi * ELL * 2 * N;
 
@@ -275,7 +318,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   if (!QDB && tid < 32) bpoly[tid] = b_parking(A.out, qi)[tid];  // parked by bside_kernel
   if (tid == 0) {
     prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
-    if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(gamma - 1) * ELL * 2 * N);
+    if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(ybody ? 1 : gamma - 1) * ELL * 2 * N);
   }
   if (QDB) {
     __syncthreads();  // the mbarrier is initialised, the seeds staged
@@ -304,15 +347,19 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     }
   }
   if (QDB) {
-    // rows that never arrive (the bound ran out) end the query with a status,
-    // after a second bounded wait for the copies still in flight
-    const bool arrived = mbar_wait(rbar, 0);
+    // rows that do not arrive within A.stage_wait_iters end the query with
+    // a status, after a second bounded wait for the copies still in flight
+    const bool arrived = mbar_wait(rbar, 0, A.stage_wait_iters);
     if (!arrived) wsb[18] = 1;
   }
   __syncthreads();
   if (QDB && wsb[18]) {
-    mbar_wait(rbar, 0);
-    if (tid == 0) *status_ptr() = ERR_STAGE;
+    // The CTA must not exit while its bulk copies can still write into its
+    // shared memory (the next CTA on this SM would own it).  If even the
+    // drain wait runs out, ERR_STAGE_LOST tells the host to drop every
+    // result of this launch.
+    const int lost = __syncthreads_or(!mbar_wait(rbar, 0, STAGE_DRAIN_ITERS));
+    if (tid == 0) *status_ptr() = lost ? ERR_STAGE_LOST : ERR_STAGE;
     return;  // uniform over the CTA
   }
   // the query's status is written once, by one thread
@@ -393,7 +440,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     uint4 wv[4], yv[4];
     {
       const uint4* w4 = reinterpret_cast<const uint4*>(A.what + off);
-      const uint4* y4 = reinterpret_cast<const uint4*>(Y + off);
+      const uint4* y4 = reinterpret_cast<const uint4*>(Y + (ybody ? off - (size_t)i * ELL * 2 * N : off));
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
         wv[r4] = __ldg(w4 + r4);
@@ -403,6 +450,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
     ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    if (ybody) rotate_key_run(yv, i, x);
     {
       const int f = (x >> 1) & 3;
       uint32_t* accp = ACC + 16 * x;

@@ -17,8 +17,11 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <thread>
+
+#include <cuda.h>
 
 #include "host.h"
 
@@ -56,6 +59,7 @@ struct Rec {
   int64_t t_arrival = 0, t_done = 0;
   int64_t t_enqueue = 0;  // when the query became pending
   int cuda_error = 0;  // nonzero: the batch failed on the host side
+  bool batch_lost = false;  // a CTA of the query's batch exited with copies in flight
 };
 
 struct Slot {
@@ -117,6 +121,7 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   a.nclients = (int)ctx->client_ptrs.size();
   a.what = ctx->what.as<uint32_t>();
   a.qdesc = s.ddesc.as<QueryDesc>();
+  a.stage_wait_iters = cfg.stage_wait_iters;
   CUDA_TRY(launch_respond(a, true, s.st));
   CUDA_TRY(cudaEventRecord(s.ev, s.st));
   return INSPIRE_OK;
@@ -146,6 +151,13 @@ void inspire_server::run() {
       for (size_t k = 0; k < finished.size(); k++) {
         Slot& s = *finished[k];
         const cudaError_t e = fin_err[k];
+        // one query whose staged rows were still in flight when its CTA
+        // exited makes every result of the launch unreliable
+        bool lost = false;
+        if (e == cudaSuccess)
+          for (int i : s.recs)
+            lost |= *reinterpret_cast<const volatile int32_t*>(rec_ptr(i) + REC_STATUS) == ERR_STAGE_LOST;
+        for (int i : s.recs) recs[i].batch_lost = lost;
         for (int i : s.recs) {
           recs[i].state = DONE;
           recs[i].t_done = t;
@@ -212,10 +224,67 @@ void inspire_server::run() {
   }
 }
 
+namespace {
+
+// Allocations made by inspire_pinned_alloc (base -> bytes).
+std::mutex g_pinned_mu;
+std::map<uintptr_t, size_t> g_pinned;
+
+bool in_own_pinned(const void* p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  auto it = g_pinned.upper_bound(a);
+  if (it == g_pinned.begin()) return false;
+  --it;
+  return a >= it->first && bytes <= it->second && a - it->first <= it->second - bytes;
+}
+
+// cuPointerGetAttribute, reached through the runtime's driver entry point so
+// that the library does not link against libcuda itself.
+using PtrAttrFn = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+PtrAttrFn ptr_attr_fn() {
+  static const PtrAttrFn f = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult st = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &st) != cudaSuccess ||
+        st != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return static_cast<PtrAttrFn>(nullptr);
+    }
+    return reinterpret_cast<PtrAttrFn>(fn);
+  }();
+  return f;
+}
+
+// Whether [p, p + bytes) lies inside the one allocation that p belongs to,
+// by the driver's record of that allocation's address range.
+bool within_one_allocation(const void* p, size_t bytes) {
+  const PtrAttrFn f = ptr_attr_fn();
+  if (!f) return false;
+  CUdeviceptr start = 0;
+  size_t size = 0;
+  const CUdeviceptr a = (CUdeviceptr) reinterpret_cast<uintptr_t>(p);
+  if (f(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, a) != CUDA_SUCCESS ||
+      f(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, a) != CUDA_SUCCESS)
+    return false;
+  return a >= start && bytes <= size && a - start <= size - bytes;
+}
+
+}  // namespace
+
 namespace ighost {
 
-// Device address of a page-locked host range [p, p + bytes), or null.
+// Device address of a page-locked host range [p, p + bytes), or null.  The
+// whole range must lie in ONE page-locked allocation: checking its two ends
+// alone would accept a range that spans two adjacent allocations with
+// ordinary memory between them, which a kernel would then read.  Ranges in
+// memory from inspire_pinned_alloc are checked against the library's own
+// record of those allocations; other page-locked memory (cudaHostAlloc,
+// cudaHostRegister) against the driver's record of the allocation's range.
+// Anything unconfirmed is refused (callers then stage through device
+// buffers, or report the error).
 const uint8_t* mapped_range(const void* p, size_t bytes) {
+  if (bytes == 0) return nullptr;
   cudaPointerAttributes a{}, b{};
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
     cudaGetLastError();
@@ -227,6 +296,7 @@ const uint8_t* mapped_range(const void* p, size_t bytes) {
     cudaGetLastError();
     return nullptr;
   }
+  if (!in_own_pinned(p, bytes) && !within_one_allocation(p, bytes)) return nullptr;
   return static_cast<const uint8_t*>(a.devicePointer);
 }
 
@@ -241,6 +311,7 @@ void inspire_server_config_default(inspire_server_config* cfg) {
   cfg->capacity = 4096;
   cfg->device_budget = 0;
   cfg->batch_wait_us = 100;
+  cfg->stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
 }
 
 int64_t inspire_now_ns(void) { return now_ns(); }
@@ -426,11 +497,18 @@ int inspire_pinned_alloc(size_t bytes, void** out) {
   *out = nullptr;
   if (bytes == 0) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "zero-size allocation");
   CUDA_TRY(cudaHostAlloc(out, bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  g_pinned[reinterpret_cast<uintptr_t>(*out)] = bytes;
   return INSPIRE_OK;
 }
 
 void inspire_pinned_free(void* p) {
-  if (p) cudaFreeHost(p);
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned.erase(reinterpret_cast<uintptr_t>(p));
+  }
+  cudaFreeHost(p);
 }
 
 int inspire_server_poll(inspire_server* s, uint64_t ticket, uint64_t* out_ct, int64_t* done_ns, int32_t timeout_us) {
@@ -453,11 +531,12 @@ int inspire_server_poll(inspire_server* s, uint64_t ticket, uint64_t* out_ct, in
   if (r.gen != gen || r.state != DONE) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ticket already collected");
   r.state = COLLECTING;  // this caller owns the record until it frees it
   const int cuda_error = r.cuda_error;
+  const bool batch_lost = r.batch_lost;
   const int64_t t_done = r.t_done;
   lk.unlock();
   const uint8_t* p = s->rec_ptr((int)idx);
   const int32_t kstatus = *reinterpret_cast<const volatile int32_t*>(p + REC_STATUS);
-  if (out_ct && !cuda_error && !kstatus) memcpy(out_ct, p + REC_OUT, sizeof(uint64_t) * 4 * N);
+  if (out_ct && !cuda_error && !kstatus && !batch_lost) memcpy(out_ct, p + REC_OUT, sizeof(uint64_t) * 4 * N);
   if (done_ns) *done_ns = t_done;
   lk.lock();
   r.gen++;
@@ -466,6 +545,12 @@ int inspire_server_poll(inspire_server* s, uint64_t ticket, uint64_t* out_ct, in
   const std::string werr = s->worker_error;
   lk.unlock();
   if (cuda_error) return fail(INSPIRE_ERR_CUDA, werr.empty() ? "serving batch failed" : werr);
+  if (batch_lost)
+    return fail(INSPIRE_ERR_DEVICE_STATUS, "batch dropped: a query's rows were still being copied when its "
+                                           "Respond CTA gave up waiting (ticket " + std::to_string(ticket) + ")");
+  if (kstatus == ERR_STAGE)
+    return fail(INSPIRE_ERR_DEVICE_STATUS, "query rows did not reach the GPU within stage_wait_iters (ticket " +
+                                               std::to_string(ticket) + ")");
   if (kstatus)
     return fail(INSPIRE_ERR_DEVICE_STATUS, "respond kernel status " + std::to_string(kstatus) + " for ticket " +
                                                std::to_string(ticket));

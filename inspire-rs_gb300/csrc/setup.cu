@@ -120,9 +120,10 @@ __global__ void __launch_bounds__(BLOCK) crs_what_kernel(const DevParams P, cons
 // Client key table from y_body: generate_rotations (inspiring2.rs:1309-1323)
 // followed by the forward NTT of packing_online (:1199-1213).  tau in the
 // coefficient domain is the slot permutation in the NTT domain on both
-// residues.  Stored times n^-1 2^32.
+// residues.  Stored times n^-1 2^32.  The first nrot rotations are written
+// (nrot = 1: the body table NTT(y_body[k]), rotated by the Respond kernel).
 __global__ void __launch_bounds__(BLOCK) client_ybody_kernel(const DevParams P, const uint64_t* __restrict__ yb,
-                                                             uint32_t* __restrict__ yhat) {
+                                                             uint32_t* __restrict__ yhat, int nrot) {
   __shared__ __align__(16) uint32_t W[2][N];
   __shared__ uint32_t SC[2][NTT_SCRATCH];
   const int k = blockIdx.x, tid = threadIdx.x, g = tid >> 7, x = tid & 127;
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(BLOCK) client_ybody_kernel(const DevParams P, 
     for (int rr = 0; rr < 16; rr++) W[g][16 * x + rr] = mul_shoup(v[rr], C.ninv_mont, C.ninv_mont_p, C.q);
   }
   __syncthreads();
-  for (int i = 0; i + 1 < gamma; i++) {
+  for (int i = 0; i + 1 < gamma && i < nrot; i++) {
     const uint32_t tg = gen_pow(gamma, i);
     for (int v = 0; v < N / BLOCK; v++) {
       const int s = tid + BLOCK * v;
@@ -193,9 +194,10 @@ cudaError_t launch_crs_what(const DevParams& P, const uint32_t* wmask, uint32_t*
   return cudaGetLastError();
 }
 
-cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat, cudaStream_t st) {
+cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat, int nrot,
+                                     cudaStream_t st) {
   if (P.gamma < 2) return cudaSuccess;
-  client_ybody_kernel<<<ELL, BLOCK, 0, st>>>(P, ybody, yhat);
+  client_ybody_kernel<<<ELL, BLOCK, 0, st>>>(P, ybody, yhat, nrot);
   return cudaGetLastError();
 }
 

@@ -26,7 +26,6 @@
 // Ciphertexts of the tree live in a per-query global work area (31 buffers
 // of 2 polys x 2 residues, L2-resident); the key switch works in shared
 // memory.
-#include <mutex>
 
 #include "kernels.h"
 
@@ -280,19 +279,16 @@ __device__ __align__(256) unsigned char g_tree_noalloc_scratch[TREE_NOALLOC_MAX_
 
 size_t tree_noalloc_query_bytes() { return NOALLOC_QUERY_BYTES; }
 
-// Device address of the static scratch on the current device, looked up once
-// per device (the symbol has one instance per device context).
+// Device address of the static scratch in the current device's context.
+// Looked up on every call rather than cached: the lookup is cheap and
+// allocates nothing, and a cached address would go stale if the context were
+// destroyed and re-created (cudaDeviceReset) within the process.
 cudaError_t tree_noalloc_scratch(int device, void** ptr) {
-  static std::mutex mu;
-  static void* addr[64] = {};
-  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(mu);
-  if (!addr[device]) {
-    cudaError_t e = cudaGetSymbolAddress(&addr[device], g_tree_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-  }
-  *ptr = addr[device];
-  return cudaSuccess;
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return e;
+  if (cur != device) return cudaErrorInvalidDevice;  // the caller makes `device` current first
+  return cudaGetSymbolAddress(ptr, g_tree_noalloc_scratch);
 }
 
 size_t tree_smem_bytes() { return sizeof(uint32_t) * (size_t)S_TOTAL; }

@@ -72,6 +72,7 @@ class ServerConfigC(C.Structure):
         ("capacity", C.c_uint32),
         ("device_budget", C.c_uint64),
         ("batch_wait_us", C.c_uint32),
+        ("stage_wait_iters", C.c_uint32),
     ]
 
 
@@ -136,6 +137,7 @@ def load(path: str = LIB_PATH):
         "inspire_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStatsC)]),
         "inspire_now_ns": (C.c_int64, []),
         "inspire_mulmod_rate_device": (C.c_int, [vp, u32, u32, vp, vp]),
+        "inspire_int8_mma_rate_device": (C.c_int, [vp, u32, u32, vp, vp, vp, vp]),
         "inspire_extract_inspiring_device": (C.c_int, [vp, vp, vp, u32, u32, vp, vp]),
         "inspire_query_seeded_device": (C.c_int, [vp, vp, C.c_char_p, u64, u32, vp, vp, vp, vp, vp]),
         "inspire_crs_load_galois_keys": (C.c_int, [vp, vp, u32]),

@@ -586,6 +586,14 @@ def mulmod_rate_device(crs: ServerCrs, blocks: int, iters: int, d_sink: int, str
     return blocks * 256 * 8 * iters
 
 
+def int8_mma_rate_device(crs: ServerCrs, blocks: int, iters: int, d_a: int, d_b: int, d_out: int, stream: int) -> int:
+    """INT8 tensor-core probe (mma.sync m16n8k32 s8): returns the integer
+    operations issued (blocks * 8 warps * 4 chains * iters * 8192)."""
+    _check(crs.L.inspire_int8_mma_rate_device(crs.h, blocks, iters, C.c_void_p(d_a), C.c_void_p(d_b),
+                                              C.c_void_p(d_out), C.c_void_p(stream)))
+    return blocks * 8 * 4 * iters * 8192
+
+
 def external_product_device(crs: ServerCrs, d_ct: int, d_rgsw: int, d_out: int, npairs: int, stream: int) -> None:
     """Batched external_product (external_product.rs:88-150) on device u32 data."""
     _check(crs.L.inspire_external_product_device(crs.h, C.c_void_p(d_ct), C.c_void_p(d_rgsw), C.c_void_p(d_out),
@@ -609,7 +617,7 @@ class Server:
     ServerCrs.register_client; queries may name any database of the CRS."""
 
     def __init__(self, crs: ServerCrs, max_batch: int = 128, max_inflight: int = 4, capacity: int = 4096,
-                 device_budget: int = 0, batch_wait_us: int = 100):
+                 device_budget: int = 0, batch_wait_us: int = 100, stage_wait_iters: Optional[int] = None):
         self.crs = crs
         self.L = crs.L
         cfg = nat.ServerConfigC()
@@ -617,6 +625,8 @@ class Server:
         cfg.max_batch, cfg.max_inflight, cfg.capacity, cfg.device_budget = max_batch, max_inflight, capacity, \
             device_budget
         cfg.batch_wait_us = batch_wait_us
+        if stage_wait_iters is not None:
+            cfg.stage_wait_iters = stage_wait_iters
         h = C.c_void_p()
         _check(self.L.inspire_server_create(crs.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -133,3 +133,23 @@ def test_external_product_rgsw_one_decrypts(env):
     torch.cuda.synchronize()
     out = from_dev(dout).reshape(2, 2 * N).astype(np.uint64)
     assert np.array_equal(cl.decrypt(out), np.arange(N, dtype=np.uint64) % ctx.p)
+
+
+def test_int8_mma_probe_exact(env):
+    """The INT8 tensor-core probe (mma.sync m16n8k32 s8 -> s32) accumulates
+    exactly: every accumulator equals iters * (A B), which pins the fragment
+    layout the probe assumes."""
+    torch, inspire, crs, ctx = env
+    rng = np.random.default_rng(8)
+    a = rng.integers(-128, 128, size=(16, 32), dtype=np.int8)
+    b = rng.integers(-128, 128, size=(32, 8), dtype=np.int8)
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    out = torch.zeros(4 * 16 * 8, dtype=torch.int32, device="cuda")
+    for iters in (1, 37, 4096):
+        inspire.pir.int8_mma_rate_device(crs, 3, iters, da.data_ptr(), db.data_ptr(), out.data_ptr(),
+                                         torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        want = iters * (a.astype(np.int64) @ b.astype(np.int64))
+        got = out.cpu().numpy().reshape(4, 16, 8)
+        for c in range(4):
+            assert np.array_equal(got[c], want), (iters, c)

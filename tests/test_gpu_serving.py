@@ -217,3 +217,41 @@ def test_borrowed_rows_mixed_databases_one_call(world):
     srv.close()
     sb.close()
     bb.close()
+
+
+def test_stage_wait_running_out(world):
+    """The serving variant's bounded wait for a query's rows (copied from
+    pinned host memory into shared memory) made to run out at once
+    (stage_wait_iters = 0): every query of the batch fails with a device
+    status after the kernel has drained its copies, the context stays
+    usable, and the next batches are answered correctly."""
+    W = world
+    inspire = W["inspire"]
+    qs = make_queries(W, 12)
+    want = [alone(W, q) for q in qs]
+
+    def serve(srv, qs):
+        tickets, rc = srv.submit([W["dbs"][q["db"]] for q in qs], [q["shard"] for q in qs],
+                                 np.stack([q["seeds"] for q in qs]), np.stack([q["b_rows"] for q in qs]),
+                                 [W["ids"][q["client"]] for q in qs])
+        assert rc == 0 and len(tickets) == len(qs)
+        return tickets
+
+    srv = inspire.Server(W["crs"], max_batch=8, max_inflight=2, capacity=32, stage_wait_iters=0)
+    tickets = serve(srv, qs)
+    out = np.zeros((2, 2 * N), np.uint64)
+    for t in tickets:
+        with pytest.raises(inspire.PirError, match="did not reach the GPU"):
+            srv.poll(int(t), out)
+    st = srv.stats()
+    assert st["completed"] == len(qs) and st["pending"] == 0
+    srv.close()
+    # the same context, a server with the default bound: correct answers
+    srv = inspire.Server(W["crs"], max_batch=8, max_inflight=2, capacity=32)
+    for _ in range(2):
+        tickets = serve(srv, qs)
+        got = np.zeros((len(qs), 2, 2 * N), np.uint64)
+        srv.poll_batch(tickets, got)
+        for k in range(len(qs)):
+            assert np.array_equal(got[k], want[k]), k
+    srv.close()

@@ -143,10 +143,47 @@ def test_seeded_query_json_number_forms(wire):
     bad = [(b"1234567890123456", "not reduced"), (b"99999999999999999", "not reduced"),
            (b"18446744073709551615", "not reduced"), (b"18446744073709551616", "overflow"),
            (b"123456789012345678901", "overflow"), (b"12.5", "integer"), (b"1e3", "integer"),
-           (b"-4", "unsigned"), (b"12a", "expected")]
+           (b"-4", "unsigned"), (b"12a", "expected"),
+           # serde_json rejects leading zeros: through the compact run, the
+           # one-number fast path and the checked path alike
+           (b"007", "leading zero"), (b"00", "leading zero"), (b"0" + first, "leading zero")]
+    # every length from 10 to 16 digits is above both moduli: rejected, not
+    # misparsed into a value below q
+    bad += [(b"9" * n, "not reduced") for n in range(10, 17)]
+    bad += [(b"1" + b"0" * (n - 1), "not reduced") for n in range(10, 17)]
     for num, msg in bad:
         with pytest.raises(inspire.PirError, match=msg):
             w.seeded_query_from_json(params, good.replace(key, b'"coeffs":[' + num + b","))
+        # the same number as the last element of the array, and after a space
+        last = str(int(b_rows[2, 2 * N - 1])).encode()
+        lkey = b"," + last + b'],"moduli"'
+        if good.count(lkey) == 1:
+            with pytest.raises(inspire.PirError, match=msg):
+                w.seeded_query_from_json(params, good.replace(lkey, b"," + num + b'],"moduli"'))
+        with pytest.raises(inspire.PirError, match=msg):
+            w.seeded_query_from_json(params, good.replace(key, b'"coeffs":[ ' + num + b","))
+
+
+def test_json_number_paths_exhaustive(tmp_path):
+    """The codec's three unsigned-integer paths (compact run, one-number fast
+    path, checked path) give the exact value for every length from 1 to 16
+    digits at every distance from the end of the buffer, and reject what
+    serde_json rejects (leading zeros, signs, fractions, overflow): a C++
+    driver built against json_codec.h with g++."""
+    import os
+    import shutil
+    import subprocess
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    here = os.path.dirname(os.path.abspath(__file__))
+    csrc = os.path.join(os.path.dirname(here), "inspire-rs_gb300", "csrc")
+    exe = str(tmp_path / "json_numbers")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", csrc, os.path.join(here, "native", "json_numbers.cpp"), "-o", exe],
+                   check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout
 
 
 def test_response_json_and_bincode(wire):
