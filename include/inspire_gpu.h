@@ -123,6 +123,49 @@ int inspire_crs_info(inspire_ctx *ctx, uint8_t *w_seed, uint32_t *num_columns, i
  * are skipped. */
 int inspire_crs_load_json(inspire_ctx *ctx, const char *json, size_t len);
 
+/* setup's InspiRING offline precomputation (src/pir/setup.rs:194-224):
+ * packing_offline (src/inspiring/inspiring2.rs:926-1041) over the CRS's
+ * num_columns a-polys a_polys [num_columns][poly] (coefficient form; setup
+ * takes the first num_columns crs_a_vectors), with the loaded CRS's
+ * OfflinePackingKeys.  a_hat receives PrecompInsPIR.a_hat [poly] and bold_t
+ * PrecompInsPIR.bold_t [(num_columns-1)][gadget_len][poly], both in
+ * coefficient form (the crate's layout; bold_t may be NULL when
+ * num_columns = 1).  Computed on the GPU, host buffers, synchronous. */
+int inspire_inspiring_precomp(inspire_ctx *ctx, const uint64_t *a_polys, uint64_t *a_hat, uint64_t *bold_t);
+
+/* Number of crs_a_vectors in the crs.json last loaded with
+ * inspire_crs_load_json (the server's /params reports it,
+ * src/bin/server.rs:99-118); 0 for a CRS loaded otherwise. */
+uint64_t inspire_crs_a_vectors_count(const inspire_ctx *ctx);
+
+/* The parts of ServerCrs (src/pir/setup.rs:52-87) for writing crs.json.
+ * Key-switching matrices are [gadget_len][a, b][poly] (the layout
+ * inspire_setup_keygen_device writes); NULL optional parts are written as
+ * null (packing_k_g, packing_k_h, inspiring_precomp). */
+typedef struct {
+  const uint64_t *k_g;
+  const uint64_t *k_h;
+  const uint64_t *galois_keys;   /* [n_galois][gadget_len][a, b][poly] */
+  uint32_t n_galois;
+  const uint64_t *crs_a_vectors; /* [n_crs_a][poly] */
+  uint32_t n_crs_a;
+  const uint64_t *packing_k_g;
+  const uint64_t *packing_k_h;
+  const uint64_t *precomp_a_hat;  /* PrecompInsPIR.a_hat [poly], or NULL */
+  const uint64_t *precomp_bold_t; /* [(num_columns-1)][gadget_len][poly] */
+  uint8_t inspiring_w_seed[32];
+  uint8_t inspiring_v_seed[32];
+  uint32_t inspiring_num_columns;
+} inspire_server_crs;
+
+/* Write crs.json at `path` as setup's binary writes it (serde_json::to_writer
+ * of ServerCrs, src/bin/setup.rs:183-190): serde's field order and compact
+ * form, the skipped fields (inspiring_pack_params, inspiring_packing_key,
+ * PrecompInsPIR.bold_t_ntt) left out.  params.security_level is written as
+ * Bits128 (inspire_params has no such field; secure_128_d2048's value).
+ * inspire_crs_load_json reads the file back. */
+int inspire_crs_write_json(const inspire_params *params, const inspire_server_crs *crs, const char *path);
+
 /* The server's encoded_db.json (src/bin/server.rs:292-301): serde_json of
  * EncodedDatabase {shards: [ShardData {id, polynomials: [Poly]}], config:
  * ShardConfig} (src/pir/setup.rs:104-120, src/params.rs:432-450) made
@@ -367,15 +410,26 @@ int64_t inspire_now_ns(void);
  * QueryResponse, src/bin/server.rs:88-92); bincode 1.3's default encoding for
  * ServerResponse::to_binary (pir/respond.rs:43-50). */
 
-/* Parse a SeededClientQuery JSON body (the /query/seeded request) into the
- * inspire_seeded_query layout: seeds[2*gadget_len][32],
- * b_rows[2*gadget_len][poly], *packing_mode 0 = inspiring / 1 = tree,
- * *has_keys = whether inspiring_packing_keys is present, y_body[gadget_len][poly]
- * (may be NULL to skip).  Polynomials must be in coefficient form over the
- * parameters' moduli. */
+/* Parse a SeededClientQuery JSON body (the server's /query_seeded request,
+ * src/bin/server.rs:179-236) into the inspire_seeded_query layout:
+ * seeds[2*gadget_len][32], b_rows[2*gadget_len][poly], *packing_mode 0 =
+ * inspiring / 1 = tree, *has_keys = 0 when inspiring_packing_keys is absent
+ * or null, 1 when it carries y_body (gadget_len polys into y_body, which may
+ * be NULL to skip them), 2 when its y_body is empty (respond then reports
+ * the keys invalid).  Polynomials must be in coefficient form over the
+ * parameters' moduli; numbers follow serde_json's grammar (no leading
+ * zeros). */
 int inspire_seeded_query_from_json(const inspire_params *params, const char *json, size_t len, uint32_t *shard_id,
                                    uint8_t *seeds, uint64_t *b_rows, int32_t *packing_mode, int32_t *has_keys,
                                    uint64_t *y_body);
+
+/* Parse a ClientQuery JSON body (the server's /query request,
+ * src/bin/server.rs:120-177; ClientQuery, src/pir/query.rs:119-132): rgsw
+ * receives the 2*gadget_len RGSW rows as [row][a, b][poly] (the
+ * inspire_query layout); the other outputs as for
+ * inspire_seeded_query_from_json. */
+int inspire_query_from_json(const inspire_params *params, const char *json, size_t len, uint32_t *shard_id,
+                            uint64_t *rgsw, int32_t *packing_mode, int32_t *has_keys, uint64_t *y_body);
 
 /* The server's JSON reply {"response": ServerResponse, "processing_time_ms": t}
  * for ciphertext ct[2][poly] and n_columns column ciphertexts
@@ -383,6 +437,15 @@ int inspire_seeded_query_from_json(const inspire_params *params, const char *jso
 int inspire_query_response_to_json(const inspire_params *params, const uint64_t *ct, uint32_t n_columns,
                                    const uint64_t *columns, uint64_t processing_time_ms, char *buf, size_t cap,
                                    size_t *len);
+
+/* The server's JSON reply for a tree-packing response (respond_one_packing,
+ * src/pir/respond.rs:213-268): ciphertext (a [poly], b [b_words words], the
+ * b polynomial's dimension being b_words / 2 -- 2*ring_dim for the crate's
+ * compat-mode b), no column ciphertexts.  buf NULL: *len receives the size
+ * only. */
+int inspire_packed_response_to_json(const inspire_params *params, const uint64_t *a, const uint64_t *b,
+                                    uint32_t b_words, uint64_t processing_time_ms, char *buf, size_t cap,
+                                    size_t *len);
 
 /* ServerResponse::to_binary (bincode) of the same response. */
 int inspire_server_response_to_bincode(const inspire_params *params, const uint64_t *ct, uint32_t n_columns,

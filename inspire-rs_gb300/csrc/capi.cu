@@ -218,6 +218,7 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
       a.nclients = (int)c->client_ptrs.size();
       a.what = c->what.as<uint32_t>();
       a.qdesc = c->d_desc.as<QueryDesc>();
+      a.stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
       CUDA_TRY(launch_respond(a, true, c->stream));
       return finish_status(c, n, "respond");
     }
@@ -593,6 +594,7 @@ int inspire_crs_load(inspire_ctx* c, const uint8_t w_seed[32], uint32_t num_colu
     return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path supports num_columns in {1, 2, 4, 8, 16}");
   const int gamma = (int)num_columns;
   c->gamma = gamma;
+  c->crs_a_count = 0;
   memcpy(c->w_seed, w_seed, 32);
   c->P.gamma = gamma;
   for (int r = 0; r < 2; r++) {

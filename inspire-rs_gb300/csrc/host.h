@@ -70,6 +70,7 @@ struct inspire_ctx {
   bool has_crs = false;
   int gamma = 0;
   uint8_t w_seed[32] = {};
+  uint64_t crs_a_count = 0;  // crs_a_vectors in the loaded crs.json
   ighost::DevMem what;
   ighost::DevMem wmask;  // [ELL][2][N] w_mask residues (client key generation)
   // tree packing: the CRS's Galois key table, the tree's work area and output

@@ -100,6 +100,83 @@ void poly_json(Out& o, const inspire_params& P, const uint64_t* c) {
   o.lit(",\"is_ntt\":false}");
 }
 
+// Poly of `dim` coefficients per residue (dim may differ from ring_dim: the
+// crate's compat tree-packing b has dimension 2 ring_dim).
+void poly_json_dim(Out& o, const inspire_params& P, const uint64_t* c, size_t dim) {
+  o.lit("{\"coeffs\":[");
+  for (size_t i = 0; i < 2 * dim; i++) {
+    if (i) o.ch(',');
+    o.num(c[i]);
+  }
+  o.lit("],\"moduli\":[");
+  o.num(P.crt_moduli[0]);
+  o.ch(',');
+  o.num(P.crt_moduli[1]);
+  o.lit("],\"q\":");
+  o.num(P.crt_moduli[0] * P.crt_moduli[1]);
+  o.lit(",\"dim\":");
+  o.num(dim);
+  o.lit(",\"crt_q0_inv_mod_q1\":");
+  o.num(q0_inv_q1(P.crt_moduli[0], P.crt_moduli[1]));
+  o.lit(",\"is_ntt\":false}");
+}
+
+// An f64 as serde_json writes it: the shortest decimal that reads back to
+// the same value, with ".0" on integral values.
+void f64_json(Out& o, double v) {
+  char b[40];
+  for (int prec = 1; prec <= 17; prec++) {
+    snprintf(b, sizeof b, "%.*g", prec, v);
+    if (strtod(b, nullptr) == v) break;
+  }
+  std::string t(b);
+  const size_t e = t.find('e');
+  if (e != std::string::npos) {  // 1e-07 -> 1e-7, 1e+21 -> 1e21
+    std::string m = t.substr(0, e), x = t.substr(e + 1);
+    bool neg = !x.empty() && x[0] == '-';
+    if (!x.empty() && (x[0] == '-' || x[0] == '+')) x = x.substr(1);
+    while (x.size() > 1 && x[0] == '0') x = x.substr(1);
+    t = m + "e" + (neg ? "-" : "") + x;
+  } else if (t.find('.') == std::string::npos) {
+    t += ".0";
+  }
+  o.lit(t.c_str());
+}
+
+void gadget_json(Out& o, const inspire_params& P) {
+  o.lit("{\"base\":");
+  o.num(P.gadget_base);
+  o.lit(",\"len\":");
+  o.num(P.gadget_len);
+  o.lit(",\"q\":");
+  o.num(P.crt_moduli[0] * P.crt_moduli[1]);
+  o.ch('}');
+}
+
+void rlwe_json(Out& o, const inspire_params& P, const uint64_t* ct);
+
+// KeySwitchingMatrix {rows: [RlweCiphertext; gadget_len], gadget} (ks/setup.rs:40-46)
+// from rows [gadget_len][a, b][poly].
+void ksm_json(Out& o, const inspire_params& P, const uint64_t* m) {
+  o.lit("{\"rows\":[");
+  for (uint32_t k = 0; k < P.gadget_len; k++) {
+    if (k) o.ch(',');
+    rlwe_json(o, P, m + (size_t)k * 4 * P.ring_dim);
+  }
+  o.lit("],\"gadget\":");
+  gadget_json(o, P);
+  o.ch('}');
+}
+
+void seed_json(Out& o, const uint8_t* s) {
+  o.ch('[');
+  for (int i = 0; i < 32; i++) {
+    if (i) o.ch(',');
+    o.num(s[i]);
+  }
+  o.ch(']');
+}
+
 void rlwe_json(Out& o, const inspire_params& P, const uint64_t* ct) {
   o.lit("{\"a\":");
   poly_json(o, P, ct);
@@ -154,12 +231,14 @@ bool params_ok(const inspire_params* P) {
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int inspire_seeded_query_from_json(const inspire_params* P, const char* json, size_t len, uint32_t* shard_id,
-                                   uint8_t* seeds, uint64_t* b_rows, int32_t* packing_mode, int32_t* has_keys,
-                                   uint64_t* y_body) {
-  if (!params_ok(P) || !json || !shard_id || !seeds || !b_rows || !packing_mode || !has_keys)
+// SeededClientQuery (seeded rows {seed, b}) or ClientQuery (full rows
+// {a, b}, RgswCiphertext rgsw/types.rs:100-110) JSON; see the header.
+int query_from_json(const inspire_params* P, const char* json, size_t len, bool seeded, uint32_t* shard_id,
+                    uint8_t* seeds, uint64_t* rows, int32_t* packing_mode, int32_t* has_keys, uint64_t* y_body) {
+  const char* what_q = seeded ? "SeededClientQuery JSON: " : "ClientQuery JSON: ";
+  if (!params_ok(P) || !json || !shard_id || (seeded && !seeds) || !rows || !packing_mode || !has_keys)
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument or unsupported parameters");
   const size_t plen = 2 * (size_t)P->ring_dim;
   const uint32_t rows_want = 2 * P->gadget_len;
@@ -181,10 +260,10 @@ int inspire_seeded_query_from_json(const inspire_params* P, const char* json, si
           return j.array([&](size_t i) -> bool {
             if (i >= rows_want) return j.fail("too many RGSW rows");
             nrows = (uint32_t)i + 1;
-            bool have_seed = false, have_b = false;
+            bool have_first = false, have_b = false;
             const bool rok = j.object([&](const std::string& fk) -> bool {
-              if (fk == "seed") {
-                have_seed = true;
+              if (seeded && fk == "seed") {
+                have_first = true;
                 size_t nb = 0;
                 return j.array([&](size_t bi) -> bool {
                   uint64_t v;
@@ -194,13 +273,17 @@ int inspire_seeded_query_from_json(const inspire_params* P, const char* json, si
                   return true;
                 }) && (nb == 32 || j.fail("seed must be 32 bytes"));
               }
+              if (!seeded && fk == "a") {
+                have_first = true;
+                return parse_poly(j, *P, rows + (2 * i) * plen, "rgsw row a");
+              }
               if (fk == "b") {
                 have_b = true;
-                return parse_poly(j, *P, b_rows + i * plen, "rgsw row b");
+                return parse_poly(j, *P, rows + (seeded ? i : 2 * i + 1) * plen, "rgsw row b");
               }
               return j.skip();
             });
-            return rok && ((have_seed && have_b) || j.fail("RGSW row needs seed and b"));
+            return rok && ((have_first && have_b) || j.fail(seeded ? "RGSW row needs seed and b" : "RGSW row needs a and b"));
           }) && (nrows == rows_want || j.fail("expected 2*gadget_len RGSW rows"));
         if (rk == "gadget") {
           uint64_t base = 0, glen = 0;
@@ -223,30 +306,46 @@ int inspire_seeded_query_from_json(const inspire_params* P, const char* json, si
     }
     if (k == "inspiring_packing_keys") {
       if (j.null()) return true;  // Option::None
-      keys = 1;
       size_t ny = 0;
-      return j.object([&](const std::string& kk) -> bool {
+      const bool kok = j.object([&](const std::string& kk) -> bool {
         if (kk == "y_body")
           return j.array([&](size_t i) -> bool {
             if (i >= P->gadget_len) return j.fail("too many y_body polynomials");
             ny = i + 1;
             if (!y_body) return j.skip();
             return parse_poly(j, *P, y_body + i * plen, "y_body");
-          }) && (ny == P->gadget_len || j.fail("y_body must hold gadget_len polynomials"));
+          }) && (ny == 0 || ny == P->gadget_len || j.fail("y_body must hold gadget_len polynomials"));
         return j.skip();  // z_body, full_key, num_to_pack
       });
+      keys = ny ? 1 : 2;  // 2: keys present with an empty y_body (rejected by respond)
+      return kok;
     }
     return j.skip();
   });
-  if (!ok) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "SeededClientQuery JSON: " + j.err);
+  if (!ok) return fail(INSPIRE_ERR_INVALID_ARGUMENT, what_q + j.err);
   j.ws();
-  if (j.p != j.end) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "SeededClientQuery JSON: trailing data");
+  if (j.p != j.end) return fail(INSPIRE_ERR_INVALID_ARGUMENT, std::string(what_q) + "trailing data");
   if (!have_sid || !have_rgsw)
-    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "SeededClientQuery JSON: missing shard_id or rgsw_ciphertext");
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, std::string(what_q) + "missing shard_id or rgsw_ciphertext");
   *shard_id = (uint32_t)sid;
   *packing_mode = mode;
   *has_keys = keys;
   return INSPIRE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int inspire_seeded_query_from_json(const inspire_params* P, const char* json, size_t len, uint32_t* shard_id,
+                                   uint8_t* seeds, uint64_t* b_rows, int32_t* packing_mode, int32_t* has_keys,
+                                   uint64_t* y_body) {
+  return query_from_json(P, json, len, true, shard_id, seeds, b_rows, packing_mode, has_keys, y_body);
+}
+
+int inspire_query_from_json(const inspire_params* P, const char* json, size_t len, uint32_t* shard_id,
+                            uint64_t* rgsw, int32_t* packing_mode, int32_t* has_keys, uint64_t* y_body) {
+  return query_from_json(P, json, len, false, shard_id, nullptr, rgsw, packing_mode, has_keys, y_body);
 }
 
 int inspire_query_response_to_json(const inspire_params* P, const uint64_t* ct, uint32_t n_columns,
@@ -294,6 +393,7 @@ int inspire_crs_load_json(inspire_ctx* c, const char* json, size_t len) {
   bool have_seed = false, have_cols = false, have_params = false;
   std::vector<uint64_t> keys;  // [matrix][row][a, b][poly]
   size_t nmat = 0;
+  uint64_t n_crs_a = 0;
   const size_t pw = 2 * (size_t)P.ring_dim;
   const bool ok = j.object([&](const std::string& k) {
     if (k == "params") {
@@ -357,7 +457,12 @@ int inspire_crs_load_json(inspire_ctx* c, const char* json, size_t len) {
       have_cols = true;
       return j.u64(num_columns);
     }
-    return j.skip();  // k_g, k_h, rgsw_gadget, crs_a_vectors, packing_k_*, inspiring_precomp, inspiring_v_seed
+    if (k == "crs_a_vectors")  // counted (the server's /params reports it), not kept
+      return j.array([&](size_t) {
+        n_crs_a++;
+        return j.skip();
+      });
+    return j.skip();  // k_g, k_h, rgsw_gadget, packing_k_*, inspiring_precomp, inspiring_v_seed
   });
   if (ok) j.ws();
   if (!ok || j.p != j.end)
@@ -366,6 +471,7 @@ int inspire_crs_load_json(inspire_ctx* c, const char* json, size_t len) {
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "ServerCrs JSON: missing params, inspiring_w_seed or inspiring_num_columns");
   if (num_columns > 0xffffffffull) return fail(INSPIRE_ERR_UNSUPPORTED, "GPU path supports num_columns in {1, 2, 4, 8, 16}");
   if (int rc = inspire_crs_load(c, w_seed, (uint32_t)num_columns)) return rc;
+  c->crs_a_count = n_crs_a;
   // galois_keys is empty in CRSs made without tree packing; a tree-packing
   // call then reports the missing keys
   if (nmat > 0) return inspire_crs_load_galois_keys(c, keys.data(), (uint32_t)nmat);
@@ -442,6 +548,128 @@ int inspire_db_load_json(inspire_ctx* c, const char* json, size_t len, inspire_d
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "total_entries exceeds the shards' capacity");
   if (int rc = set_device(c)) return rc;
   return db_from_host_columns(c, H.data(), nshards, total_entries, (uint32_t)entry_size, out);
+}
+
+uint64_t inspire_crs_a_vectors_count(const inspire_ctx* c) { return c ? c->crs_a_count : 0; }
+
+int inspire_packed_response_to_json(const inspire_params* P, const uint64_t* a, const uint64_t* b, uint32_t b_words,
+                                    uint64_t processing_time_ms, char* buf, size_t cap, size_t* len) {
+  if (!params_ok(P) || !a || !b || !len) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (b_words == 0 || b_words % 2) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "b_words must be a positive even count");
+  Out o;
+  o.s.resize((size_t)(2 * P->ring_dim + b_words) * 11 + 1024);
+  o.lit("{\"response\":{\"ciphertext\":{\"a\":");
+  poly_json_dim(o, *P, a, P->ring_dim);
+  o.lit(",\"b\":");
+  poly_json_dim(o, *P, b, b_words / 2);
+  o.lit("},\"column_ciphertexts\":[]},\"processing_time_ms\":");
+  o.num(processing_time_ms);
+  o.ch('}');
+  return copy_out(o.done(), buf, cap, len);
+}
+
+int inspire_crs_write_json(const inspire_params* P, const inspire_server_crs* crs, const char* path) {
+  if (!params_ok(P) || !crs || !path) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!crs->k_g || !crs->k_h || (crs->n_galois && !crs->galois_keys) || (crs->n_crs_a && !crs->crs_a_vectors) ||
+      (crs->precomp_a_hat && crs->inspiring_num_columns > 1 && !crs->precomp_bold_t))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "missing ServerCrs part");
+  const size_t pw = 2 * (size_t)P->ring_dim;
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(INSPIRE_ERR_INVALID_ARGUMENT, std::string("cannot create ") + path);
+  Out o;
+  o.s.resize(1 << 24);
+  bool io_ok = true;
+  auto flush = [&](bool force) {
+    if (o.n >= (1u << 23) || (force && o.n)) {
+      io_ok &= fwrite(o.s.data(), 1, o.n, f) == o.n;
+      o.n = 0;
+    }
+  };
+  const uint64_t q = P->crt_moduli[0] * P->crt_moduli[1];
+  o.lit("{\"params\":{\"ring_dim\":");
+  o.num(P->ring_dim);
+  o.lit(",\"q\":");
+  o.num(q);
+  o.lit(",\"crt_moduli\":[");
+  o.num(P->crt_moduli[0]);
+  o.ch(',');
+  o.num(P->crt_moduli[1]);
+  o.lit("],\"p\":");
+  o.num(P->p);
+  o.lit(",\"sigma\":");
+  f64_json(o, P->sigma);
+  o.lit(",\"gadget_base\":");
+  o.num(P->gadget_base);
+  o.lit(",\"gadget_len\":");
+  o.num(P->gadget_len);
+  o.lit(",\"security_level\":\"Bits128\"},\"k_g\":");
+  ksm_json(o, *P, crs->k_g);
+  o.lit(",\"k_h\":");
+  ksm_json(o, *P, crs->k_h);
+  o.lit(",\"galois_keys\":[");
+  for (uint32_t i = 0; i < crs->n_galois; i++) {
+    if (i) o.ch(',');
+    ksm_json(o, *P, crs->galois_keys + (size_t)i * P->gadget_len * 2 * pw);
+    flush(false);
+  }
+  o.lit("],\"rgsw_gadget\":");
+  gadget_json(o, *P);
+  o.lit(",\"crs_a_vectors\":[");
+  for (uint32_t i = 0; i < crs->n_crs_a; i++) {
+    if (i) o.ch(',');
+    o.ch('[');
+    const uint64_t* v = crs->crs_a_vectors + (size_t)i * pw;
+    for (size_t t = 0; t < pw; t++) {
+      if (t) o.ch(',');
+      o.num(v[t]);
+    }
+    o.ch(']');
+    flush(false);
+  }
+  o.lit("],\"packing_k_g\":");
+  if (crs->packing_k_g) ksm_json(o, *P, crs->packing_k_g);
+  else o.lit("null");
+  o.lit(",\"packing_k_h\":");
+  if (crs->packing_k_h) ksm_json(o, *P, crs->packing_k_h);
+  else o.lit("null");
+  o.lit(",\"inspiring_precomp\":");
+  if (crs->precomp_a_hat) {
+    // PrecompInsPIR (inspiring/inspiring2.rs:357-375; bold_t_ntt is not serialised)
+    o.lit("{\"a_hat\":");
+    poly_json_dim(o, *P, crs->precomp_a_hat, P->ring_dim);
+    o.lit(",\"bold_t\":[");
+    const uint32_t nt = crs->inspiring_num_columns > 0 ? crs->inspiring_num_columns - 1 : 0;
+    for (uint32_t i = 0; i < nt; i++) {
+      if (i) o.ch(',');
+      o.ch('[');
+      for (uint32_t k = 0; k < P->gadget_len; k++) {
+        if (k) o.ch(',');
+        poly_json_dim(o, *P, crs->precomp_bold_t + ((size_t)i * P->gadget_len + k) * pw, P->ring_dim);
+      }
+      o.ch(']');
+      flush(false);
+    }
+    o.lit("],\"bold_t_bar\":[],\"bold_t_hat\":[],\"num_to_pack\":");
+    o.num(crs->inspiring_num_columns);
+    o.lit(",\"ring_dim\":");
+    o.num(P->ring_dim);
+    o.lit(",\"q\":");
+    o.num(q);
+    o.ch('}');
+  } else {
+    o.lit("null");
+  }
+  o.lit(",\"inspiring_w_seed\":");
+  seed_json(o, crs->inspiring_w_seed);
+  o.lit(",\"inspiring_v_seed\":");
+  seed_json(o, crs->inspiring_v_seed);
+  o.lit(",\"inspiring_num_columns\":");
+  o.num(crs->inspiring_num_columns);
+  o.ch('}');
+  flush(true);
+  io_ok &= fclose(f) == 0;
+  if (!io_ok) return fail(INSPIRE_ERR_INVALID_ARGUMENT, std::string("write failed: ") + path);
+  return INSPIRE_OK;
 }
 
 }  // extern "C"

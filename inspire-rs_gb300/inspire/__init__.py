@@ -35,5 +35,7 @@ from .pir import (  # noqa: F401
     respond_seeded_packed_batch,
     respond_seeded_with_variant,
     respond_with_variant,
+    write_crs_json,
     setup_keygen_device,
 )
+from . import wire  # noqa: F401,E402

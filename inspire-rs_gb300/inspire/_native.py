@@ -44,6 +44,24 @@ class InspireParamsC(C.Structure):
     ]
 
 
+class ServerCrsPartsC(C.Structure):
+    _fields_ = [
+        ("k_g", C.c_void_p),
+        ("k_h", C.c_void_p),
+        ("galois_keys", C.c_void_p),
+        ("n_galois", C.c_uint32),
+        ("crs_a_vectors", C.c_void_p),
+        ("n_crs_a", C.c_uint32),
+        ("packing_k_g", C.c_void_p),
+        ("packing_k_h", C.c_void_p),
+        ("precomp_a_hat", C.c_void_p),
+        ("precomp_bold_t", C.c_void_p),
+        ("inspiring_w_seed", C.c_uint8 * 32),
+        ("inspiring_v_seed", C.c_uint8 * 32),
+        ("inspiring_num_columns", C.c_uint32),
+    ]
+
+
 class SeededQueryC(C.Structure):
     _fields_ = [
         ("shard_id", C.c_uint32),
@@ -153,6 +171,13 @@ def load(path: str = LIB_PATH):
                                                      vp, vp, vp]),
         "inspire_query_response_to_json": (C.c_int, [C.POINTER(InspireParamsC), vp, u32, vp, u64, vp, C.c_size_t,
                                                      C.POINTER(C.c_size_t)]),
+        "inspire_query_from_json": (C.c_int, [C.POINTER(InspireParamsC), C.c_char_p, C.c_size_t, vp, vp, vp, vp,
+                                              vp]),
+        "inspire_packed_response_to_json": (C.c_int, [C.POINTER(InspireParamsC), vp, vp, u32, u64, vp,
+                                                      C.c_size_t, C.POINTER(C.c_size_t)]),
+        "inspire_crs_write_json": (C.c_int, [C.POINTER(InspireParamsC), C.POINTER(ServerCrsPartsC), C.c_char_p]),
+        "inspire_crs_a_vectors_count": (u64, [vp]),
+        "inspire_inspiring_precomp": (C.c_int, [vp, vp, vp, vp]),
         "inspire_server_response_to_bincode": (C.c_int, [C.POINTER(InspireParamsC), vp, u32, vp, vp, C.c_size_t,
                                                          C.POINTER(C.c_size_t)]),
         "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),

@@ -188,6 +188,23 @@ class ServerCrs:
     def release_client(self, client_id: int) -> None:
         _check(self.L.inspire_client_release(self.h, client_id))
 
+    @property
+    def crs_a_vectors_count(self) -> int:
+        """crs_a_vectors in the loaded crs.json (0 if not loaded from one)."""
+        return int(self.L.inspire_crs_a_vectors_count(self.h))
+
+    def inspiring_precomp(self, a_polys: np.ndarray):
+        """setup's inspiring_precomp (setup.rs:194-224): packing_offline
+        (inspiring2.rs:926-1041) over num_columns a-polys (coefficient form,
+        shape (num_columns, plen)) on the GPU.  Returns (a_hat (plen,),
+        bold_t ((num_columns-1)*gadget_len, plen)), coefficient form."""
+        g, ell, plen = self.inspiring_num_columns, self.params.gadget_len, self.params.plen
+        a = _u64(a_polys).reshape(g, plen)
+        a_hat = np.zeros(plen, np.uint64)
+        bold_t = np.zeros((max(1, (g - 1) * ell), plen), np.uint64)
+        _check(self.L.inspire_inspiring_precomp(self.h, _ptr(a), _ptr(a_hat), _ptr(bold_t)))
+        return a_hat, bold_t[:(g - 1) * ell]
+
     def load_galois_keys(self, galois_keys: np.ndarray) -> None:
         """ServerCrs.galois_keys (setup.rs:164-173) for tree packing: log2(d)
         key-switching matrices of 2*gadget_len rows [a, b] each, shape
@@ -598,6 +615,50 @@ def external_product_device(crs: ServerCrs, d_ct: int, d_rgsw: int, d_out: int, 
     """Batched external_product (external_product.rs:88-150) on device u32 data."""
     _check(crs.L.inspire_external_product_device(crs.h, C.c_void_p(d_ct), C.c_void_p(d_rgsw), C.c_void_p(d_out),
                                                  npairs, C.c_void_p(stream)))
+
+
+def write_crs_json(path: str, params: InspireParams, *, k_g: np.ndarray, k_h: np.ndarray, galois_keys: np.ndarray,
+                   crs_a_vectors: np.ndarray, inspiring_w_seed: bytes, inspiring_v_seed: bytes,
+                   inspiring_num_columns: int, packing_k_g: Optional[np.ndarray] = None,
+                   packing_k_h: Optional[np.ndarray] = None, precomp: Optional[tuple] = None) -> None:
+    """Write crs.json as the crate's setup binary does (serde_json of
+    ServerCrs, setup.rs:52-87; bin/setup.rs:183-190).  Key-switching
+    matrices have shape (gadget_len, 2, plen) rows (a, b); galois_keys
+    (n, gadget_len, 2, plen); crs_a_vectors (n, plen); precomp = (a_hat,
+    bold_t) from ServerCrs.inspiring_precomp or None."""
+    L = nat.load()
+    ell, plen = params.gadget_len, params.plen
+    keep = []
+
+    def arr(a, shape):
+        if a is None:
+            return None
+        a = _u64(a).reshape(shape)
+        keep.append(a)
+        return a.ctypes.data_as(C.c_void_p)
+
+    gk = _u64(galois_keys).reshape(-1, ell, 2, plen)
+    ca = _u64(crs_a_vectors).reshape(-1, plen)
+    parts = nat.ServerCrsPartsC()
+    parts.k_g = arr(k_g, (ell, 2, plen))
+    parts.k_h = arr(k_h, (ell, 2, plen))
+    parts.galois_keys = arr(gk, gk.shape)
+    parts.n_galois = gk.shape[0]
+    parts.crs_a_vectors = arr(ca, ca.shape)
+    parts.n_crs_a = ca.shape[0]
+    parts.packing_k_g = arr(packing_k_g, (ell, 2, plen))
+    parts.packing_k_h = arr(packing_k_h, (ell, 2, plen))
+    if precomp is not None:
+        parts.precomp_a_hat = arr(precomp[0], (plen,))
+        if inspiring_num_columns > 1:
+            parts.precomp_bold_t = arr(precomp[1], ((inspiring_num_columns - 1) * ell, plen))
+    if len(inspiring_w_seed) != 32 or len(inspiring_v_seed) != 32:
+        raise ValueError("seeds must be 32 bytes")
+    parts.inspiring_w_seed[:] = list(bytes(inspiring_w_seed))
+    parts.inspiring_v_seed[:] = list(bytes(inspiring_v_seed))
+    parts.inspiring_num_columns = int(inspiring_num_columns)
+    pc = params.to_c()
+    _check(L.inspire_crs_write_json(C.byref(pc), C.byref(parts), str(path).encode()))
 
 
 def now_ns() -> int:

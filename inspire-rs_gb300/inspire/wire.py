@@ -9,7 +9,7 @@ import numpy as np
 
 from . import _native as nat
 from .params import InspireParams
-from .pir import ClientPackingKeys, PirError, SeededClientQuery, ServerResponse, _check, _ptr
+from .pir import ClientPackingKeys, ClientQuery, PirError, SeededClientQuery, ServerResponse, _check, _ptr
 
 
 def seeded_query_from_json(params: InspireParams, body: bytes | str) -> SeededClientQuery:
@@ -25,7 +25,43 @@ def seeded_query_from_json(params: InspireParams, body: bytes | str) -> SeededCl
     _check(L.inspire_seeded_query_from_json(C.byref(pc), raw, len(raw), C.byref(sid), _ptr(seeds), _ptr(b_rows),
                                             C.byref(mode), C.byref(keys), _ptr(y_body)))
     return SeededClientQuery(int(sid.value), seeds, b_rows, "tree" if mode.value else "inspiring",
-                             ClientPackingKeys(y_body=y_body) if keys.value else None)
+                             _keys(keys.value, y_body))
+
+
+def _keys(flag: int, y_body: np.ndarray):
+    # 0: no inspiring_packing_keys; 1: with y_body; 2: present with an empty
+    # y_body (respond reports the keys invalid, as the crate does)
+    return None if flag == 0 else ClientPackingKeys(y_body=y_body if flag == 1 else None)
+
+
+def query_from_json(params: InspireParams, body: bytes | str) -> ClientQuery:
+    """Parse a ClientQuery JSON body (pir/query.rs:119-132), the /query
+    request of the crate's server."""
+    L = nat.load()
+    raw = body.encode() if isinstance(body, str) else bytes(body)
+    ell, plen = params.gadget_len, params.plen
+    rgsw = np.zeros((2 * ell, 2, plen), np.uint64)
+    y_body = np.zeros((ell, plen), np.uint64)
+    sid, mode, keys = C.c_uint32(0), C.c_int32(0), C.c_int32(0)
+    pc = params.to_c()
+    _check(L.inspire_query_from_json(C.byref(pc), raw, len(raw), C.byref(sid), _ptr(rgsw), C.byref(mode),
+                                     C.byref(keys), _ptr(y_body)))
+    return ClientQuery(int(sid.value), rgsw, "tree" if mode.value else "inspiring", _keys(keys.value, y_body))
+
+
+def packed_response_to_json(params: InspireParams, a: np.ndarray, b: np.ndarray, processing_time_ms: int = 0) -> bytes:
+    """The server's JSON reply for a tree-packing response (b may have the
+    crate's compat dimension 2 ring_dim)."""
+    L = nat.load()
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    pc = params.to_c()
+    size = C.c_size_t(0)
+    cap = (a.size + b.size) * 21 + 4096
+    buf = C.create_string_buffer(cap)
+    _check(L.inspire_packed_response_to_json(C.byref(pc), _ptr(a), _ptr(b), b.size, processing_time_ms, buf, cap,
+                                             C.byref(size)))
+    return buf.raw[:size.value]
 
 
 def _ct_arrays(response: ServerResponse):
@@ -66,4 +102,5 @@ def server_response_to_bincode(params: InspireParams, response: ServerResponse) 
     return bytes(buf)[:size.value]
 
 
-__all__ = ["seeded_query_from_json", "query_response_to_json", "server_response_to_bincode", "PirError"]
+__all__ = ["seeded_query_from_json", "query_from_json", "query_response_to_json", "packed_response_to_json",
+           "server_response_to_bincode", "PirError"]

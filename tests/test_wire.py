@@ -206,3 +206,100 @@ def test_response_json_and_bincode(wire):
         want_bin = poly_bin(ct[0]) + poly_bin(ct[1]) + struct.pack("<Q", len(columns)) + b"".join(
             poly_bin(c.a) + poly_bin(c.b) for c in columns)
         assert w.server_response_to_bincode(params, resp) == want_bin
+
+
+def full_query_obj(shard_id, rgsw, y_body=None, mode=None, keys_empty=False):
+    q = {"shard_id": shard_id,
+         "rgsw_ciphertext": {"rows": [{"a": poly_obj(rgsw[i, 0]), "b": poly_obj(rgsw[i, 1])} for i in range(6)],
+                             "gadget": {"base": 1 << 20, "len": 3, "q": QC}}}
+    if mode is not None:
+        q["packing_mode"] = mode
+    if y_body is not None:
+        q["inspiring_packing_keys"] = {"y_body": [poly_obj(p) for p in y_body], "full_key": False, "num_to_pack": 16}
+    elif keys_empty:
+        q["inspiring_packing_keys"] = {"y_body": [], "full_key": False, "num_to_pack": 16}
+    return q
+
+
+def test_client_query_json(wire):
+    """ClientQuery (query.rs:119-132) JSON, the /query request: full RGSW rows
+    (a, b), packing mode, optional keys; an empty y_body is kept as 'keys
+    present, invalid' so that respond reports it as the crate does."""
+    inspire, w = wire
+    rng = np.random.default_rng(5)
+    params = inspire.InspireParams(p=1 << 16)
+    rgsw = rand_polys(rng, 12).reshape(6, 2, 2 * N)
+    y_body = rand_polys(rng, 3)
+    q = w.query_from_json(params, compact(full_query_obj(9, rgsw, y_body, mode="tree")))
+    assert q.shard_id == 9 and q.packing_mode == "tree"
+    assert np.array_equal(q.rgsw, rgsw)
+    assert np.array_equal(q.inspiring_packing_keys.y_body, y_body)
+    q = w.query_from_json(params, json.dumps(full_query_obj(3, rgsw), indent=1))
+    assert q.packing_mode == "inspiring" and q.inspiring_packing_keys is None
+    q = w.query_from_json(params, compact(full_query_obj(3, rgsw, keys_empty=True)))
+    assert q.inspiring_packing_keys is not None and q.inspiring_packing_keys.y_body is None
+    # the seeded parser keeps the same distinction
+    seeds = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+    body = query_obj(1, seeds, rgsw[:, 1])
+    body["inspiring_packing_keys"] = {"y_body": [], "full_key": False, "num_to_pack": 16}
+    sq = w.seeded_query_from_json(params, compact(body))
+    assert sq.inspiring_packing_keys is not None and sq.inspiring_packing_keys.y_body is None
+    bad = full_query_obj(3, rgsw)
+    del bad["rgsw_ciphertext"]["rows"][2]["a"]
+    with pytest.raises(inspire.PirError, match="needs a and b"):
+        w.query_from_json(params, compact(bad))
+    bad = full_query_obj(3, rgsw)
+    bad["rgsw_ciphertext"]["rows"] = bad["rgsw_ciphertext"]["rows"][:5]
+    with pytest.raises(inspire.PirError, match="2\\*gadget_len"):
+        w.query_from_json(params, compact(bad))
+
+
+def test_packed_response_json(wire):
+    """The /query reply for tree packing, with a ring_dim b and with the
+    crate's compat-mode b of dimension 2 ring_dim."""
+    inspire, w = wire
+    rng = np.random.default_rng(6)
+    params = inspire.InspireParams(p=1 << 16)
+    a = rand_polys(rng, 1)[0]
+    for b in (rand_polys(rng, 1)[0], np.concatenate([rand_polys(rng, 1)[0], rand_polys(rng, 1)[0]])):
+        dim = b.size // 2
+        pb = {"coeffs": [int(x) for x in b], "moduli": list(Q), "q": QC, "dim": dim, "crt_q0_inv_mod_q1": QINV,
+              "is_ntt": False}
+        want = compact({"response": {"ciphertext": {"a": poly_obj(a), "b": pb}, "column_ciphertexts": []},
+                        "processing_time_ms": 7})
+        assert w.packed_response_to_json(params, a, b, 7) == want
+
+
+def test_crs_json_writer(wire, tmp_path):
+    """crs.json as the crate's setup writes it (serde_json of ServerCrs,
+    setup.rs:52-87, field order of the derive, skipped fields left out):
+    built here from the derives and compared byte for byte."""
+    inspire, w = wire
+    rng = np.random.default_rng(7)
+    params = inspire.InspireParams(p=1 << 16)
+    ksm = lambda: rand_polys(rng, 6).reshape(3, 2, 2 * N)  # noqa: E731
+    k_g, k_h, pk_g = ksm(), ksm(), ksm()
+    galois = np.stack([ksm() for _ in range(2)])
+    crs_a = rand_polys(rng, 3)
+    a_hat = rand_polys(rng, 1)[0]
+    bold_t = rng.integers(0, 1 << 20, size=(15 * 3, 2 * N), dtype=np.uint64)
+    wseed, vseed = bytes(range(32)), bytes(range(100, 132))
+    path = tmp_path / "crs.json"
+    inspire.write_crs_json(str(path), params, k_g=k_g, k_h=k_h, galois_keys=galois, crs_a_vectors=crs_a,
+                           inspiring_w_seed=wseed, inspiring_v_seed=vseed, inspiring_num_columns=16,
+                           packing_k_g=pk_g, packing_k_h=None, precomp=(a_hat, bold_t))
+    gadget = {"base": 1 << 20, "len": 3, "q": QC}
+
+    def ksm_obj(m):
+        return {"rows": [{"a": poly_obj(m[k, 0]), "b": poly_obj(m[k, 1])} for k in range(3)], "gadget": gadget}
+
+    want = {"params": {"ring_dim": N, "q": QC, "crt_moduli": list(Q), "p": 1 << 16, "sigma": 6.4,
+                       "gadget_base": 1 << 20, "gadget_len": 3, "security_level": "Bits128"},
+            "k_g": ksm_obj(k_g), "k_h": ksm_obj(k_h), "galois_keys": [ksm_obj(g) for g in galois],
+            "rgsw_gadget": gadget, "crs_a_vectors": [[int(x) for x in v] for v in crs_a],
+            "packing_k_g": ksm_obj(pk_g), "packing_k_h": None,
+            "inspiring_precomp": {"a_hat": poly_obj(a_hat),
+                                  "bold_t": [[poly_obj(bold_t[3 * i + k]) for k in range(3)] for i in range(15)],
+                                  "bold_t_bar": [], "bold_t_hat": [], "num_to_pack": 16, "ring_dim": N, "q": QC},
+            "inspiring_w_seed": list(wseed), "inspiring_v_seed": list(vseed), "inspiring_num_columns": 16}
+    assert path.read_bytes() == compact(want)
