@@ -156,3 +156,18 @@ def test_errors_follow_the_crate(served):
     assert st == 415
     st, _, _ = request(url, "POST", "/query_seeded", b'{"shard_id": 007}')
     assert st == 400  # serde_json rejects leading zeros: not JSON
+
+
+def test_load_generator_closed_and_open_loop(served):
+    """inspire.http_load against the in-process server: spawned client
+    processes, keep-alive connections, every reply 200."""
+    from inspire import http_load
+
+    W = served
+    seeds, b_rows = W["client"].query_seeded(11)
+    body = http_load.seeded_query_json(0, seeds, b_rows, W["y_body"])
+    assert body == seeded_query_body(0, seeds, b_rows, W["y_body"])  # the same bytes as serde_json's
+    r = http_load.run_load(W["url"], [body], 2, duration_s=0.6, warmup_s=0.1)
+    assert r["errors"] == 0 and r["requests"] >= 1 and r["p50_ms"] > 0
+    r = http_load.run_load(W["url"], [body], 2, duration_s=0.6, warmup_s=0.1, rate=4.0)
+    assert r["errors"] == 0 and r["offered_rps"] == 4.0
