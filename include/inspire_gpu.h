@@ -84,6 +84,18 @@ void inspire_params_default(inspire_params *out);
 int inspire_ctx_create(const inspire_params *params, int device, int mode, inspire_ctx **out);
 void inspire_ctx_destroy(inspire_ctx *ctx);
 
+/* Admission by device memory.  Every device buffer of a context -- its
+ * tables, CRS and Galois key tables, resident databases, client key tables,
+ * serving-loop slots, staging buffers -- is accounted against an optional
+ * budget (0, the default: no limit).  A registration, database load or
+ * server creation that would exceed it fails with
+ * INSPIRE_ERR_OUT_OF_MEMORY before anything is allocated, and leaves the
+ * context usable; freeing objects returns their bytes.  A budget below the
+ * bytes already in use is refused. */
+int inspire_ctx_set_device_budget(inspire_ctx *ctx, uint64_t bytes);
+/* Bytes accounted now and the budget (0: none). */
+int inspire_ctx_device_memory(inspire_ctx *ctx, uint64_t *used, uint64_t *budget);
+
 /* Load the InspiRING part of ServerCrs (src/pir/setup.rs:52-87): the shared
  * seed `inspiring_w_seed` and `inspiring_num_columns` (gamma).  Builds the
  * rotated w_mask table of OfflinePackingKeys::generate

@@ -125,15 +125,13 @@ int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all,
   // or at smaller gamma, all (gamma-1)*ELL rotated polys.
   const bool body_form = !y_all && gamma == MAX_GAMMA;
   const size_t tbl_words = (size_t)std::max(1, body_form ? ELL : (gamma - 1) * ELL) * poly_words();
-  DevMem* m = new DevMem();
+  std::unique_ptr<DevMem> m(new DevMem(c->ledger));  // freed (bytes returned) on every error path
   cudaError_t e = m->ensure(tbl_words * sizeof(uint32_t));
-  if (e != cudaSuccess) {
-    delete m;
-    return fail(INSPIRE_ERR_OUT_OF_MEMORY, "client key table allocation failed");
-  }
+  if (e != cudaSuccess) return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "client key table allocation"));
   const size_t in_polys = y_all ? (size_t)(gamma - 1) * ELL : ELL;
   if (gamma > 1) {
-    CUDA_TRY(c->d_keys.ensure(in_polys * poly_words() * sizeof(uint64_t)));
+    if (c->d_keys.ensure(in_polys * poly_words() * sizeof(uint64_t)) != cudaSuccess)
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "client key upload buffer"));
     CUDA_TRY(cudaMemcpyAsync(c->d_keys.p, y_all ? y_all : y_body, in_polys * poly_words() * sizeof(uint64_t),
                              cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(y_all ? launch_client_from_yall(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream)
@@ -152,10 +150,10 @@ int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all,
     c->clients.push_back(nullptr);
     c->client_ptrs.push_back(nullptr);
   }
-  c->clients[slot] = m;
+  c->clients[slot] = m.release();
   // bit 0 of the device table entry marks a body table (allocations are
   // 256-byte aligned)
-  c->client_ptrs[slot] = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(m->as<uint32_t>()) |
+  c->client_ptrs[slot] = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(c->clients[slot]->as<uint32_t>()) |
                                                            (body_form ? 1u : 0u));
   c->client_table_dirty = true;
   *id = slot;
@@ -632,6 +630,7 @@ int inspire_db_create(inspire_ctx* c, const uint8_t* raw, uint64_t n_entries, ui
   if (!c->has_crs) return fail(INSPIRE_ERR_NO_CRS, "no CRS loaded (inspire_crs_load)");
   if (int rc = set_device(c)) return rc;
   inspire_db* db = new inspire_db();
+  db->H.ledger = db->E.ledger = c->ledger;
   db->ctx = c;
   db->device = c->device;
   db->n_entries = n_entries;
@@ -656,11 +655,11 @@ int inspire_db_create(inspire_ctx* c, const uint8_t* raw, uint64_t n_entries, ui
     if (e == cudaSuccess) e = db->E.ensure(ebytes);
     if (e != cudaSuccess) {
       delete db;
-      return fail(INSPIRE_ERR_OUT_OF_MEMORY, "database allocation failed");
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "database allocation"));
     }
     // raw bytes in chunks of whole shards
     const uint64_t shards_per_chunk = std::max<uint64_t>(1, (256ULL << 20) / ((uint64_t)N * entry_size));
-    DevMem stage;
+    DevMem stage(c->ledger);
     for (uint64_t s0 = 0; s0 < (uint64_t)db->nshards; s0 += shards_per_chunk) {
       const uint64_t s1 = std::min<uint64_t>(db->nshards, s0 + shards_per_chunk);
       const uint64_t e0 = s0 * N, e1 = std::min<uint64_t>(n_entries, s1 * N);
@@ -693,6 +692,21 @@ void inspire_db_destroy(inspire_db* db) {
   delete db;
 }
 
+int inspire_ctx_set_device_budget(inspire_ctx* c, uint64_t bytes) {
+  if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c->ledger->set_budget(bytes))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "device budget below the " + std::to_string(c->ledger->used()) +
+                                                  " bytes already in use");
+  return INSPIRE_OK;
+}
+
+int inspire_ctx_device_memory(inspire_ctx* c, uint64_t* used, uint64_t* budget) {
+  if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (used) *used = c->ledger->used();
+  if (budget) *budget = c->ledger->budget();
+  return INSPIRE_OK;
+}
+
 uint32_t inspire_db_num_shards(const inspire_db* db) { return db ? (uint32_t)db->nshards : 0; }
 
 uint64_t inspire_db_device_bytes(const inspire_db* db) { return db ? (uint64_t)(db->H.bytes + db->E.bytes) : 0; }
@@ -704,8 +718,15 @@ int inspire_client_register(inspire_ctx* c, const uint64_t* y_body, const uint64
   if (int rc = set_device(c)) return rc;
   if (int rc = register_keys(c, y_body, y_all, id)) return rc;
   // the device client table is brought up to date here, so that later
-  // launches make no copy (they can be captured in a CUDA graph)
-  return sync_client_table(c);
+  // launches make no copy (they can be captured in a CUDA graph); if it
+  // cannot grow, the registration is undone
+  if (int rc = sync_client_table(c)) {
+    const std::string msg = g_last_error;
+    release_keys(c, *id);
+    *id = -1;
+    return fail(rc, msg);
+  }
+  return INSPIRE_OK;
 }
 
 int inspire_client_release(inspire_ctx* c, int32_t id) {
@@ -792,7 +813,7 @@ int inspire_crs_load_galois_keys(inspire_ctx* c, const uint64_t* keys, uint32_t 
           return fail(INSPIRE_ERR_INVALID_ARGUMENT, "Galois key coefficients must be reduced mod each CRT modulus");
   std::lock_guard<std::mutex> lk(c->mu);
   if (int rc = set_device(c)) return rc;
-  DevMem staged;
+  DevMem staged(c->ledger);
   CUDA_TRY(staged.ensure(sizeof(uint64_t) * npolys * pw));
   CUDA_TRY(cudaMemcpyAsync(staged.p, keys, sizeof(uint64_t) * npolys * pw, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c->galois.ensure(sizeof(uint32_t) * npolys * pw));

@@ -105,6 +105,7 @@ int db_from_host_columns(inspire_ctx* c, const uint16_t* Hh, int nshards, uint64
                          inspire_db** out) {
   const int gamma = c->gamma;
   inspire_db* db = new inspire_db();
+  db->H.ledger = db->E.ledger = c->ledger;
   db->ctx = c;
   db->device = c->device;
   db->gamma = gamma;
@@ -116,7 +117,7 @@ int db_from_host_columns(inspire_ctx* c, const uint16_t* Hh, int nshards, uint64
     if (e == cudaSuccess) e = db->E.ensure(sizeof(uint32_t) * (size_t)nshards * 2 * ELL * gamma * N);
     if (e != cudaSuccess) {
       delete db;
-      return fail(INSPIRE_ERR_OUT_OF_MEMORY, "database allocation failed");
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "database allocation"));
     }
     e = cudaMemcpy(db->H.p, Hh, sizeof(uint16_t) * (size_t)nshards * gamma * N, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = launch_encode_E(c->P, db->H.as<uint16_t>(), nshards, db->E.as<uint32_t>(), c->stream);
@@ -150,6 +151,7 @@ int inspire_db_load_shards(inspire_ctx* c, const char* dir, inspire_db** out) {
   const int gamma = c->gamma;
   const int nshards = (int)count;
   inspire_db* db = new inspire_db();
+  db->H.ledger = db->E.ledger = c->ledger;
   db->ctx = c;
   db->device = c->device;
   db->gamma = gamma;
@@ -161,7 +163,7 @@ int inspire_db_load_shards(inspire_ctx* c, const char* dir, inspire_db** out) {
     if (e == cudaSuccess) e = db->E.ensure(sizeof(uint32_t) * (size_t)nshards * 2 * ELL * gamma * N);
     if (e != cudaSuccess) {
       delete db;
-      return fail(INSPIRE_ERR_OUT_OF_MEMORY, "database allocation failed");
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "database allocation"));
     }
     // shards in chunks of up to 256 MiB of raw columns
     const int per_chunk = std::max(1, (int)((256u << 20) / (sizeof(uint16_t) * gamma * N)));

@@ -4,12 +4,14 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "inspire_gpu.h"
 #include "kernels.h"
+#include "ledger.h"
 
 namespace ighost {
 
@@ -30,23 +32,37 @@ inline int fail(int code, const std::string& msg) {
                   std::string(#expr) + ": " + cudaGetErrorString(_e));                   \
   } while (0)
 
+// A device buffer that grows on demand.  Bound to a context's ledger, its
+// bytes are reserved there before cudaMalloc (a refused reservation returns
+// cudaErrorMemoryAllocation without allocating) and returned on release.
 struct DevMem {
   void* p = nullptr;
   size_t bytes = 0;
+  std::shared_ptr<Ledger> ledger;
   DevMem() = default;
+  explicit DevMem(std::shared_ptr<Ledger> l) : ledger(std::move(l)) {}
   DevMem(const DevMem&) = delete;
   DevMem& operator=(const DevMem&) = delete;
   ~DevMem() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      if (ledger) ledger->release(bytes);
+    }
     p = nullptr;
     bytes = 0;
   }
   cudaError_t ensure(size_t want) {
     if (want <= bytes) return cudaSuccess;
     release();
+    if (ledger && !ledger->reserve(want)) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&p, want);
-    if (e == cudaSuccess) bytes = want;
+    if (e == cudaSuccess) {
+      bytes = want;
+    } else {
+      p = nullptr;
+      if (ledger) ledger->release(want);
+    }
     return e;
   }
   template <class T>
@@ -59,6 +75,8 @@ struct DevMem {
 
 struct inspire_ctx {
   std::mutex mu;
+  // device-memory accounting of everything this context allocates
+  std::shared_ptr<ighost::Ledger> ledger = std::make_shared<ighost::Ledger>();
   int device = 0;
   int mode = 0;
   int sm_count = 0;
@@ -87,6 +105,11 @@ struct inspire_ctx {
   std::vector<ig::QueryDesc> h_desc;
   std::vector<int32_t> h_status;
 
+  inspire_ctx() {
+    for (ighost::DevMem* m : {&tables, &what, &wmask, &galois, &tree_work, &d_tree_out, &client_table, &d_shard,
+                              &d_seeds, &d_arows, &d_brows, &d_client, &d_out, &d_cols, &d_status, &d_keys, &d_desc})
+      m->ledger = ledger;
+  }
   ~inspire_ctx() {
     for (ighost::DevMem* m : clients) delete m;
     if (stream) cudaStreamDestroy(stream);
@@ -125,6 +148,14 @@ inline int sync_client_table(inspire_ctx* c) {
                         cudaMemcpyHostToDevice));
   c->client_table_dirty = false;
   return INSPIRE_OK;
+}
+
+// Text of a refused or failed device allocation of `what`.
+inline std::string alloc_failure(const inspire_ctx* c, const std::string& what) {
+  const uint64_t budget = c->ledger->budget();
+  if (!budget) return what + ": device out of memory";
+  return what + ": does not fit the device budget (" + std::to_string(c->ledger->used()) + " of " +
+         std::to_string(budget) + " bytes in use) or the device is out of memory";
 }
 
 inline int set_device(inspire_ctx* c) {

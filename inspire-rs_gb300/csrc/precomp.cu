@@ -154,7 +154,7 @@ extern "C" int inspire_inspiring_precomp(inspire_ctx* c, const uint64_t* a_polys
   if (gamma > 1 && !bold_t) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null bold_t");
   if (int rc = set_device(c)) return rc;
   const size_t pw = poly_words();
-  DevMem d_a, d_ahat, d_R, d_out;
+  DevMem d_a(c->ledger), d_ahat(c->ledger), d_R(c->ledger), d_out(c->ledger);
   CUDA_TRY(d_a.ensure(sizeof(uint64_t) * gamma * pw));
   CUDA_TRY(d_ahat.ensure(sizeof(uint32_t) * gamma * pw));
   CUDA_TRY(d_R.ensure(sizeof(uint32_t) * gamma * pw));

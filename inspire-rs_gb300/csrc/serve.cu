@@ -360,7 +360,9 @@ int inspire_server_create(inspire_ctx* c, const inspire_server_config* cfg, insp
         cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess ||
         cudaHostAlloc(reinterpret_cast<void**>(&sl.desc), sizeof(QueryDesc) * B, cudaHostAllocDefault) != cudaSuccess)
       return bail(fail(INSPIRE_ERR_CUDA, "serving stream setup failed"));
-    if (sl.ddesc.ensure(sizeof(QueryDesc) * B)) return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, "serving slot buffers"));
+    sl.ddesc.ledger = c->ledger;
+    if (sl.ddesc.ensure(sizeof(QueryDesc) * B))
+      return bail(fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "serving slot buffers")));
   }
   s->worker = std::thread([s] { s->run(); });
   *out = s;

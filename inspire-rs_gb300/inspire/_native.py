@@ -178,6 +178,8 @@ def load(path: str = LIB_PATH):
         "inspire_crs_write_json": (C.c_int, [C.POINTER(InspireParamsC), C.POINTER(ServerCrsPartsC), C.c_char_p]),
         "inspire_crs_a_vectors_count": (u64, [vp]),
         "inspire_inspiring_precomp": (C.c_int, [vp, vp, vp, vp]),
+        "inspire_ctx_set_device_budget": (C.c_int, [vp, u64]),
+        "inspire_ctx_device_memory": (C.c_int, [vp, C.POINTER(u64), C.POINTER(u64)]),
         "inspire_server_response_to_bincode": (C.c_int, [C.POINTER(InspireParamsC), vp, u32, vp, vp, C.c_size_t,
                                                          C.POINTER(C.c_size_t)]),
         "inspire_ntt_forward_device": (C.c_int, [vp, vp, u32, vp]),

@@ -94,7 +94,7 @@ class GpuBackend:
                 ent[1] += 1
                 self._keys.move_to_end(digest)
                 return digest, ent[0]
-        cid = self.crs.register_client(ClientPackingKeys(y_body=y_body))
+        cid = self._register(y_body)
         with self._lock:
             ent = self._keys.get(digest)
             if ent is not None:  # registered meanwhile by another connection
@@ -113,6 +113,23 @@ class GpuBackend:
                     self.crs.release_client(c)
                     over -= 1
         return digest, cid
+
+    def _register(self, y_body: np.ndarray) -> int:
+        """Register a client's keys; when the context's device budget refuses
+        them, evict idle cached clients (least recently used first) until
+        they fit or nothing idle is left."""
+        while True:
+            try:
+                return self.crs.register_client(ClientPackingKeys(y_body=y_body))
+            except PirError as e:
+                if e.status != nat.ERR_OUT_OF_MEMORY:
+                    raise
+                with self._lock:
+                    idle = next((d for d, (_, busy) in self._keys.items() if busy == 0), None)
+                    if idle is None:
+                        raise
+                    cid, _ = self._keys.pop(idle)
+                self.crs.release_client(cid)
 
     def _release_client(self, digest: bytes) -> None:
         with self._lock:

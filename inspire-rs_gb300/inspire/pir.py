@@ -188,6 +188,19 @@ class ServerCrs:
     def release_client(self, client_id: int) -> None:
         _check(self.L.inspire_client_release(self.h, client_id))
 
+    def set_device_budget(self, nbytes: int) -> None:
+        """Admission by device memory: every device buffer of this context
+        (tables, databases, client keys, serving slots, staging) counts
+        against `nbytes` (0: no limit); what would exceed it is refused with
+        PirError (status ERR_OUT_OF_MEMORY) before allocating."""
+        _check(self.L.inspire_ctx_set_device_budget(self.h, int(nbytes)))
+
+    def device_memory(self):
+        """(bytes in use, budget) of this context's device memory."""
+        used, budget = C.c_uint64(0), C.c_uint64(0)
+        _check(self.L.inspire_ctx_device_memory(self.h, C.byref(used), C.byref(budget)))
+        return int(used.value), int(budget.value)
+
     @property
     def crs_a_vectors_count(self) -> int:
         """crs_a_vectors in the loaded crs.json (0 if not loaded from one)."""

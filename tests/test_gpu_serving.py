@@ -255,3 +255,76 @@ def test_stage_wait_running_out(world):
         for k in range(len(qs)):
             assert np.array_equal(got[k], want[k]), k
     srv.close()
+
+
+def test_admission_by_device_memory(oracle_mod):
+    """A context with a device budget: a database, client keys and a serving
+    loop are admitted while they fit and refused with ERR_OUT_OF_MEMORY
+    (before anything is allocated) when they do not; freeing returns the
+    bytes; a budget below what is in use is refused; the HTTP backend evicts
+    idle cached clients to make room."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import inspire
+    from inspire import _native as nat
+    from inspire.http_server import GpuBackend
+
+    O = oracle_mod
+    ctx = O.Ctx()
+    crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
+    base, budget = crs.device_memory()
+    assert base > 0 and budget == 0
+    db = np.random.default_rng(8).integers(0, 256, size=2 * N * ENTRY, dtype=np.uint8)  # 2 shards
+    key_bytes = 3 * 2 * N * 4  # one client's body table
+    edb = inspire.EncodedDatabase(crs, db, ENTRY)
+    used0, _ = crs.device_memory()
+    assert used0 >= base + 2 * (16 * N * 2 + 2 * 3 * 16 * N * 4)  # raw columns + contracted form
+    # room for the key upload buffer, the client table and three clients' keys
+    crs.set_device_budget(used0 + 3 * 2 * N * 8 + 256 * 8 + 3 * key_bytes + 1024)
+    with pytest.raises(inspire.PirError, match="does not fit the device budget") as ei:
+        inspire.EncodedDatabase(crs, db, ENTRY)
+    assert ei.value.status == nat.ERR_OUT_OF_MEMORY
+    assert crs.device_memory()[0] == used0  # nothing of the refused database stays reserved
+    pack = O.Pack(ctx, 16, W_SEED, mode=O.MODE_CRT_FIXED)
+    clients = [O.Client(ctx, seed=50 + s, rng_seed=500 + s) for s in range(8)]
+    ybs = [c.packing_keys(pack)[0] for c in clients]
+    ids = []
+    with pytest.raises(inspire.PirError) as ei:
+        for yb in ybs:
+            ids.append(crs.register_client(inspire.ClientPackingKeys(y_body=yb)))
+    assert ei.value.status == nat.ERR_OUT_OF_MEMORY and len(ids) == 3
+    used, budget = crs.device_memory()
+    assert used <= budget
+    with pytest.raises(inspire.PirError, match="below"):
+        crs.set_device_budget(used - 1)
+    # freeing returns the bytes: another client fits again
+    crs.release_client(ids.pop())
+    ids.append(crs.register_client(inspire.ClientPackingKeys(y_body=ybs[3])))
+    # a serving loop needs slot buffers: refused while the budget is full
+    with pytest.raises(inspire.PirError) as ei:
+        inspire.Server(crs, max_batch=1024, max_inflight=64, capacity=4096)
+    assert ei.value.status == nat.ERR_OUT_OF_MEMORY
+    # the admitted clients answer correctly (without a budget: the call's
+    # staging buffers need room too)
+    crs.set_device_budget(0)
+    seeds, b_rows = clients[3].query_seeded(77)
+    out = inspire.respond_seeded_batch(crs, edb, [1], seeds[None], b_rows[None], [ids[-1]])
+    assert np.array_equal(clients[3].extract_inspiring(out[0], ENTRY), db[(N + 77) * ENTRY:(N + 78) * ENTRY])
+    for i in ids:
+        crs.release_client(i)
+    # the HTTP backend's client cache makes room by evicting idle clients
+    crs.set_device_budget(0)
+    backend = GpuBackend(crs, edb, max_batch=8, max_inflight=1, capacity=16)
+    used, _ = crs.device_memory()
+    crs.set_device_budget(used + 2 * key_bytes + 4096)
+    for k, c in enumerate(clients[:6]):
+        yb = ybs[k]
+        s, b = c.query_seeded(k)
+        got = backend.respond_seeded_inspiring(inspire.SeededClientQuery(
+            0, s, b, inspiring_packing_keys=inspire.ClientPackingKeys(y_body=yb)))
+        assert np.array_equal(c.extract_inspiring(got, ENTRY), db[k * ENTRY:(k + 1) * ENTRY])
+    assert len(backend._keys) <= 2
+    backend.close()
+    edb.close()
+    crs.close()

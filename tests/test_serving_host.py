@@ -119,3 +119,24 @@ def test_run_against_fake_server(serving, rate):
     for db_idx, shard, pidx, out in res["samples"]:
         assert out[0][0] == 1000 + pidx
         assert shard < (3, 50)[db_idx]
+
+
+def test_device_memory_ledger_host(tmp_path):
+    """The context's device-memory accounting (csrc/ledger.h) on the host:
+    reservations up to the budget, refusal beyond it with nothing reserved,
+    release, and concurrent reservations that never pass the budget; a C++
+    driver built with g++."""
+    import os
+    import shutil
+    import subprocess
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    here = os.path.dirname(os.path.abspath(__file__))
+    csrc = os.path.join(os.path.dirname(here), "inspire-rs_gb300", "csrc")
+    exe = str(tmp_path / "ledger_check")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-pthread", "-I", csrc, os.path.join(here, "native", "ledger_check.cpp"),
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
