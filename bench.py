@@ -837,14 +837,17 @@ def http_bench(inspire, crs, edb, db_raw, nshards, clients, seeds, brows, n_bodi
     """The HTTP front end (the crate's /query_seeded route) on loopback:
     SeededClientQuery JSON bodies with the client's packing keys inline, as
     the crate's client posts them, from spawned client processes over
-    keep-alive connections.  Closed loop at 1, 8 and 32 connections, then
-    Poisson arrivals at 50 % and 90 % of the best closed-loop rate.  One
+    keep-alive connections.  The library's native server (csrc/http.cu):
+    closed loop at 1, 8, 32 and 64 connections, then Poisson arrivals at
+    50 % and 90 % of the best closed-loop rate; the Python server
+    (inspire.http_server.PirHttpServer) closed loop at 8 connections.  One
     reply per distinct body is decrypted first and checked against the
     database entry."""
+    import http.client
     import json as _json
 
     from inspire import http_load
-    from inspire.http_server import GpuBackend, PirHttpServer
+    from inspire.http_server import GpuBackend, NativeHttpServer, PirHttpServer
 
     rng = np.random.default_rng(17)
     picks = []
@@ -854,11 +857,8 @@ def http_bench(inspire, crs, edb, db_raw, nshards, clients, seeds, brows, n_bodi
         sid = int(rng.integers(0, nshards))
         picks.append((i, sid))
         bodies.append(http_load.seeded_query_json(sid, seeds[i], brows[i], clients.y_bodies[clients.client_of[i]]))
-    backend = GpuBackend(crs, edb, max_batch=128, max_inflight=4, capacity=4096)
-    srv = PirHttpServer(backend).start()
-    try:
-        import http.client
 
+    def verify(srv):
         host, port = srv.address
         conn = http.client.HTTPConnection(host, port, timeout=60)
         ok = 0
@@ -874,18 +874,33 @@ def http_bench(inspire, crs, edb, db_raw, nshards, clients, seeds, brows, n_bodi
             gi = sid * N + int(clients.locals_[i])
             ok += int(np.array_equal(got, db_raw[gi * ENTRY:(gi + 1) * ENTRY]))
         conn.close()
-        closed = [http_load.run_load(srv.url, bodies, c, duration_s=duration_s) for c in (1, 8, 32)]
+        return ok
+
+    res = {"route": "POST /query_seeded (SeededClientQuery JSON, packing keys inline)",
+           "body_bytes": len(bodies[0]), "distinct_bodies": n_bodies,
+           "resident_client_keys": "cached by y_body (the first query of a client registers its keys)"}
+    native = NativeHttpServer(crs, edb, max_batch=128, max_inflight=4, capacity=4096)
+    try:
+        ok = verify(native)
+        closed = [http_load.run_load(native.url, bodies, c, duration_s=duration_s) for c in (1, 8, 32, 64)]
         best = max(c["achieved_rps"] for c in closed)
-        open_loop = [dict(http_load.run_load(srv.url, bodies, 64, duration_s=duration_s, rate=f * best), load_frac=f)
+        open_loop = [dict(http_load.run_load(native.url, bodies, 64, duration_s=duration_s, rate=f * best), load_frac=f)
                      for f in (0.5, 0.9)]
     finally:
-        srv.close()
+        native.close()
+    res["native"] = {"server": "csrc/http.cu (C++ thread per connection; native JSON codecs; GPU serving loop)",
+                     "verified_replies": ok, "closed_loop": closed, "open_loop": open_loop}
+    backend = GpuBackend(crs, edb, max_batch=128, max_inflight=4, capacity=4096)
+    py = PirHttpServer(backend).start()
+    try:
+        ok = verify(py)
+        closed = [http_load.run_load(py.url, bodies, 8, duration_s=duration_s)]
+    finally:
+        py.close()
         backend.close()
-    return {"route": "POST /query_seeded (SeededClientQuery JSON, packing keys inline)",
-            "body_bytes": len(bodies[0]), "distinct_bodies": n_bodies, "verified_replies": ok,
-            "server": "inspire.http_server (thread per connection; native JSON codecs; GPU serving loop)",
-            "closed_loop": closed, "open_loop": open_loop,
-            "resident_client_keys": "cached by y_body (the first query of a client registers its keys)"}
+    res["python"] = {"server": "inspire.http_server.PirHttpServer (http.server thread per connection)",
+                     "verified_replies": ok, "closed_loop": closed}
+    return res
 
 
 def shard_file_bench(inspire, crs, seeds, brows, y_body, log2_entries=20):

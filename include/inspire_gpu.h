@@ -463,6 +463,41 @@ int inspire_packed_response_to_json(const inspire_params *params, const uint64_t
 int inspire_server_response_to_bincode(const inspire_params *params, const uint64_t *ct, uint32_t n_columns,
                                        const uint64_t *columns, uint8_t *buf, size_t cap, size_t *len);
 
+/* ---- HTTP front end ----
+ * The crate's server binary (src/bin/server.rs:242-337) over this ABI: the
+ * routes GET /health, GET /params, GET /crs, POST /query, POST /query_seeded
+ * with the crate's JSON shapes, status codes and error texts (QueryResponse
+ * {response, processing_time_ms}; 400 {"error": ...}; 400/422/415 for bodies
+ * that are not JSON, not the target type, or not application/json).  One
+ * thread per connection, HTTP/1.1 keep-alive.  Seeded InspiRING queries go
+ * through `srv` (a serving loop on `ctx`; NULL: the synchronous call), the
+ * other kinds through the synchronous entry points on (ctx, db).  The client
+ * keys of each query stay registered, keyed by a hash of y_body, evicted
+ * least-recently-used beyond max_clients or when the context's device budget
+ * refuses new keys.  ctx, db and srv must outlive the server. */
+typedef struct inspire_http_server inspire_http_server;
+
+typedef struct {
+  const char *host;     /* IPv4 address to bind ("0.0.0.0", "127.0.0.1") */
+  uint16_t port;        /* 0: any free port (inspire_http_port tells which) */
+  uint32_t max_clients; /* resident client keys kept */
+  uint64_t max_body;    /* request body limit in bytes (413 beyond) */
+  const char *version;  /* /params: metadata.json's version, entry_count, shard_count */
+  uint64_t entry_count;
+  uint64_t shard_count;
+} inspire_http_config;
+
+/* host 127.0.0.1, port 0, max_clients 4096, max_body 64 MiB, version "1.0.0". */
+void inspire_http_config_default(inspire_http_config *cfg);
+/* Start serving (accepting in a thread of its own); crs_json (may be NULL)
+ * is what GET /crs returns. */
+int inspire_http_start(inspire_ctx *ctx, const inspire_db *db, inspire_server *srv, const inspire_http_config *cfg,
+                       const char *crs_json, size_t crs_len, inspire_http_server **out);
+uint16_t inspire_http_port(const inspire_http_server *http);
+/* Stop accepting, close every connection (requests in progress finish
+ * first), release the cached client keys, free the server. */
+void inspire_http_stop(inspire_http_server *http);
+
 /* Batched NttContext::forward / inverse (src/math/ntt.rs:223-325) on device
  * data polys[npolys][2][ring_dim] (u32 residues), in place.  Forward outputs
  * the crate's NTT-domain values (Montgomery form, R = 2^64, bit-reversed slot

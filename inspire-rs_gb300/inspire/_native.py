@@ -62,6 +62,18 @@ class ServerCrsPartsC(C.Structure):
     ]
 
 
+class HttpConfigC(C.Structure):
+    _fields_ = [
+        ("host", C.c_char_p),
+        ("port", C.c_uint16),
+        ("max_clients", C.c_uint32),
+        ("max_body", C.c_uint64),
+        ("version", C.c_char_p),
+        ("entry_count", C.c_uint64),
+        ("shard_count", C.c_uint64),
+    ]
+
+
 class SeededQueryC(C.Structure):
     _fields_ = [
         ("shard_id", C.c_uint32),
@@ -179,6 +191,11 @@ def load(path: str = LIB_PATH):
         "inspire_crs_a_vectors_count": (u64, [vp]),
         "inspire_inspiring_precomp": (C.c_int, [vp, vp, vp, vp]),
         "inspire_ctx_set_device_budget": (C.c_int, [vp, u64]),
+        "inspire_http_config_default": (None, [C.POINTER(HttpConfigC)]),
+        "inspire_http_start": (C.c_int, [vp, vp, vp, C.POINTER(HttpConfigC), C.c_char_p, C.c_size_t,
+                                         C.POINTER(vp)]),
+        "inspire_http_port": (C.c_uint16, [vp]),
+        "inspire_http_stop": (None, [vp]),
         "inspire_ctx_device_memory": (C.c_int, [vp, C.POINTER(u64), C.POINTER(u64)]),
         "inspire_server_response_to_bincode": (C.c_int, [C.POINTER(InspireParamsC), vp, u32, vp, vp, C.c_size_t,
                                                          C.POINTER(C.c_size_t)]),

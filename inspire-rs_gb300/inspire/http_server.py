@@ -386,6 +386,62 @@ class PirHttpServer:
         return cls(backend, host, port)
 
 
+class NativeHttpServer:
+    """The same routes served by the library itself (csrc/http.cu,
+    inspire_http_start): C++ threads per connection, no interpreter on the
+    request path.  Seeded InspiRING queries go through a serving loop on
+    the context (one is created unless `server` is given); client keys are
+    cached as GpuBackend caches them.  Same interface as PirHttpServer."""
+
+    def __init__(self, crs: ServerCrs, encoded_db: EncodedDatabase, host: str = "127.0.0.1", port: int = 0, *,
+                 server: Optional[Server] = None, crs_json: Optional[bytes] = None, metadata: Optional[dict] = None,
+                 max_clients: int = 4096, max_body: int = 64 << 20, max_batch: int = 128, max_inflight: int = 4,
+                 capacity: int = 4096):
+        self.L = nat.load()
+        self.crs, self.edb = crs, encoded_db
+        self._own_server = server is None
+        self.server = server if server is not None else Server(crs, max_batch=max_batch, max_inflight=max_inflight,
+                                                               capacity=capacity)
+        md = metadata or {"version": "1.0.0", "entry_count": int(encoded_db.total_entries),
+                          "shard_count": int(encoded_db.num_shards)}
+        cfg = nat.HttpConfigC()
+        self.L.inspire_http_config_default(C.byref(cfg))
+        self._host = host.encode()
+        self._version = str(md["version"]).encode()
+        cfg.host, cfg.port, cfg.max_clients, cfg.max_body = self._host, port, max_clients, max_body
+        cfg.version, cfg.entry_count, cfg.shard_count = self._version, int(md["entry_count"]), int(md["shard_count"])
+        h = C.c_void_p()
+        data = crs_json or b""
+        _check(self.L.inspire_http_start(crs.h, encoded_db.h, self.server.h, C.byref(cfg), data, len(data), C.byref(h)))
+        self.h = h
+
+    @property
+    def address(self):
+        return self._host.decode(), int(self.L.inspire_http_port(self.h))
+
+    @property
+    def url(self) -> str:
+        h, p = self.address
+        return f"http://{h}:{p}"
+
+    def start(self) -> "NativeHttpServer":
+        return self  # accepting since construction
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.inspire_http_stop(self.h)
+            self.h = None
+        if self._own_server and self.server is not None:
+            self.server.close()
+            self.server = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def main(argv=None):
     """inspire-server's command line (server.rs:30-46): --data-dir, --bind,
     --mmap; plus --mode and --device of the GPU build."""
@@ -397,15 +453,29 @@ def main(argv=None):
     ap.add_argument("--mmap", action="store_true")
     ap.add_argument("--mode", default="crt_fixed", choices=["crt_fixed", "compat"])
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--python", action="store_true", help="serve from Python (http.server) instead of the library")
     a = ap.parse_args(argv)
     host, port = a.bind.rsplit(":", 1)
     srv = PirHttpServer.from_data_dir(a.data_dir, mode=a.mode, device=a.device, mmap=a.mmap, host=host,
-                                      port=int(port))
-    print(f"Listening on: {srv.url}", flush=True)
+                                      port=0 if not a.python else int(port))
+    if a.python:
+        print(f"Listening on: {srv.url}", flush=True)
+        try:
+            srv.serve_forever()
+        finally:
+            srv.backend.close()
+        return
+    b = srv.backend
+    srv.close()
+    native = NativeHttpServer(b.crs, b.edb, host, int(port), server=b.server, crs_json=b.crs_json(),
+                              metadata=b.metadata())
+    print(f"Listening on: {native.url}", flush=True)
     try:
-        srv.serve_forever()
+        while True:
+            time.sleep(3600)
     finally:
-        srv.backend.close()
+        native.close()
+        b.close()
 
 
 if __name__ == "__main__":

@@ -40,17 +40,22 @@ def _reply_for(inspire, params, ct, body):
     return inspire.wire.query_response_to_json(params, resp, ms)
 
 
-def test_http_inspiring_served(world):
+@pytest.mark.parametrize("impl", ["native", "python"])
+def test_http_inspiring_served(world, impl):
     W = world
     O, inspire, ctx = W["O"], W["inspire"], W["ctx"]
-    from inspire.http_server import GpuBackend, PirHttpServer
+    from inspire.http_server import GpuBackend, NativeHttpServer, PirHttpServer
 
     crs = inspire.ServerCrs(inspire.InspireParams(p=1 << 16), W_SEED, 16, mode="crt_fixed")
     edb = inspire.EncodedDatabase(crs, W["db"], ENTRY)
     pack = O.Pack(ctx, 16, W_SEED, mode=O.MODE_CRT_FIXED)
     keys = [c.packing_keys(pack)[0] for c in W["clients"]]
-    backend = GpuBackend(crs, edb, max_clients=2, max_batch=8, max_inflight=2, capacity=64)
-    srv = PirHttpServer(backend).start()
+    backend = None
+    if impl == "python":
+        backend = GpuBackend(crs, edb, max_clients=2, max_batch=8, max_inflight=2, capacity=64)
+        srv = PirHttpServer(backend).start()
+    else:
+        srv = NativeHttpServer(crs, edb, max_clients=2, max_batch=8, max_inflight=2, capacity=64)
     url = srv.url
     rng = np.random.default_rng(5)
     jobs = []
@@ -82,7 +87,8 @@ def test_http_inspiring_served(world):
         got = W["clients"][c].extract_inspiring(ciphertext_of(body), ENTRY)
         assert np.array_equal(got, W["db"][idx * ENTRY:(idx + 1) * ENTRY])
     # at most max_clients keys stay resident once nothing is in flight
-    assert len(backend._keys) <= 3
+    if backend is not None:
+        assert len(backend._keys) <= 3
     # /query (full RGSW rows) equals respond_inspiring
     seeds, b_rows = W["clients"][1].query_seeded(300)
     rgsw = ctx.expand_rgsw(seeds, b_rows)
@@ -97,13 +103,27 @@ def test_http_inspiring_served(world):
     assert st == 400 and json.loads(body) == {"error": "Seeded query processing failed: Shard 4 not found"}
     st, _, body = request(url, "POST", "/query", full_query_body(4, rgsw, keys[0]))
     assert st == 400 and json.loads(body) == {"error": "Query processing failed: Shard 4 not found"}
+    # the crate's health and params replies
+    st, _, body = request(url, "GET", "/health", ctype=None)
+    assert st == 200 and body == b'{"status":"ok","version":"0.1.2"}'
+    st, _, body = request(url, "GET", "/params", ctype=None)
+    assert st == 200 and json.loads(body)["shard_count"] == 4 and json.loads(body)["entry_count"] == 3 * N + 100
+    # extractor rejections
+    st, _, body = request(url, "POST", "/query_seeded", b'{"shard_id": 1,')
+    assert st == 400 and body.startswith(b"Failed to parse the request body as JSON")
+    st, _, body = request(url, "POST", "/query_seeded", b'{"shard_id": 1}')
+    assert st == 422 and body.startswith(b"Failed to deserialize the JSON body")
+    st, _, _ = request(url, "POST", "/query_seeded", seeded_query_body(0, seeds, b_rows, keys[0]), ctype="text/plain")
+    assert st == 415
     srv.close()
-    backend.close()
+    if backend is not None:
+        backend.close()
     edb.close()
     crs.close()
 
 
-def test_http_tree_and_data_dir(world, tmp_path):
+@pytest.mark.parametrize("impl", ["native", "python"])
+def test_http_tree_and_data_dir(world, tmp_path, impl):
     """packing_mode "tree" on both routes (respond_seeded_packed /
     respond_one_packing), compat mode, from a data directory laid out as the
     crate's setup writes it (crs.json with Galois keys, shards/, metadata.json)."""
@@ -126,8 +146,14 @@ def test_http_tree_and_data_dir(world, tmp_path):
     (tmp_path / "metadata.json").write_text(json.dumps({"version": "9.9.9", "ring_dim": N, "modulus": str(params.q),
                                                         "plaintext_modulus": 65536, "entry_count": 3 * N + 100,
                                                         "shard_count": 4}))
+    from inspire.http_server import NativeHttpServer
+
     srv = PirHttpServer.from_data_dir(str(tmp_path), params, mode="compat", mmap=True, host="127.0.0.1",
                                       port=0).start()
+    py_srv = srv
+    if impl == "native":
+        b = srv.backend
+        srv = NativeHttpServer(b.crs, b.edb, server=b.server, crs_json=b.crs_json(), metadata=b.metadata())
     url = srv.url
     st, _, body = request(url, "GET", "/params", ctype=None)
     p = json.loads(body)
@@ -146,6 +172,8 @@ def test_http_tree_and_data_dir(world, tmp_path):
     ms = json.loads(body)["processing_time_ms"]
     assert st == 200 and body == inspire.wire.packed_response_to_json(params, want.ciphertext.a, want.ciphertext.b, ms)
     srv.close()
-    srv.backend.close()
+    if impl == "native":
+        py_srv.close()
+    py_srv.backend.close()
     edb0.close()
     crs0.close()
