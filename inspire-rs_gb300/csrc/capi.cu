@@ -530,6 +530,14 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     C.ninv_mont_p = shoup(nm, qm);
     C.mont = (uint32_t)r32;
     C.mont_p = shoup(r32, qm);
+    const uint64_t zinv = inv_prime((1ULL << ZBITS) % qm, qm), z2inv = (uint64_t)((u128)zinv * zinv % qm);
+    const uint64_t nz2 = (uint64_t)((u128)N * z2inv % qm);
+    C.d2_nz2 = (uint32_t)nz2;
+    C.d2_nz2_p = shoup(nz2, qm);
+    C.d2_z2 = (uint32_t)z2inv;
+    C.d2_z2_p = shoup(z2inv, qm);
+    C.d2_z1 = (uint32_t)zinv;
+    C.d2_z1_p = shoup(zinv, qm);
     int lz = __builtin_clzll(qm);
     C.zone = (qm << lz) - 1;
   }

@@ -30,6 +30,9 @@ struct ResidueConsts {
   uint32_t ninv_mont, ninv_mont_p;   // n^-1 * 2^32 mod q
   uint32_t mont, mont_p;             // 2^32 mod q
   uint32_t e_scale, e_scale_p;       // gamma^-1 * n^-1 * 2^96 mod q (database contraction)
+  uint32_t d2_nz2, d2_nz2_p;         // n z^-2 mod q  (third gadget digit's transform, z = 2^20)
+  uint32_t d2_z2, d2_z2_p;           // z^-2 mod q
+  uint32_t d2_z1, d2_z1_p;           // z^-1 mod q
   uint64_t zone;                     // rand 0.8 rejection zone for gen_range(0..q)
 };
 

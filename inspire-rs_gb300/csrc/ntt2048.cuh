@@ -201,6 +201,97 @@ __device__ __forceinline__ void ntt_inv_noscale(uint32_t v[16], uint32_t* sc, Tw
   stage<0, 4, false>(v, tw, 0, q, q2);
 }
 
+// ---- Inverse transform on a 256-thread team, 8 values per thread ----
+// Used where one residue's inverse NTT is on the critical path and two
+// groups are free to run it: half the dependent butterflies per thread of
+// the 128-thread transform, one more exchange.  Slot layout in (thread t
+// holds A[8t + r]), coefficient layout out (v[r] = a[t + 256 r]), values in
+// [0, 2q) both ways, no n^-1 factor.  Register phases run stages 10-8, 7-5,
+// 4-2 and 1-0; three exchanges through `sc` (2048 words) re-pair the values:
+//   after stage 8:  idx = (t & 7) + 8 r + 64 (t >> 3)
+//   after stage 5:  idx = (t & 63) + 64 r + 512 (t >> 6)
+//   after stage 2:  idx = t + 256 r
+// stored at idx ^ ((idx >> 3) & 31) (first two exchanges) and
+// idx ^ ((idx >> 10) & 15) (third); both maps are permutations of [0, 2048)
+// and keep every 32-bit access of a warp on 32 distinct banks.  Stage s pairs
+// j with j + 1024 / 2^s and uses twiddle 2^s + (j >> (11 - s)), as the
+// 128-thread transform does.
+
+// Barrier over the 256 threads of a team (named barrier `id`).
+__device__ __forceinline__ void team_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(2 * NTT_GT) : "memory");
+}
+
+__device__ __forceinline__ int x12(int i) { return i ^ ((i >> 3) & 31); }
+__device__ __forceinline__ int x3(int i) { return i ^ ((i >> 10) & 15); }
+
+// One GS stage over the 8 registers: element r pairs with r + H when
+// (r & H) == 0, twiddle run[r >> SH].
+template <int H, int SH, int CNT>
+__device__ __forceinline__ void inv8_stage(uint32_t v[8], const uint2 (&run)[CNT], uint32_t q, uint32_t q2) {
+#pragma unroll
+  for (int r = 0; r < 8; r++)
+    if ((r & H) == 0) gs_bfly(v[r], v[r + H], run[r >> SH], q, q2);
+}
+
+__device__ __forceinline__ void ntt_inv_noscale8(uint32_t v[8], uint32_t* sc, TwiddleRef tw, uint32_t q, int t,
+                                                 int bar) {
+  const uint32_t q2 = 2 * q;
+  {
+    uint2 r4[4], r2[2], r1[1];
+    tw_run<4>(tw, 1024 + 4 * t, r4);
+    inv8_stage<1, 1, 4>(v, r4, q, q2);
+    tw_run<2>(tw, 512 + 2 * t, r2);
+    inv8_stage<2, 2, 2>(v, r2, q, q2);
+    tw_run<1>(tw, 256 + t, r1);
+    inv8_stage<4, 3, 1>(v, r1, q, q2);
+  }
+  team_sync(bar);
+#pragma unroll
+  for (int r = 0; r < 8; r++) sc[x12(8 * t + r)] = v[r];
+  team_sync(bar);
+  const int b3 = t >> 3, b6 = t >> 6;
+#pragma unroll
+  for (int r = 0; r < 8; r++) v[r] = sc[x12((t & 7) + (r << 3) + (b3 << 6))];
+  {
+    uint2 r4[4], r2[2], r1[1];
+    tw_run<4>(tw, 128 + 4 * b3, r4);
+    inv8_stage<1, 1, 4>(v, r4, q, q2);
+    tw_run<2>(tw, 64 + 2 * b3, r2);
+    inv8_stage<2, 2, 2>(v, r2, q, q2);
+    tw_run<1>(tw, 32 + b3, r1);
+    inv8_stage<4, 3, 1>(v, r1, q, q2);
+  }
+  team_sync(bar);
+#pragma unroll
+  for (int r = 0; r < 8; r++) sc[x12((t & 7) + (r << 3) + (b3 << 6))] = v[r];
+  team_sync(bar);
+#pragma unroll
+  for (int r = 0; r < 8; r++) v[r] = sc[x12((t & 63) + (r << 6) + (b6 << 9))];
+  {
+    uint2 r4[4], r2[2], r1[1];
+    tw_run<4>(tw, 16 + 4 * b6, r4);
+    inv8_stage<1, 1, 4>(v, r4, q, q2);
+    tw_run<2>(tw, 8 + 2 * b6, r2);
+    inv8_stage<2, 2, 2>(v, r2, q, q2);
+    tw_run<1>(tw, 4 + b6, r1);
+    inv8_stage<4, 3, 1>(v, r1, q, q2);
+  }
+  team_sync(bar);
+#pragma unroll
+  for (int r = 0; r < 8; r++) sc[x3((t & 63) + (r << 6) + (b6 << 9))] = v[r];
+  team_sync(bar);
+#pragma unroll
+  for (int r = 0; r < 8; r++) v[r] = sc[x3(t + 256 * r)];
+  {
+    uint2 r2[2], r1[1];
+    tw_run<2>(tw, 2, r2);
+    inv8_stage<2, 2, 2>(v, r2, q, q2);
+    tw_run<1>(tw, 1, r1);
+    inv8_stage<4, 3, 1>(v, r1, q, q2);
+  }
+}
+
 // Slot-layout arrays in shared memory are stored with this XOR swizzle, which
 // moves 4-word chunks inside each 16-word block so that the 128-bit accesses
 // of load16/store16 (thread x: words 16x..16x+15) hit eight distinct bank

@@ -181,8 +181,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
 // 2brv(s)+1 = h_i (2brv(u)+1) mod 2n, where h_i = g^-i
 // (inspiring2.rs:952-981 with the tables of :208-263).  Threads p in
 // [0, nthr) handle u = p + nthr * v.
+// In compat mode `dst1`, if not null, receives residue 1 rebuilt from each
+// residue-0 value as the crate's apply_automorphism_ntt does.
 __device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint32_t* __restrict__ Eg, const uint32_t* Ag,
-                                          int astride, uint32_t* dst, int p, int nthr, uint32_t q, uint32_t qinv) {
+                                          int astride, uint32_t* dst, int p, int nthr, uint32_t q, uint32_t qinv,
+                                          uint32_t* dst1 = nullptr) {
   const int gamma = P.gamma;
   const uint32_t mi = (uint32_t)(gamma - i) & (uint32_t)(gamma - 1);
   const uint32_t hi = (1u + (uint32_t)(2 * N / gamma) * mi) & (2 * N - 1);
@@ -195,7 +198,9 @@ __device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint3
     const uint64_t T = (uint64_t)__ldg(ek) * Ag[us] + (uint64_t)__ldg(ek + (size_t)gamma * N) * Ag[astride + us] +
                        (uint64_t)__ldg(ek + (size_t)2 * gamma * N) * Ag[2 * astride + us];
     const uint32_t s = brv11(((hi * e) & (2 * N - 1)) >> 1);
-    dst[swz(s)] = redc(T, q, qinv);
+    const uint32_t val = redc(T, q, qinv);
+    dst[swz(s)] = val;
+    if (dst1) dst1[swz(s)] = compat_residue1_ninv(P, val);
   }
 }
 
@@ -240,18 +245,56 @@ __device__ __forceinline__ void rotate_key_run(uint4 (&y)[4], int i, int x) {
 // Shared-memory layout in u32 words (NR = residues of the a side).
 template <int NR>
 struct Smem {
-  static constexpr int AHAT = 0;                           // [ELL][NR][N]
-  static constexpr int SC = AHAT + ELL * NR * N;           // [RG][NTT_SCRATCH]
-  static constexpr int T = SC + RG * NTT_SCRATCH;          // [3][N] digits (T0/T1 also hold the INTT output)
-  static constexpr int SCAT = T + 3 * N;                   // [2][N] R_i (slot layout, swizzled)
-  static constexpr int PB = SCAT + 2 * N;                  // [2][2][N] partial products of digits 1, 2
-  static constexpr int ACC = PB + 4 * N;                   // [RG][N] per-group b accumulators
-  // SCAT..ACC (12N words) also hold the query's raw b rows (u64) until the b side
-  static constexpr int MISC = ACC + RG * N;                // bpoly[32], ws[3][20], staged seeds (96 B)
+  static constexpr int AHAT = 0;                    // [ELL][NR][N] row transforms
+  static constexpr int SC = AHAT + ELL * NR * N;    // [RG][NTT_SCRATCH] per-group exchange scratch
+  static constexpr int T = SC + RG * NTT_SCRATCH;   // [2][N] R_{i+1} (slots) -> its inverse (coefficients) -> digits d0, d1
+  static constexpr int RS = T + 2 * N;              // [2][N] copy of R_{i+1} (slots), for the third digit's transform
+  static constexpr int X0 = RS + 2 * N;             // [2][N] NTT(d0), lazily reduced
+  static constexpr int X1 = X0 + 2 * N;             // [2][N] NTT(d1), lazily reduced
+  static constexpr int SCAT = X1 + 2 * N;           // [2 steps][2][N] query-only term of R_i (slots)
+  static constexpr int ACC = SCAT + 4 * N;          // [2][N] b accumulators
+  // T..ACC+2N (14N words) also hold the query's raw b rows (u64, 12N words)
+  // until the b side; T..X0 (6N words) the unseeded rows' a parts
+  static constexpr int MISC = ACC + 2 * N;          // bpoly[32], ws[3][20], staged seeds (96 B), mbarrier
   static constexpr int TOTAL = MISC + 128;
 };
 
+// NTT(d2) of one slot from the slot's R_{i+1} (times n^-1, canonical) and the
+// transforms of the two lower digits (any u32): the composite coefficient is
+// c = d0 + z d1 + z^2 d2 (gadget_decompose, rgsw/external_product.rs:16-37)
+// and c = INTT(R_{i+1}) mod q_r, so NTT(d2) = z^-2 (n R - NTT(d0) - z NTT(d1))
+// mod q_r, exactly.
+__device__ __forceinline__ uint32_t third_digit(const ResidueConsts& C, uint32_t rs, uint32_t v0, uint32_t v1) {
+  const uint32_t a = mul_shoup(rs, C.d2_nz2, C.d2_nz2_p, C.q);
+  const uint32_t b = mul_shoup(v0, C.d2_z2, C.d2_z2_p, C.q);
+  const uint32_t c = mul_shoup(v1, C.d2_z1, C.d2_z1_p, C.q);
+  return sub_mod(sub_mod(a, b, C.q), c, C.q);
+}
+
+// Load a 16-slot run of a key slice (uint4 x 4; y: rotated from the body
+// table when `ybody`).
+__device__ __forceinline__ void key_run(const uint32_t* p, uint4 (&k)[4]) {
+  const uint4* k4 = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+  for (int r4 = 0; r4 < 4; r4++) k[r4] = __ldg(k4 + r4);
+}
+
+__device__ __forceinline__ uint32_t u4e(const uint4& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
+
 // One query (index qi) by the whole CTA; every return is uniform over the CTA.
+//
+// Per recursion step i (gamma-2 .. 0), residue r's three groups:
+//  [A] (r,0)+(r,1) as one 256-thread team: inverse NTT of R_{i+1} (T[r],
+//      copied to RS[r]); (r,2) idle;
+//  [B] all threads: CRT compose + gadget digits d0, d1 into T (d2 is never
+//      formed: its transform is derived in [D]);
+//  [C] (r,0): NTT(d0) -> X0, partial R_i = SCAT + NTT(d0) w[i][0] (held in
+//      registers), b accumulator += NTT(d0) y[i][0]; (r,1): NTT(d1) -> X1;
+//      (r,2): the query-only term of the NEXT step, R_{i-1}, into the other
+//      SCAT buffer (off the critical path);
+//  [D] (r,0): NTT(d2) from RS, X0, X1; R_i += NTT(d1) w[i][1] + NTT(d2)
+//      w[i][2] -> T[r] (slots) for the next step; (r,1): the same NTT(d2),
+//      b accumulator += NTT(d1) y[i][1] + NTT(d2) y[i][2].
 template <int MODE, bool SEEDED, bool QDB>
 __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
@@ -260,15 +303,17 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   uint32_t* Ahat = smem + L::AHAT;
   uint32_t* SC = smem + L::SC;
   uint32_t* T = smem + L::T;
+  uint32_t* RS = smem + L::RS;
+  uint32_t* X0 = smem + L::X0;
+  uint32_t* X1 = smem + L::X1;
   uint32_t* SCAT = smem + L::SCAT;
-  uint32_t* PB = smem + L::PB;
   uint32_t* bpoly = smem + L::MISC;
   int* wsb = (int*)(smem + L::MISC + 32);
 
   const DevParams& P = A.P;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
-  const int r = g / 3, kd = g - 3 * r;  // residue, gadget digit of this group
-  uint32_t* ACC = smem + L::ACC + g * N;  // this group's b accumulator
+  const int r = g / 3, kd = g - 3 * r;  // residue, role of this group
+  uint32_t* ACC = smem + L::ACC + r * N;  // this residue's b accumulator
   const int gamma = P.gamma;
   // QDB (serving loop): this query's fields come from its descriptor in
   // device memory, its rows and response from / to pinned host memory;
@@ -295,16 +340,17 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   const uintptr_t ytag = reinterpret_cast<uintptr_t>(A.yhat_table[cid]);
   const bool ybody = (ytag & 1) != 0;
   const uint32_t* Y = reinterpret_cast<const uint32_t*>(ytag & ~(uintptr_t)1);
-  const uint32_t q = P.r[r].q, qinv = P.r[r].qinv, q2 = 2 * q;
+  const ResidueConsts& C = P.r[r];
+  const uint32_t q = C.q, qinv = C.qinv, q2 = 2 * q;
   const uint64_t* brows = QDB ? D->brows : A.brows + (size_t)qi * ELL * 2 * N;
 
   // Serving loop (rows in host memory): the query's b rows (96 KiB) are
-  // bulk-copied (TMA) into shared memory (SCAT..ACC) while the rows are
+  // bulk-copied (TMA) into shared memory (T..ACC) while the rows are
   // expanded, so the host link's latency stays off the critical path, and the
   // b side follows the row NTTs.  Rows in device memory: bside_kernel has
   // already computed the b side and parked it in the response slot; the
   // contracted shard and client keys are streamed into L2 from the start.
-  uint64_t* raw = reinterpret_cast<uint64_t*>(SCAT);           // 16-byte aligned
+  uint64_t* raw = reinterpret_cast<uint64_t*>(T);                      // 16-byte aligned
   uint64_t* rbar = reinterpret_cast<uint64_t*>(smem + L::MISC + 120);  // the rows' mbarrier
   if (QDB && tid == 0) {
     mbar_init(rbar);
@@ -333,8 +379,8 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   {
     const int t = tid >> 8, lt = tid & 255;
     uint64_t* cand = reinterpret_cast<uint64_t*>(SC) + t * N;  // 3 x 16 KiB within SC
-    // serving loop: in place of the row's transforms (SCAT..ACC hold the
-    // staged rows); otherwise within T..PB
+    // serving loop: in place of the row's transforms (T..ACC hold the
+    // staged rows); otherwise within T..X0
     uint32_t* a0 = QDB ? Ahat + t * NR * N : T + t * 2 * N;
     uint32_t* a1 = a0 + N;
     if (SEEDED) {
@@ -369,7 +415,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     const uint32_t* src = QDB ? Ahat + (kd * NR + r) * N : T + kd * 2 * N + r * N;
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = src[x + 128 * j];
-    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = canon16(v[j], q);
     store16(Ahat + (kd * NR + r) * N, x, v);
@@ -379,154 +425,180 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   // ---- serving loop: b part of the column products (bp in SC, rows staged) ----
   if (QDB) column_b0<RBLOCK>(P, H, raw, SC, bpoly);
 
-  // scatter roles: fixed mode -> groups (r,1),(r,2) do residue r;
-  // compat -> groups with digit 1, 2 of both residues do residue 0
-  const int sres = MODE == MODE_CRT_FIXED ? r : 0;
-  const int sp = MODE == MODE_CRT_FIXED ? (kd - 1) * NTT_GT + x : ((r * 2 + (kd - 1)) * NTT_GT + x);
-  const int snthr = MODE == MODE_CRT_FIXED ? 2 * NTT_GT : 4 * NTT_GT;
-  const bool scatters = kd != 0;
-  // Eg: this group's residue of the contracted shard; with per-query
+  // Eg: the scatter's residue of the contracted shard; with per-query
   // databases it is re-derived at each use from the query's view
-  const uint32_t* Eg_fixed = QDB ? nullptr : E + (size_t)sres * ELL * gamma * N;
-  auto Eg_at = [&]() -> const uint32_t* {
-    if (!QDB) return Eg_fixed;
+  const uint32_t* Eg_fixed = QDB ? nullptr : E;
+  auto Eg_at = [&](int sres) -> const uint32_t* {
+    if (!QDB) return Eg_fixed + (size_t)sres * ELL * gamma * N;
     const uint32_t sh = *reinterpret_cast<const volatile uint32_t*>(&D->shard);
     return reload_ptr(&D->db.E) + ((size_t)sh * 2 * ELL + (size_t)sres * ELL) * gamma * N;
   };
-  const uint32_t* Ag = Ahat + sres * N;
-  const uint32_t sq = P.r[sres].q, sqinv = P.r[sres].qinv;
 
-  uint32_t vR[16];
+  // ---- R_{gamma-1} into T, R_{gamma-2} into SCAT[(gamma-2) & 1], by all
+  //      groups (fixed: each residue's 384 threads; compat: residue 0 by all) ----
   {
-    const uint32_t zero[16] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    store16(ACC, x, zero);
+    const int sres = MODE == MODE_CRT_FIXED ? r : 0;
+    const int sp = MODE == MODE_CRT_FIXED ? kd * NTT_GT + x : tid;
+    const int snthr = MODE == MODE_CRT_FIXED ? 3 * NTT_GT : RBLOCK;
+    const uint32_t sq = P.r[sres].q, sqinv = P.r[sres].qinv;
+    const uint32_t* Ag = Ahat + sres * N;
+    scatter_r(P, gamma - 1, Eg_at(sres), Ag, NR * N, T + sres * N, sp, snthr, sq, sqinv,
+              MODE == MODE_COMPAT ? T + N : nullptr);
+    if (gamma > 1) {
+      uint32_t* sc2 = SCAT + ((gamma - 2) & 1) * 2 * N;
+      scatter_r(P, gamma - 2, Eg_at(sres), Ag, NR * N, sc2 + sres * N, sp, snthr, sq, sqinv,
+                MODE == MODE_COMPAT ? sc2 + N : nullptr);
+    }
+    for (int j = tid; j < 2 * N; j += RBLOCK) smem[L::ACC + j] = 0;
   }
-
-  // R_{gamma-1}
-  if (scatters) scatter_r(P, gamma - 1, Eg_at(), Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
   __syncthreads();
-  if (kd == 0) {
-    load16(SCAT + (MODE == MODE_CRT_FIXED ? r : 0) * N, x, vR);
-    if (MODE == MODE_COMPAT && r == 1)
-#pragma unroll
-      for (int j = 0; j < 16; j++) vR[j] = compat_residue1_ninv(P, vR[j]);
-  }
-  __syncthreads();  // the scatter buffer is reused by the first step
 
+  const int team_t = tid - 384 * r;  // thread of residue r's (r,0)+(r,1) team, valid for kd < 2
+  uint32_t* team_sc = SC + 3 * r * NTT_SCRATCH;  // the team's exchange scratch (two groups' worth)
   for (int i = gamma - 2; i >= 0; i--) {
-    // [A] INTT(R_{i+1}) by groups (r,0); scatter of R_i by the others
-    if (kd == 0) {
-      ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
+    // [A] inverse NTT of R_{i+1} by residue r's team; RS keeps R_{i+1}
+    if (kd < 2) {
+      uint32_t v[8];
+      const int s0 = 8 * team_t;
+      const uint4 lo = *reinterpret_cast<const uint4*>(T + r * N + swz(s0));
+      const uint4 hi = *reinterpret_cast<const uint4*>(T + r * N + swz(s0 + 4));
+      *reinterpret_cast<uint4*>(RS + r * N + swz(s0)) = lo;
+      *reinterpret_cast<uint4*>(RS + r * N + swz(s0 + 4)) = hi;
+      v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
+      v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
+      ntt_inv_noscale8(v, team_sc, inv_tw(C), q, team_t, 7 + r);
 #pragma unroll
-      for (int j = 0; j < 16; j++) T[r * N + x + 128 * j] = canon2(vR[j], q);
-    } else {
-      scatter_r(P, i, Eg_at(), Ag, NR * N, SCAT + sres * N, sp, snthr, sq, sqinv);
+      for (int j = 0; j < 8; j++) T[r * N + team_t + 256 * j] = canon2(v[j], q);
     }
     __syncthreads();
-    // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37)
+    // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37):
+    //     digits 0 and 1 only
     for (int j = tid; j < N; j += RBLOCK) {
       const uint64_t c = crt_compose(P, T[j], T[N + j]);
       T[j] = (uint32_t)c & 0xFFFFFu;
       T[N + j] = (uint32_t)(c >> 20) & 0xFFFFFu;
-      T[2 * N + j] = (uint32_t)(c >> 40);
     }
     __syncthreads();
-    // [C] group (r,k): NTT of digit k mod q_r, products with w_all[i][k]
-    //     (R_i accumulator) and y_all[i][k] (b accumulator)
-    uint32_t v[16];
-    const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
-    // the key slices of this step are fetched before the transform so their
-    // L2 latency overlaps it
-    uint4 wv[4], yv[4];
-    {
-      const uint4* w4 = reinterpret_cast<const uint4*>(A.what + off);
-      const uint4* y4 = reinterpret_cast<const uint4*>(Y + (ybody ? off - (size_t)i * ELL * 2 * N : off));
-#pragma unroll
-      for (int r4 = 0; r4 < 4; r4++) {
-        wv[r4] = __ldg(w4 + r4);
-        yv[r4] = __ldg(y4 + r4);
+    // [C]
+    if (kd < 2) {
+      const size_t off0 = ((size_t)(i * ELL + 0) * 2 + r) * N + 16 * x;
+      uint4 wv[4], yv[4];
+      if (kd == 0) {  // this step's key slices, fetched before the transform
+        key_run(A.what + off0, wv);
+        key_run(Y + (ybody ? off0 - (size_t)i * ELL * 2 * N : off0), yv);
       }
-    }
+      uint32_t v[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
-    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
-    if (ybody) rotate_key_run(yv, i, x);
-    {
-      const int f = (x >> 1) & 3;
-      uint32_t* accp = ACC + 16 * x;
-      const uint32_t* sb = SCAT + (MODE == MODE_CRT_FIXED ? r : 0) * N + 16 * x;
+      for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
+      ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);  // slots 16x.., [0, 14q)
+      store16((kd == 0 ? X0 : X1) + r * N, x, v);
+      if (kd == 0) {
+        if (ybody) rotate_key_run(yv, i, x);
+        const int f = (x >> 1) & 3;
+        uint32_t* sb = SCAT + (i & 1) * 2 * N + r * N + 16 * x;  // this thread's slots only
 #pragma unroll
-      for (int r4 = 0; r4 < 4; r4++) {
-        const uint32_t ww[4] = {wv[r4].x, wv[r4].y, wv[r4].z, wv[r4].w};
-        const uint32_t yy[4] = {yv[r4].x, yv[r4].y, yv[r4].z, yv[r4].w};
-        uint4* ap = reinterpret_cast<uint4*>(accp + 4 * (r4 ^ f));
-        const uint4 a4 = *ap;
-        uint32_t ab[4] = {a4.x, a4.y, a4.z, a4.w};
-        uint32_t hh[4] = {0, 0, 0, 0};
-        if (kd == 0) {
-          const uint4 h4 = *reinterpret_cast<const uint4*>(sb + 4 * (r4 ^ f));
-          hh[0] = h4.x; hh[1] = h4.y; hh[2] = h4.z; hh[3] = h4.w;
-        }
+        for (int r4 = 0; r4 < 4; r4++) {
+          uint4* ap = reinterpret_cast<uint4*>(ACC + 16 * x + 4 * (r4 ^ f));
+          const uint4 a4 = *ap;
+          uint32_t ab[4] = {a4.x, a4.y, a4.z, a4.w};
+          uint4* hp = reinterpret_cast<uint4*>(sb + 4 * (r4 ^ f));
+          const uint4 h4 = *hp;
+          uint32_t pr[4];
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-          const int j = 4 * r4 + e;
-          ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v[j] * yy[e], q, qinv), q2);
-          uint32_t pr = redc_lazy((uint64_t)v[j] * ww[e], q, qinv);  // [0, 2q)
-          if (kd == 0) {
-            const uint32_t h = (MODE == MODE_COMPAT && r == 1) ? compat_residue1_ninv(P, hh[e]) : hh[e];
-            pr += h;  // [0, 3q)
+          for (int e = 0; e < 4; e++) {
+            const int j = 4 * r4 + e;
+            ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v[j] * u4e(yv[r4], e), q, qinv), q2);
+            pr[e] = redc_lazy((uint64_t)v[j] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 3q)
           }
-          v[j] = pr;
+          *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
+          *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);  // partial R_i, in place of the query-only term
         }
-        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
       }
+    } else if (i >= 1) {
+      // the query-only term of the next step (compat: residue 1 rebuilt as the crate does)
+      const int sres = MODE == MODE_CRT_FIXED ? r : 0;
+      const int sp = MODE == MODE_CRT_FIXED ? x : r * NTT_GT + x;
+      const int snthr = MODE == MODE_CRT_FIXED ? NTT_GT : 2 * NTT_GT;
+      uint32_t* sc2 = SCAT + ((i - 1) & 1) * 2 * N;
+      scatter_r(P, i - 1, Eg_at(sres), Ahat + sres * N, NR * N, sc2 + sres * N, sp, snthr, P.r[sres].q,
+                P.r[sres].qinv, MODE == MODE_COMPAT ? sc2 + N : nullptr);
     }
-    if (kd != 0) store16(PB + (r * 2 + kd - 1) * N, x, v);
     __syncthreads();
-    // [D] R_i = scatter + sum_k products, by groups (r,0)
-    if (kd == 0) {
+    // [D] the third digit's transform; R_i (group (r,0)), b accumulator (group (r,1))
+    if (kd < 2) {
+      uint4 k1[4], k2[4];
+      const size_t off1 = ((size_t)(i * ELL + 1) * 2 + r) * N + 16 * x;
+      const size_t off2 = ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x;
+      if (kd == 0) {
+        key_run(A.what + off1, k1);
+        key_run(A.what + off2, k2);
+      } else {
+        const size_t yoff = ybody ? (size_t)i * ELL * 2 * N : 0;
+        key_run(Y + off1 - yoff, k1);
+        key_run(Y + off2 - yoff, k2);
+        if (ybody) {
+          rotate_key_run(k1, i, x);
+          rotate_key_run(k2, i, x);
+        }
+      }
       const int f = (x >> 1) & 3;
-      const uint32_t* pb0 = PB + (r * 2 + 0) * N + 16 * x;
-      const uint32_t* pb1 = PB + (r * 2 + 1) * N + 16 * x;
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
-        const int o = 4 * (r4 ^ f);
-        const uint4 a4 = *reinterpret_cast<const uint4*>(pb0 + o);
-        const uint4 b4 = *reinterpret_cast<const uint4*>(pb1 + o);
-        const uint32_t aa[4] = {a4.x, a4.y, a4.z, a4.w}, bb[4] = {b4.x, b4.y, b4.z, b4.w};
+        const int o = 16 * x + 4 * (r4 ^ f);  // slots 16x + 4 r4 .. + 3 (swizzled chunk)
+        const uint4 a0 = *reinterpret_cast<const uint4*>(X0 + r * N + o);
+        const uint4 a1 = *reinterpret_cast<const uint4*>(X1 + r * N + o);
+        const uint4 ar = *reinterpret_cast<const uint4*>(RS + r * N + o);
+        if (kd == 0) {
+          const uint4 pa = *reinterpret_cast<const uint4*>(SCAT + (i & 1) * 2 * N + r * N + o);  // partial R_i
+          uint32_t outv[4];
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-          const int j = 4 * r4 + e;
-          uint32_t sum = v[j] + aa[e] + bb[e];  // < 7q < 2^31
-          sum = min(sum, sum - 4 * q);
-          sum = min(sum, sum - 2 * q);
-          vR[j] = min(sum, sum - q);
+          for (int e = 0; e < 4; e++) {
+            const uint32_t v1 = u4e(a1, e);
+            const uint32_t v2 = third_digit(C, u4e(ar, e), u4e(a0, e), v1);
+            uint32_t sum = u4e(pa, e) + redc_lazy((uint64_t)v1 * u4e(k1[r4], e), q, qinv) +
+                           redc_lazy((uint64_t)v2 * u4e(k2[r4], e), q, qinv);  // < 7q < 2^31
+            sum = min(sum, sum - 4 * q);
+            sum = min(sum, sum - 2 * q);
+            outv[e] = min(sum, sum - q);
+          }
+          // R_i (slots) for the next step
+          *reinterpret_cast<uint4*>(T + r * N + o) = make_uint4(outv[0], outv[1], outv[2], outv[3]);
+        } else {
+          uint4* ap = reinterpret_cast<uint4*>(ACC + o);
+          const uint4 a4 = *ap;
+          uint32_t ab[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+          for (int e = 0; e < 4; e++) {
+            const uint32_t v1 = u4e(a1, e);
+            const uint32_t v2 = third_digit(C, u4e(ar, e), u4e(a0, e), v1);
+            ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v1 * u4e(k1[r4], e), q, qinv), q2);
+            ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v2 * u4e(k2[r4], e), q, qinv), q2);
+          }
+          *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
         }
       }
     }
+    __syncthreads();
   }
 
-  // ---- outputs: a_hat = INTT(R_0) (inspiring2.rs:1027-1029),
-  //      b = b_poly + INTT(sum y_all * bold_t) (inspiring2.rs:1217-1221) ----
-  // (the b accumulators were last written before the final barrier)
+  // ---- outputs: a_hat = INTT(R_0) (inspiring2.rs:1027-1029) by each
+  //      residue's team, b = b_poly + INTT(sum y_all * bold_t)
+  //      (inspiring2.rs:1217-1221) by group (r,2) ----
   uint64_t* out = QDB ? reload_ptr(&D->out) : A.out + (size_t)qi * 4 * N;
-  if (kd == 0) {
-    ntt_inv_noscale(vR, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
+  if (kd < 2) {
+    uint32_t v[8];
+    const int s0 = 8 * team_t;
+    const uint4 lo = *reinterpret_cast<const uint4*>(T + r * N + swz(s0));
+    const uint4 hi = *reinterpret_cast<const uint4*>(T + r * N + swz(s0 + 4));
+    v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
+    v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
+    ntt_inv_noscale8(v, team_sc, inv_tw(C), q, team_t, 7 + r);
 #pragma unroll
-    for (int j = 0; j < 16; j++) out[r * N + x + 128 * j] = canon2(vR[j], q);
-  } else if (kd == 1) {
-    uint32_t b0[16], b1[16], b2[16];
-    load16(smem + L::ACC + (3 * r + 0) * N, x, b0);
-    load16(smem + L::ACC + (3 * r + 1) * N, x, b1);
-    load16(smem + L::ACC + (3 * r + 2) * N, x, b2);
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-      uint32_t s2 = b0[j] + b1[j] + b2[j];  // < 6q
-      s2 = min(s2, s2 - 4 * q);
-      s2 = min(s2, s2 - 2 * q);
-      b0[j] = min(s2, s2 - q);
-    }
-    ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(P.r[r]), q, x, 1 + g);
+    for (int j = 0; j < 8; j++) out[r * N + team_t + 256 * j] = canon2(v[j], q);
+  } else {
+    uint32_t b0[16];
+    load16(ACC, x, b0);  // [0, 2q)
+    ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);
 #pragma unroll
     for (int j = 0; j < 16; j++) b0[j] = canon2(b0[j], q);
     if (x < gamma) b0[0] = add_mod(b0[0], bpoly[r * 16 + x], q);
