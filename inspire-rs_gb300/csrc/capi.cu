@@ -137,6 +137,8 @@ int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all,
     CUDA_TRY(y_all ? launch_client_from_yall(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream)
                    : launch_client_from_ybody(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(),
                                               body_form ? 1 : gamma - 1, c->stream));
+    // the Respond kernel multiplies the third key by R_{i+1} instead of NTT(d2)
+    CUDA_TRY(launch_fold_third_digit(c->P, m->as<uint32_t>(), body_form ? 1 : gamma - 1, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
   }
   int slot = -1;
@@ -214,7 +216,7 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
       a.nq = (int)n;
       a.yhat_table = c->client_table.as<const uint32_t*>();
       a.nclients = (int)c->client_ptrs.size();
-      a.what = c->what.as<uint32_t>();
+      a.what = c->what3.as<uint32_t>();
       a.qdesc = c->d_desc.as<QueryDesc>();
       a.stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
       CUDA_TRY(launch_respond(a, true, c->stream));
@@ -256,7 +258,7 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
   a.nshards = db->nshards;
   a.E = db->E.as<uint32_t>();
   a.H = db->H.as<uint16_t>();
-  a.what = c->what.as<uint32_t>();
+  a.what = c->what3.as<uint32_t>();
   a.out = c->d_out.as<uint64_t>();
   a.status = c->d_status.as<int>();
   CUDA_TRY(launch_respond(a, seeded, c->stream));
@@ -623,6 +625,9 @@ int inspire_crs_load(inspire_ctx* c, const uint8_t w_seed[32], uint32_t num_colu
   CUDA_TRY(cudaMemcpy(c->wmask.p, wm.data(), wm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
   CUDA_TRY(c->what.ensure(sizeof(uint32_t) * (size_t)std::max(1, (gamma - 1) * ELL) * 2 * N));
   CUDA_TRY(launch_crs_what(c->P, c->wmask.as<uint32_t>(), c->what.as<uint32_t>(), c->stream));
+  CUDA_TRY(c->what3.ensure(c->what.bytes));
+  CUDA_TRY(cudaMemcpyAsync(c->what3.p, c->what.p, c->what.bytes, cudaMemcpyDeviceToDevice, c->stream));
+  CUDA_TRY(launch_fold_third_digit(c->P, c->what3.as<uint32_t>(), gamma - 1, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   // key tables of registered clients were built for the previous gamma
   for (size_t i = 0; i < c->clients.size(); i++) release_keys(c, (int32_t)i);
@@ -979,7 +984,7 @@ int inspire_respond_seeded_batch_device_grid(inspire_ctx* c, const inspire_db* d
   a.nshards = db->nshards;
   a.E = db->E.as<uint32_t>();
   a.H = db->H.as<uint16_t>();
-  a.what = c->what.as<uint32_t>();
+  a.what = c->what3.as<uint32_t>();
   a.out = d_out_ct;
   a.status = d_status;
   CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream, (int)max_ctas));

@@ -89,7 +89,8 @@ struct inspire_ctx {
   int gamma = 0;
   uint8_t w_seed[32] = {};
   uint64_t crs_a_count = 0;  // crs_a_vectors in the loaded crs.json
-  ighost::DevMem what;
+  ighost::DevMem what;   // rotated w_mask table (setup's precomputation reads it as is)
+  ighost::DevMem what3;  // the same with the third gadget digit folded in (the Respond kernel's)
   ighost::DevMem wmask;  // [ELL][2][N] w_mask residues (client key generation)
   // tree packing: the CRS's Galois key table, the tree's work area and output
   bool has_galois = false;
@@ -106,7 +107,7 @@ struct inspire_ctx {
   std::vector<int32_t> h_status;
 
   inspire_ctx() {
-    for (ighost::DevMem* m : {&tables, &what, &wmask, &galois, &tree_work, &d_tree_out, &client_table, &d_shard,
+    for (ighost::DevMem* m : {&tables, &what, &what3, &wmask, &galois, &tree_work, &d_tree_out, &client_table, &d_shard,
                               &d_seeds, &d_arows, &d_brows, &d_client, &d_out, &d_cols, &d_status, &d_keys, &d_desc})
       m->ledger = ledger;
   }

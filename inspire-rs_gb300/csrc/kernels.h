@@ -50,12 +50,12 @@ struct RespondArgs {
   const int32_t* client;         // [nq] client id
   // [nclients] -> client key table: [(gamma-1)][ELL][2][N] rotated keys,
   // or, when the pointer's bit 0 is set (gamma = 16 only), the body table
-  // [ELL][2][N] whose rotations the kernel forms
+  // [ELL][2][N] whose rotations the kernel forms; third digit folded in
   const uint32_t* const* yhat_table;
   int nclients, nshards;
   const uint32_t* E;             // [nshards][2][ELL][gamma][N] contracted database
   const uint16_t* H;             // [nshards][gamma][N] raw 16-bit columns
-  const uint32_t* what;          // [(gamma-1)][ELL][2][N] rotated w_mask (CRS)
+  const uint32_t* what;          // [(gamma-1)][ELL][2][N] rotated w_mask (CRS), third digit folded in
   uint64_t* out;                 // [nq][2][2][N] response (a_hat, b) residues
   int* status;                   // [nq]
   // Serving loop: per-query descriptors in device memory (override shard,
@@ -187,6 +187,10 @@ cudaError_t launch_encode_E(const DevParams& P, const uint16_t* H, int nshards, 
                             cudaStream_t st);
 cudaError_t launch_crs_what(const DevParams& P, const uint32_t* wmask, uint32_t* what,
                             cudaStream_t st);
+// Fold the third gadget digit into ngroups key triples [g][k<3][2][N] in
+// place (k0 - z^-2 k2, k1 - z^-1 k2, n z^-2 k2): the Respond kernel then
+// multiplies the third key by R_{i+1} instead of by NTT(d2).
+cudaError_t launch_fold_third_digit(const DevParams& P, uint32_t* tbl, int ngroups, cudaStream_t st);
 // The first nrot rotations y_all[0..nrot) of the client key table (nrot =
 // gamma - 1: the full table; 1: the body table the Respond kernel rotates).
 cudaError_t launch_client_from_ybody(const DevParams& P, const uint64_t* ybody, uint32_t* yhat, int nrot,

@@ -185,12 +185,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
 // residue-0 value as the crate's apply_automorphism_ntt does.
 __device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint32_t* __restrict__ Eg, const uint32_t* Ag,
                                           int astride, uint32_t* dst, int p, int nthr, uint32_t q, uint32_t qinv,
-                                          uint32_t* dst1 = nullptr) {
+                                          uint32_t* dst1 = nullptr, int u0 = 0, int u1 = N) {
   const int gamma = P.gamma;
   const uint32_t mi = (uint32_t)(gamma - i) & (uint32_t)(gamma - 1);
   const uint32_t hi = (1u + (uint32_t)(2 * N / gamma) * mi) & (2 * N - 1);
 #pragma unroll 4
-  for (int u = p; u < N; u += nthr) {
+  for (int u = u0 + p; u < u1; u += nthr) {
     const uint32_t e = 2 * brv11(u) + 1;
     const uint32_t k = (e * mi) & (uint32_t)(gamma - 1);
     const uint32_t* ek = Eg + (size_t)k * N + u;
@@ -248,28 +248,16 @@ struct Smem {
   static constexpr int AHAT = 0;                    // [ELL][NR][N] row transforms
   static constexpr int SC = AHAT + ELL * NR * N;    // [RG][NTT_SCRATCH] per-group exchange scratch
   static constexpr int T = SC + RG * NTT_SCRATCH;   // [2][N] R_{i+1} (slots) -> its inverse (coefficients) -> digits d0, d1
-  static constexpr int RS = T + 2 * N;              // [2][N] copy of R_{i+1} (slots), for the third digit's transform
-  static constexpr int X0 = RS + 2 * N;             // [2][N] NTT(d0), lazily reduced
-  static constexpr int X1 = X0 + 2 * N;             // [2][N] NTT(d1), lazily reduced
-  static constexpr int SCAT = X1 + 2 * N;           // [2 steps][2][N] query-only term of R_i (slots)
+  static constexpr int RS = T + 2 * N;              // [2][N] copy of R_{i+1} (slots)
+  static constexpr int PB1 = RS + 2 * N;            // [2][N] NTT(d1) w'[i][1]
+  static constexpr int PB2 = PB1 + 2 * N;           // [2][N] R_{i+1} w'[i][2]
+  static constexpr int SCAT = PB2 + 2 * N;          // [2 steps][2][N] query-only term of R_i (slots), then partial R_i
   static constexpr int ACC = SCAT + 4 * N;          // [2][N] b accumulators
   // T..ACC+2N (14N words) also hold the query's raw b rows (u64, 12N words)
-  // until the b side; T..X0 (6N words) the unseeded rows' a parts
+  // until the b side; T..PB1 (6N words) the unseeded rows' a parts
   static constexpr int MISC = ACC + 2 * N;          // bpoly[32], ws[3][20], staged seeds (96 B), mbarrier
   static constexpr int TOTAL = MISC + 128;
 };
-
-// NTT(d2) of one slot from the slot's R_{i+1} (times n^-1, canonical) and the
-// transforms of the two lower digits (any u32): the composite coefficient is
-// c = d0 + z d1 + z^2 d2 (gadget_decompose, rgsw/external_product.rs:16-37)
-// and c = INTT(R_{i+1}) mod q_r, so NTT(d2) = z^-2 (n R - NTT(d0) - z NTT(d1))
-// mod q_r, exactly.
-__device__ __forceinline__ uint32_t third_digit(const ResidueConsts& C, uint32_t rs, uint32_t v0, uint32_t v1) {
-  const uint32_t a = mul_shoup(rs, C.d2_nz2, C.d2_nz2_p, C.q);
-  const uint32_t b = mul_shoup(v0, C.d2_z2, C.d2_z2_p, C.q);
-  const uint32_t c = mul_shoup(v1, C.d2_z1, C.d2_z1_p, C.q);
-  return sub_mod(sub_mod(a, b, C.q), c, C.q);
-}
 
 // Load a 16-slot run of a key slice (uint4 x 4; y: rotated from the body
 // table when `ybody`).
@@ -283,18 +271,23 @@ __device__ __forceinline__ uint32_t u4e(const uint4& v, int e) { return e == 0 ?
 
 // One query (index qi) by the whole CTA; every return is uniform over the CTA.
 //
-// Per recursion step i (gamma-2 .. 0), residue r's three groups:
+// The recursion step of packing_offline (inspiring2.rs:984-1008) with
+// packing_online interleaved needs, per residue, sum_k NTT(d_k) w[i][k] for
+// R_i and sum_k NTT(d_k) y[i][k] for b, over the three gadget digits d_k of
+// INTT(R_{i+1}).  The key tables here have the third digit folded in
+// (fold_third_digit_kernel, setup.cu): with keys k' the sums are
+// k'0 NTT(d0) + k'1 NTT(d1) + k'2 R_{i+1}, so d2 is never formed and only two
+// digit transforms run per residue and step.  Per step i (gamma-2 .. 0),
+// residue r's three groups:
 //  [A] (r,0)+(r,1) as one 256-thread team: inverse NTT of R_{i+1} (T[r],
-//      copied to RS[r]); (r,2) idle;
-//  [B] all threads: CRT compose + gadget digits d0, d1 into T (d2 is never
-//      formed: its transform is derived in [D]);
-//  [C] (r,0): NTT(d0) -> X0, partial R_i = SCAT + NTT(d0) w[i][0] (held in
-//      registers), b accumulator += NTT(d0) y[i][0]; (r,1): NTT(d1) -> X1;
-//      (r,2): the query-only term of the NEXT step, R_{i-1}, into the other
-//      SCAT buffer (off the critical path);
-//  [D] (r,0): NTT(d2) from RS, X0, X1; R_i += NTT(d1) w[i][1] + NTT(d2)
-//      w[i][2] -> T[r] (slots) for the next step; (r,1): the same NTT(d2),
-//      b accumulator += NTT(d1) y[i][1] + NTT(d2) y[i][2].
+//      copied to RS[r]); (r,2): first half of the next step's query-only
+//      term R_{i-1} (into the other SCAT buffer);
+//  [B] all threads: CRT compose + digits d0, d1 into T;
+//  [C] (r,0): NTT(d0); SCAT[r] += NTT(d0) w'0 (in place), b += NTT(d0) y'0;
+//      (r,1): NTT(d1); PB1 = NTT(d1) w'1;
+//      (r,2): PB2 = R_{i+1} w'2; second half of R_{i-1};
+//  [D] (r,0): R_i = SCAT[r] + PB1 + PB2 -> T[r] (slots) for the next step;
+//      (r,1): b += NTT(d1) y'1 + R_{i+1} y'2.
 template <int MODE, bool SEEDED, bool QDB>
 __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
@@ -304,8 +297,8 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   uint32_t* SC = smem + L::SC;
   uint32_t* T = smem + L::T;
   uint32_t* RS = smem + L::RS;
-  uint32_t* X0 = smem + L::X0;
-  uint32_t* X1 = smem + L::X1;
+  uint32_t* PB1 = smem + L::PB1;
+  uint32_t* PB2 = smem + L::PB2;
   uint32_t* SCAT = smem + L::SCAT;
   uint32_t* bpoly = smem + L::MISC;
   int* wsb = (int*)(smem + L::MISC + 32);
@@ -380,7 +373,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     const int t = tid >> 8, lt = tid & 255;
     uint64_t* cand = reinterpret_cast<uint64_t*>(SC) + t * N;  // 3 x 16 KiB within SC
     // serving loop: in place of the row's transforms (T..ACC hold the
-    // staged rows); otherwise within T..X0
+    // staged rows); otherwise within T..PB1
     uint32_t* a0 = QDB ? Ahat + t * NR * N : T + t * 2 * N;
     uint32_t* a1 = a0 + N;
     if (SEEDED) {
@@ -449,13 +442,27 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
       scatter_r(P, gamma - 2, Eg_at(sres), Ag, NR * N, sc2 + sres * N, sp, snthr, sq, sqinv,
                 MODE == MODE_COMPAT ? sc2 + N : nullptr);
     }
-    for (int j = tid; j < 2 * N; j += RBLOCK) smem[L::ACC + j] = 0;
+    for (int j = tid; j < 2 * N; j += RBLOCK) {
+      smem[L::ACC + j] = 0;
+      SC[(3 * (j >> LOGN) + 2) * NTT_SCRATCH + (j & (N - 1))] = 0;  // group (r,1)'s accumulator
+    }
   }
   __syncthreads();
 
   const int team_t = tid - 384 * r;  // thread of residue r's (r,0)+(r,1) team, valid for kd < 2
   uint32_t* team_sc = SC + 3 * r * NTT_SCRATCH;  // the team's exchange scratch (two groups' worth)
+  // the next step's query-only term by the (r,2) groups, in two halves
+  auto scatter_next = [&](int i, int u0, int u1) {
+    const int sres = MODE == MODE_CRT_FIXED ? r : 0;
+    const int sp = MODE == MODE_CRT_FIXED ? x : r * NTT_GT + x;
+    const int snthr = MODE == MODE_CRT_FIXED ? NTT_GT : 2 * NTT_GT;
+    uint32_t* sc2 = SCAT + ((i - 1) & 1) * 2 * N;
+    scatter_r(P, i - 1, Eg_at(sres), Ahat + sres * N, NR * N, sc2 + sres * N, sp, snthr, P.r[sres].q, P.r[sres].qinv,
+              MODE == MODE_COMPAT ? sc2 + N : nullptr, u0, u1);
+  };
+  const int f = (x >> 1) & 3;  // chunk swizzle of this thread's 16-slot run (store16 / load16)
   for (int i = gamma - 2; i >= 0; i--) {
+    const size_t yoff = ybody ? (size_t)i * ELL * 2 * N : 0;  // body tables: the key slices of i = 0, rotated
     // [A] inverse NTT of R_{i+1} by residue r's team; RS keeps R_{i+1}
     if (kd < 2) {
       uint32_t v[8];
@@ -469,10 +476,12 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
       ntt_inv_noscale8(v, team_sc, inv_tw(C), q, team_t, 7 + r);
 #pragma unroll
       for (int j = 0; j < 8; j++) T[r * N + team_t + 256 * j] = canon2(v[j], q);
+    } else if (i >= 1) {
+      scatter_next(i, 0, N / 2);
     }
     __syncthreads();
     // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37):
-    //     digits 0 and 1 only
+    //     digits 0 and 1 (the third is folded into the keys)
     for (int j = tid; j < N; j += RBLOCK) {
       const uint64_t c = crt_compose(P, T[j], T[N + j]);
       T[j] = (uint32_t)c & 0xFFFFFu;
@@ -480,102 +489,84 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     }
     __syncthreads();
     // [C]
+    uint4 k2[4];  // group (r,1): the b side's third key slice, in flight across the barrier
     if (kd < 2) {
-      const size_t off0 = ((size_t)(i * ELL + 0) * 2 + r) * N + 16 * x;
+      const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
       uint4 wv[4], yv[4];
-      if (kd == 0) {  // this step's key slices, fetched before the transform
-        key_run(A.what + off0, wv);
-        key_run(Y + (ybody ? off0 - (size_t)i * ELL * 2 * N : off0), yv);
-      }
+      key_run(A.what + off, wv);  // this step's key slices, fetched before the transform
+      key_run(Y + off - yoff, yv);
       uint32_t v[16];
 #pragma unroll
       for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
       ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);  // slots 16x.., [0, 14q)
-      store16((kd == 0 ? X0 : X1) + r * N, x, v);
-      if (kd == 0) {
-        if (ybody) rotate_key_run(yv, i, x);
-        const int f = (x >> 1) & 3;
-        uint32_t* sb = SCAT + (i & 1) * 2 * N + r * N + 16 * x;  // this thread's slots only
-#pragma unroll
-        for (int r4 = 0; r4 < 4; r4++) {
-          uint4* ap = reinterpret_cast<uint4*>(ACC + 16 * x + 4 * (r4 ^ f));
-          const uint4 a4 = *ap;
-          uint32_t ab[4] = {a4.x, a4.y, a4.z, a4.w};
-          uint4* hp = reinterpret_cast<uint4*>(sb + 4 * (r4 ^ f));
-          const uint4 h4 = *hp;
-          uint32_t pr[4];
-#pragma unroll
-          for (int e = 0; e < 4; e++) {
-            const int j = 4 * r4 + e;
-            ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v[j] * u4e(yv[r4], e), q, qinv), q2);
-            pr[e] = redc_lazy((uint64_t)v[j] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 3q)
-          }
-          *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
-          *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);  // partial R_i, in place of the query-only term
-        }
-      }
-    } else if (i >= 1) {
-      // the query-only term of the next step (compat: residue 1 rebuilt as the crate does)
-      const int sres = MODE == MODE_CRT_FIXED ? r : 0;
-      const int sp = MODE == MODE_CRT_FIXED ? x : r * NTT_GT + x;
-      const int snthr = MODE == MODE_CRT_FIXED ? NTT_GT : 2 * NTT_GT;
-      uint32_t* sc2 = SCAT + ((i - 1) & 1) * 2 * N;
-      scatter_r(P, i - 1, Eg_at(sres), Ahat + sres * N, NR * N, sc2 + sres * N, sp, snthr, P.r[sres].q,
-                P.r[sres].qinv, MODE == MODE_COMPAT ? sc2 + N : nullptr);
-    }
-    __syncthreads();
-    // [D] the third digit's transform; R_i (group (r,0)), b accumulator (group (r,1))
-    if (kd < 2) {
-      uint4 k1[4], k2[4];
-      const size_t off1 = ((size_t)(i * ELL + 1) * 2 + r) * N + 16 * x;
-      const size_t off2 = ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x;
-      if (kd == 0) {
-        key_run(A.what + off1, k1);
-        key_run(A.what + off2, k2);
-      } else {
-        const size_t yoff = ybody ? (size_t)i * ELL * 2 * N : 0;
-        key_run(Y + off1 - yoff, k1);
-        key_run(Y + off2 - yoff, k2);
-        if (ybody) {
-          rotate_key_run(k1, i, x);
-          rotate_key_run(k2, i, x);
-        }
-      }
-      const int f = (x >> 1) & 3;
+      if (ybody) rotate_key_run(yv, i, x);
+      // group (r,0): the b accumulator ACC and the partial R_i in place of the
+      // query-only term; group (r,1): its own b accumulator (the scratch of
+      // group (r,2), free during the recursion) and PB1
+      uint32_t* accb = kd == 0 ? ACC : SC + (3 * r + 2) * NTT_SCRATCH;
+      uint32_t* pdst = kd == 0 ? SCAT + (i & 1) * 2 * N + r * N : PB1 + r * N;
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
-        const int o = 16 * x + 4 * (r4 ^ f);  // slots 16x + 4 r4 .. + 3 (swizzled chunk)
-        const uint4 a0 = *reinterpret_cast<const uint4*>(X0 + r * N + o);
-        const uint4 a1 = *reinterpret_cast<const uint4*>(X1 + r * N + o);
-        const uint4 ar = *reinterpret_cast<const uint4*>(RS + r * N + o);
-        if (kd == 0) {
-          const uint4 pa = *reinterpret_cast<const uint4*>(SCAT + (i & 1) * 2 * N + r * N + o);  // partial R_i
-          uint32_t outv[4];
+        const int o = 16 * x + 4 * (r4 ^ f);
+        uint4* ap = reinterpret_cast<uint4*>(accb + o);
+        const uint4 a4 = *ap;
+        uint4* hp = reinterpret_cast<uint4*>(pdst + o);
+        const uint4 h4 = kd == 0 ? *hp : make_uint4(0, 0, 0, 0);
+        uint32_t ab[4], pr[4];
 #pragma unroll
-          for (int e = 0; e < 4; e++) {
-            const uint32_t v1 = u4e(a1, e);
-            const uint32_t v2 = third_digit(C, u4e(ar, e), u4e(a0, e), v1);
-            uint32_t sum = u4e(pa, e) + redc_lazy((uint64_t)v1 * u4e(k1[r4], e), q, qinv) +
-                           redc_lazy((uint64_t)v2 * u4e(k2[r4], e), q, qinv);  // < 7q < 2^31
-            sum = min(sum, sum - 4 * q);
-            sum = min(sum, sum - 2 * q);
-            outv[e] = min(sum, sum - q);
-          }
-          // R_i (slots) for the next step
-          *reinterpret_cast<uint4*>(T + r * N + o) = make_uint4(outv[0], outv[1], outv[2], outv[3]);
-        } else {
-          uint4* ap = reinterpret_cast<uint4*>(ACC + o);
-          const uint4 a4 = *ap;
-          uint32_t ab[4] = {a4.x, a4.y, a4.z, a4.w};
-#pragma unroll
-          for (int e = 0; e < 4; e++) {
-            const uint32_t v1 = u4e(a1, e);
-            const uint32_t v2 = third_digit(C, u4e(ar, e), u4e(a0, e), v1);
-            ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v1 * u4e(k1[r4], e), q, qinv), q2);
-            ab[e] = acc_2q(ab[e], redc_lazy((uint64_t)v2 * u4e(k2[r4], e), q, qinv), q2);
-          }
-          *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
+        for (int e = 0; e < 4; e++) {
+          const int j = 4 * r4 + e;
+          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)v[j] * u4e(yv[r4], e), q, qinv), q2);
+          pr[e] = redc_lazy((uint64_t)v[j] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 3q)
         }
+        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
+        *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+      }
+      if (kd == 1) key_run(Y + ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x - yoff, k2);
+    } else {
+      const size_t off2 = ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x;
+      uint4 wv[4];
+      key_run(A.what + off2, wv);
+      uint32_t rs[16], pr[16];
+      load16(RS + r * N, x, rs);
+#pragma unroll
+      for (int j = 0; j < 16; j++) pr[j] = redc_lazy((uint64_t)rs[j] * u4e(wv[j >> 2], j & 3), q, qinv);
+      store16(PB2 + r * N, x, pr);
+      if (i >= 1) scatter_next(i, N / 2, N);
+    }
+    __syncthreads();
+    // [D] R_i (group (r,0)); the b accumulator's other two products (group (r,1))
+    if (kd == 0) {
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        const int o = r * N + 16 * x + 4 * (r4 ^ f);
+        const uint4 pa = *reinterpret_cast<const uint4*>(SCAT + (i & 1) * 2 * N + o);
+        const uint4 p1 = *reinterpret_cast<const uint4*>(PB1 + o);
+        const uint4 p2 = *reinterpret_cast<const uint4*>(PB2 + o);
+        uint32_t outv[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          uint32_t sum = u4e(pa, e) + u4e(p1, e) + u4e(p2, e);  // < 7q < 2^31
+          sum = min(sum, sum - 4 * q);
+          sum = min(sum, sum - 2 * q);
+          outv[e] = min(sum, sum - q);
+        }
+        *reinterpret_cast<uint4*>(T + o) = make_uint4(outv[0], outv[1], outv[2], outv[3]);  // R_i for the next step
+      }
+    } else if (kd == 1) {
+      if (ybody) rotate_key_run(k2, i, x);
+      uint32_t* accb = SC + (3 * r + 2) * NTT_SCRATCH;
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        const int o = 16 * x + 4 * (r4 ^ f);
+        const uint4 rr = *reinterpret_cast<const uint4*>(RS + r * N + o);
+        uint4* ap = reinterpret_cast<uint4*>(accb + o);
+        const uint4 a4 = *ap;
+        uint32_t ab[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)u4e(rr, e) * u4e(k2[r4], e), q, qinv), q2);
+        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
       }
     }
     __syncthreads();
@@ -596,9 +587,12 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
 #pragma unroll
     for (int j = 0; j < 8; j++) out[r * N + team_t + 256 * j] = canon2(v[j], q);
   } else {
-    uint32_t b0[16];
-    load16(ACC, x, b0);  // [0, 2q)
-    ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);
+    uint32_t b0[16], b1[16];
+    load16(ACC, x, b0);                    // [0, 2q)
+    load16(SC + g * NTT_SCRATCH, x, b1);  // group (r,1)'s accumulator, in this group's scratch
+#pragma unroll
+    for (int j = 0; j < 16; j++) b0[j] = acc_2q(b0[j], b1[j], q2);
+    ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);  // first exchange after a group barrier
 #pragma unroll
     for (int j = 0; j < 16; j++) b0[j] = canon2(b0[j], q);
     if (x < gamma) b0[0] = add_mod(b0[0], bpoly[r * 16 + x], q);

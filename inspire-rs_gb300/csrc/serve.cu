@@ -119,7 +119,7 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   a.nq = n;
   a.yhat_table = ctx->client_table.as<const uint32_t*>();
   a.nclients = (int)ctx->client_ptrs.size();
-  a.what = ctx->what.as<uint32_t>();
+  a.what = ctx->what3.as<uint32_t>();
   a.qdesc = s.ddesc.as<QueryDesc>();
   a.stage_wait_iters = cfg.stage_wait_iters;
   CUDA_TRY(launch_respond(a, true, s.st));

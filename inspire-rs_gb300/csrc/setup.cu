@@ -1,6 +1,8 @@
 // setup.cu -- setup-time GPU kernels: resident database, CRS key table and
 // per-client key tables.  All outputs stay in HBM for the lifetime of their
 // handles; Respond then reads them without further preprocessing.
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace ig {
@@ -165,7 +167,39 @@ __global__ void __launch_bounds__(BLOCK) client_yall_kernel(const DevParams P, c
     yhat[((size_t)p * 2 + g) * N + 16 * x + rr] = mul_shoup(v[rr], C.ninv_mont, C.ninv_mont_p, C.q);
 }
 
+// Key tables with the third gadget digit folded in.  In the NTT domain of
+// residue r, the digits of the composite coefficient c = INTT(R) satisfy
+// NTT(d0) + z NTT(d1) + z^2 NTT(d2) = R (mod q_r), so for any key triple
+// (k0, k1, k2):  k0 NTT(d0) + k1 NTT(d1) + k2 NTT(d2)
+//   = (k0 - z^-2 k2) NTT(d0) + (k1 - z^-1 k2) NTT(d1) + (z^-2 k2) R.
+// With R kept as n^-1 R (the Respond kernel's R_{i+1}), the third key is
+// n z^-2 k2.  `tbl` holds ngroups triples [g][k<3][2][N] (any constant
+// scaling, applied alike to the three keys), rewritten in place.
+__global__ void __launch_bounds__(BLOCK) fold_third_digit_kernel(const DevParams P, uint32_t* __restrict__ tbl,
+                                                                 int ngroups) {
+  const size_t per = (size_t)2 * N;
+  const size_t total = (size_t)ngroups * per;
+  for (size_t idx = (size_t)blockIdx.x * BLOCK + threadIdx.x; idx < total; idx += (size_t)gridDim.x * BLOCK) {
+    const size_t g = idx / per, rs = idx - g * per;
+    const int r = (int)(rs >> LOGN);
+    const ResidueConsts& C = P.r[r];
+    uint32_t* t = tbl + g * 3 * per + rs;
+    const uint32_t k0 = t[0], k1 = t[per], k2 = t[2 * per];
+    t[0] = sub_mod(k0, mul_shoup(k2, C.d2_z2, C.d2_z2_p, C.q), C.q);
+    t[per] = sub_mod(k1, mul_shoup(k2, C.d2_z1, C.d2_z1_p, C.q), C.q);
+    t[2 * per] = mul_shoup(k2, C.d2_nz2, C.d2_nz2_p, C.q);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_fold_third_digit(const DevParams& P, uint32_t* tbl, int ngroups, cudaStream_t st) {
+  if (ngroups <= 0) return cudaSuccess;
+  const size_t total = (size_t)ngroups * 2 * N;
+  const unsigned blocks = (unsigned)std::min<size_t>((total + BLOCK - 1) / BLOCK, 4096);
+  fold_third_digit_kernel<<<blocks, BLOCK, 0, st>>>(P, tbl, ngroups);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_columns_from_raw(const uint8_t* raw, uint64_t n_entries, int entry_size, int gamma,
                                     int nshards, uint16_t* H, cudaStream_t st) {
