@@ -96,6 +96,17 @@ int inspire_ctx_set_device_budget(inspire_ctx *ctx, uint64_t bytes);
 /* Bytes accounted now and the budget (0: none). */
 int inspire_ctx_device_memory(inspire_ctx *ctx, uint64_t *used, uint64_t *budget);
 
+/* Respond launches of at most `max_queries` queries (batch calls, device
+ * batches, serving-loop batches) run each query on a cluster of two CTAs, one
+ * per CRT residue, which halves a lone query's latency; larger launches use
+ * one CTA per query, which needs half the SMs per query.  Both give the same
+ * responses bit for bit.  Default: half the device's SM count (every query of
+ * the launch then has its two SMs); 0 turns the cluster kernel off.  The
+ * capped-grid call (inspire_respond_seeded_batch_device_grid with max_ctas)
+ * always uses one CTA per query. */
+int inspire_ctx_set_pair_threshold(inspire_ctx *ctx, uint32_t max_queries);
+uint32_t inspire_ctx_pair_threshold(const inspire_ctx *ctx);
+
 /* Load the InspiRING part of ServerCrs (src/pir/setup.rs:52-87): the shared
  * seed `inspiring_w_seed` and `inspiring_num_columns` (gamma).  Builds the
  * rotated w_mask table of OfflinePackingKeys::generate

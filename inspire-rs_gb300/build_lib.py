@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libinspire_gpu.so")
-SOURCES = ["respond.cu", "nopacking.cu", "setup.cu", "ops.cu", "capi.cu", "serve.cu", "dbio.cu", "wire.cu", "client.cu", "tree.cu", "precomp.cu", "http.cu"]
+SOURCES = ["respond.cu", "respond_pair.cu", "nopacking.cu", "setup.cu", "ops.cu", "capi.cu", "serve.cu", "dbio.cu", "wire.cu", "client.cu", "tree.cu", "precomp.cu", "http.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

@@ -177,6 +177,9 @@ void release_keys(inspire_ctx* c, int32_t id) {
 // (ELL contiguous seeds, query pitch `seed_stride` bytes).
 int finish_status(inspire_ctx* c, uint32_t n, const char* what);
 
+// Batches up to this size stage their inputs through page-locked memory.
+constexpr uint32_t STAGE_PINNED_MAX = 64;
+
 int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
               size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
               const int32_t* client_ids, uint64_t* out_ct) {
@@ -194,22 +197,26 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
                                 : nullptr;
     const uint8_t* d_outp = d_rows ? mapped_range(out_ct, out_span) : nullptr;
     if (d_rows && d_outp) {
-      CUDA_TRY(c->d_status.ensure(sizeof(int32_t) * n));
+      // descriptors and status words in page-locked memory: the descriptors
+      // go over by DMA, the kernel writes each status word in place
       CUDA_TRY(c->d_desc.ensure(sizeof(QueryDesc) * n));
-      c->h_desc.resize(n);
+      CUDA_TRY(c->h_desc.ensure(sizeof(QueryDesc) * n));
+      CUDA_TRY(c->h_qstatus.ensure(sizeof(int32_t) * n));
+      QueryDesc* hd = c->h_desc.host<QueryDesc>();
+      int32_t* hs = c->h_qstatus.host<int32_t>();
       const DbView view{db->E.as<uint32_t>(), db->H.as<uint16_t>(), db->nshards, 0};
       for (uint32_t i = 0; i < n; i++) {
-        QueryDesc& d = c->h_desc[i];
+        QueryDesc& d = hd[i];
         memcpy(d.seeds, seeds + i * seed_stride, sizeof(d.seeds));
         d.brows = reinterpret_cast<const uint64_t*>(d_rows + i * row_bytes);
         d.out = const_cast<uint64_t*>(reinterpret_cast<const uint64_t*>(d_outp)) + (size_t)i * 2 * pw;
-        d.status = c->d_status.as<int32_t>() + i;
+        d.status = c->h_qstatus.dev<int32_t>() + i;
         d.db = view;
         d.shard = shard_ids[i];
         d.client = client_ids[i];
+        hs[i] = -1;
       }
-      CUDA_TRY(cudaMemcpyAsync(c->d_desc.p, c->h_desc.data(), sizeof(QueryDesc) * n, cudaMemcpyHostToDevice,
-                               c->stream));
+      CUDA_TRY(cudaMemcpyAsync(c->d_desc.p, hd, sizeof(QueryDesc) * n, cudaMemcpyHostToDevice, c->stream));
       if (int rc = sync_client_table(c)) return rc;
       RespondArgs a{};
       a.P = c->P;
@@ -219,29 +226,57 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
       a.what = c->what3.as<uint32_t>();
       a.qdesc = c->d_desc.as<QueryDesc>();
       a.stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
-      CUDA_TRY(launch_respond(a, true, c->stream));
-      return finish_status(c, n, "respond");
+      CUDA_TRY(launch_respond(a, true, c->stream, 0, c->pair_max));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+      for (uint32_t i = 0; i < n; i++)
+        if (hs[i] != 0)
+          return fail(INSPIRE_ERR_DEVICE_STATUS,
+                      "respond kernel status " + std::to_string(hs[i]) + " for query " + std::to_string(i));
+      return INSPIRE_OK;
     }
   }
   CUDA_TRY(c->d_shard.ensure(sizeof(uint32_t) * n));
   CUDA_TRY(c->d_client.ensure(sizeof(int32_t) * n));
   CUDA_TRY(c->d_brows.ensure(sizeof(uint64_t) * n * ELL * pw));
   CUDA_TRY(c->d_out.ensure(sizeof(uint64_t) * n * 2 * pw));
-  CUDA_TRY(c->d_status.ensure(sizeof(int32_t) * n));
-  CUDA_TRY(cudaMemcpyAsync(c->d_shard.p, shard_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(c->d_client.p, client_ids, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
-  // b rows ELL..2ELL-1 of each query: one strided copy
-  CUDA_TRY(cudaMemcpy2DAsync(c->d_brows.p, sizeof(uint64_t) * ELL * pw, b_rows, sizeof(uint64_t) * stride_polys * pw,
-                             sizeof(uint64_t) * ELL * pw, n, cudaMemcpyHostToDevice, c->stream));
   const bool seeded = seeds != nullptr;
-  if (seeded) {
-    CUDA_TRY(c->d_seeds.ensure((size_t)32 * ELL * n));
-    CUDA_TRY(cudaMemcpy2DAsync(c->d_seeds.p, (size_t)32 * ELL, seeds, seed_stride, (size_t)32 * ELL, n,
-                               cudaMemcpyHostToDevice, c->stream));
+  const size_t rows_b = sizeof(uint64_t) * ELL * pw;  // rows ELL..2ELL-1 of one query, b (or a) polys
+  if (seeded) CUDA_TRY(c->d_seeds.ensure((size_t)32 * ELL * n));
+  else CUDA_TRY(c->d_arows.ensure(rows_b * n));
+  CUDA_TRY(c->h_qstatus.ensure(sizeof(int32_t) * n));
+  if (n <= STAGE_PINNED_MAX) {
+    // small batches: the inputs are gathered into page-locked memory on the
+    // host and go over by DMA without the driver's staging of pageable
+    // copies; the kernel writes the status words in place
+    const size_t a_b = seeded ? (size_t)32 * ELL * n : rows_b * n;
+    CUDA_TRY(c->h_stage.ensure(rows_b * n + a_b + sizeof(uint32_t) * 2 * n));
+    uint8_t* hb = c->h_stage.host<uint8_t>();
+    uint8_t* ha = hb + rows_b * n;
+    uint32_t* hsid = reinterpret_cast<uint32_t*>(ha + a_b);
+    int32_t* hcid = reinterpret_cast<int32_t*>(hsid + n);
+    for (uint32_t i = 0; i < n; i++) {
+      memcpy(hb + rows_b * i, b_rows + i * stride_polys * pw, rows_b);
+      if (seeded) memcpy(ha + (size_t)32 * ELL * i, seeds + i * seed_stride, (size_t)32 * ELL);
+      else memcpy(ha + rows_b * i, a_rows + i * stride_polys * pw, rows_b);
+      hsid[i] = shard_ids[i];
+      hcid[i] = client_ids[i];
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->d_brows.p, hb, rows_b * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(seeded ? c->d_seeds.p : c->d_arows.p, ha, a_b, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->d_shard.p, hsid, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->d_client.p, hcid, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
   } else {
-    CUDA_TRY(c->d_arows.ensure(sizeof(uint64_t) * n * ELL * pw));
-    CUDA_TRY(cudaMemcpy2DAsync(c->d_arows.p, sizeof(uint64_t) * ELL * pw, a_rows, sizeof(uint64_t) * stride_polys * pw,
-                               sizeof(uint64_t) * ELL * pw, n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->d_shard.p, shard_ids, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->d_client.p, client_ids, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
+    // b rows ELL..2ELL-1 of each query: one strided copy
+    CUDA_TRY(cudaMemcpy2DAsync(c->d_brows.p, rows_b, b_rows, sizeof(uint64_t) * stride_polys * pw, rows_b, n,
+                               cudaMemcpyHostToDevice, c->stream));
+    if (seeded)
+      CUDA_TRY(cudaMemcpy2DAsync(c->d_seeds.p, (size_t)32 * ELL, seeds, seed_stride, (size_t)32 * ELL, n,
+                                 cudaMemcpyHostToDevice, c->stream));
+    else
+      CUDA_TRY(cudaMemcpy2DAsync(c->d_arows.p, rows_b, a_rows, sizeof(uint64_t) * stride_polys * pw, rows_b, n,
+                                 cudaMemcpyHostToDevice, c->stream));
   }
   int rc = sync_client_table(c);
   if (rc) return rc;
@@ -260,17 +295,16 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
   a.H = db->H.as<uint16_t>();
   a.what = c->what3.as<uint32_t>();
   a.out = c->d_out.as<uint64_t>();
-  a.status = c->d_status.as<int>();
-  CUDA_TRY(launch_respond(a, seeded, c->stream));
+  int32_t* hs = c->h_qstatus.host<int32_t>();
+  for (uint32_t i = 0; i < n; i++) hs[i] = -1;
+  a.status = c->h_qstatus.dev<int32_t>();
+  CUDA_TRY(launch_respond(a, seeded, c->stream, 0, c->pair_max));
   CUDA_TRY(cudaMemcpyAsync(out_ct, c->d_out.p, sizeof(uint64_t) * n * 2 * pw, cudaMemcpyDeviceToHost, c->stream));
-  c->h_status.resize(n);
-  CUDA_TRY(cudaMemcpyAsync(c->h_status.data(), c->d_status.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
-                           c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   for (uint32_t i = 0; i < n; i++)
-    if (c->h_status[i] != 0)
+    if (hs[i] != 0)
       return fail(INSPIRE_ERR_DEVICE_STATUS,
-                  "respond kernel status " + std::to_string(c->h_status[i]) + " for query " + std::to_string(i));
+                  "respond kernel status " + std::to_string(hs[i]) + " for query " + std::to_string(i));
   return INSPIRE_OK;
 }
 
@@ -493,6 +527,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     delete c;
     return fail(INSPIRE_ERR_CUDA, "cannot read the SM count");
   }
+  c->pair_max = c->sm_count / 2;
   // tables per residue: fwd pairs (2N words), inv pairs (2N words), psi_pow (2N)
   const size_t per = 6 * (size_t)N;
   std::vector<uint32_t> host(2 * per);
@@ -575,6 +610,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     P.r[r].psi_pow = base + 4 * N;
   }
   e = prepare_respond_kernels();
+  if (e == cudaSuccess) e = prepare_respond_pair_kernels();
   if (e == cudaSuccess) e = prepare_nopacking_kernels();
   if (e == cudaSuccess) e = prepare_ops_kernels();
   if (e == cudaSuccess) e = prepare_setup_kernels();
@@ -712,6 +748,16 @@ int inspire_ctx_set_device_budget(inspire_ctx* c, uint64_t bytes) {
                                                   " bytes already in use");
   return INSPIRE_OK;
 }
+
+int inspire_ctx_set_pair_threshold(inspire_ctx* c, uint32_t max_queries) {
+  if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (max_queries > (1u << 30)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "max_queries out of range");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->pair_max = (int)max_queries;
+  return INSPIRE_OK;
+}
+
+uint32_t inspire_ctx_pair_threshold(const inspire_ctx* c) { return c ? (uint32_t)c->pair_max : 0; }
 
 int inspire_ctx_device_memory(inspire_ctx* c, uint64_t* used, uint64_t* budget) {
   if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
@@ -987,7 +1033,7 @@ int inspire_respond_seeded_batch_device_grid(inspire_ctx* c, const inspire_db* d
   a.what = c->what3.as<uint32_t>();
   a.out = d_out_ct;
   a.status = d_status;
-  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream, (int)max_ctas));
+  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream, (int)max_ctas, c->pair_max));
   return INSPIRE_OK;
 }
 

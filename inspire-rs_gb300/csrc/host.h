@@ -73,6 +73,51 @@ struct DevMem {
 
 }  // namespace ighost
 
+namespace ighost {
+// Page-locked, device-mapped host memory of at least `bytes` (grown on
+// demand, contents not kept): the host-buffer calls' descriptors and status
+// words, which the GPU reads by DMA and writes in place.
+struct HostPinned {
+  void* p = nullptr;  // host address
+  void* d = nullptr;  // device address of the same memory
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    e = cudaHostGetDevicePointer(&d, p, 0);
+    if (e != cudaSuccess) {
+      cudaFreeHost(p);
+      p = d = nullptr;
+      return e;
+    }
+    bytes = n;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = d = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* host() const {
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* dev() const {
+    return static_cast<T*>(d);
+  }
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+  ~HostPinned() { release(); }
+};
+}  // namespace ighost
+
 struct inspire_ctx {
   std::mutex mu;
   // device-memory accounting of everything this context allocates
@@ -80,6 +125,9 @@ struct inspire_ctx {
   int device = 0;
   int mode = 0;
   int sm_count = 0;
+  // batches of at most this many queries run on the two-CTA cluster kernel
+  // (one SM per CRT residue; lower latency while the SMs are not all busy)
+  int pair_max = 0;
   inspire_params params{};
   uint64_t q = 0;  // composite modulus
   ig::DevParams P{};
@@ -103,8 +151,10 @@ struct inspire_ctx {
   // staging for host-buffer calls
   cudaStream_t stream = nullptr;
   ighost::DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys, d_desc;
-  std::vector<ig::QueryDesc> h_desc;
   std::vector<int32_t> h_status;
+  ighost::HostPinned h_desc;    // descriptors of page-locked batch calls
+  ighost::HostPinned h_qstatus; // status words of the batch calls, written by the kernel
+  ighost::HostPinned h_stage;   // small batches' inputs, gathered for one DMA each
 
   inspire_ctx() {
     for (ighost::DevMem* m : {&tables, &what, &what3, &wmask, &galois, &tree_work, &d_tree_out, &client_table, &d_shard,

@@ -178,7 +178,12 @@ cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t s
 
 size_t respond_smem_bytes(int mode);
 // max_ctas > 0 caps the grid: each CTA then answers several queries in turn.
-cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st, int max_ctas = 0);
+// Otherwise batches of at most pair_max queries run on the two-CTA cluster
+// kernel (respond_pair.cu), larger ones on the one-CTA kernel.
+cudaError_t launch_respond(const RespondArgs& a, bool seeded, cudaStream_t st, int max_ctas = 0, int pair_max = 0);
+size_t respond_pair_smem_bytes();
+cudaError_t prepare_respond_pair_kernels();
+cudaError_t launch_respond_pair(const RespondArgs& a, bool seeded, cudaStream_t st);
 
 // setup-time kernels
 cudaError_t launch_columns_from_raw(const uint8_t* raw, uint64_t n_entries, int entry_size,

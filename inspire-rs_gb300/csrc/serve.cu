@@ -122,7 +122,7 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   a.what = ctx->what3.as<uint32_t>();
   a.qdesc = s.ddesc.as<QueryDesc>();
   a.stage_wait_iters = cfg.stage_wait_iters;
-  CUDA_TRY(launch_respond(a, true, s.st));
+  CUDA_TRY(launch_respond(a, true, s.st, 0, ctx->pair_max));
   CUDA_TRY(cudaEventRecord(s.ev, s.st));
   return INSPIRE_OK;
 }

@@ -191,6 +191,8 @@ def load(path: str = LIB_PATH):
         "inspire_crs_a_vectors_count": (u64, [vp]),
         "inspire_inspiring_precomp": (C.c_int, [vp, vp, vp, vp]),
         "inspire_ctx_set_device_budget": (C.c_int, [vp, u64]),
+        "inspire_ctx_set_pair_threshold": (C.c_int, [vp, u32]),
+        "inspire_ctx_pair_threshold": (u32, [vp]),
         "inspire_http_config_default": (None, [C.POINTER(HttpConfigC)]),
         "inspire_http_start": (C.c_int, [vp, vp, vp, C.POINTER(HttpConfigC), C.c_char_p, C.c_size_t,
                                          C.POINTER(vp)]),

@@ -195,6 +195,18 @@ class ServerCrs:
         PirError (status ERR_OUT_OF_MEMORY) before allocating."""
         _check(self.L.inspire_ctx_set_device_budget(self.h, int(nbytes)))
 
+    @property
+    def pair_threshold(self) -> int:
+        """Launches of at most this many queries run each query on a cluster
+        of two CTAs, one per CRT residue (lower latency); larger ones on one
+        CTA per query.  Default: half the SM count; 0 disables the cluster
+        kernel.  Responses are identical either way."""
+        return int(self.L.inspire_ctx_pair_threshold(self.h))
+
+    @pair_threshold.setter
+    def pair_threshold(self, max_queries: int) -> None:
+        _check(self.L.inspire_ctx_set_pair_threshold(self.h, int(max_queries)))
+
     def device_memory(self):
         """(bytes in use, budget) of this context's device memory."""
         used, budget = C.c_uint64(0), C.c_uint64(0)

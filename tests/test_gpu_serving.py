@@ -219,16 +219,29 @@ def test_borrowed_rows_mixed_databases_one_call(world):
     bb.close()
 
 
-def test_stage_wait_running_out(world):
+@pytest.mark.parametrize("kernel", ["pair", "single"])
+def test_stage_wait_running_out(world, kernel):
     """The serving variant's bounded wait for a query's rows (copied from
     pinned host memory into shared memory) made to run out at once
     (stage_wait_iters = 0): every query of the batch fails with a device
     status after the kernel has drained its copies, the context stays
-    usable, and the next batches are answered correctly."""
+    usable, and the next batches are answered correctly.  Both Respond
+    kernels: the two-CTA cluster kernel (batches up to the pair threshold;
+    the two CTAs agree on the outcome before either returns) and the
+    one-CTA kernel."""
     W = world
     inspire = W["inspire"]
     qs = make_queries(W, 12)
     want = [alone(W, q) for q in qs]
+    old_threshold = W["crs"].pair_threshold
+    W["crs"].pair_threshold = 64 if kernel == "pair" else 0
+    try:
+        _stage_wait_running_out(W, inspire, qs, want)
+    finally:
+        W["crs"].pair_threshold = old_threshold
+
+
+def _stage_wait_running_out(W, inspire, qs, want):
 
     def serve(srv, qs):
         tickets, rc = srv.submit([W["dbs"][q["db"]] for q in qs], [q["shard"] for q in qs],
