@@ -20,6 +20,9 @@ response is decrypted and extracted on the device with its client's key.
   serving: Poisson arrivals at swept rates through the same loop, p50/p99
           latency; the mixed workload adds 8 resident databases of 2^18..2^26
           entries.
+  small batches (batch_sweep_qps, plain_single_query_host): launches of at
+          most pair_threshold queries run on the two-CTA cluster kernel (one
+          SM per CRT residue); *_one_cta repeats them on one CTA per query.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -660,20 +663,31 @@ def main():
         verified = int(np.all(got_all == want_all, axis=2).sum())
         assert verified == nb * B, f"{nb * B - verified} timed responses failed to decrypt"
 
-    # batch-size sweep (single query = the plain GPU path)
-    sweep = {}
-    for bs in (1, 8, 32, 128):
-        if bs > B:
-            continue
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = 20 if bs < 32 else 5
-        e0.record(stream)
-        for r in range(reps):
-            launch(r, bs)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        sweep[str(bs)] = bs * reps / (e0.elapsed_time(e1) / 1e3)
+    # batch-size sweep (single query = the plain GPU path): launches of at
+    # most pair_threshold queries run on the two-CTA cluster kernel, the rest
+    # on one CTA per query; the second sweep forces one CTA per query
+    pair_threshold = crs.pair_threshold
+
+    def batch_sweep():
+        out = {}
+        for bs in (1, 8, 32, 128):
+            if bs > B:
+                continue
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 20 if bs < 32 else 5
+            e0.record(stream)
+            for r in range(reps):
+                launch(r, bs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out[str(bs)] = bs * reps / (e0.elapsed_time(e1) / 1e3)
+        return out
+
+    sweep = batch_sweep()
+    crs.pair_threshold = 0
+    sweep_one_cta = batch_sweep()
+    crs.pair_threshold = pair_threshold
     # C4 same-shard variant: every query of the launch names shard 0 (the
     # shard's contracted form is read once into L2 and shared)
     same_shard = None
@@ -720,19 +734,25 @@ def main():
     d2h = B * (2 * 2 * N * 8 + 4)
 
     # plain single-query path: one synchronous host-buffer call per query
-    single_lat = []
-    for k in range(200):
-        s = k % nb
-        hs1, hb1, ho1 = hs[:1], hb[:1], ho[:1]
-        hs1[:] = seeds[pool_idx[s, :1]]
-        hb1[:] = brows[pool_idx[s, :1]]
-        t0 = time.perf_counter()
-        _respond_into(crs, edb, shard_ids[s, :1], hs1, hb1, qcid[pool_idx[s, :1]], ho1)
-        single_lat.append(time.perf_counter() - t0)
-    single_lat = np.array(single_lat[10:]) * 1e3
-    plain = {"qps": float(1e3 / single_lat.mean()), "p50_ms": float(np.percentile(single_lat, 50)),
-             "p99_ms": float(np.percentile(single_lat, 99)),
-             "path": "inspire_respond_seeded_batch with n=1 from host buffers, one call at a time"}
+    def single_calls():
+        lat = []
+        for k in range(200):
+            s = k % nb
+            hs1, hb1, ho1 = hs[:1], hb[:1], ho[:1]
+            hs1[:] = seeds[pool_idx[s, :1]]
+            hb1[:] = brows[pool_idx[s, :1]]
+            t0 = time.perf_counter()
+            _respond_into(crs, edb, shard_ids[s, :1], hs1, hb1, qcid[pool_idx[s, :1]], ho1)
+            lat.append(time.perf_counter() - t0)
+        lat = np.array(lat[10:]) * 1e3
+        return {"qps": float(1e3 / lat.mean()), "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99))}
+
+    plain = dict(single_calls(), path="inspire_respond_seeded_batch with n=1 from host buffers (page-locked), one "
+                                      "call at a time; two-CTA cluster kernel (one SM per CRT residue)")
+    crs.pair_threshold = 0
+    plain_one_cta = dict(single_calls(), path="the same call on the one-CTA kernel")
+    crs.pair_threshold = pair_threshold
 
     c3 = c3_bench(inspire, crs, seeds[c0], brows[c0], y_body) if rank == 0 else None
     shard_files = shard_file_bench(inspire, crs, seeds[c0], brows[c0], y_body) if rank == 0 else None
@@ -811,8 +831,11 @@ def main():
             "value_one_call": value_one_call,
             "db_scan_gbs": value * DB_BYTES_PER_QUERY / 1e9,
             "batch_sweep_qps": sweep,
+            "batch_sweep_qps_one_cta": sweep_one_cta,
+            "pair_threshold": pair_threshold,
             "plain_single_query_qps": sweep.get("1"),
             "plain_single_query_host": plain,
+            "plain_single_query_host_one_cta": plain_one_cta,
             "same_shard_batch_qps": same_shard,
             "c3_single_query": c3,
             "shard_files": shard_files,

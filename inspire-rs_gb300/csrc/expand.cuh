@@ -138,49 +138,34 @@ __device__ bool expand_seeded_row(const DevParams& P, const uint8_t* __restrict_
 // 0's last accepted draw.  Returns the index after the last accepted
 // candidate, or -1 if the iteration bound was hit.
 //
-// The first batch draws SUB + EXPAND_EXTRA_BLOCKS blocks (threads below
-// EXPAND_EXTRA_BLOCKS draw a second one into cand_x), so that the draws
-// rejected within it (about one in 4096) rarely leave the residue short and a
-// second batch -- a whole ChaCha20 latency -- is rarely needed.
-//
 // Speculative start (spec_blk > 0): the first batch, from block spec_blk on,
 // is drawn before `first` is known; then every thread calls get_first(),
 // which returns it (at least 8 spec_blk for residue 1, whose position the
 // other CTA finds).  Candidates before `first` are skipped, and blocks wholly
 // before it are not drawn after the first batch, so the result does not
 // depend on the guess.
-constexpr int EXPAND_EXTRA_BLOCKS = 8;
-
 template <class GetFirst>
 __device__ long long expand_residue(const DevParams& P, const uint32_t key[8], int res, uint64_t first,
-                                    uint64_t spec_blk, GetFirst&& get_first, uint64_t* cand, uint64_t* cand_x,
-                                    uint32_t* dst, int* ws, int bar, int lt) {
-  constexpr int XB = EXPAND_EXTRA_BLOCKS;
+                                    uint64_t spec_blk, GetFirst&& get_first, uint64_t* cand, uint32_t* dst, int* ws,
+                                    int bar, int lt) {
   const uint64_t q = P.r[res].q, zone = P.r[res].zone;
   uint64_t blk = spec_blk ? spec_blk : first / 8;
   int pos = 0;
   for (int it = 0; it < 64; it++) {
     const int nblk = min(SUB, ((N - pos) * 9) / 64 + 3);
-    const bool ext = it == 0;
-    // one block per thread, a second one for threads below XB in the first
-    // batch (one instance of the block function: the kernel's code stays small)
-    const int nb = lt < nblk ? ((ext && lt < XB) ? 2 : 1) : 0;
-#pragma unroll 1
-    for (int b = 0; b < nb; b++) {
+    if (lt < nblk) {
       uint32_t w[16];
-      chacha20_block(key, b ? blk + nblk + lt : blk + lt, P.one, w);
-      uint64_t* cd = b ? cand_x + lt : cand + lt;
-      const int cs = b ? XB : SUB;
+      chacha20_block(key, blk + lt, P.one, w);
 #pragma unroll
-      for (int k = 0; k < 8; k++) cd[k * cs] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
+      for (int k = 0; k < 8; k++) cand[k * SUB + lt] = (uint64_t)w[2 * k] | ((uint64_t)w[2 * k + 1] << 32);
     }
-    const uint64_t gbase = 8 * blk;  // global index of local candidate 0; extra ones follow the nblk blocks
-    blk += nblk + (ext ? XB : 0);
+    const uint64_t gbase = 8 * blk;  // global index of local candidate 0
+    blk += nblk;
     named_sync(bar, SUB);
     if (it == 0 && spec_blk) first = get_first();
-    uint32_t vals[8], xvals[8];
-    unsigned fl = 0, flx = 0;
-    int cnt = 0, cntx = 0;
+    uint32_t vals[8];
+    unsigned fl = 0;
+    int cnt = 0;
     if (lt < nblk) {
 #pragma unroll
       for (int k = 0; k < 8; k++)
@@ -189,29 +174,8 @@ __device__ long long expand_residue(const DevParams& P, const uint32_t key[8], i
           cnt++;
         }
     }
-    int xexcl = 0;
-    if (ext && lt < 32) {  // the extra blocks' draws: exclusive scan over warp 0's lanes
-      if (lt < XB) {
-#pragma unroll
-        for (int k = 0; k < 8; k++)
-          if (gbase + 8 * (nblk + lt) + k >= first && uniform_accept(cand_x[k * XB + lt], q, zone, xvals[k])) {
-            flx |= 1u << k;
-            cntx++;
-          }
-      }
-      int incl = cntx;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lt >= o) incl += t;
-      }
-      xexcl = incl - cntx;
-      const int xtot = __shfl_sync(0xffffffffu, incl, 31);
-      if (lt == 0) ws[18] = xtot;  // published by the scan's barriers
-    }
     int total;
     int p = pos + sub_scan_excl(cnt, ws, total, bar, lt);
-    const int xtotal = ext ? ws[18] : 0;
 #pragma unroll
     for (int k = 0; k < 8; k++)
       if ((fl >> k) & 1u) {
@@ -219,17 +183,6 @@ __device__ long long expand_residue(const DevParams& P, const uint32_t key[8], i
         if (p == N - 1) ws[16] = 8 * lt + k;
         p++;
       }
-    if (flx) {
-      int px = pos + total + xexcl;
-#pragma unroll
-      for (int k = 0; k < 8; k++)
-        if ((flx >> k) & 1u) {
-          if (px < N) dst[px] = xvals[k];
-          if (px == N - 1) ws[16] = 8 * (nblk + lt) + k;
-          px++;
-        }
-    }
-    total += xtotal;
     named_sync(bar, SUB);
     if (pos + total >= N) {
       const long long end = (long long)(gbase + (uint64_t)ws[16] + 1);

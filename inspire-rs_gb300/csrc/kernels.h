@@ -20,7 +20,7 @@ constexpr uint32_t STAGE_DRAIN_ITERS = 1u << 22;
 
 // One resident database as the Respond kernel sees it.
 struct DbView {
-  const uint32_t* E;  // [nshards][2][ELL][gamma][N] contracted database
+  const uint32_t* E;  // [nshards][2][gamma][ELL][N] contracted database, by recursion step
   const uint16_t* H;  // [nshards][gamma][N] raw 16-bit columns
   int nshards;
   int pad;
@@ -53,7 +53,7 @@ struct RespondArgs {
   // [ELL][2][N] whose rotations the kernel forms; third digit folded in
   const uint32_t* const* yhat_table;
   int nclients, nshards;
-  const uint32_t* E;             // [nshards][2][ELL][gamma][N] contracted database
+  const uint32_t* E;             // [nshards][2][gamma][ELL][N] contracted database, by recursion step
   const uint16_t* H;             // [nshards][gamma][N] raw 16-bit columns
   const uint32_t* what;          // [(gamma-1)][ELL][2][N] rotated w_mask (CRS), third digit folded in
   uint64_t* out;                 // [nq][2][2][N] response (a_hat, b) residues

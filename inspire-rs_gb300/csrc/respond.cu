@@ -224,7 +224,11 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   if (QDB && tid < ELL * 32) seed_sm[tid] = D->seeds[tid];
   if (!QDB && tid < 32) bpoly[tid] = b_parking(A.out, qi)[tid];  // parked by bside_kernel
   if (tid == 0) {
-    prefetch_l2(E, sizeof(uint32_t) * (size_t)NR * ELL * gamma * N);
+    // the contracted shard's blocks of the first three steps (the rest are
+    // prefetched two steps ahead of their use in the recursion)
+    const int i0 = gamma >= 3 ? gamma - 3 : 0;
+    for (int rr = 0; rr < NR; rr++)
+      prefetch_l2(E + ((size_t)rr * gamma + i0) * ELL * N, sizeof(uint32_t) * (size_t)(gamma - i0) * ELL * N);
     if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(ybody ? 1 : gamma - 1) * ELL * 2 * N);
   }
   if (QDB) {
@@ -331,6 +335,8 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   const int f = (x >> 1) & 3;  // chunk swizzle of this thread's 16-slot run (store16 / load16)
   for (int i = gamma - 2; i >= 0; i--) {
     const size_t yoff = ybody ? (size_t)i * ELL * 2 * N : 0;  // body tables: the key slices of i = 0, rotated
+    if (tid == 0 && i >= 2)  // the block the next step's scatter reads (R_{i-2})
+      for (int rr = 0; rr < NR; rr++) prefetch_l2(Eg_at(rr) + (size_t)(i - 2) * ELL * N, sizeof(uint32_t) * ELL * N);
     // [A] inverse NTT of R_{i+1} by residue r's team; RS keeps R_{i+1}
     if (kd < 2) {
       uint32_t v[8];

@@ -17,22 +17,6 @@ __device__ __forceinline__ T* reload_ptr(T* const* p) {
   return reinterpret_cast<T*>(v);
 }
 
-// Loads of data each SM reads once per query (key slices, the contracted
-// shard, raw columns): not allocated in L1, so that they do not evict the
-// NTT twiddle tables that every transform of the kernel reads.
-__device__ __forceinline__ uint32_t ldg_stream(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
-  return v;
-}
-__device__ __forceinline__ uint4 ldg_stream4(const void* p) {
-  uint4 v;
-  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-               : "l"(p));
-  return v;
-}
-
 // L2 prefetch of a contiguous device range with bulk (TMA) prefetches.
 __device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
   const char* c = static_cast<const char*>(p);
@@ -83,8 +67,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
 // R_i (NTT domain, scaled by n^-1) of packing_offline step 1 for one residue,
 // scattered to dst[slot]: source slot u contributes to slot s with
 // 2brv(s)+1 = h_i (2brv(u)+1) mod 2n, where h_i = g^-i
-// (inspiring2.rs:952-981 with the tables of :208-263).  Threads p in
-// [0, nthr) handle u = p + nthr * v.
+// (inspiring2.rs:952-981 with the tables of :208-263).  Eg is this residue's
+// contracted shard [gamma][ELL][N], stored by step (encode_E_kernel): the
+// three rows' DFT outputs for slot u of step i sit at [i][t][u], so the loads
+// of consecutive slots are contiguous.  Threads p in [0, nthr) handle
+// u = p + nthr * v.
 // In compat mode `dst1`, if not null, receives residue 1 rebuilt from each
 // residue-0 value as the crate's apply_automorphism_ntt does (`dst` may then
 // be null: only residue 1 is written).
@@ -94,14 +81,13 @@ __device__ __forceinline__ void scatter_r(const DevParams& P, int i, const uint3
   const int gamma = P.gamma;
   const uint32_t mi = (uint32_t)(gamma - i) & (uint32_t)(gamma - 1);
   const uint32_t hi = (1u + (uint32_t)(2 * N / gamma) * mi) & (2 * N - 1);
+  const uint32_t* Ei = Eg + (size_t)i * ELL * N;
 #pragma unroll 4
   for (int u = u0 + p; u < u1; u += nthr) {
     const uint32_t e = 2 * brv11(u) + 1;
-    const uint32_t k = (e * mi) & (uint32_t)(gamma - 1);
-    const uint32_t* ek = Eg + (size_t)k * N + u;
     const int us = swz(u);
-    const uint64_t T = (uint64_t)ldg_stream(ek) * Ag[us] + (uint64_t)ldg_stream(ek + (size_t)gamma * N) * Ag[astride + us] +
-                       (uint64_t)ldg_stream(ek + (size_t)2 * gamma * N) * Ag[2 * astride + us];
+    const uint64_t T = (uint64_t)__ldg(Ei + u) * Ag[us] + (uint64_t)__ldg(Ei + N + u) * Ag[astride + us] +
+                       (uint64_t)__ldg(Ei + 2 * N + u) * Ag[2 * astride + us];
     const uint32_t s = brv11(((hi * e) & (2 * N - 1)) >> 1);
     const uint32_t val = redc(T, q, qinv);
     if (dst) dst[swz(s)] = val;
@@ -152,7 +138,7 @@ __device__ __forceinline__ void rotate_key_run(uint4 (&y)[4], int i, int x) {
 __device__ __forceinline__ void key_run(const uint32_t* p, uint4 (&k)[4]) {
   const uint4* k4 = reinterpret_cast<const uint4*>(p);
 #pragma unroll
-  for (int r4 = 0; r4 < 4; r4++) k[r4] = ldg_stream4(k4 + r4);
+  for (int r4 = 0; r4 < 4; r4++) k[r4] = __ldg(k4 + r4);
 }
 
 __device__ __forceinline__ uint32_t u4e(const uint4& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }

@@ -26,7 +26,8 @@
 //  [C] group 0: NTT(d0); partial R_i = query-only term + NTT(d0) w'0,
 //      b += NTT(d0) y'0; group 1: NTT(d1); PB1 = NTT(d1) w'1, b += NTT(d1)
 //      y'1; then group 0 sums R_i = partial + PB1 + PB2 into RN;
-//      groups 2-5: second half of R_{i-1}.
+//      groups 2-5: second half of R_{i-1}, and the b side (coefficient 0 of
+//      the column products) of one column, two in the last step.
 // TC is double-buffered by step parity: the peer writes TC[p] again only in
 // step i - 2, after the cluster barrier of step i - 1, which this CTA reaches
 // only after its last read of TC[p].  The only other remote writes are the
@@ -85,8 +86,7 @@ struct PairSmem {
   static constexpr int ROWS = W;
   static constexpr int CAND = W + 2 * ELL * N;
   static constexpr int BP = ACC + 3 * N;             // [ELL][N] negacyclic reversal of the b rows (b side)
-  static constexpr int CANDX = BP + ELL * N;         // u64 [3][8 * EXPAND_EXTRA_BLOCKS] extra candidates
-  static constexpr int MISC = CANDX + 3 * 2 * 8 * EXPAND_EXTRA_BLOCKS;
+  static constexpr int MISC = BP + ELL * N;
   // MISC words: [0, 32) b0 sums per column (u64); [32, 92) scan scratch of
   // the three sub-blocks (20 each, [17] = expansion ok); [96, 120) staged
   // seeds; [120, 123) residue 1's stream positions; [124, 126) flags by CTA
@@ -95,8 +95,7 @@ struct PairSmem {
   static constexpr int TOTAL = MISC + 160;
 };
 static_assert(PairSmem::CAND + 2 * 3 * 8 * SUB <= PairSmem::BP, "candidates fit the working region");
-static_assert(PairSmem::W % 4 == 0 && PairSmem::CAND % 4 == 0 && PairSmem::BP % 4 == 0 &&
-                  PairSmem::CANDX % 4 == 0 && PairSmem::MISC % 4 == 0,
+static_assert(PairSmem::W % 4 == 0 && PairSmem::CAND % 4 == 0 && PairSmem::BP % 4 == 0 && PairSmem::MISC % 4 == 0,
               "16-byte alignment");
 
 // The b side of the column products, coefficient 0 only (rlwe/enc.rs:195-208;
@@ -184,16 +183,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
     mbar_init(rbar);
     misc[128] = 0;
     prefetch_l2(H, sizeof(uint16_t) * (size_t)gamma * N);
-    prefetch_l2(Eg_at(), sizeof(uint32_t) * (size_t)ELL * gamma * N);
+    // the contracted shard's blocks of the first three steps (the rest are
+    // prefetched two steps ahead of their use in the recursion)
+    const int i0 = gamma >= 3 ? gamma - 3 : 0;
+    prefetch_l2(Eg_at() + (size_t)i0 * ELL * N, sizeof(uint32_t) * (size_t)(gamma - i0) * ELL * N);
     if (gamma > 1) prefetch_l2(Y, sizeof(uint32_t) * (size_t)(ybody ? 1 : gamma - 1) * ELL * 2 * N);
   }
   if (tid < MAX_GAMMA) b0sum[tid] = 0;
-  // the twiddle tables this CTA's transforms read, into L1 (16 KiB each)
-  {
-    const uint2* tw = tid < 128 ? P.r[sres].fwd : tid < 256 ? C.inv : C.fwd;
-    if (tid < 256 || (tid < 384 && sres != (int)r))
-      asm volatile("prefetch.global.L1 [%0];" ::"l"(reinterpret_cast<const char*>(tw) + 128 * (tid & 127)));
-  }
   if (QDB && tid < ELL * 32) seed_sm[tid] = D->seeds[tid];
   __syncthreads();  // the mbarrier is initialised, the seeds staged
   if (tid == 0) {
@@ -209,7 +205,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
   {
     const int t = tid >> 8, lt = tid & 255;
     uint64_t* cand = reinterpret_cast<uint64_t*>(smem + L::CAND) + (size_t)t * 8 * SUB;
-    uint64_t* cand_x = reinterpret_cast<uint64_t*>(smem + L::CANDX) + (size_t)t * 8 * EXPAND_EXTRA_BLOCKS;
     uint32_t* dst = AH + t * N;
     int* ws = misc + 32 + 20 * t;
     if (SEEDED) {
@@ -231,10 +226,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
               cluster_sync_all();
               return (uint32_t)misc[120 + t];
             },
-            cand, cand_x, dst, ws, 5 + t, lt);
+            cand, dst, ws, 5 + t, lt);
         started = true;
       } else {
-        end = expand_residue(P, key, sres, 0, 0, []() -> uint64_t { return 0; }, cand, cand_x, dst, ws, 5 + t, lt);
+        end = expand_residue(P, key, sres, 0, 0, []() -> uint64_t { return 0; }, cand, dst, ws, 5 + t, lt);
         if (MODE == MODE_CRT_FIXED) {
           cluster_wait();
           started = true;
@@ -307,7 +302,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
   if (gamma == 1 && tid >= 2 * NTT_GT) {  // no recursion step: the one column's b side here
     const uint32_t* h2 = reinterpret_cast<const uint32_t*>(H);
     const int t = tid - 2 * NTT_GT;
-    column_b0_part(P, ldg_stream(h2 + t), ldg_stream(h2 + t + 512), BP, t, b0sum);
+    column_b0_part(P, __ldg(h2 + t), __ldg(h2 + t + 512), BP, t, b0sum);
   }
   __syncthreads();
 
@@ -322,6 +317,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
     const int p = i & 1;
     uint32_t* TC = smem + L::TC + p * 2 * N;
     const size_t yoff = ybody ? (size_t)i * ELL * 2 * N : 0;  // body tables: the key slices of i = 0, rotated
+    if (tid == 0 && i >= 2) prefetch_l2(Eg_at() + (size_t)(i - 2) * ELL * N, sizeof(uint32_t) * ELL * N);
     // [A]
     if (tid < 2 * NTT_GT) {
       uint32_t v[8];
@@ -434,11 +430,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
       const bool two = i == 0;
       const uint32_t* h0 = reinterpret_cast<const uint32_t*>(H + (size_t)c0 * N);
       const uint32_t* h1 = reinterpret_cast<const uint32_t*>(H + (size_t)(gamma - 1) * N);
-      const uint32_t w0 = ldg_stream(h0 + t), w1 = ldg_stream(h0 + t + 512);
+      const uint32_t w0 = __ldg(h0 + t), w1 = __ldg(h0 + t + 512);
       uint32_t w2 = 0, w3 = 0;
       if (two) {
-        w2 = ldg_stream(h1 + t);
-        w3 = ldg_stream(h1 + t + 512);
+        w2 = __ldg(h1 + t);
+        w3 = __ldg(h1 + t + 512);
       }
       if (i >= 1) scatter_next(i, t, 4 * NTT_GT, N / 2, N);
       column_b0_part(P, w0, w1, BP, t, b0sum + c0);

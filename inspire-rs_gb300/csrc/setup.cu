@@ -64,7 +64,12 @@ __global__ void __launch_bounds__(BLOCK) encode_E_kernel(const DevParams P, cons
     for (int rr = 0; rr < 4; rr++) dst[rr] = make_uint4(v[4 * rr], v[4 * rr + 1], v[4 * rr + 2], v[4 * rr + 3]);
   }
   __syncthreads();
-  uint32_t* Eo = E + ((((size_t)s * 2 + r) * ELL + t) * gamma) * N;
+  // Stored by recursion step: the scatter of R_i reads, at source slot u, the
+  // DFT output k = (2brv(u)+1) m_i mod gamma with m_i = (gamma - i) mod gamma
+  // (scatter_r), so entry [i][t][u] holds output k of (t, u) and a warp's
+  // loads at consecutive slots are contiguous.  For odd 2brv(u)+1 the map
+  // i -> k is a bijection: the table is a permutation of the outputs.
+  uint32_t* Eo = E + (((size_t)s * 2 + r) * gamma * ELL + t) * N;
   for (int v = 0; v < N / BLOCK; v++) {
     const int u = tid + BLOCK * v;
     const uint32_t e = 2 * brv11(u) + 1;
@@ -72,14 +77,15 @@ __global__ void __launch_bounds__(BLOCK) encode_E_kernel(const DevParams P, cons
 #pragma unroll
     for (int j = 0; j < MAX_GAMMA; j++)
       if (j < gamma) c[j] = mont_mul(Dh[j * N + u], __ldg(C.psi_pow + ((e * j) & (2 * N - 1))), q, qinv);
-    for (int k = 0; k < gamma; k++) {
+    for (int i = 0; i < gamma; i++) {
+      const int k = (int)((e * ((uint32_t)(gamma - i) & (uint32_t)(gamma - 1))) & (uint32_t)(gamma - 1));
       uint64_t T = 0;
 #pragma unroll
       for (int j = 0; j < MAX_GAMMA; j++)
         if (j < gamma) T += (uint64_t)zp[(k * j) & (gamma - 1)] * c[j];
       // the two REDCs divided by 2^64; e_scale = gamma^-1 n^-1 2^96 leaves
       // the factor 2^32 gamma^-1 n^-1
-      Eo[(size_t)k * N + u] = mul_shoup(redc(T, q, qinv), C.e_scale, C.e_scale_p, q);
+      Eo[(size_t)i * ELL * N + u] = mul_shoup(redc(T, q, qinv), C.e_scale, C.e_scale_p, q);
     }
   }
 }
