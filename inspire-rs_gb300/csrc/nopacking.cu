@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
         v[j] = min(s, s - q);  // < q
       }
     }
-    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+    ntt_fwd<false>(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
 #pragma unroll
     for (int j = 0; j < 16; j++) w[j] = PB[t * 2 * N + r * N + x + 128 * j];
     __syncthreads();  // every group holds its a row: PB (row staging) is reused for products
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
 #pragma unroll
         for (int j = 0; j < 16; j++) w[j] = (uint32_t)__ldg(brow + x + 128 * j);
       }
-      ntt_fwd(w, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+      ntt_fwd<false>(w, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
       uint32_t* dst = PB + ((r * 3 + t) * 2 + ab) * N + 16 * x;
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
@@ -138,11 +138,11 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
     const ResidueConsts& C = P.r[r];
 #pragma unroll
     for (int j = 0; j < 16; j++) ah[j] = PB[t * 2 * N + r * N + x + 128 * j];
-    ntt_fwd(ah, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+    ntt_fwd<false>(ah, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
     const uint64_t* brow = A.brows + (((size_t)qi * ELL + t) * 2 + r) * N;
 #pragma unroll
     for (int j = 0; j < 16; j++) bh[j] = (uint32_t)__ldg(brow + x + 128 * j);
-    ntt_fwd(bh, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
+    ntt_fwd<false>(bh, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);
 #pragma unroll
     for (int j = 0; j < 16; j++) {
       ah[j] = mul_shoup(ah[j], C.ninv_mont, C.ninv_mont_p, q);
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(RBLOCK, 1) nopacking_kernel(const __grid_const
       const uint64_t xv = P.delta * (uint64_t)__ldg(H + (size_t)c * N + x + 128 * j);
       v[j] = (uint32_t)(xv >> (ZBITS * t)) & ((1u << ZBITS) - 1);
     }
-    ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);  // [0, 14q)
+    ntt_fwd<false>(v, SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);  // [0, 14q)
     {
       const int f = (x >> 1) & 3;
       uint32_t* da = PB + ((r * 3 + t) * 2 + 0) * N + 16 * x;

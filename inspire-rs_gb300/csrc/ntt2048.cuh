@@ -134,9 +134,55 @@ __device__ __forceinline__ void stage(uint32_t v[16], TwiddleRef tw, int first, 
   reg_stage<H, SHIFT, CNT, FWD>(v, run, q, q2);
 }
 
+// ---- exchanges within aligned 8-lane groups, by warp shuffles ----
+// A thread's register index R and its lane index within the 8-lane group
+// each carry some bits of the element index.  swap_lane_reg<J, K> exchanges
+// lane bit J with register bit K: the value at (lane bit l, register bit s)
+// moves to (lane bit s, register bit l), so values with l == s stay and the
+// others trade places with the partner lane (lane ^ 2^J) at R ^ 2^K.  Three
+// such swaps transpose an 8-lane group's values without shared memory or a
+// barrier (the 8 lanes of a group are one warp's).
+template <int NV, int J, int K>
+__device__ __forceinline__ void swap_lane_reg(uint32_t* v, bool l) {
+  constexpr int m = 1 << K;
+#pragma unroll
+  for (int R = 0; R < NV; R++) {
+    if (R & m) continue;
+    const uint32_t send = l ? v[R] : v[R | m];
+    const uint32_t recv = __shfl_xor_sync(0xffffffffu, send, 1 << J);
+    if (l) v[R] = recv;
+    else v[R | m] = recv;
+  }
+}
+
+// 128-thread transforms, between the layouts "element r is a[128 b + y + 8 r]"
+// and "element r is a[16 x + r]" (x = 8 b + y, y = x & 7; the 8 lanes of b
+// hold the same 128 elements).  Element e = y + 8 r of the block has lane
+// bits (e0, e1, e2) and register bits (e3, e4, e5, e6); the target has lane
+// bits (e4, e5, e6) and register bits (e0, e1, e2, e3).  Swapping lane bit j
+// with register bit j + 1 (j = 0, 1, 2) leaves register bits (e3, e0, e1,
+// e2), a static renaming of the registers.
+__device__ __forceinline__ void xpose_16(uint32_t* v, int y) {
+  swap_lane_reg<16, 0, 1>(v, y & 1);
+  swap_lane_reg<16, 1, 2>(v, (y >> 1) & 1);
+  swap_lane_reg<16, 2, 3>(v, (y >> 2) & 1);
+  uint32_t w[16];
+#pragma unroll
+  for (int r = 0; r < 16; r++) w[r] = v[((r >> 3) & 1) | ((r & 7) << 1)];
+#pragma unroll
+  for (int r = 0; r < 16; r++) v[r] = w[r];
+}
+
 // Forward transform (Cooley-Tukey, decimation in time), coefficient layout in
 // ([0, 4q)), slot layout out ([0, 14q)).  `sc` is this group's scratch; `bar`
-// its barrier id.
+// its barrier id.  SHFL: the second exchange by warp shuffles (xpose_16)
+// instead of shared memory and two barriers.  Measured on GB300 in one A/B
+// comparison: the batched transform 4 % faster, the Respond kernels
+// unchanged, the NoPacking and tree kernels 2-4 % slower (about their
+// run-to-run spread); those keep the shared-memory form.  The same 8-lane
+// shuffle transpose in the 256-thread inverse made the two-CTA Respond
+// kernel 15 % slower, so the inverse transforms keep shared memory.
+template <bool SHFL = true>
 __device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef tw, uint32_t q, int x, int bar) {
   const uint32_t q2 = 2 * q;
   // stages 0..3: element r is a[x + 128 r]; twiddle (1 << s) + (r >> (4 - s))
@@ -158,12 +204,16 @@ __device__ __forceinline__ void ntt_fwd(uint32_t v[16], uint32_t* sc, TwiddleRef
   stage<6, 2, true>(v, tw, b << 2, q, q2);
   stage<7, 1, true>(v, tw, b << 3, q, q2);
   reduce_8q(v, q);  // < 16q -> < 8q
-  group_sync(bar);
+  if (SHFL) {
+    xpose_16(v, y);  // within the 8 lanes of b: no shared memory, no barrier
+  } else {
+    group_sync(bar);
 #pragma unroll
-  for (int r = 0; r < 16; r++) sc[pad_b(128 * b + y + 8 * r)] = v[r];
-  group_sync(bar);
+    for (int r = 0; r < 16; r++) sc[pad_b(128 * b + y + 8 * r)] = v[r];
+    group_sync(bar);
 #pragma unroll
-  for (int r = 0; r < 16; r++) v[r] = sc[pad_b(16 * x + r)];
+    for (int r = 0; r < 16; r++) v[r] = sc[pad_b(16 * x + r)];
+  }
   // stages 8..10: element r is a[16 x + r]; twiddle (1 << s) + (x << (s - 7)) + (r >> (11 - s))
   stage<8, 3, true>(v, tw, x << 1, q, q2);
   stage<9, 2, true>(v, tw, x << 2, q, q2);

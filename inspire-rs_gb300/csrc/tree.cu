@@ -110,7 +110,7 @@ __device__ void combine(const TreeArgs& A, uint32_t* sm, const uint32_t* E, cons
     uint32_t v[16];
 #pragma unroll
     for (int j = 0; j < 16; j++) v[j] = D[kd * N + x + 128 * j];
-    ntt_fwd(v, sm + S_SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
+    ntt_fwd<false>(v, sm + S_SC + g * NTT_SCRATCH, fwd_tw(P.r[r]), q, x, 1 + g);
     uint32_t pa[16], pb[16];
 #pragma unroll
     for (int r4 = 0; r4 < 4; r4++) {
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(BLOCK) galois_prep_kernel(const DevParams P, c
   uint32_t v[16];
 #pragma unroll
   for (int j = 0; j < 16; j++) v[j] = (uint32_t)keys[((size_t)p * 2 + g) * N + x + 128 * j];
-  ntt_fwd(v, SC[g], fwd_tw(C), C.q, x, 1 + g);
+  ntt_fwd<false>(v, SC[g], fwd_tw(C), C.q, x, 1 + g);
 #pragma unroll
   for (int j = 0; j < 16; j++) ks[((size_t)p * 2 + g) * N + 16 * x + j] = mul_shoup(v[j], C.ninv_mont, C.ninv_mont_p, C.q);
 }
