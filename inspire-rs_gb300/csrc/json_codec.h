@@ -335,15 +335,72 @@ struct Out {
     memcpy(&s[n], x, k);
     n += k;
   }
+  // Decimal digits of v (1..20): for v >= 10, t = floor(bits * 1233 / 4096)
+  // (1233 / 4096 ~ log10 2) is the digit count or one less, settled by one
+  // comparison.
+  static int digits(uint64_t v) {
+    static constexpr uint64_t p10[20] = {1ull,
+                                         10ull,
+                                         100ull,
+                                         1000ull,
+                                         10000ull,
+                                         100000ull,
+                                         1000000ull,
+                                         10000000ull,
+                                         100000000ull,
+                                         1000000000ull,
+                                         10000000000ull,
+                                         100000000000ull,
+                                         1000000000000ull,
+                                         10000000000000ull,
+                                         100000000000000ull,
+                                         1000000000000000ull,
+                                         10000000000000000ull,
+                                         100000000000000000ull,
+                                         1000000000000000000ull,
+                                         10000000000000000000ull};
+    if (v < 10) return 1;
+    const int t = ((64 - __builtin_clzll(v)) * 1233) >> 12;  // t <= 19
+    return t + (v >= p10[t] ? 1 : 0);
+  }
+  // v in decimal at p (room for 20 bytes), two digits per step from the
+  // right; returns the length
+  static int put_num(char* p, uint64_t v) {
+    static constexpr char d2[201] =
+        "00010203040506070809101112131415161718192021222324252627282930313233343536373839"
+        "40414243444546474849505152535455565758596061626364656667686970717273747576777879"
+        "8081828384858687888990919293949596979899";
+    const int len = digits(v);
+    char* e = p + len;
+    while (v >= 100) {
+      const uint64_t q = v / 100;
+      const unsigned r = (unsigned)(v - q * 100);
+      e -= 2;
+      memcpy(e, d2 + 2 * r, 2);
+      v = q;
+    }
+    if (v >= 10) {
+      e -= 2;
+      memcpy(e, d2 + 2 * v, 2);
+    } else {
+      *--e = (char)('0' + v);
+    }
+    return len;
+  }
   void num(uint64_t v) {
     room(20);
-    char b[20];
-    int k = 0;
-    do {
-      b[k++] = (char)('0' + v % 10);
-      v /= 10;
-    } while (v);
-    while (k) s[n++] = b[--k];
+    n += (size_t)put_num(&s[n], v);
+  }
+  // "a0,a1,...,ak-1" (no brackets), room reserved once
+  void nums(const uint64_t* a, size_t k) {
+    room(21 * k + 1);
+    char* p = &s[n];
+    char* const p0 = p;
+    for (size_t i = 0; i < k; i++) {
+      if (i) *p++ = ',';
+      p += put_num(p, a[i]);
+    }
+    n += (size_t)(p - p0);
   }
   std::string done() {
     s.resize(n);

@@ -19,10 +19,16 @@
 // sequence lengths, bool as one byte) for ServerResponse::to_binary
 // (pir/respond.rs:43-50).
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "host.h"
 #include "json_codec.h"
@@ -32,19 +38,135 @@ using namespace igjson;
 
 namespace {
 
-// Poly in coefficient form over the context's moduli, into dst[2N].
-bool parse_poly(Json& j, const inspire_params& P, uint64_t* dst, const std::string& what) {
+// A Poly's "coeffs" array whose parse is deferred: the structural pass of a
+// large query records where each array lies and the checks its Poly needs,
+// and the arrays (independent of one another) are then parsed in parallel.
+struct PolyJob {
+  const char* lb;  // its '['
+  const char* rb;  // its ']' (the first after lb; anything else fails the job)
+  uint64_t* dst;
+  size_t plen;
+  uint64_t moduli[2];
+  uint32_t ring_dim;
+};
+
+bool run_poly_job(const PolyJob& jb) {
+  Json j{jb.lb, jb.rb + 1, "", jb.lb};
+  size_t n = 0;
+  if (!j.u64_array_into(jb.dst, jb.plen, &n) || j.p != jb.rb + 1 || n != jb.plen) return false;
+  for (size_t r = 0; r < 2; r++) {
+    const uint64_t m = jb.moduli[r], *d = jb.dst + r * jb.ring_dim;
+    uint64_t bad = 0;
+    for (size_t i = 0; i < jb.ring_dim; i++) bad |= (uint64_t)(d[i] >= m);
+    if (bad) return false;
+  }
+  return true;
+}
+
+// Worker threads for the deferred arrays, shared by every caller; a caller
+// that finds them busy parses its arrays itself.
+class ParsePool {
+ public:
+  ParsePool() : pid_(getpid()) {
+    const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
+    const unsigned n = std::min(8u, std::max(1u, hw / 2 - 1));
+    for (unsigned i = 0; i < n; i++) workers_.emplace_back([this] { work(); });
+  }
+  // Runs every job; true if all succeeded.
+  bool run(const std::vector<PolyJob>& jobs) {
+    std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+    // (a forked child has none of the workers: it parses on its own)
+    if (!busy.owns_lock() || jobs.size() < 2 || getpid() != pid_) {
+      bool ok = true;
+      for (const PolyJob& jb : jobs) ok &= run_poly_job(jb);
+      return ok;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      jobs_ = &jobs;
+      next_.store(0);
+      failed_.store(false);
+      pending_ = (int)workers_.size();
+      gen_++;
+    }
+    cv_.notify_all();
+    drain();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return pending_ == 0; });
+    jobs_ = nullptr;
+    return !failed_.load();
+  }
+
+ private:
+  void drain() {
+    const std::vector<PolyJob>& jobs = *jobs_;
+    for (size_t k; (k = next_.fetch_add(1)) < jobs.size();)
+      if (!run_poly_job(jobs[k])) failed_.store(true);
+  }
+  void work() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+      }
+      drain();
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--pending_ == 0) done_cv_.notify_one();
+    }
+  }
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  std::vector<std::thread> workers_;
+  const std::vector<PolyJob>* jobs_ = nullptr;
+  std::atomic<size_t> next_{0};
+  std::atomic<bool> failed_{false};
+  int pending_ = 0;
+  uint64_t gen_ = 0;
+  pid_t pid_;
+};
+
+ParsePool& parse_pool() {
+  // never destroyed: its threads outlive every caller
+  static ParsePool* pool = new ParsePool();
+  return *pool;
+}
+
+// Queries at least this large have their coefficient arrays parsed in
+// parallel (a SeededClientQuery with keys is ~355 KB).
+constexpr size_t PARALLEL_PARSE_MIN_BYTES = 64 * 1024;
+
+// Poly in coefficient form over the context's moduli, into dst[2N].  With
+// `jobs`, the coefficient array is located but parsed later (PolyJob); the
+// array's own checks then run with it.
+bool parse_poly(Json& j, const inspire_params& P, uint64_t* dst, const std::string& what,
+                std::vector<PolyJob>* jobs = nullptr) {
   const size_t plen = 2 * (size_t)P.ring_dim;
   uint64_t moduli[3] = {0, 0, 0};
   size_t ncoeffs = 0, nmod = 0;
   uint64_t dim = 0;
   bool is_ntt = false, have_coeffs = false, have_moduli = false;
+  size_t job = SIZE_MAX;
   const bool ok = j.object([&](const std::string& k) {
     if (k == "coeffs") {
+      if (have_coeffs) return j.fail("duplicate field `coeffs`");  // as serde's derive
       have_coeffs = true;
+      if (jobs) {
+        if (!j.eat('[')) return j.fail("expected '['");
+        const char* lb = j.p - 1;
+        const char* rb = static_cast<const char*>(memchr(j.p, ']', (size_t)(j.end - j.p)));
+        if (!rb) return j.fail("unterminated array");
+        job = jobs->size();
+        jobs->push_back({lb, rb, dst, plen, {0, 0}, P.ring_dim});
+        j.p = rb + 1;
+        ncoeffs = plen;
+        return true;
+      }
       return j.u64_array_into(dst, plen, &ncoeffs);  // parsed in place, checked below
     }
     if (k == "moduli") {
+      if (have_moduli) return j.fail("duplicate field `moduli`");
       have_moduli = true;
       return j.u64_array_into(moduli, 3, &nmod);
     }
@@ -58,6 +180,11 @@ bool parse_poly(Json& j, const inspire_params& P, uint64_t* dst, const std::stri
     return j.fail(what + ": moduli differ from the context");
   if (dim != P.ring_dim || ncoeffs != plen) return j.fail(what + ": dimension mismatch");
   if (is_ntt) return j.fail(what + ": expected coefficient form (is_ntt false)");
+  if (job != SIZE_MAX) {  // count and residues are checked by the job
+    (*jobs)[job].moduli[0] = moduli[0];
+    (*jobs)[job].moduli[1] = moduli[1];
+    return true;
+  }
   for (size_t r = 0; r < 2; r++) {  // residue-major: coefficient i of residue r at r * ring_dim + i
     const uint64_t m = moduli[r], *d = dst + r * P.ring_dim;
     uint64_t bad = 0;
@@ -83,10 +210,7 @@ uint64_t q0_inv_q1(uint64_t q0, uint64_t q1) {
 void poly_json(Out& o, const inspire_params& P, const uint64_t* c) {
   const size_t n = 2 * (size_t)P.ring_dim;
   o.lit("{\"coeffs\":[");
-  for (size_t i = 0; i < n; i++) {
-    if (i) o.ch(',');
-    o.num(c[i]);
-  }
+  o.nums(c, n);
   o.lit("],\"moduli\":[");
   o.num(P.crt_moduli[0]);
   o.ch(',');
@@ -104,10 +228,7 @@ void poly_json(Out& o, const inspire_params& P, const uint64_t* c) {
 // crate's compat tree-packing b has dimension 2 ring_dim).
 void poly_json_dim(Out& o, const inspire_params& P, const uint64_t* c, size_t dim) {
   o.lit("{\"coeffs\":[");
-  for (size_t i = 0; i < 2 * dim; i++) {
-    if (i) o.ch(',');
-    o.num(c[i]);
-  }
+  o.nums(c, 2 * dim);
   o.lit("],\"moduli\":[");
   o.num(P.crt_moduli[0]);
   o.ch(',');
@@ -235,8 +356,9 @@ namespace {
 
 // SeededClientQuery (seeded rows {seed, b}) or ClientQuery (full rows
 // {a, b}, RgswCiphertext rgsw/types.rs:100-110) JSON; see the header.
-int query_from_json(const inspire_params* P, const char* json, size_t len, bool seeded, uint32_t* shard_id,
-                    uint8_t* seeds, uint64_t* rows, int32_t* packing_mode, int32_t* has_keys, uint64_t* y_body) {
+int query_from_json_pass(const inspire_params* P, const char* json, size_t len, bool seeded, uint32_t* shard_id,
+                         uint8_t* seeds, uint64_t* rows, int32_t* packing_mode, int32_t* has_keys, uint64_t* y_body,
+                         std::vector<PolyJob>* jobs) {
   const char* what_q = seeded ? "SeededClientQuery JSON: " : "ClientQuery JSON: ";
   if (!params_ok(P) || !json || !shard_id || (seeded && !seeds) || !rows || !packing_mode || !has_keys)
     return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument or unsupported parameters");
@@ -275,11 +397,11 @@ int query_from_json(const inspire_params* P, const char* json, size_t len, bool 
               }
               if (!seeded && fk == "a") {
                 have_first = true;
-                return parse_poly(j, *P, rows + (2 * i) * plen, "rgsw row a");
+                return parse_poly(j, *P, rows + (2 * i) * plen, "rgsw row a", jobs);
               }
               if (fk == "b") {
                 have_b = true;
-                return parse_poly(j, *P, rows + (seeded ? i : 2 * i + 1) * plen, "rgsw row b");
+                return parse_poly(j, *P, rows + (seeded ? i : 2 * i + 1) * plen, "rgsw row b", jobs);
               }
               return j.skip();
             });
@@ -313,7 +435,7 @@ int query_from_json(const inspire_params* P, const char* json, size_t len, bool 
             if (i >= P->gadget_len) return j.fail("too many y_body polynomials");
             ny = i + 1;
             if (!y_body) return j.skip();
-            return parse_poly(j, *P, y_body + i * plen, "y_body");
+            return parse_poly(j, *P, y_body + i * plen, "y_body", jobs);
           }) && (ny == 0 || ny == P->gadget_len || j.fail("y_body must hold gadget_len polynomials"));
         return j.skip();  // z_body, full_key, num_to_pack
       });
@@ -331,6 +453,22 @@ int query_from_json(const inspire_params* P, const char* json, size_t len, bool 
   *packing_mode = mode;
   *has_keys = keys;
   return INSPIRE_OK;
+}
+
+// Large queries: a structural pass that defers the coefficient arrays, which
+// are then parsed in parallel.  Any failure re-parses the query in one pass,
+// which reports the first error exactly as the sequential parser does.
+int query_from_json(const inspire_params* P, const char* json, size_t len, bool seeded, uint32_t* shard_id,
+                    uint8_t* seeds, uint64_t* rows, int32_t* packing_mode, int32_t* has_keys, uint64_t* y_body) {
+  if (len >= PARALLEL_PARSE_MIN_BYTES && json) {
+    std::vector<PolyJob> jobs;
+    jobs.reserve(16);
+    if (query_from_json_pass(P, json, len, seeded, shard_id, seeds, rows, packing_mode, has_keys, y_body, &jobs) ==
+            INSPIRE_OK &&
+        parse_pool().run(jobs))
+      return INSPIRE_OK;
+  }
+  return query_from_json_pass(P, json, len, seeded, shard_id, seeds, rows, packing_mode, has_keys, y_body, nullptr);
 }
 
 }  // namespace

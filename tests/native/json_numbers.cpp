@@ -97,6 +97,39 @@ int main() {
     Json jz{z.data(), z.data() + z.size(), "", z.data()};
     check(!jz.u64(x), "u64 leading zero " + z);
   }
+  // 4. the writer: Out::num and Out::nums give std::to_string's digits for
+  // every value up to 10^6, around every power of ten, and for 10^6 values
+  // spread over the whole u64 range
+  {
+    uint64_t seed = 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+      seed ^= seed << 13;
+      seed ^= seed >> 7;
+      seed ^= seed << 17;
+      return seed;
+    };
+    std::vector<uint64_t> vals;
+    for (uint64_t v = 0; v <= 1000000; v++) vals.push_back(v);
+    uint64_t p = 1;
+    for (int k = 0; k < 20; k++) {
+      for (uint64_t d : {p - 1, p, p + 1}) vals.push_back(d);
+      if (k < 19) p *= 10;
+    }
+    vals.push_back(18446744073709551615ull);
+    for (int k = 0; k < 1000000; k++) vals.push_back(next() >> (next() & 63));
+    std::string want;
+    igjson::Out o;
+    for (size_t i = 0; i < vals.size(); i++) {
+      o.n = 0;
+      o.num(vals[i]);
+      const std::string w = std::to_string(vals[i]);
+      check(o.n == w.size() && o.s.compare(0, o.n, w) == 0, "num " + w);
+    }
+    o.n = 0;
+    o.nums(vals.data(), 5000);
+    for (size_t i = 0; i < 5000; i++) want += (i ? "," : "") + std::to_string(vals[i]);
+    check(o.n == want.size() && o.s.compare(0, o.n, want) == 0, "nums");
+  }
   if (fails) {
     std::printf("%d failures\n", fails);
     return 1;

@@ -303,3 +303,61 @@ def test_crs_json_writer(wire, tmp_path):
                                   "bold_t_bar": [], "bold_t_hat": [], "num_to_pack": 16, "ring_dim": N, "q": QC},
             "inspiring_w_seed": list(wseed), "inspiring_v_seed": list(vseed), "inspiring_num_columns": 16}
     assert path.read_bytes() == compact(want)
+
+
+def test_large_query_parallel_parse(wire):
+    """Queries of 64 KB and more have their coefficient arrays located by a
+    structural pass and parsed in parallel; any failure re-parses in one pass,
+    so errors read as the sequential parser's.  Also: duplicate fields,
+    nested arrays, and concurrent callers sharing the worker threads."""
+    import threading
+
+    inspire, w = wire
+    rng = np.random.default_rng(8)
+    params = inspire.InspireParams(p=1 << 16)
+    seeds = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+    b_rows, y_body = rand_polys(rng, 6), rand_polys(rng, 3)
+    good = compact(query_obj(5, seeds, b_rows, y_body))
+    assert len(good) > 300_000
+    q = w.seeded_query_from_json(params, good)
+    assert np.array_equal(q.b_rows, b_rows) and np.array_equal(q.inspiring_packing_keys.y_body, y_body)
+    # a bad token in the last y_body polynomial: reported at its byte offset
+    key = b'"y_body":['
+    start = good.index(key) + len(key)
+    for _ in range(2):
+        start = good.index(b'"coeffs":[', start) + len(b'"coeffs":[')
+    start = good.index(b'"coeffs":[', start) + len(b'"coeffs":[')
+    pos = good.index(b",", start + 5000) + 1
+    bad = good[:pos] + b"x" + good[pos + 1:]
+    with pytest.raises(inspire.PirError, match=f"at byte {pos}"):
+        w.seeded_query_from_json(params, bad)
+    # a duplicate coeffs field (serde's derive rejects it)
+    dup = good.replace(b'"coeffs":', b'"coeffs":[1],"coeffs":', 1)
+    with pytest.raises(inspire.PirError, match="duplicate field"):
+        w.seeded_query_from_json(params, dup)
+    # a nested array inside a coefficient array
+    nested = good.replace(b'"coeffs":[', b'"coeffs":[[1],', 1)
+    with pytest.raises(inspire.PirError):
+        w.seeded_query_from_json(params, nested)
+    # concurrent callers: every result exact
+    bodies = []
+    for k in range(8):
+        br, yb = rand_polys(rng, 6), rand_polys(rng, 3)
+        bodies.append((compact(query_obj(k, seeds, br, yb)), br, yb))
+    errors = []
+
+    def worker(k):
+        try:
+            for rep in range(5):
+                body, br, yb = bodies[(k + rep) % len(bodies)]
+                qq = w.seeded_query_from_json(params, body)
+                assert np.array_equal(qq.b_rows, br) and np.array_equal(qq.inspiring_packing_keys.y_body, yb)
+        except BaseException as e:  # reported below
+            errors.append(e)
+
+    ths = [threading.Thread(target=worker, args=(k,)) for k in range(6)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    assert not errors, errors[0]
