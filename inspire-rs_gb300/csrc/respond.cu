@@ -148,12 +148,13 @@ struct Smem {
 // digit transforms run per residue and step.  Per step i (gamma-2 .. 0),
 // residue r's three groups:
 //  [A] (r,0)+(r,1) as one 256-thread team: inverse NTT of R_{i+1} (T[r],
-//      copied to RS[r]); (r,2): first half of the next step's query-only
-//      term R_{i-1} (into the other SCAT buffer);
+//      copied to RS[r]); (r,2): the first 3/8 of the next step's query-only
+//      term R_{i-1} (into the other SCAT buffer; the split that measured
+//      fastest: [A] is the team's inverse transform, [C] has slack);
 //  [B] all threads: CRT compose + digits d0, d1 into T;
 //  [C] (r,0): NTT(d0); SCAT[r] += NTT(d0) w'0 (in place), b += NTT(d0) y'0;
 //      (r,1): NTT(d1); PB1 = NTT(d1) w'1;
-//      (r,2): PB2 = R_{i+1} w'2; second half of R_{i-1};
+//      (r,2): PB2 = R_{i+1} w'2; the rest of R_{i-1};
 //  [D] (r,0): R_i = SCAT[r] + PB1 + PB2 -> T[r] (slots) for the next step;
 //      (r,1): b += NTT(d1) y'1 + R_{i+1} y'2.
 template <int MODE, bool SEEDED, bool QDB>
@@ -323,7 +324,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
 
   const int team_t = tid - 384 * r;  // thread of residue r's (r,0)+(r,1) team, valid for kd < 2
   uint32_t* team_sc = SC + 3 * r * NTT_SCRATCH;  // the team's exchange scratch (two groups' worth)
-  // the next step's query-only term by the (r,2) groups, in two halves
+  // the next step's query-only term by the (r,2) groups, in two parts ([A] and [C])
   auto scatter_next = [&](int i, int u0, int u1) {
     const int sres = MODE == MODE_CRT_FIXED ? r : 0;
     const int sp = MODE == MODE_CRT_FIXED ? x : r * NTT_GT + x;
@@ -351,7 +352,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
 #pragma unroll
       for (int j = 0; j < 8; j++) T[r * N + team_t + 256 * j] = canon2(v[j], q);
     } else if (i >= 1) {
-      scatter_next(i, 0, N / 2);
+      scatter_next(i, 0, 3 * N / 8);
     }
     __syncthreads();
     // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37):
@@ -406,7 +407,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
 #pragma unroll
       for (int j = 0; j < 16; j++) pr[j] = redc_lazy((uint64_t)rs[j] * u4e(wv[j >> 2], j & 3), q, qinv);
       store16(PB2 + r * N, x, pr);
-      if (i >= 1) scatter_next(i, N / 2, N);
+      if (i >= 1) scatter_next(i, 3 * N / 8, N);
     }
     __syncthreads();
     // [D] R_i (group (r,0)); the b accumulator's other two products (group (r,1))
