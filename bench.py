@@ -69,8 +69,8 @@ MULMODS_PER_QUERY = 3.4e6
 DB_BYTES_PER_QUERY = (768 + 64) * 1024
 # dram__bytes_read.sum + dram__bytes_write.sum of one B=128 batch call (queries of 32
 # clients), from one ncu capture of the first timed call on the 2^20-entry database:
-# the Respond launch (95.8 MB) plus its b-side launch (19.7 MB)
-NCU_TRAFFIC_PER_LAUNCH_B128 = 115.5e6
+# the Respond launch (90.6 MB) plus its b-side launch (19.7 MB)
+NCU_TRAFFIC_PER_LAUNCH_B128 = 110.3e6
 
 
 def dist_env():
