@@ -226,7 +226,7 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
       a.what = c->what3.as<uint32_t>();
       a.qdesc = c->d_desc.as<QueryDesc>();
       a.stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
-      CUDA_TRY(launch_respond(a, true, c->stream, 0, c->pair_max));
+      CUDA_TRY(launch_respond(a, true, c->stream, 0, c->pair_max.load()));
       CUDA_TRY(cudaStreamSynchronize(c->stream));
       for (uint32_t i = 0; i < n; i++)
         if (hs[i] != 0)
@@ -298,7 +298,7 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
   int32_t* hs = c->h_qstatus.host<int32_t>();
   for (uint32_t i = 0; i < n; i++) hs[i] = -1;
   a.status = c->h_qstatus.dev<int32_t>();
-  CUDA_TRY(launch_respond(a, seeded, c->stream, 0, c->pair_max));
+  CUDA_TRY(launch_respond(a, seeded, c->stream, 0, c->pair_max.load()));
   CUDA_TRY(cudaMemcpyAsync(out_ct, c->d_out.p, sizeof(uint64_t) * n * 2 * pw, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   for (uint32_t i = 0; i < n; i++)
@@ -527,7 +527,7 @@ int inspire_ctx_create(const inspire_params* prm, int device, int mode, inspire_
     delete c;
     return fail(INSPIRE_ERR_CUDA, "cannot read the SM count");
   }
-  c->pair_max = c->sm_count / 2;
+  c->pair_max.store(c->sm_count / 2);
   // tables per residue: fwd pairs (2N words), inv pairs (2N words), psi_pow (2N)
   const size_t per = 6 * (size_t)N;
   std::vector<uint32_t> host(2 * per);
@@ -753,11 +753,11 @@ int inspire_ctx_set_pair_threshold(inspire_ctx* c, uint32_t max_queries) {
   if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   if (max_queries > (1u << 30)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "max_queries out of range");
   std::lock_guard<std::mutex> lk(c->mu);
-  c->pair_max = (int)max_queries;
+  c->pair_max.store((int)max_queries);
   return INSPIRE_OK;
 }
 
-uint32_t inspire_ctx_pair_threshold(const inspire_ctx* c) { return c ? (uint32_t)c->pair_max : 0; }
+uint32_t inspire_ctx_pair_threshold(const inspire_ctx* c) { return c ? (uint32_t)c->pair_max.load() : 0; }
 
 int inspire_ctx_device_memory(inspire_ctx* c, uint64_t* used, uint64_t* budget) {
   if (!c) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
@@ -1033,7 +1033,7 @@ int inspire_respond_seeded_batch_device_grid(inspire_ctx* c, const inspire_db* d
   a.what = c->what3.as<uint32_t>();
   a.out = d_out_ct;
   a.status = d_status;
-  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream, (int)max_ctas, c->pair_max));
+  CUDA_TRY(launch_respond(a, true, (cudaStream_t)stream, (int)max_ctas, c->pair_max.load()));
   return INSPIRE_OK;
 }
 

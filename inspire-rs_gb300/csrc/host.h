@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -127,7 +128,7 @@ struct inspire_ctx {
   int sm_count = 0;
   // batches of at most this many queries run on the two-CTA cluster kernel
   // (one SM per CRT residue; lower latency while the SMs are not all busy)
-  int pair_max = 0;
+  std::atomic<int> pair_max{0};  // read by serving dispatchers without the lock
   inspire_params params{};
   uint64_t q = 0;  // composite modulus
   ig::DevParams P{};

@@ -122,7 +122,7 @@ int inspire_server::launch(Slot& s, const std::vector<int>& batch) {
   a.what = ctx->what3.as<uint32_t>();
   a.qdesc = s.ddesc.as<QueryDesc>();
   a.stage_wait_iters = cfg.stage_wait_iters;
-  CUDA_TRY(launch_respond(a, true, s.st, 0, ctx->pair_max));
+  CUDA_TRY(launch_respond(a, true, s.st, 0, ctx->pair_max.load()));
   CUDA_TRY(cudaEventRecord(s.ev, s.st));
   return INSPIRE_OK;
 }
@@ -168,14 +168,18 @@ void inspire_server::run() {
         s.recs.clear();
         s.busy = false;
       }
-      size_t inflight_q = 0;
-      for (const auto& sp : slots) inflight_q += sp->busy ? sp->recs.size() : 0;
+      // SMs the batches in flight occupy: batches of at most pair_max
+      // queries run on the two-CTA cluster kernel, two SMs per query
+      const size_t pair_max = (size_t)std::max(0, ctx->pair_max.load(std::memory_order_relaxed));
+      auto sms_of = [&](size_t n) { return n <= pair_max ? 2 * n : n; };
+      size_t inflight_sm = 0;
+      for (const auto& sp : slots) inflight_sm += sp->busy ? sms_of(sp->recs.size()) : 0;
       for (auto& sp : slots) {
         if (sp->busy || pending.empty()) continue;
         // Batch formation: a full batch goes at once; a partial one goes at
         // once while the GPU has idle SMs, else when its oldest query has
         // waited batch_wait_us (the batches in flight keep the GPU busy).
-        if (pending.size() < cfg.max_batch && inflight_q >= (size_t)sm_count &&
+        if (pending.size() < cfg.max_batch && inflight_sm >= (size_t)sm_count &&
             now_ns() - recs[pending.front()].t_enqueue < (int64_t)cfg.batch_wait_us * 1000)
           break;
         Slot& s = *sp;
@@ -188,7 +192,7 @@ void inspire_server::run() {
         }
         s.busy = true;
         n_batches++;
-        inflight_q += s.recs.size();
+        inflight_sm += sms_of(s.recs.size());
         to_launch.push_back(&s);
       }
       bool any_busy = false;

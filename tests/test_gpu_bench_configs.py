@@ -102,6 +102,18 @@ def test_batched_2p24_entries_every_response_bit_exact(big, mode):
     got = d_out.cpu().numpy().view(np.uint64).reshape(B, 2, 2 * N)
     for k in range(B):
         assert np.array_equal(got[k], oracle(sids[k], seeds[k], brows[k], cl[k])), (mode, "device call", k)
+    # a small batch on both Respond kernels: the two-CTA cluster kernel (the
+    # default up to pair_threshold queries) and one CTA per query
+    B = 8
+    sids, locs, cl, seeds, brows = _batch_queries(W, B, forced[::-1])
+    pair = inspire.respond_seeded_batch(crs, edb, sids, seeds, brows, [ids[c] for c in cl])
+    old_threshold = crs.pair_threshold
+    crs.pair_threshold = 0
+    one = inspire.respond_seeded_batch(crs, edb, sids, seeds, brows, [ids[c] for c in cl])
+    crs.pair_threshold = old_threshold
+    assert np.array_equal(pair, one), (mode, "pair vs one CTA")
+    for k in range(B):
+        assert np.array_equal(pair[k], oracle(sids[k], seeds[k], brows[k], cl[k])), (mode, "pair", k)
     # all queries on one shard (the same-shard variant of the batch)
     B = 32
     sids, locs, cl, seeds, brows = _batch_queries(W, B, [8191] * B)
