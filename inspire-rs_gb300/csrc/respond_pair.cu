@@ -19,15 +19,15 @@
 // Per CTA (768 threads, six groups of 128), per step i (gamma-2 .. 0),
 // p = i & 1:
 //  [A] groups 0-1 (a 256-thread team): INTT(R_{i+1}) -> TC[p][r] here and in
-//      the peer CTA; group 2: PB2 = R_{i+1} w'[i][2]; group 3: b += R_{i+1}
-//      y'[i][2]; groups 4-5: first half of the query-only term R_{i-1};
+//      the peer CTA; groups 2-5: first half of the query-only term R_{i-1};
 //      cluster barrier (the peer's residue has arrived);
 //  [B] all: digits d0, d1 of the composite coefficients, in place in TC[p];
 //  [C] group 0: NTT(d0); partial R_i = query-only term + NTT(d0) w'0,
 //      b += NTT(d0) y'0; group 1: NTT(d1); PB1 = NTT(d1) w'1, b += NTT(d1)
-//      y'1; then group 0 sums R_i = partial + PB1 + PB2 into RN;
-//      groups 2-5: second half of R_{i-1}, and the b side (coefficient 0 of
-//      the column products) of one column, two in the last step.
+//      y'1; group 2: PB2 = R_{i+1} w'[i][2]; group 3: b += R_{i+1} y'[i][2];
+//      then (groups 0-3 meet) group 0 sums R_i = partial + PB1 + PB2 into
+//      RN; groups 4-5: second half of R_{i-1}, and the b side (coefficient 0
+//      of the column products) of one column, two in the last step.
 // TC is double-buffered by step parity: the peer writes TC[p] again only in
 // step i - 2, after the cluster barrier of step i - 1, which this CTA reaches
 // only after its last read of TC[p].  The only other remote writes are the
@@ -334,33 +334,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
         TC[r * N + tid + 256 * j] = c;
         st_peer(rbase + 4u * 256u * (uint32_t)j, c);
       }
-    } else if (g == 2) {
-      uint4 wv[4];
-      key_run(A.what + ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x, wv);
-      uint32_t rs[16], pr[16];
-      load16(RN, x, rs);
-#pragma unroll
-      for (int j = 0; j < 16; j++) pr[j] = redc_lazy((uint64_t)rs[j] * u4e(wv[j >> 2], j & 3), q, qinv);
-      store16(PB2, x, pr);
-    } else if (g == 3) {
-      uint4 k2[4];
-      key_run(Y + ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x - yoff, k2);
-      if (ybody) rotate_key_run(k2, i, x);
-      uint32_t* accb = ACC + 2 * N;
-#pragma unroll
-      for (int r4 = 0; r4 < 4; r4++) {
-        const int o = 16 * x + 4 * (r4 ^ f);
-        const uint4 rr = *reinterpret_cast<const uint4*>(RN + o);
-        uint4* ap = reinterpret_cast<uint4*>(accb + o);
-        const uint4 a4 = *ap;
-        uint32_t ab[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++)
-          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)u4e(rr, e) * u4e(k2[r4], e), q, qinv), q2);
-        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
-      }
     } else if (i >= 1) {
-      scatter_next(i, tid - 4 * NTT_GT, 2 * NTT_GT, 0, N / 2);
+      scatter_next(i, tid - 2 * NTT_GT, 4 * NTT_GT, 0, N / 2);  // groups 2-5
     }
     cluster_sync_all();
     // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37):
@@ -402,7 +377,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
         *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
         *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);
       }
-      named_sync(8, 2 * NTT_GT);  // PB1 and the partial R_i are complete
+      named_sync(8, 4 * NTT_GT);  // PB1, PB2, the partial R_i are complete; R_{i+1} no longer read
       if (kd == 0) {
 #pragma unroll
         for (int r4 = 0; r4 < 4; r4++) {
@@ -421,24 +396,60 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(RBLOCK, 1)
           *reinterpret_cast<uint4*>(RN + o) = make_uint4(outv[0], outv[1], outv[2], outv[3]);  // R_i
         }
       }
+    } else if (g == 2) {
+      // PB2 = R_{i+1} w'2
+      uint4 wv[4];
+      key_run(A.what + ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x, wv);
+      uint32_t rs[16], pr[16];
+      load16(RN, x, rs);
+#pragma unroll
+      for (int j = 0; j < 16; j++) pr[j] = redc_lazy((uint64_t)rs[j] * u4e(wv[j >> 2], j & 3), q, qinv);
+      store16(PB2, x, pr);
+      named_sync(8, 4 * NTT_GT);
+    } else if (g == 3) {
+      // b += R_{i+1} y'2
+      uint4 k2[4];
+      key_run(Y + ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x - yoff, k2);
+      if (ybody) rotate_key_run(k2, i, x);
+      uint32_t* accb = ACC + 2 * N;
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        const int o = 16 * x + 4 * (r4 ^ f);
+        const uint4 rr = *reinterpret_cast<const uint4*>(RN + o);
+        uint4* ap = reinterpret_cast<uint4*>(accb + o);
+        const uint4 a4 = *ap;
+        uint32_t ab[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)u4e(rr, e) * u4e(k2[r4], e), q, qinv), q2);
+        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
+      }
+      named_sync(8, 4 * NTT_GT);
     } else {
-      // groups 2-5: the second half of R_{i-1}, and the b side of this
+      // groups 4-5: the second half of R_{i-1}, and the b side of this
       // step's columns (step gamma-2-i takes column gamma-2-i; the last step
       // also column gamma-1)
-      const int t = tid - 2 * NTT_GT;
+      const int t = tid - 4 * NTT_GT;
       const int c0 = gamma - 2 - i;
       const bool two = i == 0;
       const uint32_t* h0 = reinterpret_cast<const uint32_t*>(H + (size_t)c0 * N);
       const uint32_t* h1 = reinterpret_cast<const uint32_t*>(H + (size_t)(gamma - 1) * N);
-      const uint32_t w0 = __ldg(h0 + t), w1 = __ldg(h0 + t + 512);
-      uint32_t w2 = 0, w3 = 0;
+      const uint32_t w0 = __ldg(h0 + t), w1 = __ldg(h0 + t + 512), w2 = __ldg(h0 + t + 256),
+                     w3 = __ldg(h0 + t + 768);
+      uint32_t w4 = 0, w5 = 0, w6 = 0, w7 = 0;
       if (two) {
-        w2 = __ldg(h1 + t);
-        w3 = __ldg(h1 + t + 512);
+        w4 = __ldg(h1 + t);
+        w5 = __ldg(h1 + t + 512);
+        w6 = __ldg(h1 + t + 256);
+        w7 = __ldg(h1 + t + 768);
       }
-      if (i >= 1) scatter_next(i, t, 4 * NTT_GT, N / 2, N);
+      if (i >= 1) scatter_next(i, t, 2 * NTT_GT, N / 2, N);
       column_b0_part(P, w0, w1, BP, t, b0sum + c0);
-      if (two) column_b0_part(P, w2, w3, BP, t, b0sum + gamma - 1);
+      column_b0_part(P, w2, w3, BP, t + 256, b0sum + c0);
+      if (two) {
+        column_b0_part(P, w4, w5, BP, t, b0sum + gamma - 1);
+        column_b0_part(P, w6, w7, BP, t + 256, b0sum + gamma - 1);
+      }
     }
     __syncthreads();
   }
