@@ -31,7 +31,10 @@ __device__ __forceinline__ void chacha20_block(const uint32_t key[8], uint64_t c
   uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];
   uint32_t x8 = key[4], x9 = key[5], x10 = key[6], x11 = key[7];
   uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = 0, x15 = 0;
-#pragma unroll
+  // a loop, not unrolled: the rounds' dependencies leave no cross-round
+  // overlap to gain, and the unrolled body (~1000 instructions) measured
+  // slower in the kernels that expand once per query (instruction fetch)
+#pragma unroll 1
   for (int i = 0; i < 10; i++) {
     IG_QR(x0, x4, x8, x12);
     IG_QR(x1, x5, x9, x13);
