@@ -361,3 +361,43 @@ def test_large_query_parallel_parse(wire):
     for th in ths:
         th.join()
     assert not errors, errors[0]
+
+
+def test_query_json_mutations_differential(wire):
+    """Random single-byte mutations of a full-size SeededClientQuery (the
+    parallel-parse path): the native parser accepts a body only if Python's
+    json accepts it, and then returns exactly the values json reads (when the
+    crate's field rules hold) -- never a silently different query."""
+    inspire, w = wire
+    rng = np.random.default_rng(77)
+    params = inspire.InspireParams(p=1 << 16)
+    seeds = rng.integers(0, 256, size=(6, 32), dtype=np.uint8)
+    b_rows, y_body = rand_polys(rng, 6), rand_polys(rng, 3)
+    good = compact(query_obj(9, seeds, b_rows, y_body))
+    alphabet = b'0123456789,[]{}":-. eEtrufalsnx'
+    accepted = 0
+    for trial in range(300):
+        body = bytearray(good)
+        for _ in range(int(rng.integers(1, 3))):
+            pos = int(rng.integers(0, len(body)))
+            body[pos] = alphabet[int(rng.integers(0, len(alphabet)))]
+        body = bytes(body)
+        try:
+            ref = json.loads(body)
+        except ValueError:
+            ref = None
+        try:
+            q = w.seeded_query_from_json(params, body)
+        except inspire.PirError:
+            continue
+        assert ref is not None, "native parser accepted a body json rejects"
+        accepted += 1
+        rows = ref["rgsw_ciphertext"]["rows"]
+        assert q.shard_id == ref["shard_id"]
+        assert np.array_equal(q.seeds, np.array([r["seed"] for r in rows], dtype=np.uint8))
+        assert np.array_equal(q.b_rows, np.array([r["b"]["coeffs"] for r in rows], dtype=np.uint64))
+        keys = ref.get("inspiring_packing_keys")
+        if keys is not None and keys.get("y_body"):
+            assert np.array_equal(q.inspiring_packing_keys.y_body,
+                                  np.array([p["coeffs"] for p in keys["y_body"]], dtype=np.uint64))
+    assert accepted > 20  # mutations inside numbers that keep the residues reduced
