@@ -17,9 +17,10 @@ response is decrypted and extracted on the device with its client's key.
           responses written back to pinned host memory, all inside the timed
           region.  The synchronous host-buffer batch call
           (inspire_respond_seeded_batch) is reported beside it.
-  serving: Poisson arrivals at swept rates through the same loop, p50/p99
-          latency; the mixed workload adds 8 resident databases of 2^18..2^26
-          entries.
+  serving: Poisson arrivals at swept rates through the same loop, submitted
+          at their arrival times by the library's native driver
+          (inspire_server_drive), p50/p99 latency from the scheduled arrival;
+          the mixed workload adds 8 resident databases of 2^18..2^26 entries.
   small batches (batch_sweep_qps, plain_single_query_host): launches of at
           most pair_threshold queries run on the two-CTA cluster kernel (one
           SM per CRT residue); *_one_cta repeats them on one CTA per query.
@@ -1159,17 +1160,23 @@ def serve_bench(inspire, crs, edb, nshards, clients, client_of, qcid, locals_, s
     closed = max((closed_run(srv, main, t) for t in (4, 8)), key=lambda r: r["achieved_qps"])
     check(closed.pop("samples"), [db_raw], None)
     cap = closed["achieved_qps"]
-    sv.run(srv, main, pool, cid, rate=0.25 * cap, duration_s=0.5, n_threads=4, seed=10)  # open-loop warm-up
+    # open loop: arrivals submitted by the library's native driver (a
+    # scripting-language submitter adds its own scheduling delay), one
+    # sample of responses checked per run
+    sv.run_native(srv, main, pool, cid, rate=0.25 * cap, duration_s=0.5, seed=10)  # warm-up
     sweep = []
     for frac in SERVE_RATE_FRACS:
-        r = sv.run(srv, main, pool, cid, rate=frac * cap, duration_s=SERVE_DURATION_S, n_threads=4, seed=11)
+        r = sv.run_native(srv, main, pool, cid, rate=frac * cap, duration_s=SERVE_DURATION_S, seed=11,
+                          keep_outputs=True)
+        check(r.pop("samples"), [db_raw], None)
         r["load_frac"] = frac
         sweep.append(r)
     head = next((r for r in sweep if r["load_frac"] == 0.75), sweep[-1])
     out = {"config": {**cfg, "capacity": 8192, "submitter_threads": closed["submitter_threads"],
                       "autotune": tuned["table"],
                       "query_rows": "pinned host memory, borrowed (read in place by the GPU)",
-                      "arrivals": "Poisson, offered rate = fraction x saturated closed-loop rate",
+                      "arrivals": "Poisson, offered rate = fraction x saturated closed-loop rate; submitted at "
+                                  "their arrival times by the library's native driver (inspire_server_drive)",
                       "database": f"{nshards * N} entries x 32 B"},
            "closed_loop": closed, "burst": burst, "open_loop": sweep,
            "headline": {"p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"], "offered_qps": head["offered_qps"],
@@ -1193,10 +1200,12 @@ def serve_bench(inspire, crs, edb, nshards, clients, client_of, qcid, locals_, s
         mclosed = closed_run(srv, targets, closed["submitter_threads"])
         check(mclosed.pop("samples"), raws, None)
         mcap = mclosed["achieved_qps"]
-        sv.run(srv, targets, pool, cid, rate=0.25 * mcap, duration_s=0.5, n_threads=4, seed=10)  # warm-up
+        sv.run_native(srv, targets, pool, cid, rate=0.25 * mcap, duration_s=0.5, seed=10)  # warm-up
         msweep = []
         for frac in (0.5, 0.75, 0.9):
-            r = sv.run(srv, targets, pool, cid, rate=frac * mcap, duration_s=SERVE_DURATION_S, n_threads=4, seed=12)
+            r = sv.run_native(srv, targets, pool, cid, rate=frac * mcap, duration_s=SERVE_DURATION_S, seed=12,
+                              keep_outputs=True)
+            check(r.pop("samples"), raws, None)
             r["load_frac"] = frac
             msweep.append(r)
         out["mixed"] = {"databases_log2_entries": list(MIXED_LOG2_SIZES),

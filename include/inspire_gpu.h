@@ -419,6 +419,24 @@ int inspire_server_poll(inspire_server *srv, uint64_t ticket, uint64_t *out_ct, 
 int inspire_server_poll_batch(inspire_server *srv, uint32_t n, const uint64_t *tickets, uint64_t *out_ct,
                               int64_t *done_ns, int32_t timeout_us, uint32_t *collected);
 
+/* Open-loop load driven natively (no reference counterpart; for measuring the
+ * loop without a scripting-language load generator's own delays): query k
+ * (k < n) is submitted at arrival_ns[k] (the inspire_now_ns clock, in
+ * non-decreasing order) by the calling thread, which spins on the clock and
+ * puts every query already due into one inspire_server_submit call (at most
+ * max_burst, 0 = 256), retrying on backpressure; a second thread collects
+ * the tickets in order.  Query k's rows are entry k mod pool_size of the
+ * pool (pool_seeds: pool_size x 2*gadget_len x 32 bytes; pool_b_rows:
+ * pool_size x 2*gadget_len x 2N u64; flags as for inspire_server_submit);
+ * dbs, shard_ids and client_ids are per query.  done_ns[k] receives each
+ * completion time, submit_ns[k] (may be NULL) the time of its submission
+ * call, and out_keep the responses of the first n_keep queries (n_keep x
+ * [a poly, b poly]).  Latency from arrival is done_ns - arrival_ns. */
+int inspire_server_drive(inspire_server *srv, uint32_t n, const inspire_db *const *dbs, const uint32_t *shard_ids,
+                         const int32_t *client_ids, const uint8_t *pool_seeds, const uint64_t *pool_b_rows,
+                         uint32_t pool_size, const int64_t *arrival_ns, uint32_t flags, uint32_t max_burst,
+                         int64_t *submit_ns, int64_t *done_ns, uint32_t n_keep, uint64_t *out_keep);
+
 int inspire_server_get_stats(inspire_server *srv, inspire_server_stats *out);
 
 /* Monotonic clock of the serving loop's timestamps (CLOCK_MONOTONIC, ns). */

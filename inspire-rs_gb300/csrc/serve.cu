@@ -12,6 +12,7 @@
 // kernel runs.  Batches on different streams overlap on the device, which
 // also fills the SMs a single batch leaves idle.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <condition_variable>
@@ -582,6 +583,89 @@ int inspire_server_poll_batch(inspire_server* s, uint32_t n, const uint64_t* tic
     if (rc != INSPIRE_OK) return rc;
     *collected = k + 1;
   }
+  return INSPIRE_OK;
+}
+
+int inspire_server_drive(inspire_server* s, uint32_t n, const inspire_db* const* dbs, const uint32_t* shard_ids,
+                         const int32_t* client_ids, const uint8_t* pool_seeds, const uint64_t* pool_b_rows,
+                         uint32_t pool_size, const int64_t* arrival_ns, uint32_t flags, uint32_t max_burst,
+                         int64_t* submit_ns, int64_t* done_ns, uint32_t n_keep, uint64_t* out_keep) {
+  if (!s || (n && (!dbs || !shard_ids || !client_ids || !pool_seeds || !pool_b_rows || !arrival_ns || !done_ns ||
+                   pool_size == 0 || (n_keep && !out_keep))))
+    return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
+  if (n_keep > n) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "n_keep above n");
+  for (uint32_t k = 1; k < n; k++)
+    if (arrival_ns[k] < arrival_ns[k - 1]) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "arrivals not in order");
+  if (max_burst == 0) max_burst = 256;
+  const size_t pw = poly_words();
+  const size_t seed_bytes = (size_t)64 * ELL, row_words = (size_t)2 * ELL * pw;
+  std::vector<uint64_t> tickets(n);
+  std::atomic<uint32_t> n_sub{0};
+  std::atomic<int> stop_rc{INSPIRE_OK};
+  std::string collector_err;
+  // collector: every ticket in submission order, its completion time (the
+  // serving loop's) and, for the first n_keep queries, the response
+  std::thread collector([&] {
+    uint32_t k = 0;
+    while (k < n && stop_rc.load() == INSPIRE_OK) {
+      if (k >= n_sub.load(std::memory_order_acquire)) {
+        std::this_thread::yield();
+        continue;
+      }
+      const int rc = inspire_server_poll(s, tickets[k], k < n_keep ? out_keep + (size_t)k * 2 * pw : nullptr,
+                                         done_ns + k, 2000);
+      if (rc == INSPIRE_PENDING) continue;
+      if (rc != INSPIRE_OK) {
+        collector_err = g_last_error;
+        int expected = INSPIRE_OK;
+        stop_rc.compare_exchange_strong(expected, rc);
+        break;
+      }
+      k++;
+    }
+  });
+  // submitter (this thread): each query at its arrival time, every query
+  // already due in one call (one contiguous run of the pool), retrying on
+  // backpressure
+  uint32_t k = 0;
+  int rc = INSPIRE_OK;
+  std::string submit_err;
+  while (k < n && stop_rc.load() == INSPIRE_OK) {
+    const int64_t now = now_ns();
+    if (arrival_ns[k] > now) {
+      const int64_t gap = arrival_ns[k] - now;
+      if (gap > 200000) std::this_thread::sleep_for(std::chrono::nanoseconds(gap - 100000));
+      continue;  // spin the last 100 us
+    }
+    const uint32_t pk = k % pool_size;
+    uint32_t j = k + 1;
+    while (j < n && j - k < max_burst && j - k < pool_size - pk && arrival_ns[j] <= now) j++;
+    uint32_t acc = 0;
+    const int64_t t_call = now_ns();
+    rc = inspire_server_submit(s, j - k, dbs + k, shard_ids + k, pool_seeds + (size_t)pk * seed_bytes,
+                               pool_b_rows + (size_t)pk * row_words, client_ids + k, arrival_ns + k, flags,
+                               tickets.data() + k, &acc);
+    if (acc) {
+      if (submit_ns)
+        for (uint32_t i = k; i < k + acc; i++) submit_ns[i] = t_call;
+      k += acc;
+      n_sub.store(k, std::memory_order_release);
+    }
+    if (rc == INSPIRE_ERR_BUSY) {
+      std::this_thread::yield();
+      continue;
+    }
+    if (rc != INSPIRE_OK) {
+      submit_err = g_last_error;
+      int expected = INSPIRE_OK;
+      stop_rc.compare_exchange_strong(expected, rc);
+      break;
+    }
+  }
+  collector.join();
+  const int final_rc = stop_rc.load();
+  if (final_rc != INSPIRE_OK)
+    return fail(final_rc, "drive: " + (submit_err.empty() ? collector_err : submit_err));
   return INSPIRE_OK;
 }
 

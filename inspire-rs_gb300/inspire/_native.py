@@ -164,6 +164,7 @@ def load(path: str = LIB_PATH):
         "inspire_pinned_free": (None, [vp]),
         "inspire_server_poll": (C.c_int, [vp, u64, vp, C.POINTER(C.c_int64), i32]),
         "inspire_server_poll_batch": (C.c_int, [vp, u32, vp, vp, vp, i32, C.POINTER(u32)]),
+        "inspire_server_drive": (C.c_int, [vp, u32, vp, vp, vp, vp, vp, u32, vp, u32, u32, vp, vp, u32, vp]),
         "inspire_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStatsC)]),
         "inspire_now_ns": (C.c_int64, []),
         "inspire_mulmod_rate_device": (C.c_int, [vp, u32, u32, vp, vp]),

@@ -784,6 +784,37 @@ class Server:
             raise PirError(nat.last_error(), rc)
         return done[:got.value]
 
+    def drive(self, db_handles, shard_ids, client_ids, pool_seeds: np.ndarray, pool_b_rows: np.ndarray,
+              arrival_ns: np.ndarray, borrow: bool = False, max_burst: int = 256, n_keep: int = 0):
+        """Open-loop load driven natively (inspire_server_drive): query k is
+        submitted at arrival_ns[k] (now_ns clock, non-decreasing) with the
+        rows of pool entry k mod len(pool_seeds), by a native thread spinning
+        on the clock; a second native thread collects.  db_handles
+        (handle_of values), shard_ids and client_ids are per query.  Returns
+        (submit_ns, done_ns, responses of the first n_keep queries or None)."""
+        arr = np.ascontiguousarray(arrival_ns, dtype=np.int64)
+        n = arr.size
+        dbs = np.ascontiguousarray(db_handles, dtype=np.uint64)
+        sid = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+        cid = np.ascontiguousarray(client_ids, dtype=np.int32)
+        if dbs.size != n or sid.size != n or cid.size != n:
+            raise ValueError("one database, shard and client per query")
+        if borrow:
+            sd, br = pool_seeds, pool_b_rows
+            if not (sd.flags.c_contiguous and br.flags.c_contiguous and sd.dtype == np.uint8 and
+                    br.dtype == np.uint64):
+                raise ValueError("borrowed rows must be C-contiguous uint8 seeds / uint64 b_rows")
+        else:
+            sd = np.ascontiguousarray(pool_seeds, dtype=np.uint8)
+            br = _u64(pool_b_rows)
+        submit = np.zeros(n, dtype=np.int64)
+        done = np.zeros(n, dtype=np.int64)
+        keep = np.zeros((n_keep, 2, self.plen), dtype=np.uint64) if n_keep else None
+        _check(self.L.inspire_server_drive(self.h, n, _ptr(dbs), _ptr(sid), _ptr(cid), _ptr(sd), _ptr(br),
+                                           sd.shape[0], _ptr(arr), nat.SUBMIT_BORROW if borrow else 0, max_burst,
+                                           _ptr(submit), _ptr(done), n_keep, _ptr(keep)))
+        return submit, done, keep
+
     def stats(self) -> dict:
         st = nat.ServerStatsC()
         _check(self.L.inspire_server_get_stats(self.h, C.byref(st)))

@@ -304,3 +304,39 @@ def autotune(make_server, targets: List[Target], pool: QueryPool, client_id: int
                               "qps": r["achieved_qps"], "p50_ms": r["p50_ms"]})
     best = max(table, key=lambda t: t["qps"])
     return {"best": {k: best[k] for k in ("max_batch", "max_inflight", "batch_wait_us")}, "table": table}
+
+def run_native(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate: float,
+               duration_s: float = 2.0, seed: int = 0, keep_outputs: bool = False, settle_frac: float = 0.1,
+               max_burst: int = 256) -> dict:
+    """Open loop at `rate` q/s for duration_s, driven by the library's native
+    submitter and collector threads (Server.drive): Poisson arrivals, query
+    k on pool entry k mod Q, database and shard drawn as in run().  Returns
+    latency_summary() from the scheduled arrival, the same from the
+    submission call (from_submit_*), the offered rate and, if keep_outputs,
+    a few (db_idx, shard, pool_idx, response) samples."""
+    rng = np.random.default_rng(seed)
+    handles = np.array([server.handle_of(t.db) for t in targets], dtype=np.uint64)
+    offs = poisson_offsets_ns(rate, duration_s, rng)
+    n = len(offs)
+    dbi, shards = _choose(targets, n, rng)
+    pidx = np.arange(n) % pool.q
+    cids = pool.client_ids[pidx] if pool.client_ids is not None else np.full(n, client_id, np.int32)
+    t0 = now_ns() + 20_000_000
+    arrivals = t0 + offs
+    n_keep = min(16, n) if keep_outputs else 0
+    gc_was_enabled = gc.isenabled()
+    gc.disable()
+    try:
+        sub, done, kept = server.drive(handles[dbi], shards, cids, pool.seeds, pool.b_rows, arrivals,
+                                       borrow=pool.borrow, max_burst=max_burst, n_keep=n_keep)
+    finally:
+        if gc_was_enabled:
+            gc.enable()
+    keep = arrivals >= t0 + int(settle_frac * duration_s * 1e9)
+    out = latency_summary(arrivals[keep], done[keep])
+    fs = latency_summary(sub[keep], done[keep])
+    out.update({"from_submit_p50_ms": fs.get("p50_ms"), "from_submit_p99_ms": fs.get("p99_ms"),
+                "n_total": int(n), "offered_qps": rate, "driver": "native (Server.drive)"})
+    if keep_outputs:
+        out["samples"] = [(int(dbi[k]), int(shards[k]), int(pidx[k]), kept[k]) for k in range(n_keep)]
+    return out

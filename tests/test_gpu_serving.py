@@ -341,3 +341,48 @@ def test_admission_by_device_memory(oracle_mod):
     backend.close()
     edb.close()
     crs.close()
+
+
+def test_native_open_loop_driver(world):
+    """Server.drive (inspire_server_drive): queries submitted at their
+    arrival times by the library's own threads, through backpressure (more
+    queries than slots); every query is submitted no earlier than its arrival
+    and completes after it, and the kept responses equal the queries'
+    responses alone."""
+    W = world
+    inspire = W["inspire"]
+    from inspire.pir import now_ns
+
+    qs = make_queries(W, 8)
+    want = [alone(W, q) for q in qs]
+    pool_seeds = np.ascontiguousarray(np.stack([q["seeds"] for q in qs]))
+    pool_rows = np.ascontiguousarray(np.stack([q["b_rows"] for q in qs]))
+    n = 3000
+    srv = inspire.Server(W["crs"], max_batch=64, max_inflight=4, capacity=256)
+    try:
+        handles = np.array([srv.handle_of(W["dbs"][qs[k % 8]["db"]]) for k in range(n)], dtype=np.uint64)
+        shards = np.array([qs[k % 8]["shard"] for k in range(n)], dtype=np.uint32)
+        cids = np.array([W["ids"][qs[k % 8]["client"]] for k in range(n)], dtype=np.int32)
+        gaps = np.random.default_rng(5).exponential(1e9 / 200_000, size=n).astype(np.int64)  # ~200 K q/s
+        arrivals = now_ns() + 5_000_000 + np.cumsum(gaps)
+        sub, done, kept = srv.drive(handles, shards, cids, pool_seeds, pool_rows, arrivals, n_keep=16)
+        assert (sub >= arrivals).all() and (done >= arrivals).all()
+        for k in range(16):
+            assert np.array_equal(kept[k], want[k % 8]), k
+        st = srv.stats()
+        assert st["completed"] == n and st["pending"] == 0
+        # borrowed rows from page-locked memory
+        ps = inspire.PinnedBuffer(pool_seeds.shape, np.uint8)
+        pr = inspire.PinnedBuffer(pool_rows.shape, np.uint64)
+        ps.array[:] = pool_seeds
+        pr.array[:] = pool_rows
+        arrivals = now_ns() + 2_000_000 + np.cumsum(gaps[:500])
+        _, done, kept = srv.drive(handles[:500], shards[:500], cids[:500], ps.array, pr.array, arrivals, borrow=True,
+                                  n_keep=8)
+        assert (done >= arrivals).all()
+        for k in range(8):
+            assert np.array_equal(kept[k], want[k]), k
+        ps.close()
+        pr.close()
+    finally:
+        srv.close()
