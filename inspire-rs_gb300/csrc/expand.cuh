@@ -13,6 +13,12 @@ constexpr int SUB = 256;              // threads of one expansion sub-block
 __device__ __forceinline__ void named_sync(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
+// Arrive at named barrier `id` without waiting (the other participants wait
+// in named_sync); orders this thread's earlier shared-memory accesses before
+// theirs after the barrier.
+__device__ __forceinline__ void named_arrive(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
 
 // Exclusive scan over one 256-thread sub-block (lt = thread index in it);
 // ws needs 17 ints.

@@ -176,7 +176,7 @@ cudaError_t launch_client_keys(const KeyGenArgs& a, int n, cudaStream_t st);
 size_t nopacking_smem_bytes();
 cudaError_t launch_nopacking(const NoPackingArgs& a, bool seeded, cudaStream_t st);
 
-size_t respond_smem_bytes(int mode);
+size_t respond_smem_bytes(int mode, bool qdb);
 // max_ctas > 0 caps the grid: each CTA then answers several queries in turn.
 // Otherwise batches of at most pair_max queries run on the two-CTA cluster
 // kernel (respond_pair.cu), larger ones on the one-CTA kernel.

@@ -120,22 +120,26 @@ __global__ void __launch_bounds__(BSIDE_THREADS) bside_kernel(const __grid_const
   if (threadIdx.x < 32) b_parking(A.out, qi)[threadIdx.x] = bpoly[threadIdx.x];
 }
 
-// Shared-memory layout in u32 words (NR = residues of the a side).
-template <int NR>
+// Shared-memory layout in u32 words (NR = residues of the a side).  The
+// device-row variant needs 179.5 KiB, so the SM's carveout leaves 60 KiB of
+// L1 (it holds the transforms' twiddle tables); the serving variant 195.5 KiB.
+template <int NR, bool QDB>
 struct Smem {
   static constexpr int AHAT = 0;                    // [ELL][NR][N] row transforms
   static constexpr int SC = AHAT + ELL * NR * N;    // [RG][NTT_SCRATCH] per-group exchange scratch
   static constexpr int T = SC + RG * NTT_SCRATCH;   // [2][N] R_{i+1} (slots) -> its inverse (coefficients) -> digits d0, d1
-  static constexpr int RS = T + 2 * N;              // [2][N] copy of R_{i+1} (slots)
-  static constexpr int PB1 = RS + 2 * N;            // [2][N] NTT(d1) w'[i][1]
-  static constexpr int PB2 = PB1 + 2 * N;           // [2][N] R_{i+1} w'[i][2]
-  static constexpr int SCAT = PB2 + 2 * N;          // [2 steps][2][N] query-only term of R_i (slots), then partial R_i
+  static constexpr int PB1 = T + 2 * N;             // [2][N] NTT(d1) w'[i][1]
+  static constexpr int SCAT = PB1 + 2 * N;          // [2 steps][2][N] query-only term of R_i (slots), then partial R_i
   static constexpr int ACC = SCAT + 4 * N;          // [2][N] b accumulators
-  // T..ACC+2N (14N words) also hold the query's raw b rows (u64, 12N words)
-  // until the b side; T..PB1 (6N words) the unseeded rows' a parts
-  static constexpr int MISC = ACC + 2 * N;          // bpoly[32], ws[3][20], staged seeds (96 B), mbarrier
+  // T..T+6N also hold the unseeded rows' a parts; the serving variant stages
+  // the query's raw b rows (u64, 12N words) from T on until the b side
+  static constexpr int MISC = ACC + 2 * N + (QDB ? 2 * N : 0);  // bpoly[32], ws[3][20], staged seeds (96 B), mbarrier
   static constexpr int TOTAL = MISC + 128;
 };
+
+// Slots of the next step's query-only term computed by group (r,2) in [A];
+// the rest follow in [C].
+constexpr int SCATTER_SPLIT = N / 8;
 
 // One query (index qi) by the whole CTA; every return is uniform over the CTA.
 //
@@ -147,27 +151,25 @@ struct Smem {
 // k'0 NTT(d0) + k'1 NTT(d1) + k'2 R_{i+1}, so d2 is never formed and only two
 // digit transforms run per residue and step.  Per step i (gamma-2 .. 0),
 // residue r's three groups:
-//  [A] (r,0)+(r,1) as one 256-thread team: inverse NTT of R_{i+1} (T[r],
-//      copied to RS[r]); (r,2): the first 3/8 of the next step's query-only
-//      term R_{i-1} (into the other SCAT buffer; the split that measured
-//      fastest: [A] is the team's inverse transform, [C] has slack);
+//  [A] (r,0)+(r,1) as one 256-thread team: inverse NTT of R_{i+1} (T[r]),
+//      written back to T[r] once (r,2) has read it (named barrier 9 + r);
+//      (r,2): SCAT[r] += R_{i+1} w'2 and the second b accumulator += R_{i+1}
+//      y'2, then the first part of the next step's query-only term R_{i-1}
+//      (into the other SCAT buffer);
 //  [B] all threads: CRT compose + digits d0, d1 into T;
 //  [C] (r,0): NTT(d0); SCAT[r] += NTT(d0) w'0 (in place), b += NTT(d0) y'0;
-//      (r,1): NTT(d1); PB1 = NTT(d1) w'1;
-//      (r,2): PB2 = R_{i+1} w'2; the rest of R_{i-1};
-//  [D] (r,0): R_i = SCAT[r] + PB1 + PB2 -> T[r] (slots) for the next step;
-//      (r,1): b += NTT(d1) y'1 + R_{i+1} y'2.
+//      (r,1): NTT(d1); PB1 = NTT(d1) w'1, second b accumulator += NTT(d1) y'1;
+//      (r,2): the rest of R_{i-1};
+//  [D] (r,0): R_i = SCAT[r] + PB1 -> T[r] (slots) for the next step.
 template <int MODE, bool SEEDED, bool QDB>
 __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
-  using L = Smem<NR>;
+  using L = Smem<NR, QDB>;
   extern __shared__ __align__(16) uint32_t smem[];
   uint32_t* Ahat = smem + L::AHAT;
   uint32_t* SC = smem + L::SC;
   uint32_t* T = smem + L::T;
-  uint32_t* RS = smem + L::RS;
   uint32_t* PB1 = smem + L::PB1;
-  uint32_t* PB2 = smem + L::PB2;
   uint32_t* SCAT = smem + L::SCAT;
   uint32_t* bpoly = smem + L::MISC;
   int* wsb = (int*)(smem + L::MISC + 32);
@@ -338,21 +340,47 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     const size_t yoff = ybody ? (size_t)i * ELL * 2 * N : 0;  // body tables: the key slices of i = 0, rotated
     if (tid == 0 && i >= 2)  // the block the next step's scatter reads (R_{i-2})
       for (int rr = 0; rr < NR; rr++) prefetch_l2(Eg_at(rr) + (size_t)(i - 2) * ELL * N, sizeof(uint32_t) * ELL * N);
-    // [A] inverse NTT of R_{i+1} by residue r's team; RS keeps R_{i+1}
+    // [A] inverse NTT of R_{i+1} by residue r's team; the products of
+    //     R_{i+1} with the third key slices by group (r,2)
     if (kd < 2) {
       uint32_t v[8];
       const int s0 = 8 * team_t;
       const uint4 lo = *reinterpret_cast<const uint4*>(T + r * N + swz(s0));
       const uint4 hi = *reinterpret_cast<const uint4*>(T + r * N + swz(s0 + 4));
-      *reinterpret_cast<uint4*>(RS + r * N + swz(s0)) = lo;
-      *reinterpret_cast<uint4*>(RS + r * N + swz(s0 + 4)) = hi;
       v[0] = lo.x; v[1] = lo.y; v[2] = lo.z; v[3] = lo.w;
       v[4] = hi.x; v[5] = hi.y; v[6] = hi.z; v[7] = hi.w;
       ntt_inv_noscale8(v, team_sc, inv_tw(C), q, team_t, 7 + r);
+      named_sync(9 + r, 3 * NTT_GT);  // group (r,2) has read R_{i+1}
 #pragma unroll
       for (int j = 0; j < 8; j++) T[r * N + team_t + 256 * j] = canon2(v[j], q);
-    } else if (i >= 1) {
-      scatter_next(i, 0, 3 * N / 8);
+    } else {
+      uint32_t rs[16];
+      load16(T + r * N, x, rs);
+      named_arrive(9 + r, 3 * NTT_GT);
+      const size_t off2 = ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x;
+      uint4 wv[4], yv[4];
+      key_run(A.what + off2, wv);
+      key_run(Y + off2 - yoff, yv);
+      if (ybody) rotate_key_run(yv, i, x);
+      uint32_t* accb = SC + g * NTT_SCRATCH;  // group (r,1)'s b accumulator
+      uint32_t* part = SCAT + (i & 1) * 2 * N + r * N;
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        const int o = 16 * x + 4 * (r4 ^ f);
+        uint4* ap = reinterpret_cast<uint4*>(accb + o);
+        uint4* hp = reinterpret_cast<uint4*>(part + o);
+        const uint4 a4 = *ap, h4 = *hp;
+        uint32_t ab[4], pr[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const int j = 4 * r4 + e;
+          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)rs[j] * u4e(yv[r4], e), q, qinv), q2);
+          pr[e] = u4e(h4, e) + redc_lazy((uint64_t)rs[j] * u4e(wv[r4], e), q, qinv);  // [0, 3q)
+        }
+        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
+        *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+      }
+      if (i >= 1) scatter_next(i, 0, SCATTER_SPLIT);
     }
     __syncthreads();
     // [B] gadget_decompose of the composite coefficients (rgsw/external_product.rs:16-37):
@@ -364,7 +392,6 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     }
     __syncthreads();
     // [C]
-    uint4 k2[4];  // group (r,1): the b side's third key slice, in flight across the barrier
     if (kd < 2) {
       const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
       uint4 wv[4], yv[4];
@@ -392,56 +419,31 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
         for (int e = 0; e < 4; e++) {
           const int j = 4 * r4 + e;
           ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)v[j] * u4e(yv[r4], e), q, qinv), q2);
-          pr[e] = redc_lazy((uint64_t)v[j] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 3q)
+          pr[e] = redc_lazy((uint64_t)v[j] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 5q)
         }
         *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
         *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);
       }
-      if (kd == 1) key_run(Y + ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x - yoff, k2);
-    } else {
-      const size_t off2 = ((size_t)(i * ELL + 2) * 2 + r) * N + 16 * x;
-      uint4 wv[4];
-      key_run(A.what + off2, wv);
-      uint32_t rs[16], pr[16];
-      load16(RS + r * N, x, rs);
-#pragma unroll
-      for (int j = 0; j < 16; j++) pr[j] = redc_lazy((uint64_t)rs[j] * u4e(wv[j >> 2], j & 3), q, qinv);
-      store16(PB2 + r * N, x, pr);
-      if (i >= 1) scatter_next(i, 3 * N / 8, N);
+    } else if (i >= 1) {
+      scatter_next(i, SCATTER_SPLIT, N);
     }
     __syncthreads();
-    // [D] R_i (group (r,0)); the b accumulator's other two products (group (r,1))
+    // [D] R_i (group (r,0))
     if (kd == 0) {
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
         const int o = r * N + 16 * x + 4 * (r4 ^ f);
         const uint4 pa = *reinterpret_cast<const uint4*>(SCAT + (i & 1) * 2 * N + o);
         const uint4 p1 = *reinterpret_cast<const uint4*>(PB1 + o);
-        const uint4 p2 = *reinterpret_cast<const uint4*>(PB2 + o);
         uint32_t outv[4];
 #pragma unroll
         for (int e = 0; e < 4; e++) {
-          uint32_t sum = u4e(pa, e) + u4e(p1, e) + u4e(p2, e);  // < 7q < 2^31
+          uint32_t sum = u4e(pa, e) + u4e(p1, e);  // < 7q < 2^31
           sum = min(sum, sum - 4 * q);
           sum = min(sum, sum - 2 * q);
           outv[e] = min(sum, sum - q);
         }
         *reinterpret_cast<uint4*>(T + o) = make_uint4(outv[0], outv[1], outv[2], outv[3]);  // R_i for the next step
-      }
-    } else if (kd == 1) {
-      if (ybody) rotate_key_run(k2, i, x);
-      uint32_t* accb = SC + (3 * r + 2) * NTT_SCRATCH;
-#pragma unroll
-      for (int r4 = 0; r4 < 4; r4++) {
-        const int o = 16 * x + 4 * (r4 ^ f);
-        const uint4 rr = *reinterpret_cast<const uint4*>(RS + r * N + o);
-        uint4* ap = reinterpret_cast<uint4*>(accb + o);
-        const uint4 a4 = *ap;
-        uint32_t ab[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++)
-          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)u4e(rr, e) * u4e(k2[r4], e), q, qinv), q2);
-        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
       }
     }
     __syncthreads();
@@ -495,17 +497,19 @@ __global__ void __launch_bounds__(RBLOCK, 1) respond_kernel_loop(const __grid_co
 
 }  // namespace
 
-size_t respond_smem_bytes(int mode) {
-  return sizeof(uint32_t) * (mode == MODE_COMPAT ? Smem<1>::TOTAL : Smem<2>::TOTAL);
+size_t respond_smem_bytes(int mode, bool qdb) {
+  const int words = mode == MODE_COMPAT ? (qdb ? Smem<1, true>::TOTAL : Smem<1, false>::TOTAL)
+                                        : (qdb ? Smem<2, true>::TOTAL : Smem<2, false>::TOTAL);
+  return sizeof(uint32_t) * words;
 }
 
 template <int MODE, bool SEEDED, bool QDB>
 static cudaError_t set_smem_attr() {
   cudaError_t e = cudaFuncSetAttribute(respond_kernel<MODE, SEEDED, QDB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)respond_smem_bytes(MODE));
+                                       (int)respond_smem_bytes(MODE, QDB));
   if (e == cudaSuccess && !QDB)
     e = cudaFuncSetAttribute(respond_kernel_loop<MODE, SEEDED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)respond_smem_bytes(MODE));
+                             (int)respond_smem_bytes(MODE, false));
   return e;
 }
 
@@ -522,9 +526,9 @@ static cudaError_t launch_one(const RespondArgs& a, int ctas, cudaStream_t st) {
     if (e != cudaSuccess) return e;
   }
   if (!QDB && ctas < a.nq)
-    respond_kernel_loop<MODE, SEEDED><<<ctas, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
+    respond_kernel_loop<MODE, SEEDED><<<ctas, RBLOCK, respond_smem_bytes(MODE, false), st>>>(a);
   else
-    respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, respond_smem_bytes(MODE), st>>>(a);
+    respond_kernel<MODE, SEEDED, QDB><<<a.nq, RBLOCK, respond_smem_bytes(MODE, QDB), st>>>(a);
   return cudaGetLastError();
 }
 
