@@ -121,8 +121,12 @@ __global__ void __launch_bounds__(BSIDE_THREADS) bside_kernel(const __grid_const
 }
 
 // Shared-memory layout in u32 words (NR = residues of the a side).  The
-// device-row variant needs 179.5 KiB, so the SM's carveout leaves 60 KiB of
-// L1 (it holds the transforms' twiddle tables); the serving variant 195.5 KiB.
+// device-row variant needs 163 KiB (with the 1 KiB every CTA reserves, the
+// SM's 164 KiB configuration), so the SM keeps 92 KiB of L1, which holds the
+// transforms' twiddle tables; the serving variant needs 195.5 KiB.
+// Each residue's b accumulator is the scratch of its group (r,2), which runs
+// no transform during the recursion (words [0, N)); words N..N+15 of it keep
+// the parked b side of device-row launches.
 template <int NR, bool QDB>
 struct Smem {
   static constexpr int AHAT = 0;                    // [ELL][NR][N] row transforms
@@ -130,11 +134,13 @@ struct Smem {
   static constexpr int T = SC + RG * NTT_SCRATCH;   // [2][N] R_{i+1} (slots) -> its inverse (coefficients) -> digits d0, d1
   static constexpr int PB1 = T + 2 * N;             // [2][N] NTT(d1) w'[i][1]
   static constexpr int SCAT = PB1 + 2 * N;          // [2 steps][2][N] query-only term of R_i (slots), then partial R_i
-  static constexpr int ACC = SCAT + 4 * N;          // [2][N] b accumulators
-  // T..T+6N also hold the unseeded rows' a parts; the serving variant stages
-  // the query's raw b rows (u64, 12N words) from T on until the b side
-  static constexpr int MISC = ACC + 2 * N + (QDB ? 2 * N : 0);  // bpoly[32], ws[3][20], staged seeds (96 B), mbarrier
-  static constexpr int TOTAL = MISC + 128;
+  // T..T+6N also hold the unseeded rows' a parts and SCAT+2N.. the
+  // expansion's workspace ws[3][20] (device rows); the serving variant
+  // stages the query's raw b rows (u64, 12N words) from T on until the b
+  // side, then keeps bpoly[32], ws[3][20], the staged seeds (96 B) and the
+  // rows' mbarrier in MISC
+  static constexpr int MISC = QDB ? T + 12 * N : SCAT + 4 * N;
+  static constexpr int TOTAL = QDB ? MISC + 128 : MISC;
 };
 
 // Slots of the next step's query-only term computed by group (r,2) in [A];
@@ -171,13 +177,12 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   uint32_t* T = smem + L::T;
   uint32_t* PB1 = smem + L::PB1;
   uint32_t* SCAT = smem + L::SCAT;
-  uint32_t* bpoly = smem + L::MISC;
-  int* wsb = (int*)(smem + L::MISC + 32);
+  uint32_t* bpoly = QDB ? smem + L::MISC : nullptr;
+  int* wsb = reinterpret_cast<int*>(QDB ? smem + L::MISC + 32 : SCAT + 2 * N);
 
   const DevParams& P = A.P;
   const int tid = threadIdx.x, g = tid >> 7, x = tid & 127;
   const int r = g / 3, kd = g - 3 * r;  // residue, role of this group
-  uint32_t* ACC = smem + L::ACC + r * N;  // this residue's b accumulator
   const int gamma = P.gamma;
   // QDB (serving loop): this query's fields come from its descriptor in
   // device memory, its rows and response from / to pinned host memory;
@@ -209,7 +214,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   const uint64_t* brows = QDB ? D->brows : A.brows + (size_t)qi * ELL * 2 * N;
 
   // Serving loop (rows in host memory): the query's b rows (96 KiB) are
-  // bulk-copied (TMA) into shared memory (T..ACC) while the rows are
+  // bulk-copied (TMA) into shared memory (T..T+12N) while the rows are
   // expanded, so the host link's latency stays off the critical path, and the
   // b side follows the row NTTs.  Rows in device memory: bside_kernel has
   // already computed the b side and parked it in the response slot; the
@@ -225,7 +230,6 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   // (ordered before the expansion by the barrier below)
   uint8_t* seed_sm = reinterpret_cast<uint8_t*>(smem + L::MISC + 96);
   if (QDB && tid < ELL * 32) seed_sm[tid] = D->seeds[tid];
-  if (!QDB && tid < 32) bpoly[tid] = b_parking(A.out, qi)[tid];  // parked by bside_kernel
   if (tid == 0) {
     // the contracted shard's blocks of the first three steps (the rest are
     // prefetched two steps ahead of their use in the recursion)
@@ -247,7 +251,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   {
     const int t = tid >> 8, lt = tid & 255;
     uint64_t* cand = reinterpret_cast<uint64_t*>(SC) + t * N;  // 3 x 16 KiB within SC
-    // serving loop: in place of the row's transforms (T..ACC hold the
+    // serving loop: in place of the row's transforms (T..T+12N hold the
     // staged rows); otherwise within T..PB1
     uint32_t* a0 = QDB ? Ahat + t * NR * N : T + t * 2 * N;
     uint32_t* a1 = a0 + N;
@@ -317,10 +321,9 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
       scatter_r(P, gamma - 2, Eg_at(sres), Ag, NR * N, sc2 + sres * N, sp, snthr, sq, sqinv,
                 MODE == MODE_COMPAT ? sc2 + N : nullptr);
     }
-    for (int j = tid; j < 2 * N; j += RBLOCK) {
-      smem[L::ACC + j] = 0;
-      SC[(3 * (j >> LOGN) + 2) * NTT_SCRATCH + (j & (N - 1))] = 0;  // group (r,1)'s accumulator
-    }
+    for (int j = tid; j < 2 * N; j += RBLOCK) SC[(3 * (j >> LOGN) + 2) * NTT_SCRATCH + (j & (N - 1))] = 0;
+    // device rows: the b side parked by bside_kernel, residue r's beside its accumulator
+    if (!QDB && tid < 32) SC[(3 * (tid >> 4) + 2) * NTT_SCRATCH + N + (tid & 15)] = b_parking(A.out, qi)[tid];
   }
   __syncthreads();
 
@@ -362,7 +365,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
       key_run(A.what + off2, wv);
       key_run(Y + off2 - yoff, yv);
       if (ybody) rotate_key_run(yv, i, x);
-      uint32_t* accb = SC + g * NTT_SCRATCH;  // group (r,1)'s b accumulator
+      uint32_t* accb = SC + g * NTT_SCRATCH;  // the residue's b accumulator
       uint32_t* part = SCAT + (i & 1) * 2 * N + r * N;
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
@@ -392,6 +395,8 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     }
     __syncthreads();
     // [C]
+    uint32_t* accb = SC + (3 * r + 2) * NTT_SCRATCH;  // the residue's b accumulator
+    uint32_t py[16];  // group (r,1): NTT(d1) y'1, added to the b accumulator in [D]
     if (kd < 2) {
       const size_t off = ((size_t)(i * ELL + kd) * 2 + r) * N + 16 * x;
       uint4 wv[4], yv[4];
@@ -402,34 +407,42 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
       for (int j = 0; j < 16; j++) v[j] = T[kd * N + x + 128 * j];
       ntt_fwd(v, SC + g * NTT_SCRATCH, fwd_tw(C), q, x, 1 + g);  // slots 16x.., [0, 14q)
       if (ybody) rotate_key_run(yv, i, x);
-      // group (r,0): the b accumulator ACC and the partial R_i in place of the
-      // query-only term; group (r,1): its own b accumulator (the scratch of
-      // group (r,2), free during the recursion) and PB1
-      uint32_t* accb = kd == 0 ? ACC : SC + (3 * r + 2) * NTT_SCRATCH;
+      // group (r,0): the b accumulator and the partial R_i in place of the
+      // query-only term; group (r,1): PB1
       uint32_t* pdst = kd == 0 ? SCAT + (i & 1) * 2 * N + r * N : PB1 + r * N;
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
         const int o = 16 * x + 4 * (r4 ^ f);
-        uint4* ap = reinterpret_cast<uint4*>(accb + o);
-        const uint4 a4 = *ap;
         uint4* hp = reinterpret_cast<uint4*>(pdst + o);
         const uint4 h4 = kd == 0 ? *hp : make_uint4(0, 0, 0, 0);
-        uint32_t ab[4], pr[4];
+        uint32_t pr[4];
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-          const int j = 4 * r4 + e;
-          ab[e] = acc_2q(u4e(a4, e), redc_lazy((uint64_t)v[j] * u4e(yv[r4], e), q, qinv), q2);
-          pr[e] = redc_lazy((uint64_t)v[j] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 5q)
-        }
-        *ap = make_uint4(ab[0], ab[1], ab[2], ab[3]);
+        for (int e = 0; e < 4; e++)
+          pr[e] = redc_lazy((uint64_t)v[4 * r4 + e] * u4e(wv[r4], e), q, qinv) + u4e(h4, e);  // [0, 5q)
         *hp = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+#pragma unroll
+        for (int e = 0; e < 4; e++) py[4 * r4 + e] = redc_lazy((uint64_t)v[4 * r4 + e] * u4e(yv[r4], e), q, qinv);
+        if (kd == 0) {
+          uint4* ap = reinterpret_cast<uint4*>(accb + o);
+          const uint4 a4 = *ap;
+          *ap = make_uint4(acc_2q(a4.x, py[4 * r4], q2), acc_2q(a4.y, py[4 * r4 + 1], q2),
+                           acc_2q(a4.z, py[4 * r4 + 2], q2), acc_2q(a4.w, py[4 * r4 + 3], q2));
+        }
       }
     } else if (i >= 1) {
       scatter_next(i, SCATTER_SPLIT, N);
     }
     __syncthreads();
-    // [D] R_i (group (r,0))
-    if (kd == 0) {
+    // [D] R_i (group (r,0)); b += NTT(d1) y'1 (group (r,1))
+    if (kd == 1) {
+#pragma unroll
+      for (int r4 = 0; r4 < 4; r4++) {
+        uint4* ap = reinterpret_cast<uint4*>(accb + 16 * x + 4 * (r4 ^ f));
+        const uint4 a4 = *ap;
+        *ap = make_uint4(acc_2q(a4.x, py[4 * r4], q2), acc_2q(a4.y, py[4 * r4 + 1], q2),
+                         acc_2q(a4.z, py[4 * r4 + 2], q2), acc_2q(a4.w, py[4 * r4 + 3], q2));
+      }
+    } else if (kd == 0) {
 #pragma unroll
       for (int r4 = 0; r4 < 4; r4++) {
         const int o = r * N + 16 * x + 4 * (r4 ^ f);
@@ -464,15 +477,13 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
 #pragma unroll
     for (int j = 0; j < 8; j++) out[r * N + team_t + 256 * j] = canon2(v[j], q);
   } else {
-    uint32_t b0[16], b1[16];
-    load16(ACC, x, b0);                    // [0, 2q)
-    load16(SC + g * NTT_SCRATCH, x, b1);  // group (r,1)'s accumulator, in this group's scratch
-#pragma unroll
-    for (int j = 0; j < 16; j++) b0[j] = acc_2q(b0[j], b1[j], q2);
+    uint32_t b0[16];
+    load16(SC + g * NTT_SCRATCH, x, b0);  // the b accumulator, [0, 2q)
+    const uint32_t bp = x < gamma ? (QDB ? bpoly[r * 16 + x] : SC[g * NTT_SCRATCH + N + x]) : 0;
     ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);  // first exchange after a group barrier
 #pragma unroll
     for (int j = 0; j < 16; j++) b0[j] = canon2(b0[j], q);
-    if (x < gamma) b0[0] = add_mod(b0[0], bpoly[r * 16 + x], q);
+    if (x < gamma) b0[0] = add_mod(b0[0], bp, q);
 #pragma unroll
     for (int j = 0; j < 16; j++) out[2 * N + r * N + x + 128 * j] = b0[j];
   }
