@@ -120,13 +120,13 @@ __global__ void __launch_bounds__(BSIDE_THREADS) bside_kernel(const __grid_const
   if (threadIdx.x < 32) b_parking(A.out, qi)[threadIdx.x] = bpoly[threadIdx.x];
 }
 
-// Shared-memory layout in u32 words (NR = residues of the a side).  The
-// device-row variant needs 163 KiB (with the 1 KiB every CTA reserves, the
-// SM's 164 KiB configuration), so the SM keeps 92 KiB of L1, which holds the
-// transforms' twiddle tables; the serving variant needs 195.5 KiB.
-// Each residue's b accumulator is the scratch of its group (r,2), which runs
-// no transform during the recursion (words [0, N)); words N..N+15 of it keep
-// the parked b side of device-row launches.
+// Shared-memory layout in u32 words (NR = residues of the a side).  With the
+// 1 KiB every CTA reserves, the device-row variant (163 KiB) fills the SM's
+// 164 KiB configuration and the serving variant (195 KiB) its 196 KiB one,
+// so the SM keeps 92 or 60 KiB of L1, which holds the transforms' twiddle
+// tables.  Each residue's b accumulator is the scratch of its group (r,2),
+// which runs no transform during the recursion (words [0, N)); words
+// N..N+15 of it keep the residue's b side (bpoly) until the outputs.
 template <int NR, bool QDB>
 struct Smem {
   static constexpr int AHAT = 0;                    // [ELL][NR][N] row transforms
@@ -135,12 +135,14 @@ struct Smem {
   static constexpr int PB1 = T + 2 * N;             // [2][N] NTT(d1) w'[i][1]
   static constexpr int SCAT = PB1 + 2 * N;          // [2 steps][2][N] query-only term of R_i (slots), then partial R_i
   // T..T+6N also hold the unseeded rows' a parts and SCAT+2N.. the
-  // expansion's workspace ws[3][20] (device rows); the serving variant
+  // expansion's workspace ws[3][20] (device rows).  The serving variant
   // stages the query's raw b rows (u64, 12N words) from T on until the b
-  // side, then keeps bpoly[32], ws[3][20], the staged seeds (96 B) and the
-  // rows' mbarrier in MISC
-  static constexpr int MISC = QDB ? T + 12 * N : SCAT + 4 * N;
-  static constexpr int TOTAL = QDB ? MISC + 128 : MISC;
+  // side, and keeps ws[3][20], the staged seeds (96 B) and the rows'
+  // mbarrier in MISC, the words of SC past the expansion's candidates (6N
+  // words), until the row transforms reuse them
+  static constexpr int MISC = QDB ? SC + 6 * N : SCAT + 4 * N;
+  static constexpr int TOTAL = QDB ? T + 12 * N : SCAT + 4 * N;
+  static_assert(!QDB || MISC + 128 <= SC + 5 * NTT_SCRATCH + N, "MISC stays clear of the b side's words");
 };
 
 // Slots of the next step's query-only term computed by group (r,2) in [A];
@@ -177,7 +179,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   uint32_t* T = smem + L::T;
   uint32_t* PB1 = smem + L::PB1;
   uint32_t* SCAT = smem + L::SCAT;
-  uint32_t* bpoly = QDB ? smem + L::MISC : nullptr;
+  uint32_t* bpoly = QDB ? SC + 5 * NTT_SCRATCH + N : nullptr;  // serving: the b side, both residues, until the recursion
   int* wsb = reinterpret_cast<int*>(QDB ? smem + L::MISC + 32 : SCAT + 2 * N);
 
   const DevParams& P = A.P;
@@ -271,6 +273,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     if (!arrived) wsb[18] = 1;
   }
   __syncthreads();
+  const bool exp_ok = !SEEDED || (wsb[17] && wsb[37] && wsb[57]);
   if (QDB && wsb[18]) {
     // The CTA must not exit while its bulk copies can still write into its
     // shared memory (the next CTA on this SM would own it).  If even the
@@ -280,8 +283,13 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
     if (tid == 0) *status_ptr() = lost ? ERR_STAGE_LOST : ERR_STAGE;
     return;  // uniform over the CTA
   }
+  if (QDB) {
+    // the row transforms reuse the words of the workspace, seeds and mbarrier
+    if (tid == 0) mbar_inval(rbar);
+    __syncthreads();
+  }
   // the query's status is written once, by one thread
-  if (tid == 0) *status_ptr() = (!SEEDED || (wsb[17] && wsb[37] && wsb[57])) ? 0 : ERR_EXPAND;
+  if (tid == 0) *status_ptr() = exp_ok ? 0 : ERR_EXPAND;
   if (r < NR) {  // group (r, t=kd) transforms row kd, residue r
     uint32_t v[16];
     const uint32_t* src = QDB ? Ahat + (kd * NR + r) * N : T + kd * 2 * N + r * N;
@@ -322,8 +330,13 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
                 MODE == MODE_COMPAT ? sc2 + N : nullptr);
     }
     for (int j = tid; j < 2 * N; j += RBLOCK) SC[(3 * (j >> LOGN) + 2) * NTT_SCRATCH + (j & (N - 1))] = 0;
-    // device rows: the b side parked by bside_kernel, residue r's beside its accumulator
-    if (!QDB && tid < 32) SC[(3 * (tid >> 4) + 2) * NTT_SCRATCH + N + (tid & 15)] = b_parking(A.out, qi)[tid];
+    // the b side (serving: computed above; device rows: parked by
+    // bside_kernel), residue r's beside its accumulator
+    if (tid < 32) {
+      const uint32_t bv = QDB ? bpoly[tid] : b_parking(A.out, qi)[tid];
+      __syncwarp();
+      SC[(3 * (tid >> 4) + 2) * NTT_SCRATCH + N + (tid & 15)] = bv;
+    }
   }
   __syncthreads();
 
@@ -479,7 +492,7 @@ __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) 
   } else {
     uint32_t b0[16];
     load16(SC + g * NTT_SCRATCH, x, b0);  // the b accumulator, [0, 2q)
-    const uint32_t bp = x < gamma ? (QDB ? bpoly[r * 16 + x] : SC[g * NTT_SCRATCH + N + x]) : 0;
+    const uint32_t bp = x < gamma ? SC[g * NTT_SCRATCH + N + x] : 0;
     ntt_inv_noscale(b0, SC + g * NTT_SCRATCH, inv_tw(C), q, x, 1 + g);  // first exchange after a group barrier
 #pragma unroll
     for (int j = 0; j < 16; j++) b0[j] = canon2(b0[j], q);
