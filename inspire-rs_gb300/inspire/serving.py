@@ -283,12 +283,16 @@ def run(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate:
 
 def autotune(make_server, targets: List[Target], pool: QueryPool, client_id: int, *,
              batches=(128, 152, 256), inflight=(4, 8), waits_us=(100,), n_queries: int = 1 << 15,
-             n_threads: int = 4) -> dict:
+             n_threads: int = 4, tie: float = 0.01) -> dict:
     """Pick the serving configuration (max_batch, max_inflight,
-    batch_wait_us) with the highest saturated closed-loop rate.
-    make_server(max_batch=, max_inflight=, batch_wait_us=) builds a server;
-    each candidate gets a warm-up run, then a timed run of n_queries.
-    Returns {"best": config, "table": [config + rate, ...]}."""
+    batch_wait_us) by saturated closed-loop rate: among the candidates within
+    `tie` (relative) of the highest rate, the one with the most batches in
+    flight, then the smallest batches (under partial load a partial batch
+    launches at once while a stream is free, so more streams and smaller
+    batches mean less waiting).  make_server(max_batch=, max_inflight=,
+    batch_wait_us=) builds a server; each candidate gets a warm-up run, then
+    a timed run of n_queries.  Returns {"best": config, "table": [config +
+    rate, ...]}."""
     table = []
     for mb in batches:
         for mi in inflight:
@@ -302,8 +306,16 @@ def autotune(make_server, targets: List[Target], pool: QueryPool, client_id: int
                     srv.close()
                 table.append({"max_batch": mb, "max_inflight": mi, "batch_wait_us": w,
                               "qps": r["achieved_qps"], "p50_ms": r["p50_ms"]})
-    best = max(table, key=lambda t: t["qps"])
-    return {"best": {k: best[k] for k in ("max_batch", "max_inflight", "batch_wait_us")}, "table": table}
+    return {"best": pick_config(table, tie), "table": table}
+
+
+def pick_config(table: List[dict], tie: float = 0.01) -> dict:
+    """autotune's choice from its table (rows with max_batch, max_inflight,
+    batch_wait_us and qps)."""
+    top = max(t["qps"] for t in table)
+    near = [t for t in table if t["qps"] >= (1.0 - tie) * top]
+    best = min(near, key=lambda t: (-t["max_inflight"], t["max_batch"], t["batch_wait_us"]))
+    return {k: best[k] for k in ("max_batch", "max_inflight", "batch_wait_us")}
 
 def run_native(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate: float,
                duration_s: float = 2.0, seed: int = 0, keep_outputs: bool = False, settle_frac: float = 0.1,

@@ -140,3 +140,16 @@ def test_device_memory_ledger_host(tmp_path):
                     "-o", exe], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
+
+
+def test_autotune_pick_prefers_more_streams_on_near_ties(serving):
+    """Within the tie band the choice has the most batches in flight, then
+    the smallest batches; outside it the rate decides."""
+    pick = serving.pick_config
+    row = lambda mb, mi, q: {"max_batch": mb, "max_inflight": mi, "batch_wait_us": 100, "qps": q}
+    table = [row(128, 4, 917_630.0), row(128, 8, 917_649.0), row(152, 4, 917_040.0), row(152, 8, 915_908.0),
+             row(256, 4, 918_109.0), row(256, 8, 918_089.0)]
+    assert pick(table) == {"max_batch": 128, "max_inflight": 8, "batch_wait_us": 100}
+    table.append(row(256, 4, 990_000.0))  # clearly faster: the rate decides
+    assert pick(table) == {"max_batch": 256, "max_inflight": 4, "batch_wait_us": 100}
+    assert pick([row(128, 4, 1.0)], tie=0.0) == {"max_batch": 128, "max_inflight": 4, "batch_wait_us": 100}
