@@ -166,8 +166,24 @@ def test_other_column_counts(oracle_mod, entry_size, gamma):
         want = ctx.respond_inspiring(ctx.encode_shard(db, entry_size, 0), ctx.expand_rgsw(seeds, b_rows), W_SEED,
                                      mode=omode, pack=pack, y_body=y_body)
         q = inspire.SeededClientQuery(0, seeds, b_rows, inspiring_packing_keys=inspire.ClientPackingKeys(y_body=y_body))
-        r = inspire.respond_seeded_inspiring(crs, edb, q)
-        assert np.array_equal(np.stack([r.ciphertext.a, r.ciphertext.b]), want), mode
+        default = crs.pair_threshold
+        for thr in (default, 0):  # the two-CTA cluster kernel, then one CTA per query
+            crs.pair_threshold = thr
+            r = inspire.respond_seeded_inspiring(crs, edb, q)
+            assert np.array_equal(np.stack([r.ciphertext.a, r.ciphertext.b]), want), (mode, thr)
+        # the serving loop's variant of the one-CTA kernel (rows read from
+        # page-locked host memory)
+        cid = crs.register_client(inspire.ClientPackingKeys(y_body=y_body))
+        srv = inspire.Server(crs, max_batch=8, max_inflight=1, capacity=8)
+        try:
+            t, rc = srv.submit(edb, [0, 0], np.stack([seeds, seeds]), np.stack([b_rows, b_rows]), [cid, cid])
+            assert rc == 0 and len(t) == 2
+            out = np.zeros((2, 2, 2 * N), dtype=np.uint64)
+            assert len(srv.poll_batch(t, out)) == 2
+            assert np.array_equal(out[0], want) and np.array_equal(out[1], want), mode
+        finally:
+            srv.close()
+            crs.pair_threshold = default
         if mode == "crt_fixed":
             assert np.array_equal(client.extract_inspiring(want, entry_size),
                                   db[1234 * entry_size:1235 * entry_size])
