@@ -161,14 +161,16 @@ constexpr int SCATTER_SPLIT = N / 8;
 // residue r's three groups:
 //  [A] (r,0)+(r,1) as one 256-thread team: inverse NTT of R_{i+1} (T[r]),
 //      written back to T[r] once (r,2) has read it (named barrier 9 + r);
-//      (r,2): SCAT[r] += R_{i+1} w'2 and the second b accumulator += R_{i+1}
-//      y'2, then the first part of the next step's query-only term R_{i-1}
+//      (r,2): SCAT[r] += R_{i+1} w'2 and the b accumulator += R_{i+1} y'2,
+//      then the first part of the next step's query-only term R_{i-1}
 //      (into the other SCAT buffer);
 //  [B] all threads: CRT compose + digits d0, d1 into T;
-//  [C] (r,0): NTT(d0); SCAT[r] += NTT(d0) w'0 (in place), b += NTT(d0) y'0;
-//      (r,1): NTT(d1); PB1 = NTT(d1) w'1, second b accumulator += NTT(d1) y'1;
+//  [C] (r,0): NTT(d0); SCAT[r] += NTT(d0) w'0 (in place), the b
+//      accumulator += NTT(d0) y'0;
+//      (r,1): NTT(d1); PB1 = NTT(d1) w'1, NTT(d1) y'1 kept in registers;
 //      (r,2): the rest of R_{i-1};
-//  [D] (r,0): R_i = SCAT[r] + PB1 -> T[r] (slots) for the next step.
+//  [D] (r,0): R_i = SCAT[r] + PB1 -> T[r] (slots) for the next step;
+//      (r,1): the b accumulator += NTT(d1) y'1.
 template <int MODE, bool SEEDED, bool QDB>
 __device__ __forceinline__ void respond_one(const RespondArgs& A, const int qi) {
   constexpr int NR = MODE == MODE_COMPAT ? 1 : 2;
