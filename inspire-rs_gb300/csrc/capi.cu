@@ -116,49 +116,89 @@ struct HostChaCha {
 
 namespace {
 
+// Build the client key table into m from y_body or y_all.  From y_body at
+// gamma = 16 the table holds NTT(y_body) only (48 KiB, the Respond kernel
+// forms each rotation in registers); from an explicit y_all, or at smaller
+// gamma, all (gamma-1)*ELL rotated polys.  sync: wait for the build here
+// (otherwise the launches that use the table follow on the same stream).
+int build_key_table(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all, DevMem& m, bool& body_form,
+                    bool sync) {
+  const int gamma = c->gamma;
+  body_form = !y_all && gamma == MAX_GAMMA;
+  const size_t tbl_words = (size_t)std::max(1, body_form ? ELL : (gamma - 1) * ELL) * poly_words();
+  if (m.ensure(tbl_words * sizeof(uint32_t)) != cudaSuccess)
+    return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "client key table allocation"));
+  const size_t in_polys = y_all ? (size_t)(gamma - 1) * ELL : ELL;
+  if (gamma > 1) {
+    const size_t in_bytes = in_polys * poly_words() * sizeof(uint64_t);
+    if (c->d_keys.ensure(in_bytes) != cudaSuccess)
+      return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "client key upload buffer"));
+    // through page-locked memory (one DMA), once the previous upload is out of it
+    if (!c->keys_ev) CUDA_TRY(cudaEventCreateWithFlags(&c->keys_ev, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventSynchronize(c->keys_ev));
+    CUDA_TRY(c->h_keys.ensure(in_bytes));
+    memcpy(c->h_keys.p, y_all ? y_all : y_body, in_bytes);
+    CUDA_TRY(cudaMemcpyAsync(c->d_keys.p, c->h_keys.p, in_bytes, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaEventRecord(c->keys_ev, c->stream));
+    CUDA_TRY(y_all ? launch_client_from_yall(c->P, c->d_keys.as<uint64_t>(), m.as<uint32_t>(), c->stream)
+                   : launch_client_from_ybody(c->P, c->d_keys.as<uint64_t>(), m.as<uint32_t>(),
+                                              body_form ? 1 : gamma - 1, c->stream));
+    // the Respond kernel multiplies the third key by R_{i+1} instead of NTT(d2)
+    CUDA_TRY(launch_fold_third_digit(c->P, m.as<uint32_t>(), body_form ? 1 : gamma - 1, c->stream));
+    if (sync) CUDA_TRY(cudaStreamSynchronize(c->stream));
+  }
+  return INSPIRE_OK;
+}
+
+// The device table entry of a key table: bit 0 marks a body table
+// (allocations are 256-byte aligned).
+const uint32_t* table_entry(const DevMem& m, bool body_form) {
+  return reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(m.as<uint32_t>()) | (body_form ? 1u : 0u));
+}
+
+int32_t free_client_slot(inspire_ctx* c) {
+  for (size_t i = 0; i < c->clients.size(); i++)
+    if (!c->clients[i]) return (int32_t)i;
+  c->clients.push_back(nullptr);
+  c->client_ptrs.push_back(nullptr);
+  return (int32_t)c->clients.size() - 1;
+}
+
 int register_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all, int32_t* id) {
   if (!y_body && !y_all)
     return fail(INSPIRE_ERR_KEYS_INVALID, "InspiRING packing keys invalid: y_all and y_body are both empty");
-  const int gamma = c->gamma;
-  // From y_body at gamma = 16 the table holds NTT(y_body) only (48 KiB, the
-  // Respond kernel forms each rotation in registers); from an explicit y_all,
-  // or at smaller gamma, all (gamma-1)*ELL rotated polys.
-  const bool body_form = !y_all && gamma == MAX_GAMMA;
-  const size_t tbl_words = (size_t)std::max(1, body_form ? ELL : (gamma - 1) * ELL) * poly_words();
   std::unique_ptr<DevMem> m(new DevMem(c->ledger));  // freed (bytes returned) on every error path
-  cudaError_t e = m->ensure(tbl_words * sizeof(uint32_t));
-  if (e != cudaSuccess) return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "client key table allocation"));
-  const size_t in_polys = y_all ? (size_t)(gamma - 1) * ELL : ELL;
-  if (gamma > 1) {
-    if (c->d_keys.ensure(in_polys * poly_words() * sizeof(uint64_t)) != cudaSuccess)
-      return fail(INSPIRE_ERR_OUT_OF_MEMORY, alloc_failure(c, "client key upload buffer"));
-    CUDA_TRY(cudaMemcpyAsync(c->d_keys.p, y_all ? y_all : y_body, in_polys * poly_words() * sizeof(uint64_t),
-                             cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(y_all ? launch_client_from_yall(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(), c->stream)
-                   : launch_client_from_ybody(c->P, c->d_keys.as<uint64_t>(), m->as<uint32_t>(),
-                                              body_form ? 1 : gamma - 1, c->stream));
-    // the Respond kernel multiplies the third key by R_{i+1} instead of NTT(d2)
-    CUDA_TRY(launch_fold_third_digit(c->P, m->as<uint32_t>(), body_form ? 1 : gamma - 1, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
-  }
-  int slot = -1;
-  for (size_t i = 0; i < c->clients.size(); i++)
-    if (!c->clients[i]) {
-      slot = (int)i;
-      break;
-    }
-  if (slot < 0) {
-    slot = (int)c->clients.size();
-    c->clients.push_back(nullptr);
-    c->client_ptrs.push_back(nullptr);
-  }
+  bool body_form = false;
+  if (int rc = build_key_table(c, y_body, y_all, *m, body_form, true)) return rc;
+  const int32_t slot = free_client_slot(c);
   c->clients[slot] = m.release();
-  // bit 0 of the device table entry marks a body table (allocations are
-  // 256-byte aligned)
-  c->client_ptrs[slot] = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(c->clients[slot]->as<uint32_t>()) |
-                                                           (body_form ? 1u : 0u));
+  c->client_ptrs[slot] = table_entry(*c->clients[slot], body_form);
   c->client_table_dirty = true;
   *id = slot;
+  return INSPIRE_OK;
+}
+
+// The keys a query carries (respond_*_inspiring): rebuilt on every call, as
+// the crate derives them per request, into one table the context keeps for
+// these calls (no allocation per call; the call's own launches follow the
+// build on the context's stream, and the call waits for them).
+int inline_keys(inspire_ctx* c, const uint64_t* y_body, const uint64_t* y_all, int32_t* id) {
+  if (!y_body && !y_all)
+    return fail(INSPIRE_ERR_KEYS_INVALID, "InspiRING packing keys invalid: y_all and y_body are both empty");
+  if (c->inline_id < 0) {
+    const int32_t slot = free_client_slot(c);
+    c->clients[slot] = new DevMem(c->ledger);
+    c->inline_id = slot;
+  }
+  DevMem& m = *c->clients[c->inline_id];
+  bool body_form = false;
+  if (int rc = build_key_table(c, y_body, y_all, m, body_form, false)) return rc;
+  const uint32_t* entry = table_entry(m, body_form);
+  if (c->client_ptrs[c->inline_id] != entry) {
+    c->client_ptrs[c->inline_id] = entry;
+    c->client_table_dirty = true;
+  }
+  *id = c->inline_id;
   return INSPIRE_OK;
 }
 
@@ -168,6 +208,7 @@ void release_keys(inspire_ctx* c, int32_t id) {
   c->clients[id] = nullptr;
   c->client_ptrs[id] = nullptr;
   c->client_table_dirty = true;
+  if (id == c->inline_id) c->inline_id = -1;
 }
 
 // Stage n queries (rows ELL..2ELL-1 only) and run the Respond kernel.
@@ -441,7 +482,7 @@ int single_query(inspire_ctx* c, const inspire_db* db, uint32_t shard_id, const 
   if (!y_all && !y_body)
     return fail(INSPIRE_ERR_KEYS_INVALID, "InspiRING packing keys invalid: y_all and y_body are both empty");
   int32_t id = -1;
-  int rc = register_keys(c, y_body, y_all, &id);
+  int rc = inline_keys(c, y_body, y_all, &id);
   if (rc) return rc;
   if (seeds) {
     rc = run_batch(c, db, 1, &shard_id, seeds + 32 * ELL, (size_t)64 * ELL, nullptr, b_rows + (size_t)ELL * poly_words(),
@@ -456,7 +497,6 @@ int single_query(inspire_ctx* c, const inspire_db* db, uint32_t shard_id, const 
     }
     rc = run_batch(c, db, 1, &shard_id, nullptr, 0, ar.data(), br.data(), ELL, &id, out_ct);
   }
-  release_keys(c, id);
   return rc;
 }
 

@@ -149,6 +149,9 @@ struct inspire_ctx {
   std::vector<const uint32_t*> client_ptrs;
   ighost::DevMem client_table;  // device copy of client_ptrs
   bool client_table_dirty = true;
+  // client slot of the key table that queries carrying their own keys
+  // (respond_*_inspiring) rebuild on every call, or -1
+  int32_t inline_id = -1;
   // staging for host-buffer calls
   cudaStream_t stream = nullptr;
   ighost::DevMem d_shard, d_seeds, d_arows, d_brows, d_client, d_out, d_cols, d_status, d_keys, d_desc;
@@ -156,6 +159,8 @@ struct inspire_ctx {
   ighost::HostPinned h_desc;    // descriptors of page-locked batch calls
   ighost::HostPinned h_qstatus; // status words of the batch calls, written by the kernel
   ighost::HostPinned h_stage;   // small batches' inputs, gathered for one DMA each
+  ighost::HostPinned h_keys;    // client keys on their way to d_keys
+  cudaEvent_t keys_ev = nullptr;  // recorded after the copy out of h_keys
 
   inspire_ctx() {
     for (ighost::DevMem* m : {&tables, &what, &what3, &wmask, &galois, &tree_work, &d_tree_out, &client_table, &d_shard,
@@ -164,6 +169,7 @@ struct inspire_ctx {
   }
   ~inspire_ctx() {
     for (ighost::DevMem* m : clients) delete m;
+    if (keys_ev) cudaEventDestroy(keys_ev);
     if (stream) cudaStreamDestroy(stream);
   }
 };

@@ -428,3 +428,43 @@ def test_batch_from_page_locked_buffers(world):
         for b in (seeds, rows, out):
             b.close()
         crs.release_client(cid)
+
+
+def test_carried_keys_reuse_one_table(world):
+    """Queries that carry their packing keys rebuild them into one table the
+    context keeps: consecutive calls switching clients and between the y_body
+    and y_all forms, a client registration in between and a CRS reload (which
+    frees every key table) each answer as the oracle does."""
+    import ctypes as C
+
+    W = world
+    inspire, ctx, O = W["inspire"], W["ctx"], W["O"]
+    crs, edb, pack, omode = W["w"]["crt_fixed"]
+    clients = [W["client"], O.Client(ctx, seed=5, rng_seed=9)]
+    keys = [c.packing_keys(pack) for c in clients]
+
+    def call(k, form, index):
+        sid, local = divmod(index, N)
+        seeds, b_rows = clients[k].query_seeded(local)
+        yb, ya = keys[k]
+        pk = inspire.ClientPackingKeys(y_body=yb) if form == "body" else inspire.ClientPackingKeys(y_all=ya)
+        r = inspire.respond_seeded_inspiring(crs, edb, inspire.SeededClientQuery(sid, seeds, b_rows,
+                                                                               inspiring_packing_keys=pk))
+        want = oracle_response(W, "crt_fixed", sid, ctx.expand_rgsw(seeds, b_rows),
+                               **({"y_body": yb} if form == "body" else {"y_all": ya}))
+        assert np.array_equal(np.stack([r.ciphertext.a, r.ciphertext.b]), want), (k, form, index)
+
+    call(0, "body", 5)
+    call(1, "body", 2050)
+    call(0, "all", 77)
+    cid = crs.register_client(inspire.ClientPackingKeys(y_body=keys[1][0]))
+    call(1, "all", 4100)
+    call(1, "body", 9)
+    seeds, b_rows = clients[1].query_seeded(9)
+    got = inspire.respond_seeded_batch(crs, edb, [0], seeds[None], b_rows[None], [cid])[0]
+    assert np.array_equal(got, oracle_response(W, "crt_fixed", 0, ctx.expand_rgsw(seeds, b_rows), y_body=keys[1][0]))
+    # reload the same CRS: every key table (the carried keys' too) is freed
+    seed = (C.c_uint8 * 32).from_buffer_copy(W_SEED)
+    assert crs.L.inspire_crs_load(crs.h, C.cast(seed, C.c_void_p), 16) == 0
+    call(0, "body", 1)
+    call(1, "all", 2048)
