@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -320,19 +321,30 @@ struct Json {
 
 // ---------------------------------------------------------------- writer
 struct Out {
-  std::string s;
-  size_t n = 0;  // bytes used in s (s is grown ahead of the writes)
-  void room(size_t k) {
-    if (n + k > s.size()) s.resize(std::max(s.size() * 2, n + k + 4096));
+  // the output so far: n bytes of buf (uninitialised beyond them, so room
+  // reserved ahead of the writes costs no fill)
+  std::unique_ptr<char[]> buf;
+  size_t cap = 0, n = 0;
+  void reserve(size_t c) {
+    if (c <= cap) return;
+    std::unique_ptr<char[]> b(new char[c]);
+    if (n) memcpy(b.get(), buf.get(), n);
+    buf = std::move(b);
+    cap = c;
   }
+  void room(size_t k) {
+    if (n + k > cap) reserve(std::max(cap * 2, n + k + 4096));
+  }
+  const char* data() const { return buf.get(); }
+  bool equals(const std::string& w) const { return n == w.size() && (n == 0 || memcmp(buf.get(), w.data(), n) == 0); }
   void ch(char c) {
     room(1);
-    s[n++] = c;
+    buf[n++] = c;
   }
   void lit(const char* x) {
     const size_t k = strlen(x);
     room(k);
-    memcpy(&s[n], x, k);
+    memcpy(&buf[n], x, k);
     n += k;
   }
   // Decimal digits of v (1..20): for v >= 10, t = floor(bits * 1233 / 4096)
@@ -363,9 +375,41 @@ struct Out {
     const int t = ((64 - __builtin_clzll(v)) * 1233) >> 12;  // t <= 19
     return t + (v >= p10[t] ? 1 : 0);
   }
-  // v in decimal at p (room for 20 bytes), two digits per step from the
-  // right; returns the length
+  // The eight decimal digits of x < 10^8, zero-padded, as ASCII in a u64
+  // whose lowest byte (first in memory on little-endian hosts, x86-64 and
+  // AArch64 alike) is the leading digit.  SWAR: x is split into 4 + 4 digits
+  // in 32-bit lanes, then 2 + 2 in 16-bit lanes, then 1 + 1 in bytes; each
+  // lane's quotient is a multiply and shift, exact in its range
+  // (t / 100 = (t * 5243) >> 19 for t < 43699, u / 10 = (u * 103) >> 10 for
+  // u < 179), and no lane's product reaches the next lane.
+  static uint64_t ascii8(uint32_t x) {
+    const uint32_t hi = x / 10000;
+    uint64_t v = hi | ((uint64_t)(x - hi * 10000) << 32);
+    const uint64_t q = ((v * 5243) >> 19) & 0x0000007F0000007Full;
+    v = q | ((v - q * 100) << 16);
+    const uint64_t q2 = ((v * 103) >> 10) & 0x000F000F000F000Full;
+    v = q2 | ((v - q2 * 10) << 8);
+    return v | 0x3030303030303030ull;
+  }
+  // v in decimal at p; returns the length.  Needs room for 20 bytes: numbers
+  // below 10^16 are stored as whole 8-byte words, so up to 8 bytes past the
+  // number are written too (the next writes overwrite them, or done() cuts
+  // them off).
   static int put_num(char* p, uint64_t v) {
+    if (v < 100000000ull) {
+      const int len = digits(v);
+      const uint64_t w = ascii8((uint32_t)v) >> (8 * (8 - len));
+      memcpy(p, &w, 8);
+      return len;
+    }
+    if (v < 10000000000000000ull) {
+      const uint64_t hi = v / 100000000ull;
+      const int hl = put_num(p, hi);
+      const uint64_t w = ascii8((uint32_t)(v - hi * 100000000ull));
+      memcpy(p + hl, &w, 8);
+      return hl + 8;
+    }
+    // 17 to 20 digits: two per step from the right
     static constexpr char d2[201] =
         "00010203040506070809101112131415161718192021222324252627282930313233343536373839"
         "40414243444546474849505152535455565758596061626364656667686970717273747576777879"
@@ -389,23 +433,34 @@ struct Out {
   }
   void num(uint64_t v) {
     room(20);
-    n += (size_t)put_num(&s[n], v);
+    n += (size_t)put_num(&buf[n], v);
   }
-  // "a0,a1,...,ak-1" (no brackets), room reserved once
+  // "a0,a1,...,ak-1" (no brackets), room reserved once.  Values below 10^9
+  // (every residue) take a path without data-dependent branches (8- and
+  // 9-digit residues are about equally common, so a branch on the length
+  // would be mispredicted): the nine-digit zero-padded string is formed in
+  // a 128-bit value, shifted by the length and stored as 16 bytes.
   void nums(const uint64_t* a, size_t k) {
     room(21 * k + 1);
-    char* p = &s[n];
+    char* p = &buf[n];
     char* const p0 = p;
     for (size_t i = 0; i < k; i++) {
       if (i) *p++ = ',';
-      p += put_num(p, a[i]);
+      const uint64_t v = a[i];
+      if (v < 1000000000ull) {
+        const uint32_t hi = (uint32_t)(v / 100000000ull);
+        const uint64_t w = ascii8((uint32_t)(v - (uint64_t)hi * 100000000ull));
+        const int len = digits(v);
+        const unsigned __int128 z = (((unsigned __int128)w << 8) | (uint64_t)('0' + hi)) >> (8 * (9 - len));
+        memcpy(p, &z, 16);
+        p += len;
+      } else {
+        p += put_num(p, v);
+      }
     }
     n += (size_t)(p - p0);
   }
-  std::string done() {
-    s.resize(n);
-    return std::move(s);
-  }
+  std::string done() const { return std::string(buf.get(), n); }
 };
 
 }  // namespace igjson

@@ -337,13 +337,15 @@ void poly_bincode(std::string& s, const inspire_params& P, const uint64_t* c) {
   s.push_back(0);  // is_ntt
 }
 
-int copy_out(const std::string& s, char* buf, size_t cap, size_t* len) {
-  *len = s.size();
+int copy_out(const char* data, size_t size, char* buf, size_t cap, size_t* len) {
+  *len = size;
   if (!buf) return INSPIRE_OK;  // size query
-  if (cap < s.size()) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "output buffer too small");
-  memcpy(buf, s.data(), s.size());
+  if (cap < size) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "output buffer too small");
+  memcpy(buf, data, size);
   return INSPIRE_OK;
 }
+int copy_out(const std::string& s, char* buf, size_t cap, size_t* len) { return copy_out(s.data(), s.size(), buf, cap, len); }
+int copy_out(const Out& o, char* buf, size_t cap, size_t* len) { return copy_out(o.data(), o.n, buf, cap, len); }
 
 bool params_ok(const inspire_params* P) {
   return P && P->ring_dim > 0 && P->crt_count == 2 && P->gadget_len > 0 && P->crt_moduli[0] > 1 &&
@@ -491,7 +493,8 @@ int inspire_query_response_to_json(const inspire_params* P, const uint64_t* ct, 
                                    size_t* len) {
   if (!params_ok(P) || !ct || !len || (n_columns && !columns)) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   Out o;
-  o.s.resize((size_t)(2 + 2 * n_columns) * 2 * P->ring_dim * 11 + 512);
+  // every coefficient array's worst-case reservation fits without growing
+  o.reserve((size_t)(2 + 2 * n_columns) * 2 * P->ring_dim * 21 + 512);
   o.lit("{\"response\":{\"ciphertext\":");
   rlwe_json(o, *P, ct);
   o.lit(",\"column_ciphertexts\":[");
@@ -502,7 +505,7 @@ int inspire_query_response_to_json(const inspire_params* P, const uint64_t* ct, 
   o.lit("]},\"processing_time_ms\":");
   o.num(processing_time_ms);
   o.ch('}');
-  return copy_out(o.done(), buf, cap, len);
+  return copy_out(o, buf, cap, len);
 }
 
 int inspire_server_response_to_bincode(const inspire_params* P, const uint64_t* ct, uint32_t n_columns,
@@ -695,7 +698,7 @@ int inspire_packed_response_to_json(const inspire_params* P, const uint64_t* a, 
   if (!params_ok(P) || !a || !b || !len) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "null argument");
   if (b_words == 0 || b_words % 2) return fail(INSPIRE_ERR_INVALID_ARGUMENT, "b_words must be a positive even count");
   Out o;
-  o.s.resize((size_t)(2 * P->ring_dim + b_words) * 11 + 1024);
+  o.reserve((size_t)(2 * P->ring_dim + b_words) * 21 + 1024);
   o.lit("{\"response\":{\"ciphertext\":{\"a\":");
   poly_json_dim(o, *P, a, P->ring_dim);
   o.lit(",\"b\":");
@@ -703,7 +706,7 @@ int inspire_packed_response_to_json(const inspire_params* P, const uint64_t* a, 
   o.lit("},\"column_ciphertexts\":[]},\"processing_time_ms\":");
   o.num(processing_time_ms);
   o.ch('}');
-  return copy_out(o.done(), buf, cap, len);
+  return copy_out(o, buf, cap, len);
 }
 
 int inspire_crs_write_json(const inspire_params* P, const inspire_server_crs* crs, const char* path) {
@@ -715,11 +718,11 @@ int inspire_crs_write_json(const inspire_params* P, const inspire_server_crs* cr
   FILE* f = fopen(path, "wb");
   if (!f) return fail(INSPIRE_ERR_INVALID_ARGUMENT, std::string("cannot create ") + path);
   Out o;
-  o.s.resize(1 << 24);
+  o.reserve(1 << 24);
   bool io_ok = true;
   auto flush = [&](bool force) {
     if (o.n >= (1u << 23) || (force && o.n)) {
-      io_ok &= fwrite(o.s.data(), 1, o.n, f) == o.n;
+      io_ok &= fwrite(o.data(), 1, o.n, f) == o.n;
       o.n = 0;
     }
   };

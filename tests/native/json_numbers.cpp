@@ -123,12 +123,22 @@ int main() {
       o.n = 0;
       o.num(vals[i]);
       const std::string w = std::to_string(vals[i]);
-      check(o.n == w.size() && o.s.compare(0, o.n, w) == 0, "num " + w);
+      check(o.equals(w), "num " + w);
     }
     o.n = 0;
-    o.nums(vals.data(), 5000);
-    for (size_t i = 0; i < 5000; i++) want += (i ? "," : "") + std::to_string(vals[i]);
-    check(o.n == want.size() && o.s.compare(0, o.n, want) == 0, "nums");
+    o.nums(vals.data(), vals.size());
+    for (size_t i = 0; i < vals.size(); i++) want += (i ? "," : "") + std::to_string(vals[i]);
+    check(o.equals(want), "nums");
+    // after other output, and finished with done(): no byte past a number
+    // survives
+    igjson::Out o2;
+    o2.lit("[");
+    o2.nums(vals.data() + 1000000, 64);
+    o2.lit("]");
+    std::string w2 = "[";
+    for (size_t i = 0; i < 64; i++) w2 += (i ? "," : "") + std::to_string(vals[1000000 + i]);
+    w2 += "]";
+    check(o2.done() == w2, "nums between literals");
   }
   if (fails) {
     std::printf("%d failures\n", fails);
