@@ -67,9 +67,11 @@ bool run_poly_job(const PolyJob& jb) {
 // that finds them busy parses its arrays itself.
 class ParsePool {
  public:
+  // Up to 8 workers (a seeded query with keys has 9 arrays: with the caller
+  // they parse in one round), leaving two cores to the rest of the process.
   ParsePool() : pid_(getpid()) {
-    const unsigned hw = std::max(2u, std::thread::hardware_concurrency());
-    const unsigned n = std::min(8u, std::max(1u, hw / 2 - 1));
+    const unsigned hw = std::max(3u, std::thread::hardware_concurrency());
+    const unsigned n = std::min(8u, hw - 2);
     for (unsigned i = 0; i < n; i++) workers_.emplace_back([this] { work(); });
   }
   // Runs every job; true if all succeeded.
