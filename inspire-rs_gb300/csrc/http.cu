@@ -182,14 +182,18 @@ struct Reader {
       if (!fill()) return false;
     }
   }
+  // n bytes: what is buffered, then received straight into `out` (a query
+  // body of ~355 KB is not copied through the line buffer)
   bool bytes(size_t n, std::string& out) {
-    out.clear();
-    out.reserve(n);
-    while (out.size() < n) {
-      if (pos == buf.size() && !fill()) return false;
-      const size_t take = std::min(n - out.size(), buf.size() - pos);
-      out.append(buf, pos, take);
-      pos += take;
+    const size_t have = std::min(n, buf.size() - pos);
+    out.assign(buf, pos, have);
+    pos += have;
+    if (have == n) return true;
+    out.resize(n);
+    for (size_t got = have; got < n;) {
+      const ssize_t k = ::recv(fd, &out[got], n - got, 0);
+      if (k <= 0) return false;
+      got += (size_t)k;
     }
     return true;
   }
