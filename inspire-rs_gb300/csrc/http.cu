@@ -137,12 +137,16 @@ bool send_all(int fd, const char* p, size_t n) {
   return true;
 }
 
-bool reply(int fd, int status, const char* reason, const std::string& ctype, const std::string& body,
+bool reply(int fd, int status, const char* reason, const std::string& ctype, const char* body, size_t n,
            bool keep_alive) {
   std::string h = "HTTP/1.1 " + std::to_string(status) + " " + reason + "\r\ncontent-type: " + ctype +
-                  "\r\ncontent-length: " + std::to_string(body.size()) + "\r\n" +
+                  "\r\ncontent-length: " + std::to_string(n) + "\r\n" +
                   (keep_alive ? "" : "connection: close\r\n") + "\r\n";
-  return send_all(fd, h.data(), h.size()) && send_all(fd, body.data(), body.size());
+  return send_all(fd, h.data(), h.size()) && send_all(fd, body, n);
+}
+bool reply(int fd, int status, const char* reason, const std::string& ctype, const std::string& body,
+           bool keep_alive) {
+  return reply(fd, status, reason, ctype, body.data(), body.size(), keep_alive);
 }
 
 const char* JSON = "application/json";
@@ -182,14 +186,14 @@ struct Reader {
       if (!fill()) return false;
     }
   }
-  // n bytes: what is buffered, then received straight into `out` (a query
-  // body of ~355 KB is not copied through the line buffer)
+  // n bytes into `out`: what is buffered, then received straight into it (a
+  // query body of ~355 KB is not copied through the line buffer, and a
+  // connection's requests of one size reuse the string without refilling it)
   bool bytes(size_t n, std::string& out) {
     const size_t have = std::min(n, buf.size() - pos);
-    out.assign(buf, pos, have);
-    pos += have;
-    if (have == n) return true;
     out.resize(n);
+    if (have) memcpy(&out[0], buf.data() + pos, have);
+    pos += have;
     for (size_t got = have; got < n;) {
       const ssize_t k = ::recv(fd, &out[got], n - got, 0);
       if (k <= 0) return false;
@@ -301,7 +305,12 @@ bool inspire_http_server::handle(int fd, const std::string& method, const std::s
                        (ctt.rfind("application/", 0) == 0 && ctt.size() > 5 && ctt.substr(ctt.size() - 5) == "+json");
   if (!json_ct) return reply(fd, 415, "Unsupported Media Type", TEXT, "Expected request with `Content-Type: application/json`", ka);
   const size_t pw = poly_words();
-  std::vector<uint64_t> rows((seeded ? 1 : 2) * (size_t)2 * ELL * pw), y_body((size_t)ELL * pw);
+  // per connection thread, reused by its requests (no zero fill per request;
+  // the parser writes every word that is used)
+  thread_local std::vector<uint64_t> rows, y_body, ct2;
+  thread_local std::string out;
+  rows.resize((seeded ? 1 : 2) * (size_t)2 * ELL * pw);
+  y_body.resize((size_t)ELL * pw);
   uint8_t seeds[2 * ELL * 32];
   uint32_t sid = 0;
   int32_t mode = 0, keys = 0;
@@ -329,7 +338,6 @@ bool inspire_http_server::handle(int fd, const std::string& method, const std::s
   auto fail_reply = [&](const std::string& msg) {
     return reply(fd, 400, "Bad Request", JSON, "{\"error\":\"" + json_escape(prefix + msg) + "\"}", ka);
   };
-  std::string out;
   size_t len = 0;
   if (mode == 1) {  // tree packing
     std::vector<uint64_t> a(pw), b(2 * pw);
@@ -344,14 +352,13 @@ bool inspire_http_server::handle(int fd, const std::string& method, const std::s
     }
     if (rc != INSPIRE_OK) return fail_reply(inspire_last_error());
     const uint64_t ms = ms_since();
-    out.resize((pw + words) * 21 + 1024);
+    if (out.size() < (pw + words) * 21 + 1024) out.resize((pw + words) * 21 + 1024);
     if (inspire_packed_response_to_json(&P, a.data(), b.data(), words, ms, &out[0], out.size(), &len) != INSPIRE_OK)
       return reply(fd, 500, "Internal Server Error", TEXT, inspire_last_error(), ka);
-    out.resize(len);
-    return reply(fd, 200, "OK", JSON, out, ka);
+    return reply(fd, 200, "OK", JSON, out.data(), len, ka);
   }
   if (keys == 0) return reply(fd, 400, "Bad Request", JSON, std::string("{\"error\":\"") + KEYS_MISSING + "\"}", ka);
-  std::vector<uint64_t> ct2(2 * pw);
+  ct2.resize(2 * pw);
   if (keys == 2 || !seeded || !srv) {
     // keys with an empty y_body (the crate's "keys invalid"), full queries,
     // or no serving loop: the synchronous call, keys in the query
@@ -387,11 +394,10 @@ bool inspire_http_server::handle(int fd, const std::string& method, const std::s
     if (rc != INSPIRE_OK) return fail_reply(inspire_last_error());
   }
   const uint64_t ms = ms_since();
-  out.resize(2 * pw * 21 + 1024);
+  if (out.size() < 2 * pw * 21 + 1024) out.resize(2 * pw * 21 + 1024);
   if (inspire_query_response_to_json(&P, ct2.data(), 0, nullptr, ms, &out[0], out.size(), &len) != INSPIRE_OK)
     return reply(fd, 500, "Internal Server Error", TEXT, inspire_last_error(), ka);
-  out.resize(len);
-  return reply(fd, 200, "OK", JSON, out, ka);
+  return reply(fd, 200, "OK", JSON, out.data(), len, ka);
 }
 
 void inspire_http_server::serve(int fd) {
@@ -438,8 +444,8 @@ void inspire_http_server::serve(int fd) {
       reply(fd, 400, "Bad Request", TEXT, "bad content-length", false);
       break;
     }
-    body.clear();
     if (chunked) {
+      body.clear();
       for (;;) {
         if (!r.line(line)) return;
         const size_t n = strtoull(line.c_str(), nullptr, 16);
@@ -461,7 +467,8 @@ void inspire_http_server::serve(int fd) {
         reply(fd, 413, "Payload Too Large", TEXT, "length limit exceeded", false);
         break;
       }
-      if (clen && !r.bytes(clen, body)) break;
+      if (!clen) body.clear();
+      else if (!r.bytes(clen, body)) break;
     }
     if (!handle(fd, method, path, ctype, body, ka) || !ka) break;
   }
