@@ -211,25 +211,69 @@ void release_keys(inspire_ctx* c, int32_t id) {
   if (id == c->inline_id) c->inline_id = -1;
 }
 
-// Stage n queries (rows ELL..2ELL-1 only) and run the Respond kernel.
-// seeds/b_rows/a_rows use the full 2*ELL-row host layout.
-// a_rows/b_rows point at the first needed poly of query 0 (ELL contiguous
-// polys per query, query pitch `stride_polys`); seeds at the first needed seed
-// (ELL contiguous seeds, query pitch `seed_stride` bytes).
 int finish_status(inspire_ctx* c, uint32_t n, const char* what);
 
 // Batches up to this size stage their inputs through page-locked memory.
 constexpr uint32_t STAGE_PINNED_MAX = 64;
 
+// Seeded queries whose rows and responses are in page-locked host memory
+// (device addresses d_rows, row_bytes apart, and d_out): the serving variant
+// of the kernel reads each query's rows in place and writes its response
+// straight to that memory, so nothing is staged or copied back.
+int run_batch_mapped(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
+                     size_t seed_stride, const uint8_t* d_rows, size_t row_bytes, uint64_t* d_out,
+                     const int32_t* client_ids) {
+  const size_t pw = poly_words();
+  // descriptors and status words in page-locked memory: the descriptors go
+  // over by DMA, the kernel writes each status word in place
+  CUDA_TRY(c->d_desc.ensure(sizeof(QueryDesc) * n));
+  CUDA_TRY(c->h_desc.ensure(sizeof(QueryDesc) * n));
+  CUDA_TRY(c->h_qstatus.ensure(sizeof(int32_t) * n));
+  QueryDesc* hd = c->h_desc.host<QueryDesc>();
+  int32_t* hs = c->h_qstatus.host<int32_t>();
+  const DbView view{db->E.as<uint32_t>(), db->H.as<uint16_t>(), db->nshards, 0};
+  for (uint32_t i = 0; i < n; i++) {
+    QueryDesc& d = hd[i];
+    memcpy(d.seeds, seeds + i * seed_stride, sizeof(d.seeds));
+    d.brows = reinterpret_cast<const uint64_t*>(d_rows + i * row_bytes);
+    d.out = d_out + (size_t)i * 2 * pw;
+    d.status = c->h_qstatus.dev<int32_t>() + i;
+    d.db = view;
+    d.shard = shard_ids[i];
+    d.client = client_ids[i];
+    hs[i] = -1;
+  }
+  CUDA_TRY(cudaMemcpyAsync(c->d_desc.p, hd, sizeof(QueryDesc) * n, cudaMemcpyHostToDevice, c->stream));
+  if (int rc = sync_client_table(c)) return rc;
+  RespondArgs a{};
+  a.P = c->P;
+  a.nq = (int)n;
+  a.yhat_table = c->client_table.as<const uint32_t*>();
+  a.nclients = (int)c->client_ptrs.size();
+  a.what = c->what3.as<uint32_t>();
+  a.qdesc = c->d_desc.as<QueryDesc>();
+  a.stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
+  CUDA_TRY(launch_respond(a, true, c->stream, 0, c->pair_max.load()));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  for (uint32_t i = 0; i < n; i++)
+    if (hs[i] != 0)
+      return fail(INSPIRE_ERR_DEVICE_STATUS,
+                  "respond kernel status " + std::to_string(hs[i]) + " for query " + std::to_string(i));
+  return INSPIRE_OK;
+}
+
+// Stage n queries (rows ELL..2ELL-1 only) and run the Respond kernel.
+// seeds/b_rows/a_rows use the full 2*ELL-row host layout.
+// a_rows/b_rows point at the first needed poly of query 0 (ELL contiguous
+// polys per query, query pitch `stride_polys`); seeds at the first needed seed
+// (ELL contiguous seeds, query pitch `seed_stride` bytes).
 int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* shard_ids, const uint8_t* seeds,
               size_t seed_stride, const uint64_t* a_rows, const uint64_t* b_rows, size_t stride_polys,
               const int32_t* client_ids, uint64_t* out_ct) {
   if (n == 0) return INSPIRE_OK;
   const size_t pw = poly_words();
   if (seeds) {
-    // Page-locked rows and responses (16-byte aligned): the serving variant
-    // of the kernel reads each query's rows in place and writes its response
-    // straight to the caller's memory, so nothing is staged or copied back.
+    // page-locked rows and responses (16-byte aligned): read and written in place
     const size_t row_bytes = sizeof(uint64_t) * stride_polys * pw;
     const size_t rows_span = row_bytes * (n - 1) + sizeof(uint64_t) * ELL * pw;
     const size_t out_span = sizeof(uint64_t) * n * 2 * pw;
@@ -237,42 +281,22 @@ int run_batch(inspire_ctx* c, const inspire_db* db, uint32_t n, const uint32_t* 
                                 ? mapped_range(b_rows, rows_span)
                                 : nullptr;
     const uint8_t* d_outp = d_rows ? mapped_range(out_ct, out_span) : nullptr;
-    if (d_rows && d_outp) {
-      // descriptors and status words in page-locked memory: the descriptors
-      // go over by DMA, the kernel writes each status word in place
-      CUDA_TRY(c->d_desc.ensure(sizeof(QueryDesc) * n));
-      CUDA_TRY(c->h_desc.ensure(sizeof(QueryDesc) * n));
-      CUDA_TRY(c->h_qstatus.ensure(sizeof(int32_t) * n));
-      QueryDesc* hd = c->h_desc.host<QueryDesc>();
-      int32_t* hs = c->h_qstatus.host<int32_t>();
-      const DbView view{db->E.as<uint32_t>(), db->H.as<uint16_t>(), db->nshards, 0};
-      for (uint32_t i = 0; i < n; i++) {
-        QueryDesc& d = hd[i];
-        memcpy(d.seeds, seeds + i * seed_stride, sizeof(d.seeds));
-        d.brows = reinterpret_cast<const uint64_t*>(d_rows + i * row_bytes);
-        d.out = const_cast<uint64_t*>(reinterpret_cast<const uint64_t*>(d_outp)) + (size_t)i * 2 * pw;
-        d.status = c->h_qstatus.dev<int32_t>() + i;
-        d.db = view;
-        d.shard = shard_ids[i];
-        d.client = client_ids[i];
-        hs[i] = -1;
-      }
-      CUDA_TRY(cudaMemcpyAsync(c->d_desc.p, hd, sizeof(QueryDesc) * n, cudaMemcpyHostToDevice, c->stream));
-      if (int rc = sync_client_table(c)) return rc;
-      RespondArgs a{};
-      a.P = c->P;
-      a.nq = (int)n;
-      a.yhat_table = c->client_table.as<const uint32_t*>();
-      a.nclients = (int)c->client_ptrs.size();
-      a.what = c->what3.as<uint32_t>();
-      a.qdesc = c->d_desc.as<QueryDesc>();
-      a.stage_wait_iters = STAGE_WAIT_ITERS_DEFAULT;
-      CUDA_TRY(launch_respond(a, true, c->stream, 0, c->pair_max.load()));
-      CUDA_TRY(cudaStreamSynchronize(c->stream));
-      for (uint32_t i = 0; i < n; i++)
-        if (hs[i] != 0)
-          return fail(INSPIRE_ERR_DEVICE_STATUS,
-                      "respond kernel status " + std::to_string(hs[i]) + " for query " + std::to_string(i));
+    if (d_rows && d_outp)
+      return run_batch_mapped(c, db, n, shard_ids, seeds, seed_stride, d_rows, row_bytes,
+                              const_cast<uint64_t*>(reinterpret_cast<const uint64_t*>(d_outp)), client_ids);
+    if (n <= STAGE_PINNED_MAX) {
+      // small batches in other memory: the rows gathered into page-locked
+      // memory and read there in place, the responses written to page-locked
+      // memory and copied out once (no copies to and from the device)
+      const size_t rows_b = sizeof(uint64_t) * ELL * pw;
+      CUDA_TRY(c->h_stage.ensure(rows_b * n));
+      CUDA_TRY(c->h_out.ensure(out_span));
+      uint8_t* hb = c->h_stage.host<uint8_t>();
+      for (uint32_t i = 0; i < n; i++) memcpy(hb + rows_b * i, b_rows + i * stride_polys * pw, rows_b);
+      if (int rc = run_batch_mapped(c, db, n, shard_ids, seeds, seed_stride, c->h_stage.dev<uint8_t>(), rows_b,
+                                    c->h_out.dev<uint64_t>(), client_ids))
+        return rc;
+      memcpy(out_ct, c->h_out.host<uint64_t>(), out_span);
       return INSPIRE_OK;
     }
   }

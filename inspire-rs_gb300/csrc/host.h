@@ -160,6 +160,7 @@ struct inspire_ctx {
   ighost::HostPinned h_qstatus; // status words of the batch calls, written by the kernel
   ighost::HostPinned h_stage;   // small batches' inputs, gathered for one DMA each
   ighost::HostPinned h_keys;    // client keys on their way to d_keys
+  ighost::HostPinned h_out;     // responses of staged small batches, written by the kernel
   cudaEvent_t keys_ev = nullptr;  // recorded after the copy out of h_keys
 
   inspire_ctx() {
