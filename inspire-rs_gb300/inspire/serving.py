@@ -282,7 +282,7 @@ def run(server, targets: List[Target], pool: QueryPool, client_id: int, *, rate:
 
 
 def autotune(make_server, targets: List[Target], pool: QueryPool, client_id: int, *,
-             batches=(128, 152, 256), inflight=(4, 8), waits_us=(100,), n_queries: int = 1 << 15,
+             batches=(128, 152, 256), inflight=(4, 8), waits_us=(25, 100), n_queries: int = 1 << 15,
              n_threads: int = 4, tie: float = 0.01) -> dict:
     """Pick the serving configuration (max_batch, max_inflight,
     batch_wait_us) by saturated closed-loop rate: among the candidates within
