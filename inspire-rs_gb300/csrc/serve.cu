@@ -172,11 +172,13 @@ void inspire_server::run() {
       }
       // SMs the batches in flight occupy: a batch of at most pair_max
       // queries runs on the two-CTA cluster kernel (two SMs per query, the
-      // lower latency) when those SMs are idle or nearly so (up to a quarter
-      // of the SMs over: on a busy GPU an SM frees about every microsecond),
-      // else on one CTA per query (the higher rate per SM, which a loaded GPU
-      // needs).  Measured with Poisson arrivals, no slack at all lengthened
-      // the 50 %-load p99, half the SMs the 90 %-load p50.
+      // lower latency) when those SMs are idle, else on one CTA per query
+      // (the higher rate per SM, which a loaded GPU needs: the cluster kernel
+      // alone serves at most ~70 % of the one-CTA rate).  While at most half
+      // the SMs are busy a cluster batch may exceed the idle SMs by a quarter
+      // of the SM count (an SM frees about every microsecond); that slack at
+      // any load let cluster batches starve a 75 %-load stream (measured:
+      // the achieved rate fell below the offered one, p99 > 100 ms).
       const size_t pair_max = (size_t)std::max(0, ctx->pair_max.load(std::memory_order_relaxed));
       size_t inflight_sm = 0;
       for (const auto& sp : slots) inflight_sm += sp->busy ? (sp->pair ? 2 : 1) * sp->recs.size() : 0;
@@ -199,7 +201,8 @@ void inspire_server::run() {
         s.busy = true;
         n_batches++;
         const size_t nb = s.recs.size();
-        s.pair = nb <= pair_max && inflight_sm + 2 * nb <= (size_t)(sm_count + sm_count / 4);
+        const size_t slack = inflight_sm <= (size_t)sm_count / 2 ? (size_t)sm_count / 4 : 0;
+        s.pair = nb <= pair_max && inflight_sm + 2 * nb <= (size_t)sm_count + slack;
         inflight_sm += (s.pair ? 2 : 1) * nb;
         to_launch.push_back(&s);
       }
