@@ -611,14 +611,18 @@ int inspire_server_drive(inspire_server* s, uint32_t n, const inspire_db* const*
   const size_t seed_bytes = (size_t)64 * ELL, row_words = (size_t)2 * ELL * pw;
   std::vector<uint64_t> tickets(n);
   std::atomic<uint32_t> n_sub{0};
-  std::atomic<int> stop_rc{INSPIRE_OK};
+  std::atomic<int> stop_rc{INSPIRE_OK};   // a failed poll: both threads stop
+  std::atomic<bool> submit_end{false};    // the submitter has stopped (done or failed)
   std::string collector_err;
   // collector: every ticket in submission order, its completion time (the
-  // serving loop's) and, for the first n_keep queries, the response
+  // serving loop's) and, for the first n_keep queries, the response; after a
+  // failed submission it still collects every ticket already accepted, so
+  // that none is left behind in the server
   std::thread collector([&] {
     uint32_t k = 0;
     while (k < n && stop_rc.load() == INSPIRE_OK) {
       if (k >= n_sub.load(std::memory_order_acquire)) {
+        if (submit_end.load(std::memory_order_acquire) && k >= n_sub.load(std::memory_order_acquire)) break;
         std::this_thread::yield();
         continue;
       }
@@ -638,7 +642,7 @@ int inspire_server_drive(inspire_server* s, uint32_t n, const inspire_db* const*
   // already due in one call (one contiguous run of the pool), retrying on
   // backpressure
   uint32_t k = 0;
-  int rc = INSPIRE_OK;
+  int rc = INSPIRE_OK, submit_rc = INSPIRE_OK;
   std::string submit_err;
   while (k < n && stop_rc.load() == INSPIRE_OK) {
     const int64_t now = now_ns();
@@ -667,15 +671,15 @@ int inspire_server_drive(inspire_server* s, uint32_t n, const inspire_db* const*
     }
     if (rc != INSPIRE_OK) {
       submit_err = g_last_error;
-      int expected = INSPIRE_OK;
-      stop_rc.compare_exchange_strong(expected, rc);
+      submit_rc = rc;
       break;
     }
   }
+  submit_end.store(true, std::memory_order_release);
   collector.join();
+  if (submit_rc != INSPIRE_OK) return fail(submit_rc, "drive: " + submit_err);
   const int final_rc = stop_rc.load();
-  if (final_rc != INSPIRE_OK)
-    return fail(final_rc, "drive: " + (submit_err.empty() ? collector_err : submit_err));
+  if (final_rc != INSPIRE_OK) return fail(final_rc, "drive: " + collector_err);
   return INSPIRE_OK;
 }
 

@@ -386,3 +386,40 @@ def test_native_open_loop_driver(world):
         pr.close()
     finally:
         srv.close()
+
+
+def test_native_driver_stops_on_an_invalid_query(world):
+    """A query naming a missing shard in the middle of a driven stream ends
+    Server.drive with the crate's error, promptly (the collector stops too),
+    and the server keeps answering afterwards."""
+    import time
+
+    W = world
+    inspire = W["inspire"]
+    from inspire.pir import now_ns
+
+    qs = make_queries(W, 4)
+    want = alone(W, qs[0])
+    pool_seeds = np.ascontiguousarray(np.stack([q["seeds"] for q in qs]))
+    pool_rows = np.ascontiguousarray(np.stack([q["b_rows"] for q in qs]))
+    n = 400
+    srv = inspire.Server(W["crs"], max_batch=32, max_inflight=2, capacity=128)
+    try:
+        handles = np.array([srv.handle_of(W["dbs"][qs[k % 4]["db"]]) for k in range(n)], dtype=np.uint64)
+        shards = np.array([qs[k % 4]["shard"] for k in range(n)], dtype=np.uint32)
+        shards[150] = 10_000  # no such shard in any database
+        cids = np.array([W["ids"][qs[k % 4]["client"]] for k in range(n)], dtype=np.int32)
+        arrivals = now_ns() + 2_000_000 + np.arange(n, dtype=np.int64) * 5_000
+        t0 = time.monotonic()
+        with pytest.raises(inspire.PirError, match="not found"):
+            srv.drive(handles, shards, cids, pool_seeds, pool_rows, arrivals)
+        assert time.monotonic() - t0 < 10.0
+        st = srv.stats()  # every accepted query was collected
+        assert st["pending"] == 0 and st["submitted"] == st["completed"] == 150
+        t, rc = srv.submit(W["dbs"][qs[0]["db"]], [qs[0]["shard"]], qs[0]["seeds"][None], qs[0]["b_rows"][None],
+                           [W["ids"][qs[0]["client"]]])
+        assert rc == 0
+        out = np.zeros((1, 2, 2 * N), dtype=np.uint64)
+        assert len(srv.poll_batch(t, out)) == 1 and np.array_equal(out[0], want)
+    finally:
+        srv.close()
