@@ -791,7 +791,9 @@ class Server:
         rows of pool entry k mod len(pool_seeds), by a native thread spinning
         on the clock; a second native thread collects.  db_handles
         (handle_of values), shard_ids and client_ids are per query.  Returns
-        (submit_ns, done_ns, responses of the first n_keep queries or None)."""
+        (submit_ns, done_ns, responses of the first n_keep queries or None).
+        A rejected query raises PirError with the submission's error after
+        the queries accepted before it have been collected."""
         arr = np.ascontiguousarray(arrival_ns, dtype=np.int64)
         n = arr.size
         dbs = np.ascontiguousarray(db_handles, dtype=np.uint64)
