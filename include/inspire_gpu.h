@@ -433,8 +433,9 @@ int inspire_server_poll_batch(inspire_server *srv, uint32_t n, const uint64_t *t
  * call, and out_keep the responses of the first n_keep queries (n_keep x
  * [a poly, b poly]).  Latency from arrival is done_ns - arrival_ns.  A
  * rejected query (an unknown shard or client, as inspire_server_submit
- * reports it) ends the submissions; the queries accepted before it are
- * still collected, then that error is returned. */
+ * reports it) or a query that fails on the device (as inspire_server_poll
+ * reports it) ends the submissions; every query accepted until then is
+ * still collected, then the first error is returned. */
 int inspire_server_drive(inspire_server *srv, uint32_t n, const inspire_db *const *dbs, const uint32_t *shard_ids,
                          const int32_t *client_ids, const uint8_t *pool_seeds, const uint64_t *pool_b_rows,
                          uint32_t pool_size, const int64_t *arrival_ns, uint32_t flags, uint32_t max_burst,

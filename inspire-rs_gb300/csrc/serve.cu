@@ -611,16 +611,17 @@ int inspire_server_drive(inspire_server* s, uint32_t n, const inspire_db* const*
   const size_t seed_bytes = (size_t)64 * ELL, row_words = (size_t)2 * ELL * pw;
   std::vector<uint64_t> tickets(n);
   std::atomic<uint32_t> n_sub{0};
-  std::atomic<int> stop_rc{INSPIRE_OK};   // a failed poll: both threads stop
+  std::atomic<int> stop_rc{INSPIRE_OK};   // the first failed query: the submitter stops
   std::atomic<bool> submit_end{false};    // the submitter has stopped (done or failed)
   std::string collector_err;
   // collector: every ticket in submission order, its completion time (the
-  // serving loop's) and, for the first n_keep queries, the response; after a
-  // failed submission it still collects every ticket already accepted, so
-  // that none is left behind in the server
+  // serving loop's) and, for the first n_keep queries, the response.  A
+  // failed query (its ticket is consumed all the same) or a rejected
+  // submission stops the submissions, and the collector still collects every
+  // ticket already accepted, so that none is left behind in the server.
   std::thread collector([&] {
     uint32_t k = 0;
-    while (k < n && stop_rc.load() == INSPIRE_OK) {
+    while (k < n) {
       if (k >= n_sub.load(std::memory_order_acquire)) {
         if (submit_end.load(std::memory_order_acquire) && k >= n_sub.load(std::memory_order_acquire)) break;
         std::this_thread::yield();
@@ -630,10 +631,9 @@ int inspire_server_drive(inspire_server* s, uint32_t n, const inspire_db* const*
                                          done_ns + k, 2000);
       if (rc == INSPIRE_PENDING) continue;
       if (rc != INSPIRE_OK) {
-        collector_err = g_last_error;
         int expected = INSPIRE_OK;
-        stop_rc.compare_exchange_strong(expected, rc);
-        break;
+        if (stop_rc.compare_exchange_strong(expected, rc)) collector_err = g_last_error;
+        if (rc == INSPIRE_ERR_INVALID_ARGUMENT) break;  // the ticket was not ours to collect
       }
       k++;
     }

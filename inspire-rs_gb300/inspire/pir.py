@@ -792,8 +792,9 @@ class Server:
         on the clock; a second native thread collects.  db_handles
         (handle_of values), shard_ids and client_ids are per query.  Returns
         (submit_ns, done_ns, responses of the first n_keep queries or None).
-        A rejected query raises PirError with the submission's error after
-        the queries accepted before it have been collected."""
+        A rejected query, or one that fails on the device, stops the
+        submissions and raises PirError with the first error, after every
+        query accepted until then has been collected."""
         arr = np.ascontiguousarray(arrival_ns, dtype=np.int64)
         n = arr.size
         dbs = np.ascontiguousarray(db_handles, dtype=np.uint64)

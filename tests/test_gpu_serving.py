@@ -423,3 +423,32 @@ def test_native_driver_stops_on_an_invalid_query(world):
         assert len(srv.poll_batch(t, out)) == 1 and np.array_equal(out[0], want)
     finally:
         srv.close()
+
+
+@pytest.mark.gpu
+def test_native_driver_collects_every_query_after_a_device_failure(world):
+    """Every driven query fails on the device (the rows' bounded wait set to
+    run out at once): Server.drive ends with the device status of the first
+    failure, and every query submitted before the submitter stopped has been
+    collected, so that no record is left occupied in the server."""
+    W = world
+    inspire = W["inspire"]
+    from inspire.pir import now_ns
+
+    qs = make_queries(W, 4)
+    pool_seeds = np.ascontiguousarray(np.stack([q["seeds"] for q in qs]))
+    pool_rows = np.ascontiguousarray(np.stack([q["b_rows"] for q in qs]))
+    n = 300
+    srv = inspire.Server(W["crs"], max_batch=16, max_inflight=2, capacity=64, stage_wait_iters=0)
+    try:
+        handles = np.array([srv.handle_of(W["dbs"][qs[k % 4]["db"]]) for k in range(n)], dtype=np.uint64)
+        shards = np.array([qs[k % 4]["shard"] for k in range(n)], dtype=np.uint32)
+        cids = np.array([W["ids"][qs[k % 4]["client"]] for k in range(n)], dtype=np.int32)
+        arrivals = now_ns() + 2_000_000 + np.arange(n, dtype=np.int64) * 5_000
+        with pytest.raises(inspire.PirError, match="did not reach the GPU|batch dropped"):
+            srv.drive(handles, shards, cids, pool_seeds, pool_rows, arrivals)
+        st = srv.stats()
+        assert st["pending"] == 0 and st["inflight_batches"] == 0
+        assert 0 < st["submitted"] == st["completed"] <= n
+    finally:
+        srv.close()
