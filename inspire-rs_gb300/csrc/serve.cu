@@ -25,6 +25,7 @@
 #include <cuda.h>
 
 #include "host.h"
+#include "serve_policy.h"
 
 using namespace ig;
 using namespace ighost;
@@ -170,25 +171,16 @@ void inspire_server::run() {
         s.recs.clear();
         s.busy = false;
       }
-      // SMs the batches in flight occupy: a batch of at most pair_max
-      // queries runs on the two-CTA cluster kernel (two SMs per query, the
-      // lower latency) when those SMs are idle, else on one CTA per query
-      // (the higher rate per SM, which a loaded GPU needs: the cluster kernel
-      // alone serves at most ~70 % of the one-CTA rate).  While at most half
-      // the SMs are busy a cluster batch may exceed the idle SMs by a quarter
-      // of the SM count (an SM frees about every microsecond); that slack at
-      // any load let cluster batches starve a 75 %-load stream (measured:
-      // the achieved rate fell below the offered one, p99 > 100 ms).
+      // SMs the batches in flight occupy, then each free stream takes the
+      // next batch (launch_batch_now) on the kernel use_pair_kernel picks
+      // (serve_policy.h)
       const size_t pair_max = (size_t)std::max(0, ctx->pair_max.load(std::memory_order_relaxed));
       size_t inflight_sm = 0;
-      for (const auto& sp : slots) inflight_sm += sp->busy ? (sp->pair ? 2 : 1) * sp->recs.size() : 0;
+      for (const auto& sp : slots) inflight_sm += sp->busy ? batch_sms(sp->pair, sp->recs.size()) : 0;
       for (auto& sp : slots) {
         if (sp->busy || pending.empty()) continue;
-        // Batch formation: a full batch goes at once; a partial one goes at
-        // once while the GPU has idle SMs, else when its oldest query has
-        // waited batch_wait_us (the batches in flight keep the GPU busy).
-        if (pending.size() < cfg.max_batch && inflight_sm >= (size_t)sm_count &&
-            now_ns() - recs[pending.front()].t_enqueue < (int64_t)cfg.batch_wait_us * 1000)
+        if (!launch_batch_now(pending.size(), cfg.max_batch, inflight_sm, (size_t)sm_count,
+                              now_ns() - recs[pending.front()].t_enqueue, (int64_t)cfg.batch_wait_us * 1000))
           break;
         Slot& s = *sp;
         s.recs.clear();
@@ -201,9 +193,8 @@ void inspire_server::run() {
         s.busy = true;
         n_batches++;
         const size_t nb = s.recs.size();
-        const size_t slack = inflight_sm <= (size_t)sm_count / 2 ? (size_t)sm_count / 4 : 0;
-        s.pair = nb <= pair_max && inflight_sm + 2 * nb <= (size_t)sm_count + slack;
-        inflight_sm += (s.pair ? 2 : 1) * nb;
+        s.pair = use_pair_kernel(nb, pair_max, inflight_sm, (size_t)sm_count);
+        inflight_sm += batch_sms(s.pair, nb);
         to_launch.push_back(&s);
       }
       bool any_busy = false;

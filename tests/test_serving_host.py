@@ -142,6 +142,29 @@ def test_device_memory_ledger_host(tmp_path):
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
 
 
+def test_dispatch_policy_on_host(tmp_path):
+    """The serving loop's dispatch decisions (csrc/serve_policy.h) on the
+    host, for a 152-SM device: a partial batch goes at once while SMs are
+    idle and otherwise after its wait; a batch takes the two-CTA cluster
+    kernel only up to pair_max queries and when its SMs are idle, with a
+    quarter of the SMs of slack while at most half are busy; a C++ driver
+    built with g++."""
+    import os
+    import shutil
+    import subprocess
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    here = os.path.dirname(os.path.abspath(__file__))
+    csrc = os.path.join(os.path.dirname(here), "inspire-rs_gb300", "csrc")
+    exe = str(tmp_path / "serve_policy_check")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", csrc, os.path.join(here, "native", "serve_policy_check.cpp"),
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
+
+
 def test_autotune_pick_prefers_more_streams_on_near_ties(serving):
     """Within the tie band the choice has the most batches in flight, then
     the smallest batches; outside it the rate decides."""
